@@ -1,0 +1,370 @@
+"""Benchmark: depth-map layered angular-spectrum CGH frames/s at 1920x1080.
+
+Workload (one "step" = one frame): 1920x1080 uint8 intensity + uint8 depth
+(seeded Gaussian-sum scenes), 32 depth layers over z in [0.30, 0.35] m, 8 um
+pitch, 532 nm, per-pixel random phase (seeded SplitMix64 stream generated on
+the device), 2x zero-padded angular-spectrum propagation on a 3840x2160
+grid, symmetrization encoding to a real fringe; FP32 compute.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value      frames/s with inputs resident in HBM, CUDA events around each
+           step on the launching stream; L2 flushed (512 MiB write) between
+           timed steps, outside the events.
+e2e        the same frames through oh_depthmap_generate_host: pinned host
+           buffers in, host->device copy, frame, device->host copy of the
+           fringe, wall clock per call.
+roofline   the dominant kernel's device time (events around its launches on
+           its stream) against the measured HBM peak.
+cpu_baseline  the oracle port (numpy/scipy pocketfft, all host cores) on a
+           bounded sample of the same frame, extrapolated to a frame.
+--impl reference  times that CPU restatement of the reference's depth-map
+           path (Calc_Holo_CPU + encoding_CPU) alone; the reference's own CPU
+           code needs Qt and FFTW and cannot be built.
+N > 1: one process per GPU (torchrun), independent frames per rank (weak
+scaling), no collective on the data path; max of per-rank times.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "CGH frames/s at 1920×1080 vs plain GPU path at ≤1e-3 rel err; % roofline"
+NX, NY, LAYERS, PAD = 1920, 1080, 32, 2
+SCENE_SEED, PHASE_SEED = 2024, 77
+WORKLOAD = ("depth-map layered angular-spectrum CGH 1920x1080, 32 layers z 0.30-0.35 m, 2x zero-padded "
+            "3840x2160 FFT grid, per-pixel seeded random phase, symmetrization encoding, fp32")
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = Path(tempfile.gettempdir()) / f"oh_clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        try:
+            self.fh.close()
+        except Exception:
+            pass
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for ln in self.path.read_text().splitlines():
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        try:
+            self.path.unlink()
+        except Exception:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_frame_sample(img, depth, phase, layers_sampled=2, workers=None):
+    """Oracle port on the host: `layers_sampled` full-size layers plus the
+    encode, extrapolated to the 32-layer frame.  Returns (frames/s, sample text)."""
+    from oracle import depthmap as odm
+    workers = workers or os.cpu_count()
+    p = odm.DMParams(pnx=NX, pny=NY, num_of_depth=LAYERS, pad=PAD)
+    idx = list(range(0, LAYERS, max(1, LAYERS // layers_sampled)))[:layers_sampled]
+    t0 = time.perf_counter()
+    U = odm.calc_holo(img, depth, p, phase=phase, workers=workers, layers=idx)
+    t1 = time.perf_counter()
+    odm.encode_symmetrization(U, p, workers=workers)
+    t2 = time.perf_counter()
+    frame_s = (t1 - t0) * LAYERS / len(idx) + (t2 - t1)
+    return 1.0 / frame_s, (f"{len(idx)} of {LAYERS} layers of the 1920x1080 frame + full encode, float64 numpy/"
+                           f"scipy pocketfft with {workers} threads, layer time x{LAYERS / len(idx):.0f}")
+
+
+def run_reference(args, world, rank):
+    """--impl reference: the CPU restatement of the reference's depth-map path."""
+    if rank != 0:
+        return
+    from openholo_gb300 import scenes
+    img, depth = scenes.depthmap_scene(SCENE_SEED, NY, NX)
+    phase = scenes.seeded_phase(PHASE_SEED, NY, NX)
+    for _ in range(args.warmup):
+        cpu_frame_sample(img, depth, phase, layers_sampled=1)
+    vals = []
+    sample = ""
+    for _ in range(args.steps):
+        v, sample = cpu_frame_sample(img, depth, phase, layers_sampled=1)
+        vals.append(v)
+    fps = 1.0 / statistics.mean(1.0 / v for v in vals)
+    cores = os.cpu_count()
+    line = {"metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 / fps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD.replace("fp32", "float64 CPU"), "pnx": NX, "pny": NY, "layers": LAYERS,
+                       "pad": PAD},
+            "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
+                             "sample": "per step: " + sample + "; the reference's depth-map CPU code needs Qt "
+                                       "and FFTW, so its line-by-line restatement (oracle/depthmap.py) runs"},
+            "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def plain_gpu_path(img_t, depth_t, zt, lut, torch):
+    """The reference's per-layer structure (mask kernel, centred FFT, AS
+    multiply-accumulate, crop, centred IFFT, shift phase, real part) in FP32
+    with cuFFT C2C (torch.fft, plans cached) and transfer functions
+    precomputed once in FP64.  Comparison baseline only."""
+    dev = img_t.device
+    Px, Py = PAD * NX, PAD * NY
+    ox, oy = (Px - NX) // 2, (Py - NY) // 2
+    lam, pp = 532e-9, 8e-6
+    k = 2 * math.pi / lam
+    ssx, ssy = Px * pp, Py * pp
+    x = torch.arange(Px, device=dev, dtype=torch.float64)
+    y = torch.arange(Py, device=dev, dtype=torch.float64)
+    fx = (-1.0 / (2 * pp)) + x / ssx
+    fy = (1.0 / (2 * pp)) - 1.0 / ssy - y / ssy
+    s = torch.sqrt(1 - (lam * fx[None, :]) ** 2 - (lam * fy[:, None]) ** 2)
+    H = []
+    for z in zt:
+        ph = torch.remainder(k * (-z) * s + k * z, 2 * math.pi)     # carrier folded in (FP64)
+        H.append(torch.polar(torch.ones_like(ph), ph).to(torch.complex64))
+    from openholo_gb300 import scenes
+    ph0 = torch.from_numpy(scenes.seeded_phase(PHASE_SEED, NY, NX)).to(dev)
+    src = (img_t.to(torch.float32) / 255.0) * torch.polar(torch.ones_like(ph0), ph0)
+    layer_idx = torch.from_numpy(lut.astype(np.int64)).to(dev)[depth_t.long()]
+    cx1, cx2, cy1, cy2 = 0, Px - 1, Py // 2 - (Py // 2) // 2 - 1, Py // 2 - (Py // 2) // 2 - 1 + Py // 2 - 1
+    r = torch.arange(NY, device=dev, dtype=torch.float64)
+    yy = NY * pp / 2.0 - pp * r - pp
+    shy = torch.polar(torch.ones_like(yy), 2 * math.pi * (yy / (4 * pp))).to(torch.complex64)
+    u = torch.zeros((Py, Px), dtype=torch.complex64, device=dev)
+
+    def frame():
+        U = torch.zeros((Py, Px), dtype=torch.complex64, device=dev)
+        for li in range(LAYERS):
+            u.zero_()
+            u[oy:oy + NY, ox:ox + NX] = torch.where(layer_idx == li + 1, src, 0)
+            S = torch.fft.fftshift(torch.fft.fft2(torch.fft.fftshift(u)))
+            U += H[li] * S
+        Uc = torch.zeros_like(U)
+        Uc[cy1:cy2 + 1, cx1:cx2 + 1] = U[cy1:cy2 + 1, cx1:cx2 + 1]
+        h = torch.fft.fftshift(torch.fft.ifft2(torch.fft.fftshift(Uc)))[oy:oy + NY, ox:ox + NX]
+        return (h * shy[:, None]).real
+    return frame
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-baselines", action="store_true", help="skip the CPU and plain-GPU comparison legs")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import torch
+    from openholo_gb300 import Context, depthmap as dm, launch_count, scenes
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+        pg = dist
+    ctx = Context(local)
+    stream = torch.cuda.current_stream()
+    img, depth = scenes.depthmap_scene(SCENE_SEED + rank, NY, NX)
+    p = dm.make_params(pnx=NX, pny=NY, num_of_depth=LAYERS, pad=PAD, phase_mode=dm.OH_PHASE_SEEDED,
+                       seed=PHASE_SEED + rank)
+    d_img = torch.from_numpy(img).to(dev)
+    d_depth = torch.from_numpy(depth).to(dev)
+    fringe = torch.empty((NY, NX), dtype=torch.float32, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    for _ in range(args.warmup):
+        dm.generate(ctx, p, d_img, d_depth, fringe=fringe)
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    n0 = launch_count()
+    ctx.set_timing(True)
+    ctx.read_timing(reset=True)
+    with ClockSampler(local) as clk:
+        for a, b in ev:
+            flush.fill_(1.0)
+            a.record(stream)
+            dm.generate(ctx, p, d_img, d_depth, fringe=fringe)
+            b.record(stream)
+        torch.cuda.synchronize()
+    launches = launch_count() - n0
+    ctx.set_timing(False)
+    ktimes = ctx.read_timing(reset=True)
+    clocks = clk.summary()
+    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+    if pg:
+        t = torch.tensor([total_ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / args.steps
+    fps = world * 1000.0 / ms_step
+
+    # ---- end to end through the host-buffer C entry point
+    h_img = torch.from_numpy(img).pin_memory()
+    h_depth = torch.from_numpy(depth).pin_memory()
+    h_out = torch.empty((NY, NX), dtype=torch.float32).pin_memory()
+    for _ in range(2):
+        dm.generate_host(ctx, p, h_img.numpy(), h_depth.numpy(), out=h_out.numpy())
+    if pg:
+        pg.barrier()
+    wall = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dm.generate_host(ctx, p, h_img.numpy(), h_depth.numpy(), out=h_out.numpy())
+        wall.append(time.perf_counter() - t0)
+    e2e_ms = 1000.0 * sum(wall) / len(wall)
+    if pg:
+        t = torch.tensor([e2e_ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    # ---- roofline of the dominant kernel
+    peak, peak_kind = load_peaks()
+    dom = max(ktimes.items(), key=lambda kv: kv[1][0]) if ktimes else ("?", (0.0, 1))
+    dom_name, (dom_ms, dom_n) = dom
+    Np = (PAD * NX) * (PAD * NY)
+    # per-kernel share of the frame HBM model: per layer a 2-pass FFT that reads and
+    # writes 8 B/sample per pass, plus one inverse 2-pass FFT and the uint8 inputs
+    model = {"dm_row_pass": LAYERS * 16 * Np + 2 * NX * NY,
+             "dm_col_pass": LAYERS * 16 * Np + 16 * Np,
+             "dm_out_pass": 16 * Np}
+    alg_bytes = model.get(dom_name, 0)
+    achieved = alg_bytes / (dom_ms / dom_n / 1000.0) / 1e9 if dom_ms > 0 else 0.0
+    traffic_path = ROOT / "profiles" / "traffic.json"
+    traffic = None
+    if traffic_path.exists():
+        traffic = json.loads(traffic_path.read_text()).get(dom_name)
+
+    out = {"metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic: seeded Gaussian-sum uint8 intensity/depth, SplitMix64 per-pixel phase",
+           "config": {"workload": WORKLOAD, "pnx": NX, "pny": NY, "layers": LAYERS, "pad": PAD,
+                      "fft_grid": [PAD * NX, PAD * NY], "l2": "flushed between timed steps (512 MiB write)"},
+           "e2e": {"value": world * 1000.0 / e2e_ms, "unit": "frames/s", "h2d_bytes_per_step": 2 * NX * NY,
+                   "d2h_bytes_per_step": 4 * NX * NY},
+           "gpu_launches": launches,
+           "kernels_ms_per_frame": {k: v[0] / args.steps for k, v in ktimes.items()},
+           "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                        "algorithmic_bytes_per_launch": alg_bytes},
+           "clocks": clocks}
+
+    if rank == 0 and world == 1 and not args.no_baselines:
+        # accuracy of this frame against the FP64 path (pinned to the oracle in tests)
+        f64 = dm.generate(ctx, p, d_img, d_depth, precision="fp64")
+        torch.cuda.synchronize()
+        f32 = fringe.double()
+        out["accuracy"] = {"rel_err_vs_fp64": float(torch.linalg.norm(f32 - f64) / torch.linalg.norm(f64))}
+        # plain FP32 GPU path (reference structure on cuFFT)
+        try:
+            lut, zt = dm.levels(p)
+            frame = plain_gpu_path(d_img, d_depth, list(zt), lut, torch)
+            for _ in range(2):
+                ref_plain = frame()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            reps = 3
+            a.record()
+            for _ in range(reps):
+                ref_plain = frame()
+            b.record()
+            torch.cuda.synchronize()
+            plain_ms = a.elapsed_time(b) / reps
+            out["plain_gpu_path"] = {"value": 1000.0 / plain_ms, "unit": "frames/s",
+                                     "rel_err_vs_fp64": float(torch.linalg.norm(ref_plain.double() - f64) /
+                                                              torch.linalg.norm(f64)),
+                                     "what": "reference per-layer structure, FP32, cuFFT C2C via torch.fft, "
+                                             "FP64-precomputed transfer functions"}
+            del frame
+        except Exception as e:  # pragma: no cover
+            out["plain_gpu_path"] = {"error": str(e)[:200]}
+        torch.cuda.empty_cache()
+        phase = scenes.seeded_phase(PHASE_SEED, NY, NX)
+        v, sample = cpu_frame_sample(img, depth, phase, layers_sampled=2)
+        out["cpu_baseline"] = {"value": v, "unit": "frames/s", "cores": os.cpu_count(), "kind": "port",
+                               "sample": sample}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if pg:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,227 @@
+/*
+ * oh.h — C ABI of the GB300-native hologram-generation library (liboh_gb300.so).
+ *
+ * Every entry point takes plain pointers and sizes, returns an oh_status and
+ * never calls exit().  Device pointers are caller-owned; temporary device
+ * memory lives in a per-context scratch arena.  Work is enqueued on the
+ * caller's stream; no call synchronises the host unless its name ends in
+ * _host (those copy host buffers in and out and return when the result is on
+ * the host).
+ *
+ * The operators mirror the reference's hot path:
+ *   - layered angular-spectrum depth-map CGH + symmetrization encoding
+ *       (OpenHolo_DepthMap/Hologram/src/HologramGenerator.cpp:261-294,391-522,
+ *        HologramGenerator_GPU.cpp:246-368, HologramKernel.cu:49-187)
+ *   - point-cloud Rayleigh-Sommerfeld / Fresnel summation
+ *       (OpenHolo_KETI/.../ophgen_pointcloud/ophgen_pointcloud.cpp:195-365,
+ *        .../ophgen_pointcloud_gpu/ophgen_pointcloud_gpu.cpp:391-503)
+ *   - WRP accumulation + Fresnel-convolution propagation
+ *       (OpenHolo_WRP/openwrp_console_ver 1.0/openwrp/WRP.cpp:65-140,
+ *        cwo/src/cwo.cpp:2198-2279,2872-2898)
+ *   - encoders (OpenHolo_Encoding/fn_encoding.m:29-98, Hologram_WRP.m:57-60)
+ * The reference-signature launchers (cudaFFT, cudaDepthHoloKernel, ...) are
+ * declared separately in oh_reference_shims.h.
+ */
+#ifndef OH_GB300_H
+#define OH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum oh_status {
+  OH_OK = 0,
+  OH_ERR_INVALID_ARG = 1,      /* null pointer, non-positive size, bad enum */
+  OH_ERR_UNSUPPORTED_SIZE = 2, /* transform length has no plan (see oh_fft_supported) */
+  OH_ERR_CUDA = 3,             /* a CUDA runtime call failed; see oh_last_error() */
+  OH_ERR_ALLOC = 4,            /* scratch allocation failed */
+  OH_ERR_TIMEOUT = 5,          /* a bounded device-side wait ran out */
+  OH_ERR_IO = 6                /* a file could not be read or parsed */
+} oh_status;
+
+typedef enum oh_precision { OH_FP32 = 0, OH_FP64 = 1 } oh_precision;
+
+typedef struct oh_ctx oh_ctx;   /* opaque; one per device, thread-safe */
+
+/* Interleaved complex values (same layout as float2/double2, cufftComplex). */
+typedef struct oh_c64  { float  x, y; } oh_c64;
+typedef struct oh_c128 { double x, y; } oh_c128;
+
+/* ---- context ---------------------------------------------------------- */
+oh_status   oh_ctx_create(oh_ctx** ctx, int device);
+oh_status   oh_ctx_destroy(oh_ctx* ctx);
+/* Bytes currently held by the context's scratch arena. */
+size_t      oh_ctx_scratch_bytes(const oh_ctx* ctx);
+oh_status   oh_ctx_release_scratch(oh_ctx* ctx);
+const char* oh_status_string(oh_status s);
+/* Message of the last failing call on this host thread ("" if none). */
+const char* oh_last_error(void);
+/* Number of kernels this library has launched since load (all contexts). */
+uint64_t    oh_kernel_launch_count(void);
+/* Per-kernel device timing: while enabled, every kernel this context
+ * launches is bracketed by CUDA events on its stream.  oh_ctx_read_timing
+ * waits for the recorded events, accumulates milliseconds and launch counts
+ * per kernel name, fills up to `cap` entries and returns the number of
+ * kernel names (reset != 0 clears the totals). */
+oh_status   oh_ctx_set_timing(oh_ctx* ctx, int on);
+int         oh_ctx_read_timing(oh_ctx* ctx, int reset, const char** names,
+                               double* ms, long* launches, int cap);
+const char* oh_version(void);
+
+/* ---- FFT ----------------------------------------------------------------
+ * Mixed-radix complex FFT (radices 2,3,4,5,8 + generic odd prime), computed
+ * in shared memory by this library's own kernels.
+ * direction: -1 forward (e^{-2 pi i jk/n}), +1 inverse (unnormalised unless
+ * normalize != 0, then scaled by 1/(nx*ny)).
+ * shift != 0 computes fftshift(FFT(fftshift(x))) as HologramKernel.cu:10-34,
+ * 189-227 does (shift by floor(n/2) on both sides).
+ * in == out is allowed. */
+int       oh_fft_supported(int n, oh_precision prec);
+oh_status oh_fft2d(oh_ctx* ctx, oh_precision prec, int nx, int ny,
+                   const void* in, void* out, int direction, int shift,
+                   int normalize, void* stream);
+/* Batched 1-D transforms along contiguous rows (ny rows of length nx). */
+oh_status oh_fft1d_rows(oh_ctx* ctx, oh_precision prec, int nx, int ny,
+                        const void* in, void* out, int direction, int normalize,
+                        void* stream);
+
+/* ---- depth-map layered angular-spectrum CGH ------------------------------
+ * Field order follows HologramParams (HologramGenerator.h:100-120) plus the
+ * config_openholo.txt switches that HologramGenerator reads. */
+typedef enum oh_phase_mode {
+  OH_PHASE_REFERENCE = 0,  /* constant per-layer phase rand_phase (RANDOM_PHASE=0 -> 1+0i) */
+  OH_PHASE_ARRAY = 1,      /* per-pixel phase in radians, float32 [pny][pnx] */
+  OH_PHASE_SEEDED = 2      /* per-pixel phase 2*pi*u, u from SplitMix64(seed, pixel index) */
+} oh_phase_mode;
+
+typedef struct oh_depthmap_params {
+  int    pnx, pny;               /* SLM pixel counts (input image size) */
+  double ppx, ppy;               /* SLM pixel pitch [m] */
+  double lambda;                 /* wavelength [m] */
+  double field_lens;             /* FIELD_LENS [m] (viewing-window transform) */
+  double near_depthmap, far_depthmap;
+  int    num_of_depth;           /* depth levels */
+  int    flag_change_depth_quantization;   /* 1: bin dmap into num_of_depth levels */
+  int    default_depth_quantization;       /* 256 in the reference config */
+  int    transform_viewing_window;         /* 1: z' = -f z/(z-f); 0: z' = z */
+  int    pad;                    /* 1: reference grid, 2: 2x zero-padded grid */
+  int    sig_location_x, sig_location_y;   /* Encoding_Symmetrization(ivec2(x,y)) */
+  int    phase_mode;             /* oh_phase_mode */
+  uint64_t seed;                 /* OH_PHASE_SEEDED */
+  double rand_phase_re, rand_phase_im;     /* OH_PHASE_REFERENCE constant */
+  const int* render_depth;       /* 1-based levels to render (host array); NULL = 1..num_of_depth */
+  int    n_render_depth;
+} oh_depthmap_params;
+
+/* Fill p with the reference defaults used by config_openholo.txt-like runs. */
+void      oh_depthmap_params_default(oh_depthmap_params* p);
+
+/* Parse a config_openholo.txt file (positional format, arithmetic
+ * expressions allowed in the pixel-count and pitch lines, as
+ * HologramGenerator::readConfig, HologramGenerator.cpp:65-229, reads it).
+ * render_depth storage is owned by the library (valid until the next call
+ * on this thread). */
+oh_status oh_depthmap_read_config(const char* path, oh_depthmap_params* p);
+
+/* Full frame: img/depth uint8 [pny][pnx] on the device, phase float32
+ * [pny][pnx] (only for OH_PHASE_ARRAY, else NULL).
+ * fringe_out: real fringe [pny][pnx] (float for OH_FP32, double for OH_FP64),
+ *   the u255_fringe_ of HologramGenerator (before uint8 normalisation).
+ * field_out (nullable): complex hologram h before taking the real part,
+ *   [pny][pnx] oh_c64/oh_c128.
+ * spectrum_out (nullable): accumulated frequency-domain field U_complex
+ *   [P*pny][P*pnx] (P = pad) before encoding. */
+oh_status oh_depthmap_generate(oh_ctx* ctx, oh_precision prec,
+                               const oh_depthmap_params* p,
+                               const uint8_t* img, const uint8_t* depth,
+                               const float* phase, void* fringe_out,
+                               void* field_out, void* spectrum_out,
+                               void* stream);
+/* Same with host buffers; copies in and out on the given stream and waits. */
+oh_status oh_depthmap_generate_host(oh_ctx* ctx, oh_precision prec,
+                                    const oh_depthmap_params* p,
+                                    const uint8_t* img_host,
+                                    const uint8_t* depth_host,
+                                    const float* phase_host,
+                                    void* fringe_host, void* stream);
+/* Layer index per depth byte (256 entries, 0 = no layer), exactly the
+ * reference's binning (change_depth_quan_*, HologramGenerator_CPU.cpp:74-103)
+ * and the z' of each level (dlevel_transform_).  z_out holds num_of_depth
+ * doubles. */
+oh_status oh_depthmap_levels(const oh_depthmap_params* p, int16_t lut_out[256],
+                             double* z_out);
+
+/* ---- point cloud -----------------------------------------------------------
+ * Field order mirrors OphSpec (ophgen_pointcloud.h:45-70). */
+typedef struct oh_pc_params {
+  double scale_x, scale_y, scale_z;   /* pointCloudScale{X,Y,Z} */
+  double offset_depth;                /* offsetDepth */
+  double pitch_x, pitch_y;            /* samplingPitch{X,Y} */
+  int    nx, ny;
+  double lambda;
+  double tilt_x_deg, tilt_y_deg;      /* tiltAngle{X,Y} in degrees */
+} oh_pc_params;
+
+/* Points are float4 (x, y, z, amplitude) in scene units before scaling.
+ * field_out (nullable): complex field sum_j a_j exp(i phi_j) [ny][nx],
+ * fringe_out (nullable): KETI fringe, dst += sum_j a_j cos(phi_j) [ny][nx]
+ *   (accumulated into the caller's buffer, as the reference does).
+ * phi_j = k r_j - k X sin(tx) - k Y sin(ty), r exact.
+ * Precision: OH_FP32 -> oh_c64/float outputs, OH_FP64 -> oh_c128/double. */
+oh_status oh_pointcloud(oh_ctx* ctx, oh_precision prec, const oh_pc_params* p,
+                        const float* xyza, int n_points, void* field_out,
+                        void* fringe_out, void* stream);
+/* Host-buffer form (the ophGenCghPointCloud drop-in path). */
+oh_status oh_pointcloud_host(oh_ctx* ctx, oh_precision prec,
+                             const oh_pc_params* p, const float* xyza_host,
+                             int n_points, void* field_host, void* fringe_host,
+                             void* stream);
+
+/* ---- WRP ------------------------------------------------------------------ */
+typedef struct oh_wrp_params {
+  int    nx, ny;          /* WRP / hologram grid */
+  double pitch;           /* dpx = dpy */
+  double lambda;
+  double z_wrp;           /* WRP plane position */
+  int    window;          /* 0: reference formula int(|lambda dz/(2p^2)+0.5|)*2-1, >0: fixed half-width */
+} oh_wrp_params;
+/* OPHWRP::SingleWRP (WRP.cpp:75-140): points double3 (x,y,z); adds into wrp
+ * (caller zeroes it, as CWO::Create does). */
+oh_status oh_wrp_accumulate(oh_ctx* ctx, oh_precision prec,
+                            const oh_wrp_params* p, const double* xyz,
+                            int n_points, void* wrp, void* stream);
+/* CWO::Diffract(z, CWO_FRESNEL_CONV) with the default zero-pad expansion
+ * (cwo.cpp:2198-2279, 2872-2898), in place on field [ny][nx]. */
+oh_status oh_fresnel_propagate(oh_ctx* ctx, oh_precision prec, int nx, int ny,
+                               double pitch, double lambda, double z,
+                               void* field, void* stream);
+
+/* ---- encoders ------------------------------------------------------------- */
+typedef enum oh_encoding {
+  OH_ENC_REAL = 0,            /* real(U) */
+  OH_ENC_PHASE_TO_AMP = 1,    /* angle(U) + pi/(2*pi) (fn_encoding.m:57) */
+  OH_ENC_NUM_INTERFERENCE = 2,/* |U + max|U||^2 / max */
+  OH_ENC_BURCKHARDT = 3,      /* [ny][3nx] */
+  OH_ENC_TWO_PHASE = 4,       /* [ny][2nx] */
+  OH_ENC_SSB_LEFT = 5, OH_ENC_SSB_RIGHT = 6, OH_ENC_SSB_TOP = 7, OH_ENC_SSB_BOTTOM = 8,
+  OH_ENC_PHASE_ONLY_U8 = 9,   /* uint8(255*(angle+pi)/max(angle+pi)) (Hologram_WRP.m:57-60) */
+  OH_ENC_AMPLITUDE = 10       /* |U| */
+} oh_encoding;
+/* field: complex [ny][nx]; out: float/double (or uint8 for PHASE_ONLY_U8). */
+oh_status oh_encode(oh_ctx* ctx, oh_precision prec, int kind, int nx, int ny,
+                    const void* field, void* out, void* stream);
+/* min/max normalisation to uint8 as HologramGenerator::Write_Result_image
+ * (truncating, HologramGenerator.cpp:528-565) when round_half == 0, or
+ * ophNormalize with +0.5 rounding and vertical flip (oph_common.cpp:92-115)
+ * when round_half != 0. */
+oh_status oh_normalize_u8(oh_ctx* ctx, oh_precision prec, int nx, int ny,
+                          const void* in, uint8_t* out, int round_half,
+                          void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OH_GB300_H */

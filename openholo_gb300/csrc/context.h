@@ -1,0 +1,75 @@
+// Host runtime: per-device context with an FFT plan cache and a named
+// scratch arena.  Calls on one context are serialised by a mutex, and every
+// call orders its stream after the previous call's work through an event, so
+// the shared scratch is never used by two streams at once.
+#pragma once
+#include <cuda_runtime.h>
+#include <map>
+#include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
+#include "fft_core.cuh"
+
+struct oh_ctx {
+  int device = 0;
+  std::mutex mu;
+  cudaEvent_t last_done = nullptr;   // recorded at the end of every call
+  struct Buf { void* p = nullptr; size_t bytes = 0; };
+  std::map<std::string, Buf> scratch;
+  struct PlanBufs { oh::FFTPlan plan; void* tw = nullptr; int* perm = nullptr; int* iperm = nullptr; };
+  std::map<std::pair<int, int>, PlanBufs> plans;   // key (n, precision)
+  // optional per-kernel timing: events recorded around each launch on the
+  // launching stream while `timing` is set
+  bool timing = false;
+  struct Mark { const char* name; cudaEvent_t a, b; };
+  std::vector<Mark> marks;
+  std::vector<cudaEvent_t> event_pool;
+  std::map<std::string, std::pair<double, long>> timing_acc;   // name -> (ms, launches)
+};
+
+namespace oh {
+
+// Scoped guard: locks the context, makes its device current and orders
+// `stream` after the context's previous call.  On destruction records the
+// completion event on the stream.
+class CallScope {
+ public:
+  CallScope(oh_ctx* ctx, cudaStream_t stream);
+  ~CallScope();
+  oh_status status() const { return st_; }
+ private:
+  oh_ctx* ctx_;
+  cudaStream_t stream_;
+  int prev_dev_ = -1;
+  oh_status st_ = OH_OK;
+  std::unique_lock<std::mutex> lk_;
+};
+
+// Returns a device buffer of at least `bytes` under `name`, growing it if
+// needed (growth synchronises the device before freeing the old buffer).
+oh_status scratch(oh_ctx* ctx, const char* name, size_t bytes, void** out);
+
+// Plan for length n in precision prec (0 = fp32, 1 = fp64); built on first
+// use.  Fails with OH_ERR_UNSUPPORTED_SIZE when n cannot be factored.
+oh_status get_plan(oh_ctx* ctx, int n, int prec, FFTPlan* out);
+
+// Radix schedule for n (empty when unsupported).
+bool factorize(int n, int* radix, int* nst);
+
+// Largest dynamic shared memory a block may use on this device.
+size_t max_smem_per_block();
+
+// Bracket one kernel launch with timing events when ctx->timing is set.
+class KernelTimer {
+ public:
+  KernelTimer(oh_ctx* ctx, const char* name, cudaStream_t st);
+  ~KernelTimer();
+ private:
+  oh_ctx* ctx_;
+  const char* name_;
+  cudaStream_t st_;
+  cudaEvent_t a_ = nullptr;
+};
+
+}  // namespace oh

@@ -1,0 +1,629 @@
+// Layered angular-spectrum depth-map CGH with symmetrization encoding.
+//
+// Reference path (OpenHolo_DepthMap/Hologram/src):
+//   GetDepthValues / change_depth_quan   HologramGenerator.cpp:391-417, HologramKernel.cu:168-187
+//   TransformViewingWindow                HologramGenerator.cpp:423-435
+//   Calc_Holo_GPU                         HologramGenerator_GPU.cpp:246-302
+//     per layer: depth_sources_kernel (mask * rand_phase * carrier) -> cudaFFT
+//     (fftshift.FFT.fftshift) -> propagation_angularsp_kernel (U += H*F)
+//   Encoding_Symmetrization / encoding_GPU HologramGenerator.cpp:481-522, HologramGenerator_GPU.cpp:338-368
+//     cropFringe -> cudaFFT(inverse, 1/N) -> getFringe -> real part
+//
+// GB300 structure (4 launches per frame, whatever the layer count):
+//   dm_setup     per-layer tables (FP64 phase reduction, rounded to the
+//                compute precision) and per-frame flags
+//   dm_row_pass  one block per image row: builds every layer's masked source
+//                row on the fly from the uint8 image/depth bytes, x-FFTs only
+//                the layers present in that row and stores them column-strip
+//                tiled; absent (layer,row) pairs are flagged, not written
+//   dm_col_pass  one block per strip of W spectrum columns: for every layer
+//                y-FFT + angular-spectrum multiply-accumulate into registers;
+//                then SSB crop, inverse y-FFT, keep the output rows, apply the
+//                y shift phase and 1/N
+//   dm_out_pass  one block per output row: inverse x-FFT, crop the padding,
+//                x shift phase, real part
+// The 2x zero-padding (pad = 2) never materialises: padded rows are skipped
+// and padded columns are zeros written straight into shared memory.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+#include "context.h"
+#include "fft_kernels.cuh"
+
+namespace oh {
+
+constexpr int kMaxEntries = 256;
+
+// Per-frame constants, passed by value to dm_setup (no host->device copy in
+// the frame, so a frame can be captured in a CUDA graph).
+struct DMSetup {
+  int n_entries, n_uslots;
+  int16_t uslot_of_entry[kMaxEntries];
+  double zp[kMaxEntries];            // z' of each render entry
+  double cre[kMaxEntries], cim[kMaxEntries];   // per-entry complex constant
+  int16_t lut[256];                  // depth byte -> unique slot (-1: none)
+};
+
+template <typename R>
+struct DMArgs {
+  typedef typename cplx_of<R>::type C;
+  int pnx, pny, Px, Py, ox, oy, hx, hy;
+  int W, nstrips, n_entries, n_uslots;
+  int cx1, cx2, cy1, cy2;            // SSB crop window on the (padded) spectrum
+  double ppx, ppy, ssx, ssy, lambda, k;
+  const uint8_t* img;
+  const uint8_t* depth;
+  const float* phase;
+  int phase_mode;
+  uint64_t seed;
+  // device tables (written by dm_setup)
+  int16_t* lut;          // 256
+  int16_t* uslot_of_entry;
+  R* kzp;                // k*z' per entry
+  C* cst;                // per-entry constant
+  C* exc;                // [entries][Px] cst*exp(i alpha fx^2)   (fp32 path)
+  C* ey;                 // [entries][Py] exp(i alpha fy^2)       (fp32 path)
+  R* lfx;                // [Px] (lambda fx)^2
+  R* lfy;                // [Py] (lambda fy)^2
+  C* shy;                // [pny] y shift phase / (Px*Py)
+  C* shx;                // [pnx] x shift phase
+  int* slot_any;         // [uslots]
+  uint8_t* occ;          // [uslots][pny]
+  C* Rbuf;               // [uslots][nstrips][pny][W]
+  C* V;                  // [pny][Px]
+  R* fringe;             // [pny][pnx]
+  C* field;              // [pny][pnx] or null
+  C* spectrum;           // [Py][Px] or null
+  int sig_x, sig_y;
+  FFTPlan plx, ply;
+};
+
+__device__ __forceinline__ double2 cexp_d(double ph) {
+  double s, c;
+  sincos(ph, &s, &c);
+  return make_double2(c, s);
+}
+
+// exp(i*ph) for large |ph|: reduce modulo 2 pi in double first.
+__device__ __forceinline__ double2 cexp_reduced(double ph) {
+  const double two_pi = 6.283185307179586476925286766559;
+  double n = rint(ph / two_pi);
+  return cexp_d(fma(-n, two_pi, ph));
+}
+
+template <typename R>
+__global__ void dm_setup(DMArgs<R> a, DMSetup s) {
+  typedef typename cplx_of<R>::type C;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nthr = gridDim.x * blockDim.x;
+  const double pi = 3.14159265358979323846;
+  for (int i = tid; i < 256; i += nthr) a.lut[i] = s.lut[i];
+  for (int e = tid; e < s.n_entries; e += nthr) {
+    a.uslot_of_entry[e] = s.uslot_of_entry[e];
+    a.kzp[e] = (R)(a.k * s.zp[e]);
+    a.cst[e] = mk((R)s.cre[e], (R)s.cim[e]);
+  }
+  for (int u = tid; u < s.n_uslots; u += nthr) a.slot_any[u] = 0;
+  // reference frequency grid (HologramKernel.cu:85-86)
+  for (int x = tid; x < a.Px; x += nthr) {
+    double fx = (-1.0 / (2.0 * a.ppx)) + (1.0 / a.ssx) * (double)x;
+    double l = a.lambda * fx;
+    a.lfx[x] = (R)(l * l);
+  }
+  for (int y = tid; y < a.Py; y += nthr) {
+    double fy = (1.0 / (2.0 * a.ppy)) - (1.0 / a.ssy) - (1.0 / a.ssy) * (double)y;
+    double l = a.lambda * fy;
+    a.lfy[y] = (R)(l * l);
+  }
+  if constexpr (sizeof(R) == 4) {
+    // separable paraxial factors exp(i pi lambda z' f^2), reduced in double
+    for (int idx = tid; idx < s.n_entries * a.Px; idx += nthr) {
+      int e = idx / a.Px, x = idx - e * a.Px;
+      double fx = (-1.0 / (2.0 * a.ppx)) + (1.0 / a.ssx) * (double)x;
+      double2 v = cexp_reduced(pi * a.lambda * s.zp[e] * fx * fx);
+      double2 c = make_double2(s.cre[e], s.cim[e]);
+      a.exc[idx] = mk((R)(c.x * v.x - c.y * v.y), (R)(c.x * v.y + c.y * v.x));
+    }
+    for (int idx = tid; idx < s.n_entries * a.Py; idx += nthr) {
+      int e = idx / a.Py, y = idx - e * a.Py;
+      double fy = (1.0 / (2.0 * a.ppy)) - (1.0 / a.ssy) - (1.0 / a.ssy) * (double)y;
+      double2 v = cexp_reduced(pi * a.lambda * s.zp[e] * fy * fy);
+      a.ey[idx] = mk((R)v.x, (R)v.y);
+    }
+  }
+  // encoding shift phases (get_shift_phase_value, HologramGenerator_CPU.cpp:367-408)
+  const double norm = 1.0 / ((double)a.Px * (double)a.Py);
+  const double ssy0 = a.ppy * a.pny, ssx0 = a.ppx * a.pnx;
+  for (int r = tid; r < a.pny; r += nthr) {
+    double2 v = make_double2(1.0, 0.0);
+    if (a.sig_y != 0) {
+      double yy = (ssy0 / 2.0) - a.ppy * (double)r - a.ppy;
+      double ph = a.sig_y == 1 ? 2.0 * pi * (yy / (4.0 * a.ppy)) : 2.0 * pi * (-yy / (4.0 * a.ppy));
+      v = cexp_reduced(ph);
+    }
+    a.shy[r] = mk((R)(v.x * norm), (R)(v.y * norm));
+  }
+  for (int c = tid; c < a.pnx; c += nthr) {
+    double2 v = make_double2(1.0, 0.0);
+    if (a.sig_x != 0) {
+      double xx = (-ssx0 / 2.0) - a.ppx * (double)c - a.ppx;
+      double ph = a.sig_x == -1 ? 2.0 * pi * (-xx / (4.0 * a.ppx)) : 2.0 * pi * (xx / (4.0 * a.ppx));
+      v = cexp_reduced(ph);
+    }
+    a.shx[c] = mk((R)v.x, (R)v.y);
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void sincos_r(R x, R* s, R* c);
+template <> __device__ __forceinline__ void sincos_r<float>(float x, float* s, float* c) { sincosf(x, s, c); }
+template <> __device__ __forceinline__ void sincos_r<double>(double x, double* s, double* c) { sincos(x, s, c); }
+
+template <typename R>
+__global__ void __launch_bounds__(256) dm_row_pass(DMArgs<R> a) {
+  typedef typename cplx_of<R>::type C;
+  extern __shared__ unsigned char smem_raw[];
+  C* buf = reinterpret_cast<C*>(smem_raw);
+  C* v = buf + a.Px;
+  int16_t* li = reinterpret_cast<int16_t*>(v + a.pnx);
+  uint32_t* mask = reinterpret_cast<uint32_t*>(li + ((a.pnx + 1) & ~1));
+  const int r = blockIdx.x;
+  const int nwords = (a.n_uslots + 31) >> 5;
+  for (int i = threadIdx.x; i < nwords; i += blockDim.x) mask[i] = 0u;
+  __syncthreads();
+  const size_t rowoff = (size_t)r * a.pnx;
+  for (int c = threadIdx.x; c < a.pnx; c += blockDim.x) {
+    const uint8_t g = a.img[rowoff + c];
+    const int u = g > 0 ? (int)a.lut[a.depth[rowoff + c]] : -1;
+    li[c] = (int16_t)u;
+    C val = mk((R)0, (R)0);
+    if (u >= 0) {
+      const R amp = (R)g / (R)255;
+      if (a.phase_mode == OH_PHASE_REFERENCE) {
+        val = mk(amp, (R)0);
+      } else {
+        R ph;
+        if (a.phase_mode == OH_PHASE_ARRAY) ph = (R)a.phase[rowoff + c];
+        else ph = (R)u24_at(a.seed, rowoff + c) * (R)6.283185307179586476925;
+        R sn, cs;
+        sincos_r<R>(ph, &sn, &cs);
+        val = mk(amp * cs, amp * sn);
+      }
+      atomicOr(&mask[u >> 5], 1u << (u & 31));
+    }
+    v[c] = val;
+  }
+  __syncthreads();
+  for (int u = 0; u < a.n_uslots; ++u) {
+    const bool present = (mask[u >> 5] >> (u & 31)) & 1u;
+    if (threadIdx.x == 0) {
+      a.occ[(size_t)u * a.pny + r] = present ? 1 : 0;
+      if (present) a.slot_any[u] = 1;
+    }
+    if (!present) continue;
+    // shifted, zero-padded source line: a[j] = u[(j - hx) mod Px]
+    for (int j = threadIdx.x; j < a.Px; j += blockDim.x) {
+      int x = j - a.hx; if (x < 0) x += a.Px;
+      const int c = x - a.ox;
+      C val = mk((R)0, (R)0);
+      if (c >= 0 && c < a.pnx && li[c] == u) val = v[c];
+      buf[j] = val;
+    }
+    block_fft<-1>(buf, 1, a.Px, 1, a.plx, false);
+    C* dst = a.Rbuf + (size_t)u * a.nstrips * a.pny * a.W;
+    for (int kx = threadIdx.x; kx < a.Px; kx += blockDim.x) {
+      int m = kx - a.hx; if (m < 0) m += a.Px;       // S[kx] = A[(kx - hx) mod Px]
+      const int s = kx / a.W, w = kx - s * a.W;
+      dst[((size_t)s * a.pny + r) * a.W + w] = buf[a.plx.perm[m]];
+    }
+    __syncthreads();
+  }
+}
+
+template <typename R, int KMAX>
+__global__ void __launch_bounds__(512) dm_col_pass(DMArgs<R> a) {
+  typedef typename cplx_of<R>::type C;
+  extern __shared__ unsigned char smem_raw[];
+  const int W = a.W;
+  const int Py = a.Py;
+  C* buf = reinterpret_cast<C*>(smem_raw);
+  C* exw = buf + (size_t)Py * W;                  // [W]
+  R* lfxw = reinterpret_cast<R*>(exw + W);        // [W]
+  int* kyp = reinterpret_cast<int*>(lfxw + W);    // [Py] spectrum row held at storage position
+  const int s = blockIdx.x;
+  const int kx0 = s * W;
+  const int T = blockDim.x;
+  const int nel = Py * W;
+  for (int p = threadIdx.x; p < Py; p += T) {
+    int ky = a.ply.iperm[p] + a.hy; if (ky >= Py) ky -= Py;   // S[ky] = B[(ky - hy) mod Py]
+    kyp[p] = ky;
+  }
+  for (int w = threadIdx.x; w < W; w += T) lfxw[w] = a.lfx[kx0 + w];
+  C acc[KMAX];
+#pragma unroll
+  for (int k = 0; k < KMAX; ++k) acc[k] = mk((R)0, (R)0);
+  __syncthreads();
+
+  for (int e = 0; e < a.n_entries; ++e) {
+    const int u = a.uslot_of_entry[e];
+    if (!a.slot_any[u]) continue;
+    const uint8_t* occ = a.occ + (size_t)u * a.pny;
+    const C* src = a.Rbuf + ((size_t)u * a.nstrips + s) * a.pny * W;
+    for (int idx = threadIdx.x; idx < nel; idx += T) {
+      const int i = idx / W, w = idx - i * W;
+      int y = i - a.hy; if (y < 0) y += Py;
+      const int yl = y - a.oy;
+      C val = mk((R)0, (R)0);
+      if (yl >= 0 && yl < a.pny && occ[yl]) val = src[(size_t)yl * W + w];
+      buf[idx] = val;
+    }
+    if constexpr (sizeof(R) == 4) {
+      for (int w = threadIdx.x; w < W; w += T) exw[w] = a.exc[(size_t)e * a.Px + kx0 + w];
+    } else {
+      for (int w = threadIdx.x; w < W; w += T) exw[w] = a.cst[e];
+    }
+    block_fft<-1>(buf, W, 1, W, a.ply, true);
+    const R kz = a.kzp[e];
+    const C* eyr = a.ey + (size_t)e * Py;
+#pragma unroll
+    for (int k = 0; k < KMAX; ++k) {
+      const int idx = threadIdx.x + k * T;
+      if (idx < nel) {
+        const int p = idx / W, w = idx - p * W;
+        const int ky = kyp[p];
+        const R sv = lfxw[w] + a.lfy[ky];
+        C h;
+        if constexpr (sizeof(R) == 4) {
+          // residual of k z' (1 - sqrt(1-s)) beyond the separable s/2 term:
+          // k z' s^2 / (2 (1 + sqrt(1-s))^2), |.| < a few rad
+          const R rt = sqrt((R)1 - sv);
+          const R den = (R)1 + rt;
+          const R psi = kz * sv * sv / ((R)2 * den * den);
+          float sn, cs;
+          __sincosf(psi, &sn, &cs);
+          C g = cmul(exw[w], eyr[ky]);
+          h = cmul(g, mk(cs, sn));
+        } else {
+          // direct reference formula H = exp(i k d sqrt(1 - s)), d = -z'
+          const double sval = sqrt(1.0 - (double)sv) * (-(double)kz);
+          double sn, cs;
+          sincos(sval, &sn, &cs);
+          h = cmul(exw[w], mk((R)cs, (R)sn));
+        }
+        acc[k] = cadd(acc[k], cmul(h, buf[idx]));
+      }
+    }
+    __syncthreads();
+  }
+
+  // SSB crop + move the spectrum into the inverse-transform input order:
+  // b[i] = Uc[(i - hy) mod Py]  ->  spectrum row ky goes to i = (ky + hy) mod Py
+#pragma unroll
+  for (int k = 0; k < KMAX; ++k) {
+    const int idx = threadIdx.x + k * T;
+    if (idx < nel) {
+      const int p = idx / W, w = idx - p * W;
+      const int ky = kyp[p];
+      const int kx = kx0 + w;
+      if (a.spectrum) a.spectrum[(size_t)ky * a.Px + kx] = acc[k];
+      const bool keep = kx >= a.cx1 && kx <= a.cx2 && ky >= a.cy1 && ky <= a.cy2;
+      int i = ky + a.hy; if (i >= Py) i -= Py;
+      // each storage slot is written exactly once (ky is a permutation)
+      buf[i * W + w] = keep ? acc[k] : mk((R)0, (R)0);
+    }
+  }
+  block_fft<1>(buf, W, 1, W, a.ply, true);
+  for (int idx = threadIdx.x; idx < a.pny * W; idx += T) {
+    const int yl = idx / W, w = idx - yl * W;
+    int m = a.oy + yl - a.hy; if (m < 0) m += Py;   // out[y] = B[(y - hy) mod Py]
+    const C val = cmul(buf[a.ply.perm[m] * W + w], a.shy[yl]);
+    a.V[(size_t)yl * a.Px + kx0 + w] = val;
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) dm_out_pass(DMArgs<R> a) {
+  typedef typename cplx_of<R>::type C;
+  extern __shared__ unsigned char smem_raw[];
+  C* buf = reinterpret_cast<C*>(smem_raw);
+  const int yl = blockIdx.x;
+  const C* row = a.V + (size_t)yl * a.Px;
+  for (int j = threadIdx.x; j < a.Px; j += blockDim.x) {
+    int kx = j - a.hx; if (kx < 0) kx += a.Px;
+    buf[j] = row[kx];
+  }
+  block_fft<1>(buf, 1, a.Px, 1, a.plx, false);
+  for (int c = threadIdx.x; c < a.pnx; c += blockDim.x) {
+    int m = a.ox + c - a.hx; if (m < 0) m += a.Px;
+    C h = buf[a.plx.perm[m]];
+    if (a.sig_x != 0) h = cmul(h, a.shx[c]);
+    a.fringe[(size_t)yl * a.pnx + c] = h.x;
+    if (a.field) a.field[(size_t)yl * a.pnx + c] = h;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+
+struct Levels {
+  double dstep;
+  std::vector<double> dlevel;     // num_of_depth entries
+  std::vector<double> ztrans;     // z' per level
+  int16_t lut[256];               // depth byte -> level index dtr (1-based), 0 = none
+};
+
+// GetDepthValues (HologramGenerator.cpp:391-408) with the per-pixel binning
+// of change_depth_quan_* evaluated once per depth byte.  The level list is
+// built by repeated addition while val <= far, as the reference does; when
+// rounding stops it one level short of num_of_depth the addition continues
+// (the reference would read past the end of dlevel_ there).
+static oh_status compute_levels(const oh_depthmap_params* p, Levels* L) {
+  const double nearv = std::min(p->near_depthmap, p->far_depthmap);
+  const double farv = std::max(p->near_depthmap, p->far_depthmap);
+  const int nd = p->num_of_depth;
+  L->dlevel.clear();
+  if (nd > 1) {
+    L->dstep = (farv - nearv) / (nd - 1);
+    double val = nearv;
+    while (val <= farv && (int)L->dlevel.size() < nd) { L->dlevel.push_back(val); val += L->dstep; }
+    while ((int)L->dlevel.size() < nd) { L->dlevel.push_back(val); val += L->dstep; }
+  } else {
+    L->dstep = (farv + nearv) / 2;
+    L->dlevel.push_back(farv - nearv);
+  }
+  L->ztrans.resize(nd);
+  for (int i = 0; i < nd; ++i) {
+    const double d = L->dlevel[i];
+    L->ztrans[i] = p->transform_viewing_window ? -p->field_lens * d / (d - p->field_lens) : d;
+  }
+  for (int b = 0; b < 256; ++b) {
+    long idx;
+    if (p->flag_change_depth_quantization == 1) {
+      const double dmap_src = double(b) / 255.0;
+      const double dmap = (1.0 - dmap_src) * (farv - nearv) + nearv;
+      idx = 0;
+      for (int dtr = 0; dtr < nd; ++dtr) {
+        const double t = L->dlevel[dtr];
+        const double d1 = t - L->dstep / 2.0;
+        const double d2 = t + L->dstep / 2.0;
+        int hit;
+        if (dtr < nd - 1) hit = (dmap >= d1 ? 1 : 0) * (dmap < d2 ? 1 : 0);
+        else hit = (dmap >= d1 ? 1 : 0) * (dmap <= d2 ? 1 : 0);
+        idx += (long)hit * (dtr + 1);
+      }
+    } else {
+      idx = (long)p->default_depth_quantization - b;
+    }
+    L->lut[b] = (idx >= 1 && idx <= 32767) ? (int16_t)idx : (int16_t)0;
+  }
+  return OH_OK;
+}
+
+static oh_status validate(const oh_depthmap_params* p) {
+  if (!p) return fail(OH_ERR_INVALID_ARG, "null depth-map params");
+  if (p->pnx < 1 || p->pny < 1) return fail(OH_ERR_INVALID_ARG, "pnx/pny must be positive");
+  if (p->pad != 1 && p->pad != 2) return fail(OH_ERR_INVALID_ARG, "pad must be 1 or 2");
+  if (!(p->ppx > 0) || !(p->ppy > 0) || !(p->lambda > 0)) return fail(OH_ERR_INVALID_ARG, "pitch and wavelength must be positive");
+  if (p->num_of_depth < 1 || p->num_of_depth > 4096) return fail(OH_ERR_INVALID_ARG, "num_of_depth out of range");
+  if (p->phase_mode < 0 || p->phase_mode > 2) return fail(OH_ERR_INVALID_ARG, "bad phase_mode");
+  if (p->sig_location_x < -1 || p->sig_location_x > 1 || p->sig_location_y < -1 || p->sig_location_y > 1)
+    return fail(OH_ERR_INVALID_ARG, "sig_location components must be -1, 0 or 1");
+  if (p->render_depth && p->n_render_depth < 1) return fail(OH_ERR_INVALID_ARG, "empty render_depth list");
+  return OH_OK;
+}
+
+template <typename R, int KMAX>
+static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const uint8_t* img,
+                              const uint8_t* depth, const float* phase, void* fringe, void* field,
+                              void* spectrum, cudaStream_t st) {
+  typedef typename cplx_of<R>::type C;
+  const int prec = sizeof(R) == 8 ? 1 : 0;
+  Levels L;
+  OH_TRY(compute_levels(p, &L));
+  const int nd = p->num_of_depth;
+  std::vector<int> render;
+  if (p->render_depth) render.assign(p->render_depth, p->render_depth + p->n_render_depth);
+  else for (int i = 1; i <= nd; ++i) render.push_back(i);
+  if ((int)render.size() > kMaxEntries) return fail(OH_ERR_INVALID_ARG, "more than 256 render_depth entries");
+  for (int d : render) if (d < 1 || d > nd) return fail(OH_ERR_INVALID_ARG, "render_depth entry outside 1..num_of_depth");
+
+  DMSetup su;
+  std::memset(&su, 0, sizeof(su));
+  std::vector<int> udtr;              // unique level numbers in first-seen order
+  std::vector<int> uslot_of_dtr(nd + 1, -1);
+  for (size_t e = 0; e < render.size(); ++e) {
+    int d = render[e];
+    if (uslot_of_dtr[d] < 0) { uslot_of_dtr[d] = (int)udtr.size(); udtr.push_back(d); }
+    su.uslot_of_entry[e] = (int16_t)uslot_of_dtr[d];
+    const double z = L.ztrans[d - 1];
+    su.zp[e] = z;
+    const double k = 2.0 * M_PI / p->lambda;
+    // rand_phase * carrier exp(i k z') (HologramGenerator_GPU.cpp:267-273)
+    double rre = 1.0, rim = 0.0;
+    if (p->phase_mode == OH_PHASE_REFERENCE) { rre = p->rand_phase_re; rim = p->rand_phase_im; }
+    double cre = std::cos(k * z), cim = std::sin(k * z);
+    double are = rre * cre - rim * cim, aim = rre * cim + rim * cre;
+    if (prec == 0) {
+      // fp32 path folds the constant exp(-i k z') of H into the entry constant
+      double hre = std::cos(-k * z), him = std::sin(-k * z);
+      double bre = are * hre - aim * him, bim = are * him + aim * hre;
+      are = bre; aim = bim;
+    }
+    su.cre[e] = are; su.cim[e] = aim;
+  }
+  su.n_entries = (int)render.size();
+  su.n_uslots = (int)udtr.size();
+  for (int b = 0; b < 256; ++b) {
+    int d = L.lut[b];
+    su.lut[b] = (d >= 1 && d <= nd) ? (int16_t)uslot_of_dtr[d] : (int16_t)-1;
+  }
+
+  DMArgs<R> a;
+  std::memset(&a, 0, sizeof(a));
+  a.pnx = p->pnx; a.pny = p->pny;
+  a.Px = p->pad * p->pnx; a.Py = p->pad * p->pny;
+  a.ox = (a.Px - a.pnx) / 2; a.oy = (a.Py - a.pny) / 2;
+  a.hx = a.Px / 2; a.hy = a.Py / 2;
+  a.n_entries = su.n_entries; a.n_uslots = su.n_uslots;
+  a.ppx = p->ppx; a.ppy = p->ppy;
+  a.ssx = p->ppx * a.Px; a.ssy = p->ppy * a.Py;
+  a.lambda = p->lambda; a.k = 2.0 * M_PI / p->lambda;
+  a.img = img; a.depth = depth; a.phase = phase;
+  a.phase_mode = p->phase_mode; a.seed = p->seed;
+  a.sig_x = p->sig_location_x; a.sig_y = p->sig_location_y;
+  // Encoding_Symmetrization crop window (HologramGenerator.cpp:486-514), on the padded grid
+  {
+    int cropx1, cropx2, cropy1, cropy2;
+    if (p->sig_location_y == 0) { cropy1 = 1; cropy2 = a.Py; }
+    else { int cropy = a.Py / 2; cropy1 = cropy - cropy / 2; cropy2 = cropy1 + cropy - 1; }
+    if (p->sig_location_x == 0) { cropx1 = 1; cropx2 = a.Px; }
+    else { int cropx = a.Px / 2; cropx1 = cropx - cropx / 2; cropx2 = cropx1 + cropx - 1; }
+    a.cx1 = cropx1 - 1; a.cx2 = cropx2 - 1; a.cy1 = cropy1 - 1; a.cy2 = cropy2 - 1;
+  }
+  OH_TRY(get_plan(ctx, a.Px, prec, &a.plx));
+  OH_TRY(get_plan(ctx, a.Py, prec, &a.ply));
+
+  const size_t smax = max_smem_per_block();
+  const int T = 512;
+  int W = 0;
+  for (int cand : {8, 4, 2, 1}) {
+    if (a.Px % cand) continue;
+    size_t sm = (size_t)cand * a.Py * sizeof(C) + cand * (sizeof(C) + sizeof(R)) + (size_t)a.Py * sizeof(int);
+    if (sm <= smax && cand * a.Py <= T * KMAX) { W = cand; break; }
+  }
+  if (W == 0) return fail(OH_ERR_UNSUPPORTED_SIZE, "padded column length " + std::to_string(a.Py) + " too long for the column pass");
+  a.W = W; a.nstrips = a.Px / W;
+  const size_t smem_col = (size_t)W * a.Py * sizeof(C) + W * (sizeof(C) + sizeof(R)) + (size_t)a.Py * sizeof(int);
+  const size_t smem_row = (size_t)a.Px * sizeof(C) + (size_t)a.pnx * sizeof(C) + (size_t)((a.pnx + 1) & ~1) * sizeof(int16_t) +
+                          (size_t)((su.n_uslots + 31) / 32) * sizeof(uint32_t);
+  const size_t smem_out = (size_t)a.Px * sizeof(C);
+  if (smem_row > smax || smem_out > smax) return fail(OH_ERR_UNSUPPORTED_SIZE, "padded row length " + std::to_string(a.Px) + " exceeds shared memory");
+
+  // scratch
+  void* ptr;
+  const size_t nE = su.n_entries, nU = su.n_uslots;
+  OH_TRY(scratch(ctx, "dm.R", nU * a.pny * (size_t)a.Px * sizeof(C), &ptr)); a.Rbuf = (C*)ptr;
+  OH_TRY(scratch(ctx, "dm.V", (size_t)a.pny * a.Px * sizeof(C), &ptr)); a.V = (C*)ptr;
+  OH_TRY(scratch(ctx, "dm.occ", nU * a.pny + 16, &ptr)); a.occ = (uint8_t*)ptr;
+  // small tables share one buffer
+  size_t off = 0;
+  auto carve = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; };
+  size_t o_lut = carve(256 * sizeof(int16_t)), o_use = carve(nE * sizeof(int16_t)), o_kz = carve(nE * sizeof(R)),
+         o_cst = carve(nE * sizeof(C)), o_exc = carve(prec ? 0 : nE * a.Px * sizeof(C)),
+         o_ey = carve(prec ? 0 : nE * a.Py * sizeof(C)), o_lfx = carve(a.Px * sizeof(R)), o_lfy = carve(a.Py * sizeof(R)),
+         o_shy = carve(a.pny * sizeof(C)), o_shx = carve(a.pnx * sizeof(C)), o_any = carve(nU * sizeof(int));
+  OH_TRY(scratch(ctx, "dm.tables", off, &ptr));
+  char* base = (char*)ptr;
+  a.lut = (int16_t*)(base + o_lut); a.uslot_of_entry = (int16_t*)(base + o_use); a.kzp = (R*)(base + o_kz);
+  a.cst = (C*)(base + o_cst); a.exc = (C*)(base + o_exc); a.ey = (C*)(base + o_ey);
+  a.lfx = (R*)(base + o_lfx); a.lfy = (R*)(base + o_lfy); a.shy = (C*)(base + o_shy); a.shx = (C*)(base + o_shx);
+  a.slot_any = (int*)(base + o_any);
+  a.fringe = (R*)fringe; a.field = (C*)field; a.spectrum = (C*)spectrum;
+
+  OH_CUDA_TRY(cudaFuncSetAttribute(dm_row_pass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_row));
+  OH_CUDA_TRY(cudaFuncSetAttribute(dm_col_pass<R, KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col));
+  OH_CUDA_TRY(cudaFuncSetAttribute(dm_out_pass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_out));
+  {
+    KernelTimer kt(ctx, prec ? "dm_setup_f64" : "dm_setup", st);
+    dm_setup<R><<<64, 256, 0, st>>>(a, su);
+    OH_LAUNCH_CHECK();
+  }
+  {
+    KernelTimer kt(ctx, prec ? "dm_row_pass_f64" : "dm_row_pass", st);
+    dm_row_pass<R><<<a.pny, 256, smem_row, st>>>(a);
+    OH_LAUNCH_CHECK();
+  }
+  {
+    KernelTimer kt(ctx, prec ? "dm_col_pass_f64" : "dm_col_pass", st);
+    dm_col_pass<R, KMAX><<<a.nstrips, T, smem_col, st>>>(a);
+    OH_LAUNCH_CHECK();
+  }
+  {
+    KernelTimer kt(ctx, prec ? "dm_out_pass_f64" : "dm_out_pass", st);
+    dm_out_pass<R><<<a.pny, 256, smem_out, st>>>(a);
+    OH_LAUNCH_CHECK();
+  }
+  return OH_OK;
+}
+
+}  // namespace oh
+
+using namespace oh;
+
+extern "C" {
+
+void oh_depthmap_params_default(oh_depthmap_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->pnx = 1920; p->pny = 1080;
+  p->ppx = 8e-6; p->ppy = 8e-6;
+  p->lambda = 532e-9;
+  p->field_lens = 1000e-3;
+  p->near_depthmap = 0.30; p->far_depthmap = 0.35;
+  p->num_of_depth = 32;
+  p->flag_change_depth_quantization = 1;
+  p->default_depth_quantization = 256;
+  p->transform_viewing_window = 0;
+  p->pad = 2;
+  p->sig_location_x = 0; p->sig_location_y = 1;
+  p->phase_mode = OH_PHASE_REFERENCE;
+  p->seed = 0;
+  p->rand_phase_re = 1.0; p->rand_phase_im = 0.0;
+  p->render_depth = nullptr; p->n_render_depth = 0;
+}
+
+oh_status oh_depthmap_levels(const oh_depthmap_params* p, int16_t lut_out[256], double* z_out) {
+  OH_TRY(validate(p));
+  Levels L;
+  OH_TRY(compute_levels(p, &L));
+  if (lut_out) std::memcpy(lut_out, L.lut, sizeof(L.lut));
+  if (z_out) for (int i = 0; i < p->num_of_depth; ++i) z_out[i] = L.ztrans[i];
+  return OH_OK;
+}
+
+oh_status oh_depthmap_generate(oh_ctx* ctx, oh_precision prec, const oh_depthmap_params* p,
+                               const uint8_t* img, const uint8_t* depth, const float* phase,
+                               void* fringe_out, void* field_out, void* spectrum_out, void* stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  CallScope cs(ctx, st);
+  OH_TRY(cs.status());
+  OH_TRY(validate(p));
+  if (!img || !depth || !fringe_out) return fail(OH_ERR_INVALID_ARG, "img, depth and fringe_out are required");
+  if (p->phase_mode == OH_PHASE_ARRAY && !phase) return fail(OH_ERR_INVALID_ARG, "OH_PHASE_ARRAY needs a phase array");
+  if (prec == OH_FP64) return run_depthmap<double, 18>(ctx, p, img, depth, phase, fringe_out, field_out, spectrum_out, st);
+  return run_depthmap<float, 36>(ctx, p, img, depth, phase, fringe_out, field_out, spectrum_out, st);
+}
+
+oh_status oh_depthmap_generate_host(oh_ctx* ctx, oh_precision prec, const oh_depthmap_params* p,
+                                    const uint8_t* img_host, const uint8_t* depth_host,
+                                    const float* phase_host, void* fringe_host, void* stream) {
+  OH_TRY(validate(p));
+  if (!ctx || !img_host || !depth_host || !fringe_host) return fail(OH_ERR_INVALID_ARG, "null argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t n = (size_t)p->pnx * p->pny;
+  const size_t fsz = n * (prec == OH_FP64 ? sizeof(double) : sizeof(float));
+  void* dev;
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    int prev = 0; cudaGetDevice(&prev); cudaSetDevice(ctx->device);
+    oh_status s = scratch(ctx, "host.io", 2 * n + (phase_host ? 4 * n : 0) + fsz + 1024, &dev);
+    cudaSetDevice(prev);
+    if (s != OH_OK) return s;
+  }
+  uint8_t* d_img = (uint8_t*)dev;
+  uint8_t* d_depth = d_img + n;
+  size_t off = (2 * n + 255) & ~(size_t)255;
+  float* d_phase = phase_host ? (float*)((char*)dev + off) : nullptr;
+  if (phase_host) off += (4 * n + 255) & ~(size_t)255;
+  void* d_fringe = (char*)dev + off;
+  OH_CUDA_TRY(cudaMemcpyAsync(d_img, img_host, n, cudaMemcpyHostToDevice, st));
+  OH_CUDA_TRY(cudaMemcpyAsync(d_depth, depth_host, n, cudaMemcpyHostToDevice, st));
+  if (phase_host) OH_CUDA_TRY(cudaMemcpyAsync(d_phase, phase_host, 4 * n, cudaMemcpyHostToDevice, st));
+  OH_TRY(oh_depthmap_generate(ctx, prec, p, d_img, d_depth, d_phase, d_fringe, nullptr, nullptr, stream));
+  OH_CUDA_TRY(cudaMemcpyAsync(fringe_host, d_fringe, fsz, cudaMemcpyDeviceToHost, st));
+  OH_CUDA_TRY(cudaStreamSynchronize(st));
+  return OH_OK;
+}
+
+}  // extern "C"

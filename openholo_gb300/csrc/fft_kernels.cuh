@@ -1,0 +1,28 @@
+// Internal entry points shared between translation units.
+#pragma once
+#include "context.h"
+
+namespace oh {
+
+// Enqueue out = [shift] FFT2 [shift] (in), optional aux = unshifted transform.
+oh_status fft2d_enqueue(oh_ctx* ctx, int prec, int nx, int ny, const void* in, void* out, void* aux,
+                        int direction, int shift, int normalize, cudaStream_t st);
+
+// Widest column strip (8, 4, 2 or 1 columns) dividing nx whose ny-long
+// complex lines fit in smax bytes of shared memory; 0 if none fits.
+int pick_strip_width(int nx, int ny, size_t esz, size_t smax);
+
+// SplitMix64 finaliser on a counter: the per-pixel random phase generator
+// shared by the seeded depth-map mode and the synthetic scene generators.
+__host__ __device__ __forceinline__ uint64_t splitmix64_at(uint64_t seed, uint64_t idx) {
+  uint64_t z = seed + (idx + 1ull) * 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+// u in [0,1) with 24 random bits (exact in float)
+__host__ __device__ __forceinline__ float u24_at(uint64_t seed, uint64_t idx) {
+  return (float)(splitmix64_at(seed, idx) >> 40) * (1.0f / 16777216.0f);
+}
+
+}  // namespace oh

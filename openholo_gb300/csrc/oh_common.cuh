@@ -1,0 +1,61 @@
+// Shared device/host helpers: complex arithmetic on float2/double2, error
+// plumbing and the launch counter.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include "../../include/oh.h"
+
+namespace oh {
+
+template <typename R> struct cplx_of;
+template <> struct cplx_of<float>  { typedef float2  type; };
+template <> struct cplx_of<double> { typedef double2 type; };
+
+__host__ __device__ __forceinline__ float2  mk(float x, float y)   { return make_float2(x, y); }
+__host__ __device__ __forceinline__ double2 mk(double x, double y) { return make_double2(x, y); }
+
+template <typename C> __host__ __device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C> __host__ __device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b) {
+  C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+}
+// a * conj(b)
+template <typename C> __host__ __device__ __forceinline__ C cmulc(C a, C b) {
+  C r; r.x = a.x * b.x + a.y * b.y; r.y = a.y * b.x - a.x * b.y; return r;
+}
+template <typename C, typename R> __host__ __device__ __forceinline__ C cscale(C a, R s) { C r; r.x = a.x * s; r.y = a.y * s; return r; }
+// multiply by -i (forward) or +i (inverse): sgn = -1 -> -i*a, sgn = +1 -> i*a
+template <int SGN, typename C> __host__ __device__ __forceinline__ C cmul_i(C a) {
+  C r; if (SGN < 0) { r.x = a.y; r.y = -a.x; } else { r.x = -a.y; r.y = a.x; } return r;
+}
+
+// Launch accounting (read through oh_kernel_launch_count()).
+void note_launch(int n = 1);
+
+// Per-thread last-error message.
+void set_error(const std::string& msg);
+oh_status fail(oh_status s, const std::string& msg);
+oh_status cuda_fail(cudaError_t e, const char* what);
+
+}  // namespace oh
+
+#define OH_CUDA_TRY(expr)                                  \
+  do {                                                     \
+    cudaError_t _e = (expr);                               \
+    if (_e != cudaSuccess) return ::oh::cuda_fail(_e, #expr); \
+  } while (0)
+
+#define OH_TRY(expr)                     \
+  do {                                   \
+    oh_status _s = (expr);               \
+    if (_s != OH_OK) return _s;          \
+  } while (0)
+
+// Check the launch that was just enqueued.
+#define OH_LAUNCH_CHECK()                                      \
+  do {                                                         \
+    ::oh::note_launch();                                       \
+    cudaError_t _e = cudaGetLastError();                       \
+    if (_e != cudaSuccess) return ::oh::cuda_fail(_e, "kernel launch"); \
+  } while (0)

@@ -1,0 +1,254 @@
+// Point-cloud hologram: sum over points of a_j exp(i phi_j) per SLM pixel,
+//   phi_j = k r_j - k X sin(tx) - k Y sin(ty),  r_j = |(X,Y,0) - (x_j,y_j,z_j)|
+// with the KETI geometry of ophGenCghPointCloud (ophgen_pointcloud.cpp:195-249)
+// and ophKernelCghPointCloud_cuda (ophgen_pointcloud_gpu.cpp:391-416):
+//   X = (col + 0.5) px - Nx px / 2,  Y = Ny py / 2 - (row + 0.5) py,
+//   x_j = x sx, y_j = y sy, z_j = z sz + offsetDepth.
+// The KETI fringe is Re of the same sum, accumulated into the caller's
+// buffer (dst += ...).
+//
+// FP32 path: k r_j is ~1e6 rad, far beyond float resolution, so the phase is
+// split exactly as
+//   k r = [k (X-x)^2/(2z) - k X sin tx]  +  [k z + k (Y-y)^2/(2z) - k Y sin ty]
+//         - k z t^2 / (2 (1 + sqrt(1+t))^2),          t = ((X-x)^2+(Y-y)^2)/z^2
+// The two bracketed terms are per-(point, column) and per-(point, row)
+// tables computed in FP64 and reduced mod 2 pi before rounding to float; the
+// last term is a cancellation-free form of k z (sqrt(1+t) - 1 - t/2) and is
+// evaluated in FP32 per term (it is at most a few rad for paraxial scenes).
+// FP64 path: the direct formula in double precision.
+#include <cmath>
+#include <vector>
+#include "context.h"
+#include "fft_kernels.cuh"
+
+namespace oh {
+
+struct PCGeom {
+  double k, px, py, hlx, hly, sx, sy, sz, off, stx, sty;
+  int nx, ny;
+};
+
+constexpr int kPcChunk = 32768;    // points per table chunk
+constexpr int kPcTX = 32, kPcTY = 8, kPcPts = 64;
+
+// Per point: x_j, y_j, 1/z^2, -k z/2 (fp32) and the FP64-reduced tables.
+__global__ void pc_tables(PCGeom g, const float4* __restrict__ pts, int n, float4* __restrict__ prm,
+                          float* __restrict__ A, float* __restrict__ B) {
+  const double two_pi = 6.283185307179586476925286766559;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nthr = gridDim.x * blockDim.x;
+  for (int j = tid; j < n; j += nthr) {
+    float4 p = pts[j];
+    double x = (double)p.x * g.sx, y = (double)p.y * g.sy, z = (double)p.z * g.sz + g.off;
+    prm[j] = make_float4((float)x, (float)y, (float)(1.0 / (z * z)), (float)(-0.5 * g.k * z));
+  }
+  for (long long idx = tid; idx < (long long)n * g.nx; idx += nthr) {
+    int j = (int)(idx / g.nx), c = (int)(idx - (long long)j * g.nx);
+    float4 p = pts[j];
+    double x = (double)p.x * g.sx, z = (double)p.z * g.sz + g.off;
+    double X = ((double)c + 0.5) * g.px - g.hlx;
+    double dx = X - x;
+    double ph = g.k * dx * dx / (2.0 * z) - g.k * X * g.stx;
+    ph -= two_pi * rint(ph / two_pi);
+    A[idx] = (float)ph;
+  }
+  for (long long idx = tid; idx < (long long)n * g.ny; idx += nthr) {
+    int j = (int)(idx / g.ny), r = (int)(idx - (long long)j * g.ny);
+    float4 p = pts[j];
+    double y = (double)p.y * g.sy, z = (double)p.z * g.sz + g.off;
+    double Y = g.hly - ((double)r + 0.5) * g.py;
+    double dy = Y - y;
+    double kz = g.k * z;
+    double ph = (kz - two_pi * rint(kz / two_pi)) + g.k * dy * dy / (2.0 * z) - g.k * Y * g.sty;
+    ph -= two_pi * rint(ph / two_pi);
+    B[idx] = (float)ph;
+  }
+}
+
+// One thread per pixel of a 32x8 tile; points streamed through shared memory.
+__global__ void __launch_bounds__(kPcTX * kPcTY) pc_direct_f32(PCGeom g, const float4* __restrict__ pts,
+                                                              const float4* __restrict__ prm,
+                                                              const float* __restrict__ A, const float* __restrict__ B,
+                                                              int n, float2* __restrict__ field,
+                                                              float* __restrict__ fringe, int accumulate_field) {
+  __shared__ float sA[kPcPts][kPcTX];
+  __shared__ float sB[kPcPts][kPcTY];
+  __shared__ float4 sP[kPcPts];
+  __shared__ float sAmp[kPcPts];
+  const int tx = threadIdx.x % kPcTX, ty = threadIdx.x / kPcTX;
+  const int col = blockIdx.x * kPcTX + tx, row = blockIdx.y * kPcTY + ty;
+  const float X = (float)(((double)col + 0.5) * g.px - g.hlx);
+  const float Y = (float)(g.hly - ((double)row + 0.5) * g.py);
+  const float inv2pi = 0.15915494309189533577f, two_pi = 6.28318530717958647692f;
+  float re = 0.f, im = 0.f;
+  for (int j0 = 0; j0 < n; j0 += kPcPts) {
+    const int cnt = min(kPcPts, n - j0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < cnt * kPcTX; i += blockDim.x) {
+      int j = i / kPcTX, c = i - j * kPcTX;
+      int cc = blockIdx.x * kPcTX + c;
+      sA[j][c] = cc < g.nx ? A[(size_t)(j0 + j) * g.nx + cc] : 0.f;
+    }
+    for (int i = threadIdx.x; i < cnt * kPcTY; i += blockDim.x) {
+      int j = i / kPcTY, r = i - j * kPcTY;
+      int rr = blockIdx.y * kPcTY + r;
+      sB[j][r] = rr < g.ny ? B[(size_t)(j0 + j) * g.ny + rr] : 0.f;
+    }
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) { sP[i] = prm[j0 + i]; sAmp[i] = pts[j0 + i].w; }
+    __syncthreads();
+#pragma unroll 4
+    for (int j = 0; j < cnt; ++j) {
+      const float4 p = sP[j];
+      const float dx = X - p.x, dy = Y - p.y;
+      const float t = fmaf(dx, dx, dy * dy) * p.z;
+      const float s = sqrtf(1.f + t);
+      const float q = __fdividef(t, 1.f + s);
+      float ph = sA[j][tx] + sB[j][ty] + p.w * q * q;
+      ph = fmaf(-two_pi, rintf(ph * inv2pi), ph);
+      float sn, cs;
+      __sincosf(ph, &sn, &cs);
+      const float a = sAmp[j];
+      re = fmaf(a, cs, re);
+      im = fmaf(a, sn, im);
+    }
+  }
+  if (col < g.nx && row < g.ny) {
+    const size_t o = (size_t)row * g.nx + col;
+    if (field) {
+      if (accumulate_field) { float2 f = field[o]; field[o] = make_float2(f.x + re, f.y + im); }
+      else field[o] = make_float2(re, im);
+    }
+    if (fringe) fringe[o] += re;
+  }
+}
+
+__global__ void __launch_bounds__(256) pc_direct_f64(PCGeom g, const float4* __restrict__ pts, int n,
+                                                    double2* __restrict__ field, double* __restrict__ fringe) {
+  __shared__ double4 sP[kPcPts];
+  const int tx = threadIdx.x % kPcTX, ty = threadIdx.x / kPcTX;
+  const int col = blockIdx.x * kPcTX + tx, row = blockIdx.y * kPcTY + ty;
+  const double X = ((double)col + 0.5) * g.px - g.hlx;
+  const double Y = g.hly - ((double)row + 0.5) * g.py;
+  const double ref = g.k * X * g.stx + g.k * Y * g.sty;
+  double re = 0.0, im = 0.0;
+  for (int j0 = 0; j0 < n; j0 += kPcPts) {
+    const int cnt = min(kPcPts, n - j0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+      float4 p = pts[j0 + i];
+      sP[i] = make_double4((double)p.x * g.sx, (double)p.y * g.sy, (double)p.z * g.sz + g.off, (double)p.w);
+    }
+    __syncthreads();
+    for (int j = 0; j < cnt; ++j) {
+      const double4 p = sP[j];
+      const double dx = X - p.x, dy = Y - p.y;
+      const double r = sqrt(dx * dx + dy * dy + p.z * p.z);
+      double sn, cs;
+      sincos(g.k * r - ref, &sn, &cs);
+      re += p.w * cs;
+      im += p.w * sn;
+    }
+  }
+  if (col < g.nx && row < g.ny) {
+    const size_t o = (size_t)row * g.nx + col;
+    if (field) field[o] = make_double2(re, im);
+    if (fringe) fringe[o] += re;
+  }
+}
+
+static oh_status validate_pc(const oh_pc_params* p, int n) {
+  if (!p) return fail(OH_ERR_INVALID_ARG, "null point-cloud params");
+  if (p->nx < 1 || p->ny < 1) return fail(OH_ERR_INVALID_ARG, "nx/ny must be positive");
+  if (n < 0) return fail(OH_ERR_INVALID_ARG, "negative point count");
+  if (!(p->lambda > 0) || !(p->pitch_x > 0) || !(p->pitch_y > 0)) return fail(OH_ERR_INVALID_ARG, "pitch and wavelength must be positive");
+  return OH_OK;
+}
+
+static PCGeom make_geom(const oh_pc_params* p) {
+  PCGeom g;
+  g.k = 2.0 * M_PI / p->lambda;
+  g.px = p->pitch_x; g.py = p->pitch_y;
+  g.hlx = p->pitch_x * p->nx / 2.0; g.hly = p->pitch_y * p->ny / 2.0;
+  g.sx = p->scale_x; g.sy = p->scale_y; g.sz = p->scale_z; g.off = p->offset_depth;
+  g.stx = std::sin(p->tilt_x_deg * M_PI / 180.0);
+  g.sty = std::sin(p->tilt_y_deg * M_PI / 180.0);
+  g.nx = p->nx; g.ny = p->ny;
+  return g;
+}
+
+oh_status pointcloud_enqueue(oh_ctx* ctx, int prec, const oh_pc_params* p, const float* xyza, int n,
+                             void* field, void* fringe, cudaStream_t st) {
+  PCGeom g = make_geom(p);
+  dim3 grid((p->nx + kPcTX - 1) / kPcTX, (p->ny + kPcTY - 1) / kPcTY);
+  const float4* pts = reinterpret_cast<const float4*>(xyza);
+  if (n == 0) {
+    if (field) OH_CUDA_TRY(cudaMemsetAsync(field, 0, (size_t)p->nx * p->ny * (prec ? 16 : 8), st));
+    return OH_OK;
+  }
+  if (prec) {
+    pc_direct_f64<<<grid, kPcTX * kPcTY, 0, st>>>(g, pts, n, (double2*)field, (double*)fringe);
+    OH_LAUNCH_CHECK();
+    return OH_OK;
+  }
+  const int chunk = std::min(n, kPcChunk);
+  void* ptr;
+  OH_TRY(scratch(ctx, "pc.tables", (size_t)chunk * (sizeof(float4) + sizeof(float) * (p->nx + p->ny)) + 1024, &ptr));
+  float4* prm = (float4*)ptr;
+  float* A = (float*)(prm + chunk);
+  float* B = A + (size_t)chunk * p->nx;
+  for (int j0 = 0; j0 < n; j0 += chunk) {
+    const int cnt = std::min(chunk, n - j0);
+    pc_tables<<<1024, 256, 0, st>>>(g, pts + j0, cnt, prm, A, B);
+    OH_LAUNCH_CHECK();
+    pc_direct_f32<<<grid, kPcTX * kPcTY, 0, st>>>(g, pts + j0, prm, A, B, cnt, (float2*)field, (float*)fringe, j0 > 0);
+    OH_LAUNCH_CHECK();
+  }
+  return OH_OK;
+}
+
+}  // namespace oh
+
+using namespace oh;
+
+extern "C" {
+
+oh_status oh_pointcloud(oh_ctx* ctx, oh_precision prec, const oh_pc_params* p, const float* xyza, int n_points,
+                        void* field_out, void* fringe_out, void* stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  CallScope cs(ctx, st);
+  OH_TRY(cs.status());
+  OH_TRY(validate_pc(p, n_points));
+  if (!field_out && !fringe_out) return fail(OH_ERR_INVALID_ARG, "need field_out or fringe_out");
+  if (n_points > 0 && !xyza) return fail(OH_ERR_INVALID_ARG, "null points");
+  return pointcloud_enqueue(ctx, prec == OH_FP64 ? 1 : 0, p, xyza, n_points, field_out, fringe_out, st);
+}
+
+oh_status oh_pointcloud_host(oh_ctx* ctx, oh_precision prec, const oh_pc_params* p, const float* xyza_host,
+                             int n_points, void* field_host, void* fringe_host, void* stream) {
+  OH_TRY(validate_pc(p, n_points));
+  if (!ctx) return fail(OH_ERR_INVALID_ARG, "null context");
+  if (!field_host && !fringe_host) return fail(OH_ERR_INVALID_ARG, "need field_host or fringe_host");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  CallScope cs(ctx, st);
+  OH_TRY(cs.status());
+  const size_t npx = (size_t)p->nx * p->ny;
+  const size_t es = prec == OH_FP64 ? 8 : 4;
+  const size_t pbytes = (size_t)std::max(n_points, 1) * 16;
+  void* ptr;
+  OH_TRY(scratch(ctx, "host.pc", pbytes + npx * es * 3 + 1024, &ptr));
+  char* base = (char*)ptr;
+  float* d_pts = (float*)base;
+  size_t off = (pbytes + 255) & ~(size_t)255;
+  void* d_field = field_host ? base + off : nullptr;
+  if (field_host) off += (npx * es * 2 + 255) & ~(size_t)255;
+  void* d_fringe = fringe_host ? base + off : nullptr;
+  if (n_points > 0) OH_CUDA_TRY(cudaMemcpyAsync(d_pts, xyza_host, (size_t)n_points * 16, cudaMemcpyHostToDevice, st));
+  if (d_fringe) OH_CUDA_TRY(cudaMemcpyAsync(d_fringe, fringe_host, npx * es, cudaMemcpyHostToDevice, st));
+  OH_TRY(pointcloud_enqueue(ctx, prec == OH_FP64 ? 1 : 0, p, d_pts, n_points, d_field, d_fringe, st));
+  if (d_field) OH_CUDA_TRY(cudaMemcpyAsync(field_host, d_field, npx * es * 2, cudaMemcpyDeviceToHost, st));
+  if (d_fringe) OH_CUDA_TRY(cudaMemcpyAsync(fringe_host, d_fringe, npx * es, cudaMemcpyDeviceToHost, st));
+  OH_CUDA_TRY(cudaStreamSynchronize(st));
+  return OH_OK;
+}
+
+}  // extern "C"

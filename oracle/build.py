@@ -1,0 +1,67 @@
+"""Build recipe for the oracle — TEST INFRASTRUCTURE ONLY.
+
+build_oracle():    oracle/pointcloud.c -> oracle/_build/liboracle.so (gcc, -O2,
+                   -ffp-contract=off so float results match the reference's
+                   operation order exactly).
+build_reference(): when the reference tree is present, compiles the
+                   reference's own point-cloud library source where it lies
+                   (OpenHolo_KETI/.../ophgen_pointcloud/ophgen_pointcloud.cpp)
+                   together with oracle/keti_ref_harness.cpp into
+                   oracle/_ref/libketi_ref.so (sequential; the reference's
+                   OpenMP loop races on its output) and
+                   oracle/_ref/libketi_ref_omp.so (-fopenmp, timing only).
+                   Nothing is copied out of the reference tree.  The depth-map
+                   and WRP sources need Qt, FFTW or the closed CWO DLL and are
+                   not built.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+REF_OUT = HERE / "_ref"
+REFERENCE_ROOT = Path(os.environ.get("OH_REFERENCE_ROOT", "/root/reference"))
+KETI_DIR = REFERENCE_ROOT / "OpenHolo_KETI/VS/Openholo_Generation_PointCloud_Library_beta_v1.0/ophgen_pointcloud"
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"{' '.join(map(str, cmd))}\n{r.stdout}\n{r.stderr}")
+
+
+def _fresh(out: Path, deps) -> bool:
+    return out.exists() and all(out.stat().st_mtime >= Path(d).stat().st_mtime for d in deps)
+
+
+def build_oracle() -> Path:
+    BUILD.mkdir(exist_ok=True)
+    out = BUILD / "liboracle.so"
+    src = HERE / "pointcloud.c"
+    if not _fresh(out, [src]):
+        _run(["gcc", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-o", str(out), str(src), "-lm"])
+    return out
+
+
+def build_reference() -> Path | None:
+    src = KETI_DIR / "ophgen_pointcloud.cpp"
+    if not src.exists():
+        return None
+    REF_OUT.mkdir(exist_ok=True)
+    harness = HERE / "keti_ref_harness.cpp"
+    outs = {"libketi_ref.so": [], "libketi_ref_omp.so": ["-fopenmp"]}
+    for name, extra in outs.items():
+        out = REF_OUT / name
+        if _fresh(out, [src, harness]):
+            continue
+        _run(["g++", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-w", *extra, "-I", str(KETI_DIR),
+              "-o", str(out), str(src), str(harness)])
+    return REF_OUT / "libketi_ref.so"
+
+
+if __name__ == "__main__":
+    print(build_oracle())
+    print(build_reference())

@@ -1,0 +1,39 @@
+"""CPU oracle for Fresnel propagation — TEST INFRASTRUCTURE ONLY.
+
+fresnel_conv: CWO::Diffract(z, CWO_FRESNEL_CONV) structure (WRPC/cwo/src/
+cwo.cpp:2198-2279 zero-pad expand at offset N/2, DiffractConv FRESNEL_CONV
+:2872-2898 FFT * FFT(kernel) -> IFFT -> 1/N, crop), with the impulse response
+written from the mathematics (the DLL bodies are not in the tree):
+h = exp(ikz)/(i lambda z) exp(i pi (x^2+y^2)/(lambda z)) dp^2, origin at
+index 0.  Parity unpinned.
+fresnel_tf: the transfer-function form of FresnelPropagation.m:1-16.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def fresnel_conv(U, dp, lam, z):
+    ny, nx = U.shape
+    NX, NY = 2 * nx, 2 * ny
+    a = np.zeros((NY, NX), np.complex128)
+    a[ny // 2:ny // 2 + ny, nx // 2:nx // 2 + nx] = U
+    jx = np.where(np.arange(NX) < NX // 2, np.arange(NX), np.arange(NX) - NX)
+    jy = np.where(np.arange(NY) < NY // 2, np.arange(NY), np.arange(NY) - NY)
+    x = jx * dp
+    y = jy * dp
+    k = 2 * np.pi / lam
+    h = np.exp(1j * k * z) / (1j * lam * z) * np.exp(1j * np.pi * (x[None, :] ** 2 + y[:, None] ** 2) / (lam * z)) * dp * dp
+    out = np.fft.ifft2(np.fft.fft2(a) * np.fft.fft2(h))
+    return out[ny // 2:ny // 2 + ny, nx // 2:nx // 2 + nx]
+
+
+def fresnel_tf(field, dx, dy, z, lam):
+    k = 2 * np.pi / lam
+    ny, nx = field.shape
+    fx = 1.0 / (nx * dx)
+    fy = 1.0 / (ny * dy)
+    xi = np.concatenate([np.arange(0, (nx - 1) // 2 + 1), np.arange(-((nx + 2) // 2) + 1, 0)]) * fx
+    yi = np.concatenate([np.arange(0, (ny - 1) // 2 + 1), np.arange(-((ny + 2) // 2) + 1, 0)]) * fy
+    H = np.exp(1j * k * z) * np.exp(-1j * np.pi * lam * z * (xi[None, :] ** 2 + yi[:, None] ** 2))
+    return np.fft.ifft2(np.fft.fft2(field) * H)

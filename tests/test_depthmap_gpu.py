@@ -1,0 +1,180 @@
+"""Depth-map CGH on the GPU (through the C ABI) against the CPU oracle.
+
+Tolerances: FP64 mode 1e-7 relative field error (the benchmark spec's bound is
+1e-5); FP32 mode 1e-3 relative (the bound for the fast forms).
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from openholo_gb300 import depthmap as dm
+from openholo_gb300 import scenes
+from openholo_gb300._lib import OhError
+from oracle import depthmap as odm
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-7
+TOL32 = 1e-3
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+
+
+def run(ctx, dev, img, depth, p, phase=None, precision="fp32", want_field=False, want_spec=False):
+    ti = torch.from_numpy(img).to(dev)
+    td = torch.from_numpy(depth).to(dev)
+    tp = torch.from_numpy(phase).to(dev) if phase is not None else None
+    cdt = torch.complex128 if precision == "fp64" else torch.complex64
+    field = torch.empty((p.pny, p.pnx), dtype=cdt, device=dev) if want_field else None
+    spec = torch.empty((p.pny * p.pad, p.pnx * p.pad), dtype=cdt, device=dev) if want_spec else None
+    fr = dm.generate(ctx, p, ti, td, tp, precision=precision, field=field, spectrum=spec)
+    torch.cuda.synchronize()
+    out = [fr.cpu().numpy()]
+    if want_field:
+        out.append(field.cpu().numpy())
+    if want_spec:
+        out.append(spec.cpu().numpy())
+    return out if len(out) > 1 else out[0]
+
+
+def oparams(p, **extra):
+    return odm.DMParams(pnx=p.pnx, pny=p.pny, ppx=p.ppx, ppy=p.ppy, lam=p.lambda_, near=p.near_depthmap,
+                        far=p.far_depthmap, num_of_depth=p.num_of_depth,
+                        flag_change_depth_quantization=p.flag_change_depth_quantization,
+                        transform_viewing_window=p.transform_viewing_window, field_lens=p.field_lens, pad=p.pad,
+                        sig_location=(p.sig_location_x, p.sig_location_y),
+                        rand_phase=complex(p.rand_phase_re, p.rand_phase_im), **extra)
+
+
+@pytest.mark.parametrize("pad", [1, 2])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_depthmap_vs_oracle(ctx, dev, pad, precision):
+    ny, nx, L = 90, 160, 12
+    img, depth = scenes.depthmap_scene(21, ny, nx)
+    phase = scenes.seeded_phase(5, ny, nx)
+    p = dm.make_params(pnx=nx, pny=ny, num_of_depth=L, pad=pad, phase_mode=dm.OH_PHASE_ARRAY)
+    fr, field, spec = run(ctx, dev, img, depth, p, phase, precision, want_field=True, want_spec=True)
+    ref_fr, ref_field, ref_U = odm.generate(img, depth, oparams(p), phase=phase)
+    tol = TOL64 if precision == "fp64" else TOL32
+    assert rel(spec, ref_U) < tol
+    assert rel(field, ref_field) < tol
+    assert rel(fr, ref_fr) < tol
+
+
+def test_reference_mode_matches_oracle(ctx, dev):
+    """pad = 1, constant rand phase, viewing-window transform: the reference's own configuration."""
+    ny, nx, L = 60, 96, 16
+    img, depth = scenes.depthmap_scene(8, ny, nx)
+    p = dm.make_params(pnx=nx, pny=ny, num_of_depth=L, pad=1, near=0.2, far=0.7, transform_viewing_window=1,
+                       field_lens=1.0, rand_phase=complex(math.cos(0.3), math.sin(0.3)), lam=522e-9,
+                       ppx=25.4e-3 / 2250 / 3, ppy=25.4e-3 / 2250)
+    fr = run(ctx, dev, img, depth, p, None, "fp64")
+    ref = odm.generate(img, depth, oparams(p))[0]
+    assert rel(fr, ref) < TOL64
+
+
+def test_seeded_phase_mode(ctx, dev):
+    ny, nx, L = 64, 96, 8
+    img, depth = scenes.depthmap_scene(2, ny, nx)
+    p = dm.make_params(pnx=nx, pny=ny, num_of_depth=L, pad=2, phase_mode=dm.OH_PHASE_SEEDED, seed=1234)
+    fr = run(ctx, dev, img, depth, p, None, "fp32")
+    ref = odm.generate(img, depth, oparams(p), phase=scenes.seeded_phase(1234, ny, nx))[0]
+    assert rel(fr, ref) < TOL32
+
+
+@pytest.mark.parametrize("kw", [
+    dict(num_of_depth=16),                                   # repeated-addition level quirk
+    dict(num_of_depth=256, flag_change_depth_quantization=0),  # 256 - d layer index
+    dict(num_of_depth=8, render_depth=[3, 5, 5, 8]),           # subset with a duplicate level
+    dict(num_of_depth=1),
+    dict(num_of_depth=6, sig_location=(1, 0)),
+    dict(num_of_depth=6, sig_location=(-1, -1)),
+])
+def test_depthmap_edge_configs(ctx, dev, kw):
+    ny, nx = 48, 80
+    img, depth = scenes.depthmap_scene(13, ny, nx)
+    p = dm.make_params(pnx=nx, pny=ny, pad=2, **kw)
+    fr = run(ctx, dev, img, depth, p, None, "fp64")
+    op = oparams(p, render_depth=kw.get("render_depth"))
+    ref = odm.generate(img, depth, op)[0]
+    assert rel(fr, ref) < TOL64
+
+
+@pytest.mark.parametrize("shape", [(45, 75), (49, 63), (50, 98)])
+def test_depthmap_odd_and_generic_sizes(ctx, dev, shape):
+    """odd sizes (shift by floor(n/2)) and sizes with radix 7 / generic factors"""
+    ny, nx = shape
+    img, depth = scenes.depthmap_scene(17, ny, nx)
+    p = dm.make_params(pnx=nx, pny=ny, num_of_depth=5, pad=1)
+    fr = run(ctx, dev, img, depth, p, None, "fp64")
+    ref = odm.generate(img, depth, oparams(p))[0]
+    assert rel(fr, ref) < TOL64
+
+
+def test_empty_image_gives_zero(ctx, dev):
+    ny, nx = 32, 48
+    img = np.zeros((ny, nx), np.uint8)
+    depth = np.full((ny, nx), 77, np.uint8)
+    p = dm.make_params(pnx=nx, pny=ny, num_of_depth=8, pad=2)
+    fr = run(ctx, dev, img, depth, p, None, "fp32")
+    assert np.all(fr == 0)
+
+
+def test_flat_depth_is_single_layer_propagation(ctx, dev):
+    """A flat depth map collapses to one angular-spectrum propagation."""
+    ny, nx = 64, 96
+    img, _ = scenes.depthmap_scene(31, ny, nx)
+    depth = np.full((ny, nx), 128, np.uint8)
+    p = dm.make_params(pnx=nx, pny=ny, num_of_depth=10, pad=2)
+    fr = run(ctx, dev, img, depth, p, None, "fp64")
+    op = oparams(p)
+    lvl = odm.depth_lut(op)[128]
+    op1 = oparams(p, render_depth=[int(lvl)])
+    ref = odm.generate(img, depth, op1)[0]
+    assert rel(fr, ref) < TOL64
+
+
+def test_full_size_linearity_and_fp64_agreement(ctx, dev):
+    """1920x1080, 32 layers, 2x pad (the benchmark frame): the oracle is too
+    slow here, so check size-independent properties: linearity of the
+    fringe in the source amplitude over disjoint supports, and FP32 against
+    the FP64 path (itself pinned to the oracle above)."""
+    ny, nx = 1080, 1920
+    img, depth = scenes.depthmap_scene(42, ny, nx)
+    p = dm.make_params(phase_mode=dm.OH_PHASE_SEEDED, seed=99)
+    f32 = run(ctx, dev, img, depth, p, None, "fp32").astype(np.float64)
+    f64 = run(ctx, dev, img, depth, p, None, "fp64")
+    assert rel(f32, f64) < TOL32
+    mask = (np.arange(nx)[None, :] + np.arange(ny)[:, None]) % 3 == 0
+    a = np.where(mask, img, 0).astype(np.uint8)
+    b = np.where(mask, 0, img).astype(np.uint8)
+    fa = run(ctx, dev, a, depth, p, None, "fp64")
+    fb = run(ctx, dev, b, depth, p, None, "fp64")
+    assert rel(fa + fb, f64) < 1e-9
+
+
+def test_host_entry_point_matches_device(ctx, dev):
+    ny, nx = 72, 120
+    img, depth = scenes.depthmap_scene(3, ny, nx)
+    p = dm.make_params(pnx=nx, pny=ny, num_of_depth=9, phase_mode=dm.OH_PHASE_SEEDED, seed=7)
+    fr_dev = run(ctx, dev, img, depth, p, None, "fp32")
+    fr_host = dm.generate_host(ctx, p, img, depth)
+    assert np.array_equal(fr_dev, fr_host)
+
+
+def test_invalid_arguments_raise(ctx, dev):
+    img = torch.zeros((8, 8), dtype=torch.uint8, device=dev)
+    with pytest.raises(OhError):
+        dm.generate(ctx, dm.make_params(pnx=8, pny=8, pad=3), img, img)
+    with pytest.raises(OhError):
+        dm.generate(ctx, dm.make_params(pnx=8, pny=8, num_of_depth=4, render_depth=[5]), img, img)
+    with pytest.raises(OhError):   # 67 is a prime above the generic-radix limit
+        dm.generate(ctx, dm.make_params(pnx=67, pny=8, pad=1, num_of_depth=2),
+                    torch.zeros((8, 67), dtype=torch.uint8, device=dev),
+                    torch.zeros((8, 67), dtype=torch.uint8, device=dev))
+    with pytest.raises(OhError):
+        dm.generate(ctx, dm.make_params(pnx=8, pny=8, phase_mode=dm.OH_PHASE_ARRAY), img, img)

@@ -1,0 +1,104 @@
+"""Encoders, uint8 normalisation, WRP accumulation and Fresnel propagation on
+the GPU against CPU restatements (oracle)."""
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from openholo_gb300 import _lib, scenes
+from openholo_gb300._lib import WrpParams
+from oracle import depthmap as odm
+from oracle import encoding as oenc
+from oracle import pointcloud as opc
+from oracle import wrp as owrp
+
+pytestmark = pytest.mark.gpu
+
+
+def S():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def field_sample(ny=48, nx=64, seed=0):
+    rng = np.random.default_rng(seed)
+    return rng.standard_normal((ny, nx)) + 1j * rng.standard_normal((ny, nx))
+
+
+KINDS = {0: "real", 1: "p2a", 2: "ni", 3: "burckhardt", 4: "two_phase", 5: "ssb_left", 6: "ssb_right",
+         7: "ssb_top", 8: "ssb_bottom", 9: "phase_only_u8", 10: "amplitude"}
+
+
+@pytest.mark.parametrize("kind", sorted(KINDS))
+def test_encoders(ctx, kind):
+    U = field_sample()
+    ny, nx = U.shape
+    t = torch.from_numpy(U).cuda()
+    width = {3: 3, 4: 2}.get(kind, 1)
+    out = torch.empty((ny, nx * width), dtype=torch.uint8 if kind == 9 else torch.float64, device="cuda")
+    _lib.call("oh_encode", ctx.handle, 1, kind, nx, ny, C.c_void_p(t.data_ptr()), C.c_void_p(out.data_ptr()), S())
+    torch.cuda.synchronize()
+    ref = oenc.encode(U, KINDS[kind])
+    got = out.cpu().numpy()
+    if kind == 9:
+        assert np.abs(got.astype(int) - ref.astype(int)).max() <= 1
+        assert np.mean(got != ref) < 1e-3
+    else:
+        assert np.allclose(got, ref, rtol=1e-9, atol=1e-9)
+
+
+@pytest.mark.parametrize("round_half", [0, 1])
+def test_normalize_u8(ctx, round_half):
+    f = np.random.default_rng(2).standard_normal((40, 50))
+    t = torch.from_numpy(f).cuda()
+    out = torch.empty((40, 50), dtype=torch.uint8, device="cuda")
+    _lib.call("oh_normalize_u8", ctx.handle, 1, 50, 40, C.c_void_p(t.data_ptr()), C.c_void_p(out.data_ptr()),
+              round_half, S())
+    torch.cuda.synchronize()
+    ref = oenc.keti_normalize(f.astype(np.float32)) if round_half else odm.normalize_u8(f)
+    assert np.array_equal(out.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("fixed_w,precision", [(8, "fp64"), (8, "fp32"), (0, "fp64")])
+def test_wrp_accumulate(ctx, fixed_w, precision):
+    pts = scenes.wrp_scene(4, 200, box=(0.6e-3, 0.4e-3, 0.2e-3), zc=0.01)
+    nx, ny, dp, lam = 96, 80, 8e-6, 532e-9
+    z = 0.01 - 0.1e-3 - 0.4e-3 if fixed_w else 0.012   # formula mode: dz ~ 2 mm -> w ~ 15
+    p = WrpParams(nx, ny, dp, lam, z, fixed_w)
+    tp = torch.from_numpy(pts).cuda()
+    cdt = torch.complex128 if precision == "fp64" else torch.complex64
+    w = torch.zeros((ny, nx), dtype=cdt, device="cuda")
+    _lib.call("oh_wrp_accumulate", ctx.handle, 1 if precision == "fp64" else 0, C.byref(p),
+              C.c_void_p(tp.data_ptr()), pts.shape[0], C.c_void_p(w.data_ptr()), S())
+    torch.cuda.synchronize()
+    ref = opc.wrp_f64(pts, nx, ny, dp, lam, z, fixed_w)
+    tol = 1e-9 if precision == "fp64" else 1e-4
+    assert np.linalg.norm(w.cpu().numpy() - ref) <= tol * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("shape", [(64, 64), (48, 80)])
+def test_fresnel_propagate(ctx, shape):
+    ny, nx = shape
+    U = field_sample(ny, nx, 7)
+    dp, lam, z = 8e-6, 532e-9, 0.02
+    for precision, tol in (("fp64", 1e-10), ("fp32", 1e-4)):
+        t = torch.from_numpy(U).to(torch.complex128 if precision == "fp64" else torch.complex64).cuda()
+        _lib.call("oh_fresnel_propagate", ctx.handle, 1 if precision == "fp64" else 0, nx, ny, dp, lam, z,
+                  C.c_void_p(t.data_ptr()), S())
+        torch.cuda.synchronize()
+        ref = owrp.fresnel_conv(U, dp, lam, z)
+        assert np.linalg.norm(t.cpu().numpy() - ref) <= tol * np.linalg.norm(ref), precision
+
+
+def test_fresnel_point_focus(ctx):
+    """Known answer: a WRP point field propagated back by -z refocuses to a spot."""
+    n, dp, lam, z = 128, 8e-6, 532e-9, 0.03
+    U = np.zeros((n, n), np.complex128)
+    U[n // 2, n // 2] = 1.0
+    t = torch.from_numpy(U).cuda()
+    _lib.call("oh_fresnel_propagate", ctx.handle, 1, n, n, dp, lam, z, C.c_void_p(t.data_ptr()), S())
+    _lib.call("oh_fresnel_propagate", ctx.handle, 1, n, n, dp, lam, -z, C.c_void_p(t.data_ptr()), S())
+    torch.cuda.synchronize()
+    back = np.abs(t.cpu().numpy())
+    assert np.unravel_index(np.argmax(back), back.shape) == (n // 2, n // 2)
