@@ -1,5 +1,6 @@
 // Context, scratch arena, FFT plan cache and error plumbing.
 #include "context.h"
+#include "fft_fast.cuh"
 
 #include <atomic>
 #include <cmath>
@@ -55,6 +56,16 @@ oh_status scratch(oh_ctx* ctx, const char* name, size_t bytes, void** out) {
 
 bool factorize(int n, int* radix, int* nst) {
   if (n < 1) return false;
+  // lengths with a compile-time schedule use exactly that schedule
+#define OH_SCHED_CASE(len, ...)                                   \
+  if (n == len) {                                                  \
+    const int rs[] = {__VA_ARGS__};                                \
+    *nst = (int)(sizeof(rs) / sizeof(rs[0]));                      \
+    for (int s = 0; s < *nst; ++s) radix[s] = rs[s];               \
+    return true;                                                   \
+  }
+  OH_FAST_SCHEDULES(OH_SCHED_CASE)
+#undef OH_SCHED_CASE
   int m = n, s = 0;
   int twos = 0;
   while (m % 2 == 0) { m /= 2; ++twos; }

@@ -160,7 +160,7 @@ __device__ __forceinline__ void sincos_r(R x, R* s, R* c);
 template <> __device__ __forceinline__ void sincos_r<float>(float x, float* s, float* c) { sincosf(x, s, c); }
 template <> __device__ __forceinline__ void sincos_r<double>(double x, double* s, double* c) { sincos(x, s, c); }
 
-template <typename R>
+template <typename R, int NX>
 __global__ void __launch_bounds__(256) dm_row_pass(DMArgs<R> a) {
   typedef typename cplx_of<R>::type C;
   extern __shared__ unsigned char smem_raw[];
@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(256) dm_row_pass(DMArgs<R> a) {
       if (c >= 0 && c < a.pnx && li[c] == u) val = v[c];
       buf[j] = val;
     }
-    block_fft<-1>(buf, 1, a.Px, 1, a.plx, false);
+    block_fft_n<NX, -1>(buf, 1, a.Px, 1, a.plx, false);
     C* dst = a.Rbuf + (size_t)u * a.nstrips * a.pny * a.W;
     for (int kx = threadIdx.x; kx < a.Px; kx += blockDim.x) {
       int m = kx - a.hx; if (m < 0) m += a.Px;       // S[kx] = A[(kx - hx) mod Px]
@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(256) dm_row_pass(DMArgs<R> a) {
   }
 }
 
-template <typename R, int KMAX>
+template <typename R, int KMAX, int NY>
 __global__ void __launch_bounds__(512) dm_col_pass(DMArgs<R> a) {
   typedef typename cplx_of<R>::type C;
   extern __shared__ unsigned char smem_raw[];
@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(512) dm_col_pass(DMArgs<R> a) {
     } else {
       for (int w = threadIdx.x; w < W; w += T) exw[w] = a.cst[e];
     }
-    block_fft<-1>(buf, W, 1, W, a.ply, true);
+    block_fft_n<NY, -1>(buf, W, 1, W, a.ply, true);
     const R kz = a.kzp[e];
     const C* eyr = a.ey + (size_t)e * Py;
 #pragma unroll
@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(512) dm_col_pass(DMArgs<R> a) {
       buf[i * W + w] = keep ? acc[k] : mk((R)0, (R)0);
     }
   }
-  block_fft<1>(buf, W, 1, W, a.ply, true);
+  block_fft_n<NY, 1>(buf, W, 1, W, a.ply, true);
   for (int idx = threadIdx.x; idx < a.pny * W; idx += T) {
     const int yl = idx / W, w = idx - yl * W;
     int m = a.oy + yl - a.hy; if (m < 0) m += Py;   // out[y] = B[(y - hy) mod Py]
@@ -322,7 +322,7 @@ __global__ void __launch_bounds__(512) dm_col_pass(DMArgs<R> a) {
   }
 }
 
-template <typename R>
+template <typename R, int NX>
 __global__ void __launch_bounds__(256) dm_out_pass(DMArgs<R> a) {
   typedef typename cplx_of<R>::type C;
   extern __shared__ unsigned char smem_raw[];
@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(256) dm_out_pass(DMArgs<R> a) {
     int kx = j - a.hx; if (kx < 0) kx += a.Px;
     buf[j] = row[kx];
   }
-  block_fft<1>(buf, 1, a.Px, 1, a.plx, false);
+  block_fft_n<NX, 1>(buf, 1, a.Px, 1, a.plx, false);
   for (int c = threadIdx.x; c < a.pnx; c += blockDim.x) {
     int m = a.ox + c - a.hx; if (m < 0) m += a.Px;
     C h = buf[a.plx.perm[m]];
@@ -521,29 +521,46 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   a.slot_any = (int*)(base + o_any);
   a.fringe = (R*)fringe; a.field = (C*)field; a.spectrum = (C*)spectrum;
 
-  OH_CUDA_TRY(cudaFuncSetAttribute(dm_row_pass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_row));
-  OH_CUDA_TRY(cudaFuncSetAttribute(dm_col_pass<R, KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col));
-  OH_CUDA_TRY(cudaFuncSetAttribute(dm_out_pass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_out));
   {
     KernelTimer kt(ctx, prec ? "dm_setup_f64" : "dm_setup", st);
     dm_setup<R><<<64, 256, 0, st>>>(a, su);
     OH_LAUNCH_CHECK();
   }
-  {
+  // the FP32 path uses the compile-time FFT schedules; FP64 the generic engine
+  oh_status rs = OH_OK;
+  with_fast_n_if<sizeof(R) == 4>(a.Px, [&](auto nc) {
+    constexpr int NX = decltype(nc)::value;
+    cudaError_t e = cudaFuncSetAttribute(dm_row_pass<R, NX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_row);
+    if (e != cudaSuccess) { rs = cuda_fail(e, "cudaFuncSetAttribute(dm_row_pass)"); return; }
     KernelTimer kt(ctx, prec ? "dm_row_pass_f64" : "dm_row_pass", st);
-    dm_row_pass<R><<<a.pny, 256, smem_row, st>>>(a);
-    OH_LAUNCH_CHECK();
-  }
-  {
+    dm_row_pass<R, NX><<<a.pny, 256, smem_row, st>>>(a);
+    note_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) rs = cuda_fail(e, "dm_row_pass launch");
+  });
+  OH_TRY(rs);
+  with_fast_n_if<sizeof(R) == 4>(a.Py, [&](auto nc) {
+    constexpr int NY = decltype(nc)::value;
+    cudaError_t e = cudaFuncSetAttribute(dm_col_pass<R, KMAX, NY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col);
+    if (e != cudaSuccess) { rs = cuda_fail(e, "cudaFuncSetAttribute(dm_col_pass)"); return; }
     KernelTimer kt(ctx, prec ? "dm_col_pass_f64" : "dm_col_pass", st);
-    dm_col_pass<R, KMAX><<<a.nstrips, T, smem_col, st>>>(a);
-    OH_LAUNCH_CHECK();
-  }
-  {
+    dm_col_pass<R, KMAX, NY><<<a.nstrips, T, smem_col, st>>>(a);
+    note_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) rs = cuda_fail(e, "dm_col_pass launch");
+  });
+  OH_TRY(rs);
+  with_fast_n_if<sizeof(R) == 4>(a.Px, [&](auto nc) {
+    constexpr int NX = decltype(nc)::value;
+    cudaError_t e = cudaFuncSetAttribute(dm_out_pass<R, NX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_out);
+    if (e != cudaSuccess) { rs = cuda_fail(e, "cudaFuncSetAttribute(dm_out_pass)"); return; }
     KernelTimer kt(ctx, prec ? "dm_out_pass_f64" : "dm_out_pass", st);
-    dm_out_pass<R><<<a.pny, 256, smem_out, st>>>(a);
-    OH_LAUNCH_CHECK();
-  }
+    dm_out_pass<R, NX><<<a.pny, 256, smem_out, st>>>(a);
+    note_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) rs = cuda_fail(e, "dm_out_pass launch");
+  });
+  OH_TRY(rs);
   return OH_OK;
 }
 

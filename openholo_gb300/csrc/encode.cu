@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(256) reduce_partial(const void* __restrict__ i
     if (op == RED_MINMAX_REAL) v = static_cast<const R*>(in)[i];
     else {
       C c = static_cast<const C*>(in)[i];
-      if (op == RED_MAX_ABS) v = sqrt(c.x * c.x + c.y * c.y);
+      if (op == RED_MAX_ABS) v = hypot(c.x, c.y);
       else if (op == RED_MAX_NI) { R re = c.x + ref; v = re * re + c.y * c.y; }
       else if (op == RED_MAX_PHASE) v = ratan2<R>(c.y, c.x) + (R)3.14159265358979323846;
       else v = c.x;   // RED_MINMAX_SSB: real part
@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(256) encode_map(int kind, int nx, int ny, cons
     R* o = static_cast<R*>(out);
     switch (kind) {
       case OH_ENC_REAL: o[i] = u.x; break;
-      case OH_ENC_AMPLITUDE: o[i] = sqrt(u.x * u.x + u.y * u.y); break;
+      case OH_ENC_AMPLITUDE: o[i] = hypot(u.x, u.y); break;
       case OH_ENC_PHASE_TO_AMP: o[i] = ratan2<R>(u.y, u.x) + pi / ((R)2 * pi); break;   // fn_encoding.m:57 as written
       case OH_ENC_NUM_INTERFERENCE: {
         const R ref = red1[1];
@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(256) encode_map(int kind, int nx, int ny, cons
         const R m = red1[1];
         const R cr = u.x / m, ci = u.y / m;
         const R ph = ratan2<R>(ci, cr) + pi;
-        const R am = sqrt(cr * cr + ci * ci);
+        const R am = hypot(cr, ci);
         const R s3 = (R)1.7320508075688772935;
         R a1 = 0, a2 = 0, a3 = 0;
         if (ph >= 0 && ph < 2 * pi / 3) {
@@ -122,9 +122,10 @@ __global__ void __launch_bounds__(256) encode_map(int kind, int nx, int ny, cons
       case OH_ENC_TWO_PHASE: {
         const R m = red1[1];
         const R cr = u.x / m, ci = u.y / m;
-        const R am = sqrt(cr * cr + ci * ci);
+        const R am = hypot(cr, ci);
         const R ph = ratan2<R>(ci, cr) + pi;
-        const R del = acos(am);
+        // MATLAB's acos of a rounding-level 1+eps is complex; its real part is 0
+        const R del = acos(am < (R)1 ? am : (R)1);
         const size_t r = i / nx, c = i - r * nx;
         R* row = o + r * (size_t)(2 * nx);
         row[2 * c] = ph + del; row[2 * c + 1] = ph - del;

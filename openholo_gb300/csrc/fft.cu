@@ -13,7 +13,7 @@
 
 namespace oh {
 
-template <typename R, int SGN>
+template <typename R, int SGN, int N>
 __global__ void __launch_bounds__(256) fft_rows_kernel(const typename cplx_of<R>::type* __restrict__ in,
                                                        typename cplx_of<R>::type* __restrict__ out,
                                                        int nx, int ny, int rpb, int shift, R scale,
@@ -29,7 +29,7 @@ __global__ void __launch_bounds__(256) fft_rows_kernel(const typename cplx_of<R>
     int src = j - hx; if (src < 0) src += nx;
     buf[l * nx + j] = in[(size_t)(row0 + l) * nx + src];
   }
-  block_fft<SGN>(buf, nrows, nx, 1, pl, false);
+  block_fft_n<N, SGN>(buf, nrows, nx, 1, pl, false);
   for (int idx = threadIdx.x; idx < nrows * nx; idx += blockDim.x) {
     int l = idx / nx, k = idx - l * nx;
     int m = k - hx; if (m < 0) m += nx;     // out[k] = A[(k - hx) mod nx]
@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(256) fft_rows_kernel(const typename cplx_of<R>
 // Column pass over strips of W columns.  aux (nullable) receives the
 // unshifted transform FFT2(shift(in)) as cudaFFT leaves it in its input
 // buffer (HologramKernel.cu:207-210).
-template <typename R, int SGN>
+template <typename R, int SGN, int N>
 __global__ void __launch_bounds__(512) fft_cols_kernel(typename cplx_of<R>::type* data,
                                                        typename cplx_of<R>::type* aux,
                                                        int nx, int ny, int W, int shift, R scale,
@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(512) fft_cols_kernel(typename cplx_of<R>::type
     int src = i - hy; if (src < 0) src += ny;
     buf[idx] = data[(size_t)src * nx + x0 + w];
   }
-  block_fft<SGN>(buf, W, 1, W, pl, true);
+  block_fft_n<N, SGN>(buf, W, 1, W, pl, true);
   for (int idx = threadIdx.x; idx < ny * W; idx += blockDim.x) {
     int k = idx / W, w = idx - k * W;
     int m = k - hy; if (m < 0) m += ny;
@@ -91,22 +91,34 @@ static oh_status launch_fft2d(oh_ctx* ctx, int nx, int ny, const void* in, void*
   R scale = normalize ? (R)(1.0 / ((double)nx * (double)ny)) : (R)1;
   const C* cin = static_cast<const C*>(in);
   C* cout_ = static_cast<C*>(out);
-  if (direction < 0) {
-    OH_CUDA_TRY(cudaFuncSetAttribute(fft_rows_kernel<R, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)srow));
-    OH_CUDA_TRY(cudaFuncSetAttribute(fft_cols_kernel<R, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scol));
-    fft_rows_kernel<R, -1><<<(ny + rpb - 1) / rpb, 256, srow, st>>>(cin, cout_, nx, ny, rpb, shift, (R)1, px);
-    OH_LAUNCH_CHECK();
-    fft_cols_kernel<R, -1><<<nx / W, 512, scol, st>>>(cout_, static_cast<C*>(aux), nx, ny, W, shift, scale, py);
-    OH_LAUNCH_CHECK();
-  } else {
-    OH_CUDA_TRY(cudaFuncSetAttribute(fft_rows_kernel<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)srow));
-    OH_CUDA_TRY(cudaFuncSetAttribute(fft_cols_kernel<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scol));
-    fft_rows_kernel<R, 1><<<(ny + rpb - 1) / rpb, 256, srow, st>>>(cin, cout_, nx, ny, rpb, shift, (R)1, px);
-    OH_LAUNCH_CHECK();
-    fft_cols_kernel<R, 1><<<nx / W, 512, scol, st>>>(cout_, static_cast<C*>(aux), nx, ny, W, shift, scale, py);
-    OH_LAUNCH_CHECK();
-  }
-  return OH_OK;
+  oh_status rs = OH_OK;
+  auto rows = [&](auto sg) {
+    constexpr int SG = decltype(sg)::value;
+    with_fast_n_if<sizeof(R) == 4>(nx, [&](auto nc) {
+      constexpr int NX = decltype(nc)::value;
+      cudaError_t e = cudaFuncSetAttribute(fft_rows_kernel<R, SG, NX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)srow);
+      if (e != cudaSuccess) { rs = cuda_fail(e, "cudaFuncSetAttribute(fft_rows)"); return; }
+      KernelTimer kt(ctx, "fft_rows", st);
+      fft_rows_kernel<R, SG, NX><<<(ny + rpb - 1) / rpb, 256, srow, st>>>(cin, cout_, nx, ny, rpb, shift, (R)1, px);
+      note_launch();
+      if ((e = cudaGetLastError()) != cudaSuccess) rs = cuda_fail(e, "fft_rows launch");
+    });
+  };
+  auto cols = [&](auto sg) {
+    constexpr int SG = decltype(sg)::value;
+    with_fast_n_if<sizeof(R) == 4>(ny, [&](auto nc) {
+      constexpr int NY = decltype(nc)::value;
+      cudaError_t e = cudaFuncSetAttribute(fft_cols_kernel<R, SG, NY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scol);
+      if (e != cudaSuccess) { rs = cuda_fail(e, "cudaFuncSetAttribute(fft_cols)"); return; }
+      KernelTimer kt(ctx, "fft_cols", st);
+      fft_cols_kernel<R, SG, NY><<<nx / W, 512, scol, st>>>(cout_, static_cast<C*>(aux), nx, ny, W, shift, scale, py);
+      note_launch();
+      if ((e = cudaGetLastError()) != cudaSuccess) rs = cuda_fail(e, "fft_cols launch");
+    });
+  };
+  if (direction < 0) { rows(std::integral_constant<int, -1>{}); OH_TRY(rs); cols(std::integral_constant<int, -1>{}); }
+  else { rows(std::integral_constant<int, 1>{}); OH_TRY(rs); cols(std::integral_constant<int, 1>{}); }
+  return rs;
 }
 
 template <typename R>
@@ -122,11 +134,11 @@ static oh_status launch_fft_rows(oh_ctx* ctx, int nx, int ny, const void* in, vo
   if (srow > max_smem_per_block()) return fail(OH_ERR_UNSUPPORTED_SIZE, "row length exceeds shared memory");
   R scale = normalize ? (R)(1.0 / (double)nx) : (R)1;
   if (direction < 0) {
-    OH_CUDA_TRY(cudaFuncSetAttribute(fft_rows_kernel<R, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)srow));
-    fft_rows_kernel<R, -1><<<(ny + rpb - 1) / rpb, 256, srow, st>>>(static_cast<const C*>(in), static_cast<C*>(out), nx, ny, rpb, 0, scale, px);
+    OH_CUDA_TRY(cudaFuncSetAttribute(fft_rows_kernel<R, -1, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)srow));
+    fft_rows_kernel<R, -1, 0><<<(ny + rpb - 1) / rpb, 256, srow, st>>>(static_cast<const C*>(in), static_cast<C*>(out), nx, ny, rpb, 0, scale, px);
   } else {
-    OH_CUDA_TRY(cudaFuncSetAttribute(fft_rows_kernel<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)srow));
-    fft_rows_kernel<R, 1><<<(ny + rpb - 1) / rpb, 256, srow, st>>>(static_cast<const C*>(in), static_cast<C*>(out), nx, ny, rpb, 0, scale, px);
+    OH_CUDA_TRY(cudaFuncSetAttribute(fft_rows_kernel<R, 1, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)srow));
+    fft_rows_kernel<R, 1, 0><<<(ny + rpb - 1) / rpb, 256, srow, st>>>(static_cast<const C*>(in), static_cast<C*>(out), nx, ny, rpb, 0, scale, px);
   }
   OH_LAUNCH_CHECK();
   return OH_OK;

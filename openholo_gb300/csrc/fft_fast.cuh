@@ -1,0 +1,223 @@
+// Compile-time scheduled shared-memory FFT for the line lengths of the
+// hologram workloads.  Same in-place decimation-in-frequency recursion and
+// output order (perm table) as the generic engine in fft_core.cuh, but the
+// radix schedule, strides and twiddle steps are template constants, so the
+// butterfly index arithmetic compiles to shifts/multiplies and every stage
+// is a straight-line radix-R kernel.  Radices 9 and 16 are split 3x3 / 4x4
+// (Cooley-Tukey with constant twiddles); 6, 10, 12, 15 and 18 use the
+// Good-Thomas prime-factor mapping (no internal twiddles).
+//
+// The schedules listed in OH_FAST_SCHEDULES are also what the host-side plan
+// builder uses for these lengths, so both engines agree on output order.
+#pragma once
+#include "fft_core.cuh"
+
+// length, then the radices in stage order
+#define OH_FAST_SCHEDULES(X) \
+  X(1024, 16, 16, 4)         \
+  X(1080, 8, 9, 15)          \
+  X(1536, 16, 16, 6)         \
+  X(1920, 16, 8, 15)         \
+  X(2048, 16, 16, 8)         \
+  X(2160, 16, 9, 15)         \
+  X(3072, 16, 16, 12)        \
+  X(3840, 16, 16, 15)        \
+  X(4096, 16, 16, 16)        \
+  X(4320, 16, 18, 15)        \
+  X(7680, 16, 16, 30)
+
+namespace oh {
+
+// ---- small DFTs on register arrays ----------------------------------------
+
+template <int R, int SGN, typename C> struct DFT;
+
+template <int SGN, typename C> struct DFT<2, SGN, C> {
+  __device__ __forceinline__ static void run(C* x) { dft2<SGN>(x[0], x[1]); }
+};
+template <int SGN, typename C> struct DFT<3, SGN, C> {
+  __device__ __forceinline__ static void run(C* x) { dft3<SGN>(x[0], x[1], x[2]); }
+};
+template <int SGN, typename C> struct DFT<4, SGN, C> {
+  __device__ __forceinline__ static void run(C* x) { dft4<SGN>(x[0], x[1], x[2], x[3]); }
+};
+template <int SGN, typename C> struct DFT<5, SGN, C> {
+  __device__ __forceinline__ static void run(C* x) { dft5<SGN>(x[0], x[1], x[2], x[3], x[4]); }
+};
+template <int SGN, typename C> struct DFT<8, SGN, C> {
+  __device__ __forceinline__ static void run(C* x) { dft8<SGN>(x); }
+};
+
+// cos/sin(2 pi m / 16) and (2 pi m / 9), m = 0..4
+__device__ __forceinline__ double w16c(int m) {
+  return m == 0 ? 1.0 : m == 1 ? 0.9238795325112867561282 : m == 2 ? 0.7071067811865475244008
+       : m == 3 ? 0.3826834323650897717285 : 0.0;
+}
+__device__ __forceinline__ double w16s(int m) {
+  return m == 0 ? 0.0 : m == 1 ? 0.3826834323650897717285 : m == 2 ? 0.7071067811865475244008
+       : m == 3 ? 0.9238795325112867561282 : 1.0;
+}
+__device__ __forceinline__ double w9c(int m) {
+  return m == 0 ? 1.0 : m == 1 ? 0.7660444431189780352024 : m == 2 ? 0.1736481776669303488517
+       : m == 3 ? -0.5 : -0.9396926207859083840541;
+}
+__device__ __forceinline__ double w9s(int m) {
+  return m == 0 ? 0.0 : m == 1 ? 0.6427876096865393263226 : m == 2 ? 0.9848077530122080593667
+       : m == 3 ? 0.8660254037844386467637 : 0.3420201433256687330441;
+}
+
+// multiply by W_N^m = exp(SGN * 2 pi i m / N) for N in {16, 9}, m small
+template <int N, int SGN, typename C>
+__device__ __forceinline__ C wmul(C a, int m) {
+  typedef decltype(a.x) R;
+  if (m == 0) return a;
+  R c, s;
+  if (N == 16) {
+    // reduce m in [1, 9] to the first quadrant: W16^m for m = 4 is -i (fwd)
+    if (m == 4) return cmul_i<SGN>(a);
+    if (m < 4) { c = (R)w16c(m); s = (R)w16s(m); }
+    else if (m < 8) { c = -(R)w16c(8 - m); s = (R)w16s(8 - m); }   // angle pi - a
+    else if (m == 8) { C r; r.x = -a.x; r.y = -a.y; return r; }
+    else { c = -(R)w16c(m - 8); s = -(R)w16s(m - 8); }              // angle pi + a
+  } else {
+    c = (R)w9c(m); s = (R)w9s(m);
+  }
+  C w; w.x = c; w.y = (R)SGN * s;
+  return cmul(a, w);
+}
+
+// Cooley-Tukey N1 x N2 with constant twiddles W_N^{n2 k1}
+template <int N1, int N2, int SGN, typename C>
+__device__ __forceinline__ void dft_ct(C* x) {
+  constexpr int N = N1 * N2;
+  C a[N];
+#pragma unroll
+  for (int n2 = 0; n2 < N2; ++n2) {
+    C v[N1];
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) v[n1] = x[n2 + N2 * n1];
+    DFT<N1, SGN, C>::run(v);
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) a[n2 * N1 + k1] = wmul<N, SGN>(v[k1], n2 * k1);
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < N1; ++k1) {
+    C v[N2];
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2) v[n2] = a[n2 * N1 + k1];
+    DFT<N2, SGN, C>::run(v);
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) x[k1 + N1 * k2] = v[k2];
+  }
+}
+
+// Good-Thomas prime-factor N1 x N2 (gcd 1): n = (n1 N2 + n2 N1) mod N,
+// X[k] = DFT_N2( DFT_N1 ) at (k mod N1, k mod N2)
+template <int N1, int N2, int SGN, typename C>
+__device__ __forceinline__ void dft_pfa(C* x) {
+  constexpr int N = N1 * N2;
+  C b[N];
+#pragma unroll
+  for (int n2 = 0; n2 < N2; ++n2) {
+    C v[N1];
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) v[n1] = x[(n1 * N2 + n2 * N1) % N];
+    DFT<N1, SGN, C>::run(v);
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) b[k1 * N2 + n2] = v[k1];
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < N1; ++k1) {
+    DFT<N2, SGN, C>::run(b + k1 * N2);
+  }
+#pragma unroll
+  for (int k = 0; k < N; ++k) x[k] = b[(k % N1) * N2 + (k % N2)];
+}
+
+template <int SGN, typename C> struct DFT<16, SGN, C> {
+  __device__ __forceinline__ static void run(C* x) { dft_ct<4, 4, SGN>(x); }
+};
+template <int SGN, typename C> struct DFT<9, SGN, C> {
+  __device__ __forceinline__ static void run(C* x) { dft_ct<3, 3, SGN>(x); }
+};
+template <int SGN, typename C> struct DFT<6, SGN, C> {
+  __device__ __forceinline__ static void run(C* x) { dft_pfa<2, 3, SGN>(x); }
+};
+template <int SGN, typename C> struct DFT<10, SGN, C> {
+  __device__ __forceinline__ static void run(C* x) { dft_pfa<2, 5, SGN>(x); }
+};
+template <int SGN, typename C> struct DFT<12, SGN, C> {
+  __device__ __forceinline__ static void run(C* x) { dft_pfa<4, 3, SGN>(x); }
+};
+template <int SGN, typename C> struct DFT<15, SGN, C> {
+  __device__ __forceinline__ static void run(C* x) { dft_pfa<3, 5, SGN>(x); }
+};
+template <int SGN, typename C> struct DFT<18, SGN, C> {
+  __device__ __forceinline__ static void run(C* x) { dft_pfa<2, 9, SGN>(x); }
+};
+template <int SGN, typename C> struct DFT<30, SGN, C> {
+  __device__ __forceinline__ static void run(C* x) { dft_pfa<2, 15, SGN>(x); }
+};
+
+// ---- one stage --------------------------------------------------------------
+
+template <int N, int R, int M, int SGN, typename C>
+__device__ __forceinline__ void fstage(C* buf, int nl, int ls, int es, const C* __restrict__ tw,
+                                       bool line_fastest) {
+  constexpr int Q = M / R;         // stride of the butterfly inputs
+  constexpr int TWS = N / M;       // twiddle step
+  constexpr int NB = N / R;        // butterflies per line
+  const int total = NB * nl;
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    int line, b;
+    if (line_fastest) { b = idx / nl; line = idx - b * nl; }
+    else { line = idx / NB; b = idx - line * NB; }
+    const int blk = b / Q, j = b - blk * Q;
+    const int base = line * ls + (blk * M + j) * es;
+    const int st = Q * es;
+    C x[R];
+#pragma unroll
+    for (int t = 0; t < R; ++t) x[t] = buf[base + t * st];
+    DFT<R, SGN, C>::run(x);
+    if (Q > 1 && j) {
+#pragma unroll
+      for (int f = 1; f < R; ++f) x[f] = cmul(x[f], twiddle<SGN>(tw, j * f * TWS));
+    }
+#pragma unroll
+    for (int t = 0; t < R; ++t) buf[base + t * st] = x[t];
+  }
+}
+
+template <int N, int M, int SGN, typename C, int R, int... Rest>
+__device__ __forceinline__ void fstages(C* buf, int nl, int ls, int es, const C* tw, bool line_fastest) {
+  __syncthreads();
+  fstage<N, R, M, SGN>(buf, nl, ls, es, tw, line_fastest);
+  if constexpr (sizeof...(Rest) > 0) fstages<N, M / R, SGN, C, Rest...>(buf, nl, ls, es, tw, line_fastest);
+}
+
+template <int N> struct FastSched { static constexpr bool ok = false; };
+#define OH_DEFINE_SCHED(n, ...)                                                   \
+  template <> struct FastSched<n> {                                               \
+    static constexpr bool ok = true;                                              \
+    template <int SGN, typename C>                                                \
+    __device__ __forceinline__ static void run(C* buf, int nl, int ls, int es,    \
+                                               const C* tw, bool lf) {            \
+      fstages<n, n, SGN, C, __VA_ARGS__>(buf, nl, ls, es, tw, lf);               \
+    }                                                                             \
+  };
+OH_FAST_SCHEDULES(OH_DEFINE_SCHED)
+#undef OH_DEFINE_SCHED
+
+// In-place transform of nl lines with the compile-time schedule for N when
+// N > 0, else the generic engine; ends with __syncthreads().
+template <int N, int SGN, typename C>
+__device__ __forceinline__ void block_fft_n(C* buf, int nl, int ls, int es, const FFTPlan& pl, bool line_fastest) {
+  if constexpr (N > 0) {
+    FastSched<N>::template run<SGN>(buf, nl, ls, es, static_cast<const C*>(pl.tw), line_fastest);
+    __syncthreads();
+  } else {
+    block_fft<SGN>(buf, nl, ls, es, pl, line_fastest);
+  }
+}
+
+}  // namespace oh

@@ -1,6 +1,8 @@
 // Internal entry points shared between translation units.
 #pragma once
+#include <type_traits>
 #include "context.h"
+#include "fft_fast.cuh"
 
 namespace oh {
 
@@ -23,6 +25,27 @@ __host__ __device__ __forceinline__ uint64_t splitmix64_at(uint64_t seed, uint64
 // u in [0,1) with 24 random bits (exact in float)
 __host__ __device__ __forceinline__ float u24_at(uint64_t seed, uint64_t idx) {
   return (float)(splitmix64_at(seed, idx) >> 40) * (1.0f / 16777216.0f);
+}
+
+// Calls f(std::integral_constant<int, n>) when n has a compile-time
+// schedule, else f(std::integral_constant<int, 0>) (generic engine).
+template <class F>
+inline void with_fast_n(int n, F&& f) {
+  switch (n) {
+#define OH_WITH_CASE(len, ...) \
+    case len: f(std::integral_constant<int, len>{}); return;
+    OH_FAST_SCHEDULES(OH_WITH_CASE)
+#undef OH_WITH_CASE
+    default: f(std::integral_constant<int, 0>{}); return;
+  }
+}
+
+// Same, restricted to the generic engine unless Enable (keeps FP64
+// instantiations to one per kernel).
+template <bool Enable, class F>
+inline void with_fast_n_if(int n, F&& f) {
+  if constexpr (Enable) with_fast_n(n, f);
+  else f(std::integral_constant<int, 0>{});
 }
 
 }  // namespace oh

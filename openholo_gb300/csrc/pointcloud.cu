@@ -7,14 +7,18 @@
 // The KETI fringe is Re of the same sum, accumulated into the caller's
 // buffer (dst += ...).
 //
-// FP32 path: k r_j is ~1e6 rad, far beyond float resolution, so the phase is
-// split exactly as
-//   k r = [k (X-x)^2/(2z) - k X sin tx]  +  [k z + k (Y-y)^2/(2z) - k Y sin ty]
-//         - k z t^2 / (2 (1 + sqrt(1+t))^2),          t = ((X-x)^2+(Y-y)^2)/z^2
-// The two bracketed terms are per-(point, column) and per-(point, row)
-// tables computed in FP64 and reduced mod 2 pi before rounding to float; the
-// last term is a cancellation-free form of k z (sqrt(1+t) - 1 - t/2) and is
-// evaluated in FP32 per term (it is at most a few rad for paraxial scenes).
+// FP32 path: k r_j reaches 1e6 rad, far beyond float resolution, so the
+// phase is split exactly into FP64-reduced tables plus a small FP32 residual.
+// With r_y = sqrt((Y-y)^2 + z^2) (per point and row) and a per-point anchor
+// distance rb = sqrt(y^2 + z^2) (the SLM-centre row):
+//   k r = k dx^2/(2 rb) - k X sin tx                      table A[point][col]
+//       + k r_y        - k Y sin ty                      table B[point][row]
+//       + k dx^2 (2 rb - r - r_y) / (2 rb (r + r_y))     FP32 residual
+// since r - r_y = dx^2/(r + r_y).  The residual is evaluated without
+// cancellation as (k/(2rb)) dx^2 (-2E - dx^2/(r+r_y)) / (r+r_y) with
+// E = r_y - rb tabulated per point and row; it stays at a few rad both for
+// paraxial scenes and for strongly off-axis ones such as the KETI sample
+// (points tens of mm off-axis at 5 mm depth).
 // FP64 path: the direct formula in double precision.
 #include <cmath>
 #include <vector>
@@ -31,24 +35,27 @@ struct PCGeom {
 constexpr int kPcChunk = 32768;    // points per table chunk
 constexpr int kPcTX = 32, kPcTY = 8, kPcPts = 64;
 
-// Per point: x_j, y_j, 1/z^2, -k z/2 (fp32) and the FP64-reduced tables.
+// Per point: x_j, k/(2 rb), amplitude; per point and column: A; per point
+// and row: B, r_y, E = r_y - rb.
 __global__ void pc_tables(PCGeom g, const float4* __restrict__ pts, int n, float4* __restrict__ prm,
-                          float* __restrict__ A, float* __restrict__ B) {
+                          float* __restrict__ A, float* __restrict__ B, float* __restrict__ RY, float* __restrict__ E) {
   const double two_pi = 6.283185307179586476925286766559;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int nthr = gridDim.x * blockDim.x;
   for (int j = tid; j < n; j += nthr) {
     float4 p = pts[j];
     double x = (double)p.x * g.sx, y = (double)p.y * g.sy, z = (double)p.z * g.sz + g.off;
-    prm[j] = make_float4((float)x, (float)y, (float)(1.0 / (z * z)), (float)(-0.5 * g.k * z));
+    double rb = sqrt(y * y + z * z);
+    prm[j] = make_float4((float)x, (float)(g.k / (2.0 * rb)), p.w, 0.f);
   }
   for (long long idx = tid; idx < (long long)n * g.nx; idx += nthr) {
     int j = (int)(idx / g.nx), c = (int)(idx - (long long)j * g.nx);
     float4 p = pts[j];
-    double x = (double)p.x * g.sx, z = (double)p.z * g.sz + g.off;
+    double x = (double)p.x * g.sx, y = (double)p.y * g.sy, z = (double)p.z * g.sz + g.off;
+    double rb = sqrt(y * y + z * z);
     double X = ((double)c + 0.5) * g.px - g.hlx;
     double dx = X - x;
-    double ph = g.k * dx * dx / (2.0 * z) - g.k * X * g.stx;
+    double ph = g.k * dx * dx / (2.0 * rb) - g.k * X * g.stx;
     ph -= two_pi * rint(ph / two_pi);
     A[idx] = (float)ph;
   }
@@ -58,27 +65,30 @@ __global__ void pc_tables(PCGeom g, const float4* __restrict__ pts, int n, float
     double y = (double)p.y * g.sy, z = (double)p.z * g.sz + g.off;
     double Y = g.hly - ((double)r + 0.5) * g.py;
     double dy = Y - y;
-    double kz = g.k * z;
-    double ph = (kz - two_pi * rint(kz / two_pi)) + g.k * dy * dy / (2.0 * z) - g.k * Y * g.sty;
+    double ry = sqrt(dy * dy + z * z), rb = sqrt(y * y + z * z);
+    double kr = g.k * ry;
+    double ph = (kr - two_pi * rint(kr / two_pi)) - g.k * Y * g.sty;
     ph -= two_pi * rint(ph / two_pi);
     B[idx] = (float)ph;
+    RY[idx] = (float)ry;
+    E[idx] = (float)((dy * dy - y * y) / (ry + rb));     // r_y - rb without cancellation
   }
 }
 
 // One thread per pixel of a 32x8 tile; points streamed through shared memory.
-__global__ void __launch_bounds__(kPcTX * kPcTY) pc_direct_f32(PCGeom g, const float4* __restrict__ pts,
-                                                              const float4* __restrict__ prm,
+__global__ void __launch_bounds__(kPcTX * kPcTY) pc_direct_f32(PCGeom g, const float4* __restrict__ prm,
                                                               const float* __restrict__ A, const float* __restrict__ B,
+                                                              const float* __restrict__ RY, const float* __restrict__ E,
                                                               int n, float2* __restrict__ field,
                                                               float* __restrict__ fringe, int accumulate_field) {
   __shared__ float sA[kPcPts][kPcTX];
   __shared__ float sB[kPcPts][kPcTY];
+  __shared__ float sR[kPcPts][kPcTY];
+  __shared__ float sE[kPcPts][kPcTY];
   __shared__ float4 sP[kPcPts];
-  __shared__ float sAmp[kPcPts];
   const int tx = threadIdx.x % kPcTX, ty = threadIdx.x / kPcTX;
   const int col = blockIdx.x * kPcTX + tx, row = blockIdx.y * kPcTY + ty;
   const float X = (float)(((double)col + 0.5) * g.px - g.hlx);
-  const float Y = (float)(g.hly - ((double)row + 0.5) * g.py);
   const float inv2pi = 0.15915494309189533577f, two_pi = 6.28318530717958647692f;
   float re = 0.f, im = 0.f;
   for (int j0 = 0; j0 < n; j0 += kPcPts) {
@@ -92,24 +102,28 @@ __global__ void __launch_bounds__(kPcTX * kPcTY) pc_direct_f32(PCGeom g, const f
     for (int i = threadIdx.x; i < cnt * kPcTY; i += blockDim.x) {
       int j = i / kPcTY, r = i - j * kPcTY;
       int rr = blockIdx.y * kPcTY + r;
-      sB[j][r] = rr < g.ny ? B[(size_t)(j0 + j) * g.ny + rr] : 0.f;
+      size_t o = (size_t)(j0 + j) * g.ny + rr;
+      sB[j][r] = rr < g.ny ? B[o] : 0.f;
+      sR[j][r] = rr < g.ny ? RY[o] : 1.f;
+      sE[j][r] = rr < g.ny ? E[o] : 0.f;
     }
-    for (int i = threadIdx.x; i < cnt; i += blockDim.x) { sP[i] = prm[j0 + i]; sAmp[i] = pts[j0 + i].w; }
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) sP[i] = prm[j0 + i];
     __syncthreads();
 #pragma unroll 4
     for (int j = 0; j < cnt; ++j) {
       const float4 p = sP[j];
-      const float dx = X - p.x, dy = Y - p.y;
-      const float t = fmaf(dx, dx, dy * dy) * p.z;
-      const float s = sqrtf(1.f + t);
-      const float q = __fdividef(t, 1.f + s);
-      float ph = sA[j][tx] + sB[j][ty] + p.w * q * q;
+      const float dx = X - p.x;
+      const float dx2 = dx * dx;
+      const float ry = sR[j][ty];
+      const float r = sqrtf(fmaf(ry, ry, dx2));
+      const float inv = __fdividef(1.f, r + ry);
+      const float u = fmaf(-2.f, sE[j][ty], -dx2 * inv);
+      float ph = sA[j][tx] + sB[j][ty] + p.y * dx2 * u * inv;
       ph = fmaf(-two_pi, rintf(ph * inv2pi), ph);
       float sn, cs;
       __sincosf(ph, &sn, &cs);
-      const float a = sAmp[j];
-      re = fmaf(a, cs, re);
-      im = fmaf(a, sn, im);
+      re = fmaf(p.z, cs, re);
+      im = fmaf(p.z, sn, im);
     }
   }
   if (col < g.nx && row < g.ny) {
@@ -186,21 +200,28 @@ oh_status pointcloud_enqueue(oh_ctx* ctx, int prec, const oh_pc_params* p, const
     return OH_OK;
   }
   if (prec) {
+    KernelTimer kt(ctx, "pc_direct_f64", st);
     pc_direct_f64<<<grid, kPcTX * kPcTY, 0, st>>>(g, pts, n, (double2*)field, (double*)fringe);
     OH_LAUNCH_CHECK();
     return OH_OK;
   }
   const int chunk = std::min(n, kPcChunk);
   void* ptr;
-  OH_TRY(scratch(ctx, "pc.tables", (size_t)chunk * (sizeof(float4) + sizeof(float) * (p->nx + p->ny)) + 1024, &ptr));
+  OH_TRY(scratch(ctx, "pc.tables", (size_t)chunk * (sizeof(float4) + sizeof(float) * (p->nx + 3 * (size_t)p->ny)) + 1024, &ptr));
   float4* prm = (float4*)ptr;
   float* A = (float*)(prm + chunk);
   float* B = A + (size_t)chunk * p->nx;
+  float* RY = B + (size_t)chunk * p->ny;
+  float* E = RY + (size_t)chunk * p->ny;
   for (int j0 = 0; j0 < n; j0 += chunk) {
     const int cnt = std::min(chunk, n - j0);
-    pc_tables<<<1024, 256, 0, st>>>(g, pts + j0, cnt, prm, A, B);
-    OH_LAUNCH_CHECK();
-    pc_direct_f32<<<grid, kPcTX * kPcTY, 0, st>>>(g, pts + j0, prm, A, B, cnt, (float2*)field, (float*)fringe, j0 > 0);
+    {
+      KernelTimer kt(ctx, "pc_tables", st);
+      pc_tables<<<1024, 256, 0, st>>>(g, pts + j0, cnt, prm, A, B, RY, E);
+      OH_LAUNCH_CHECK();
+    }
+    KernelTimer kt(ctx, "pc_direct_f32", st);
+    pc_direct_f32<<<grid, kPcTX * kPcTY, 0, st>>>(g, prm, A, B, RY, E, cnt, (float2*)field, (float*)fringe, j0 > 0);
     OH_LAUNCH_CHECK();
   }
   return OH_OK;

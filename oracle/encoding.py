@@ -71,7 +71,7 @@ def two_phase(U):
     U = U / np.abs(U).max()
     amp = np.abs(U)
     phase = np.angle(U) + np.pi
-    d = np.arccos(amp)
+    d = np.arccos(np.minimum(amp, 1.0))     # real part of MATLAB's acos for a rounding-level 1+eps
     out = np.zeros((ny, 2 * nx))
     out[:, 0::2] = phase + d
     out[:, 1::2] = phase - d

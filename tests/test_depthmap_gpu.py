@@ -90,7 +90,7 @@ def test_seeded_phase_mode(ctx, dev):
     dict(num_of_depth=16),                                   # repeated-addition level quirk
     dict(num_of_depth=256, flag_change_depth_quantization=0),  # 256 - d layer index
     dict(num_of_depth=8, render_depth=[3, 5, 5, 8]),           # subset with a duplicate level
-    dict(num_of_depth=1),
+    dict(num_of_depth=1, near=0.1, far=0.3),                # one level at far-near, bin width (far+near)/2
     dict(num_of_depth=6, sig_location=(1, 0)),
     dict(num_of_depth=6, sig_location=(-1, -1)),
 ])
