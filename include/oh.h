@@ -70,6 +70,10 @@ oh_status   oh_ctx_set_timing(oh_ctx* ctx, int on);
 int         oh_ctx_read_timing(oh_ctx* ctx, int reset, const char** names,
                                double* ms, long* launches, int cap);
 const char* oh_version(void);
+/* Synchronises `stream` and reports OH_ERR_TIMEOUT if a kernel of this
+ * context gave up a bounded wait since the last check (the flag is then
+ * cleared); OH_OK otherwise. */
+oh_status   oh_ctx_device_status(oh_ctx* ctx, void* stream);
 
 /* ---- FFT ----------------------------------------------------------------
  * Mixed-radix complex FFT (radices 2,3,4,5,8 + generic odd prime), computed

@@ -71,6 +71,7 @@ SIGNATURES = {
     "oh_kernel_launch_count": (C.c_uint64, []),
     "oh_version": (C.c_char_p, []),
     "oh_ctx_set_timing": (_i, [_vp, _i]),
+    "oh_ctx_device_status": (_i, [_vp, _vp]),
     "oh_ctx_read_timing": (_i, [_vp, _i, C.POINTER(C.c_char_p), C.POINTER(_d), C.POINTER(C.c_long), _i]),
     "oh_fft_supported": (_i, [_i, _i]),
     "oh_fft2d": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _i, _i, _vp]),

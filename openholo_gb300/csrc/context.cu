@@ -217,8 +217,10 @@ oh_status oh_ctx_create(oh_ctx** ctx, int device) {
   oh_ctx* c = new oh_ctx();
   c->device = device;
   e = cudaEventCreateWithFlags(&c->last_done, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaMalloc(&c->dev_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(c->dev_err, 0, sizeof(int));
   cudaSetDevice(prev);
-  if (e != cudaSuccess) { delete c; return cuda_fail(e, "cudaEventCreate"); }
+  if (e != cudaSuccess) { delete c; return cuda_fail(e, "context set-up"); }
   *ctx = c;
   return OH_OK;
 }
@@ -234,6 +236,7 @@ oh_status oh_ctx_destroy(oh_ctx* ctx) {
   for (auto& m : ctx->marks) { cudaEventDestroy(m.a); cudaEventDestroy(m.b); }
   for (auto e : ctx->event_pool) cudaEventDestroy(e);
   cudaEventDestroy(ctx->last_done);
+  cudaFree(ctx->dev_err);
   cudaSetDevice(prev);
   delete ctx;
   return OH_OK;
@@ -273,6 +276,20 @@ const char* oh_status_string(oh_status s) {
 }
 
 const char* oh_last_error(void) { return t_last_error.c_str(); }
+
+oh_status oh_ctx_device_status(oh_ctx* ctx, void* stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  CallScope cs(ctx, st);
+  OH_TRY(cs.status());
+  int h = 0;
+  OH_CUDA_TRY(cudaMemcpyAsync(&h, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  OH_CUDA_TRY(cudaStreamSynchronize(st));
+  if (h) {
+    OH_CUDA_TRY(cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), st));
+    return fail(OH_ERR_TIMEOUT, "a bounded device-side wait ran out (copy into shared memory did not complete)");
+  }
+  return OH_OK;
+}
 
 oh_status oh_ctx_set_timing(oh_ctx* ctx, int on) {
   if (!ctx) return fail(OH_ERR_INVALID_ARG, "null context");

@@ -76,6 +76,8 @@ struct DMArgs {
   C* field;              // [pny][pnx] or null
   C* spectrum;           // [Py][Px] or null
   int sig_x, sig_y;
+  int occ_stride;        // bytes per layer row of occ (multiple of 16)
+  int* err;              // device error word (bounded waits that ran out)
   FFTPlan plx, ply;
 };
 
@@ -167,10 +169,13 @@ __global__ void __launch_bounds__(256) dm_row_pass(DMArgs<R> a) {
   C* buf = reinterpret_cast<C*>(smem_raw);
   C* v = buf + a.Px;
   int16_t* li = reinterpret_cast<int16_t*>(v + a.pnx);
-  uint32_t* mask = reinterpret_cast<uint32_t*>(li + ((a.pnx + 1) & ~1));
+  uint32_t* mask = reinterpret_cast<uint32_t*>(li + ((a.pnx + 7) & ~7));   // keeps 16-byte alignment
+  C* twlo = reinterpret_cast<C*>(mask + 8);          // 64 + ceil(Px/64) twiddles (fast path)
+  C* twhi = twlo + 64;
   const int r = blockIdx.x;
   const int nwords = (a.n_uslots + 31) >> 5;
   for (int i = threadIdx.x; i < nwords; i += blockDim.x) mask[i] = 0u;
+  if constexpr (NX > 0) load_tw_split(twlo, twhi, static_cast<const C*>(a.plx.tw), NX);
   __syncthreads();
   const size_t rowoff = (size_t)r * a.pnx;
   for (int c = threadIdx.x; c < a.pnx; c += blockDim.x) {
@@ -198,7 +203,7 @@ __global__ void __launch_bounds__(256) dm_row_pass(DMArgs<R> a) {
   for (int u = 0; u < a.n_uslots; ++u) {
     const bool present = (mask[u >> 5] >> (u & 31)) & 1u;
     if (threadIdx.x == 0) {
-      a.occ[(size_t)u * a.pny + r] = present ? 1 : 0;
+      a.occ[(size_t)u * a.occ_stride + r] = present ? 1 : 0;
       if (present) a.slot_any[u] = 1;
     }
     if (!present) continue;
@@ -210,7 +215,12 @@ __global__ void __launch_bounds__(256) dm_row_pass(DMArgs<R> a) {
       if (c >= 0 && c < a.pnx && li[c] == u) val = v[c];
       buf[j] = val;
     }
-    block_fft_n<NX, -1>(buf, 1, a.Px, 1, a.plx, false);
+    if constexpr (NX > 0) {
+      FastSched<NX>::template run_t<-1>(buf, 1, a.Px, 1, TwSplit<C>{twlo, twhi}, false);
+      __syncthreads();
+    } else {
+      block_fft<-1>(buf, 1, a.Px, 1, a.plx, false);
+    }
     C* dst = a.Rbuf + (size_t)u * a.nstrips * a.pny * a.W;
     for (int kx = threadIdx.x; kx < a.Px; kx += blockDim.x) {
       int m = kx - a.hx; if (m < 0) m += a.Px;       // S[kx] = A[(kx - hx) mod Px]
@@ -248,7 +258,7 @@ __global__ void __launch_bounds__(512) dm_col_pass(DMArgs<R> a) {
   for (int e = 0; e < a.n_entries; ++e) {
     const int u = a.uslot_of_entry[e];
     if (!a.slot_any[u]) continue;
-    const uint8_t* occ = a.occ + (size_t)u * a.pny;
+    const uint8_t* occ = a.occ + (size_t)u * a.occ_stride;
     const C* src = a.Rbuf + ((size_t)u * a.nstrips + s) * a.pny * W;
     for (int idx = threadIdx.x; idx < nel; idx += T) {
       const int i = idx / W, w = idx - i * W;
@@ -327,13 +337,21 @@ __global__ void __launch_bounds__(256) dm_out_pass(DMArgs<R> a) {
   typedef typename cplx_of<R>::type C;
   extern __shared__ unsigned char smem_raw[];
   C* buf = reinterpret_cast<C*>(smem_raw);
+  C* twlo = buf + a.Px;
+  C* twhi = twlo + 64;
   const int yl = blockIdx.x;
   const C* row = a.V + (size_t)yl * a.Px;
+  if constexpr (NX > 0) load_tw_split(twlo, twhi, static_cast<const C*>(a.plx.tw), NX);
   for (int j = threadIdx.x; j < a.Px; j += blockDim.x) {
     int kx = j - a.hx; if (kx < 0) kx += a.Px;
     buf[j] = row[kx];
   }
-  block_fft_n<NX, 1>(buf, 1, a.Px, 1, a.plx, false);
+  if constexpr (NX > 0) {
+    FastSched<NX>::template run_t<1>(buf, 1, a.Px, 1, TwSplit<C>{twlo, twhi}, false);
+    __syncthreads();
+  } else {
+    block_fft<1>(buf, 1, a.Px, 1, a.plx, false);
+  }
   for (int c = threadIdx.x; c < a.pnx; c += blockDim.x) {
     int m = a.ox + c - a.hx; if (m < 0) m += a.Px;
     C h = buf[a.plx.perm[m]];
@@ -342,6 +360,10 @@ __global__ void __launch_bounds__(256) dm_out_pass(DMArgs<R> a) {
     if (a.field) a.field[(size_t)yl * a.pnx + c] = h;
   }
 }
+
+}  // namespace oh
+#include "dm_col_fast.cuh"
+namespace oh {
 
 // ---------------------------------------------------------------------------
 // host side
@@ -486,18 +508,35 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
 
   const size_t smax = max_smem_per_block();
   const int T = 512;
-  int W = 0;
-  for (int cand : {8, 4, 2, 1}) {
-    if (a.Px % cand) continue;
-    size_t sm = (size_t)cand * a.Py * sizeof(C) + cand * (sizeof(C) + sizeof(R)) + (size_t)a.Py * sizeof(int);
-    if (sm <= smax && cand * a.Py <= T * KMAX) { W = cand; break; }
+  const int occ_stride = (a.pny + 15) & ~15;
+  a.occ_stride = occ_stride;
+  a.err = ctx->dev_err;
+  // FP32 with a compile-time FFT length: bulk-copy pipelined column pass
+  // (dm_col_fast) with the widest strip whose shared-memory layout fits
+  int Wfast = 0;
+  bool fastlen = false;
+  with_fast_n(a.Py, [&](auto nc) { fastlen = decltype(nc)::value > 0; });
+  if (prec == 0 && fastlen) {
+    for (int cand : {4, 2}) {
+      if (a.Px % cand) continue;
+      if ((size_t)col_layout(a.Py, a.pny, cand, occ_stride, su.n_entries).total <= smax) { Wfast = cand; break; }
+    }
+  }
+  int W = Wfast;
+  if (W == 0) {
+    for (int cand : {8, 4, 2, 1}) {
+      if (a.Px % cand) continue;
+      size_t sm = (size_t)cand * a.Py * sizeof(C) + cand * (sizeof(C) + sizeof(R)) + (size_t)a.Py * sizeof(int);
+      if (sm <= smax && cand * a.Py <= T * KMAX) { W = cand; break; }
+    }
   }
   if (W == 0) return fail(OH_ERR_UNSUPPORTED_SIZE, "padded column length " + std::to_string(a.Py) + " too long for the column pass");
   a.W = W; a.nstrips = a.Px / W;
-  const size_t smem_col = (size_t)W * a.Py * sizeof(C) + W * (sizeof(C) + sizeof(R)) + (size_t)a.Py * sizeof(int);
-  const size_t smem_row = (size_t)a.Px * sizeof(C) + (size_t)a.pnx * sizeof(C) + (size_t)((a.pnx + 1) & ~1) * sizeof(int16_t) +
-                          (size_t)((su.n_uslots + 31) / 32) * sizeof(uint32_t);
-  const size_t smem_out = (size_t)a.Px * sizeof(C);
+  const size_t smem_col = Wfast ? (size_t)col_layout(a.Py, a.pny, W, occ_stride, su.n_entries).total
+                                : (size_t)W * a.Py * sizeof(C) + W * (sizeof(C) + sizeof(R)) + (size_t)a.Py * sizeof(int);
+  const size_t smem_row = (size_t)a.Px * sizeof(C) + (size_t)a.pnx * sizeof(C) + (size_t)((a.pnx + 7) & ~7) * sizeof(int16_t) +
+                          8 * sizeof(uint32_t) + (64 + (size_t)(a.Px + 63) / 64) * sizeof(C);
+  const size_t smem_out = (size_t)a.Px * sizeof(C) + (64 + (size_t)(a.Px + 63) / 64) * sizeof(C);
   if (smem_row > smax || smem_out > smax) return fail(OH_ERR_UNSUPPORTED_SIZE, "padded row length " + std::to_string(a.Px) + " exceeds shared memory");
 
   // scratch
@@ -505,7 +544,7 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   const size_t nE = su.n_entries, nU = su.n_uslots;
   OH_TRY(scratch(ctx, "dm.R", nU * a.pny * (size_t)a.Px * sizeof(C), &ptr)); a.Rbuf = (C*)ptr;
   OH_TRY(scratch(ctx, "dm.V", (size_t)a.pny * a.Px * sizeof(C), &ptr)); a.V = (C*)ptr;
-  OH_TRY(scratch(ctx, "dm.occ", nU * a.pny + 16, &ptr)); a.occ = (uint8_t*)ptr;
+  OH_TRY(scratch(ctx, "dm.occ", nU * (size_t)occ_stride + 16, &ptr)); a.occ = (uint8_t*)ptr;
   // small tables share one buffer
   size_t off = 0;
   auto carve = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; };
@@ -539,17 +578,34 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
     if (e != cudaSuccess) rs = cuda_fail(e, "dm_row_pass launch");
   });
   OH_TRY(rs);
-  with_fast_n_if<sizeof(R) == 4>(a.Py, [&](auto nc) {
-    constexpr int NY = decltype(nc)::value;
-    cudaError_t e = cudaFuncSetAttribute(dm_col_pass<R, KMAX, NY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col);
-    if (e != cudaSuccess) { rs = cuda_fail(e, "cudaFuncSetAttribute(dm_col_pass)"); return; }
+  if constexpr (sizeof(R) == 4) {
+    if (Wfast) {
+      with_fast_n(a.Py, [&](auto nc) {
+        constexpr int NY = decltype(nc)::value;
+        if constexpr (NY > 0) {
+          auto launch = [&](auto wc) {
+            constexpr int WW = decltype(wc)::value;
+            cudaError_t e = cudaFuncSetAttribute(dm_col_fast<NY, WW, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col);
+            if (e != cudaSuccess) { rs = cuda_fail(e, "cudaFuncSetAttribute(dm_col_fast)"); return; }
+            KernelTimer kt(ctx, "dm_col_pass", st);
+            dm_col_fast<NY, WW, 512><<<a.nstrips, 512, smem_col, st>>>(a);
+            note_launch();
+            if ((e = cudaGetLastError()) != cudaSuccess) rs = cuda_fail(e, "dm_col_fast launch");
+          };
+          if (Wfast == 4) launch(std::integral_constant<int, 4>{});
+          else launch(std::integral_constant<int, 2>{});
+        }
+      });
+      OH_TRY(rs);
+    }
+  }
+  if (!Wfast) {
+    cudaError_t e = cudaFuncSetAttribute(dm_col_pass<R, KMAX, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(dm_col_pass)");
     KernelTimer kt(ctx, prec ? "dm_col_pass_f64" : "dm_col_pass", st);
-    dm_col_pass<R, KMAX, NY><<<a.nstrips, T, smem_col, st>>>(a);
-    note_launch();
-    e = cudaGetLastError();
-    if (e != cudaSuccess) rs = cuda_fail(e, "dm_col_pass launch");
-  });
-  OH_TRY(rs);
+    dm_col_pass<R, KMAX, 0><<<a.nstrips, T, smem_col, st>>>(a);
+    OH_LAUNCH_CHECK();
+  }
   with_fast_n_if<sizeof(R) == 4>(a.Px, [&](auto nc) {
     constexpr int NX = decltype(nc)::value;
     cudaError_t e = cudaFuncSetAttribute(dm_out_pass<R, NX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_out);

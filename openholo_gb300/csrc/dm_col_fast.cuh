@@ -1,0 +1,251 @@
+// Fast column pass of the depth-map pipeline (FP32, compile-time FFT length).
+//
+// One block owns a strip of W spectrum columns for the whole frame.  For each
+// non-empty layer it
+//   1. waits for the layer's data in a shared-memory staging buffer: the
+//      strip of row-pass output (pny x W complex, contiguous), the row
+//      occupancy flags and the layer's Ey row.  One thread issues the three
+//      copies with cp.async.bulk on an mbarrier one layer ahead (double
+//      buffered), so the loads overlap the previous layer's FFT;
+//   2. runs FFT stage 0 straight from the staging buffer (only the pny image
+//      rows are read; padded rows are implicit zeros) into the work buffer,
+//      then the remaining stages in place, twiddles from a two-level
+//      shared-memory table;
+//   3. multiplies by the layer's transfer function and accumulates into
+//      registers (fixed element ownership across layers).
+// The epilogue applies the SSB crop, the inverse y-FFT and the y shift phase
+// and writes the pny output rows of the strip.
+//
+// Every mbarrier wait is bounded (about one second of SM clock); on timeout
+// the block sets the frame's error word, waits (bounded) for its own copies
+// still in flight and leaves the layer loop.
+#pragma once
+#include "fft_fast.cuh"
+
+namespace oh {
+
+struct ColLayout {
+  int buf, stg0, stg1, ey0, ey1, occ0, occ1, lfy, kyp, twlo, twhi, exw, lfxw, list, mbar, total;
+};
+
+__host__ __device__ inline int col_take(int* o, int bytes) {
+  const int r = *o;
+  *o += (bytes + 127) & ~127;
+  return r;
+}
+
+__host__ __device__ inline ColLayout col_layout(int Py, int pny, int W, int occ_stride, int n_entries) {
+  ColLayout L;
+  int o = 0;
+  L.buf = col_take(&o, Py * W * 8);
+  L.stg0 = col_take(&o, pny * W * 8);
+  L.stg1 = col_take(&o, pny * W * 8);
+  L.ey0 = col_take(&o, Py * 8);
+  L.ey1 = col_take(&o, Py * 8);
+  L.occ0 = col_take(&o, occ_stride);
+  L.occ1 = col_take(&o, occ_stride);
+  L.lfy = col_take(&o, Py * 4);
+  L.kyp = col_take(&o, Py * 2);
+  L.twlo = col_take(&o, 64 * 8);
+  L.twhi = col_take(&o, ((Py + 63) / 64) * 8);
+  L.exw = col_take(&o, W * 8);
+  L.lfxw = col_take(&o, W * 4);
+  L.list = col_take(&o, n_entries * 2 + 2);
+  L.mbar = col_take(&o, 16);
+  L.total = o;
+  return L;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t n) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(n) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* b) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(b))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Wait for the phase with the given parity; give up after ~1 s of SM clock.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* b, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(b, parity)) {
+    if (clock64() - t0 > 2000000000LL) return false;
+  }
+  return true;
+}
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+template <int NY, int W, int T>
+__global__ void __launch_bounds__(T) dm_col_fast(DMArgs<float> a) {
+  typedef float2 C;
+  constexpr int R0 = FastSched<NY>::r0;
+  constexpr int Q0 = NY / R0;
+  constexpr int NEL = NY * W;
+  constexpr int KM = (NEL + T - 1) / T;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const ColLayout Lo = col_layout(NY, a.pny, W, a.occ_stride, a.n_entries);
+  C* buf = reinterpret_cast<C*>(smem + Lo.buf);
+  // staging buffers are selected with conditionals (no dynamically indexed local arrays)
+  C* const stg0 = reinterpret_cast<C*>(smem + Lo.stg0);
+  C* const stg1 = reinterpret_cast<C*>(smem + Lo.stg1);
+  C* const ey0 = reinterpret_cast<C*>(smem + Lo.ey0);
+  C* const ey1 = reinterpret_cast<C*>(smem + Lo.ey1);
+  uint8_t* const occ0 = smem + Lo.occ0;
+  uint8_t* const occ1 = smem + Lo.occ1;
+  float* lfy = reinterpret_cast<float*>(smem + Lo.lfy);
+  int16_t* kyp = reinterpret_cast<int16_t*>(smem + Lo.kyp);
+  C* twlo = reinterpret_cast<C*>(smem + Lo.twlo);
+  C* twhi = reinterpret_cast<C*>(smem + Lo.twhi);
+  C* exw = reinterpret_cast<C*>(smem + Lo.exw);
+  float* lfxw = reinterpret_cast<float*>(smem + Lo.lfxw);
+  int16_t* list = reinterpret_cast<int16_t*>(smem + Lo.list);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + Lo.mbar);
+  __shared__ int s_nact;
+
+  const int tid = threadIdx.x;
+  const int s = blockIdx.x;
+  const int kx0 = s * W;
+  const int pny = a.pny;
+  if (tid == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    fence_mbar_init();
+    int n = 0;
+    for (int e = 0; e < a.n_entries; ++e)
+      if (a.slot_any[a.uslot_of_entry[e]]) list[n++] = (int16_t)e;
+    s_nact = n;
+  }
+  load_tw_split(twlo, twhi, static_cast<const C*>(a.ply.tw), NY);
+  for (int p = tid; p < NY; p += T) {
+    int ky = a.ply.iperm[p] + a.hy;
+    if (ky >= NY) ky -= NY;
+    kyp[p] = (int16_t)ky;
+    lfy[p] = a.lfy[p];
+  }
+  if (tid < W) lfxw[tid] = a.lfx[kx0 + tid];
+  __syncthreads();
+  const int nact = s_nact;
+  const TwSplit<C> tw{twlo, twhi};
+  const uint32_t strip_bytes = (uint32_t)(pny * W * 8);
+  const uint32_t layer_bytes = strip_bytes + (uint32_t)a.occ_stride + (uint32_t)(NY * 8);
+
+  auto issue = [&](int k, int bi) {
+    const int e = list[k];
+    const int u = a.uslot_of_entry[e];
+    uint64_t* bar = bi ? &mbar[1] : &mbar[0];
+    mbar_expect_tx(bar, layer_bytes);
+    bulk_g2s(bi ? stg1 : stg0, a.Rbuf + ((size_t)u * a.nstrips + s) * pny * W, strip_bytes, bar);
+    bulk_g2s(bi ? occ1 : occ0, a.occ + (size_t)u * a.occ_stride, (uint32_t)a.occ_stride, bar);
+    bulk_g2s(bi ? ey1 : ey0, a.ey + (size_t)e * NY, (uint32_t)(NY * 8), bar);
+  };
+  if (tid == 0 && nact > 0) issue(0, 0);
+
+  C acc[KM];
+#pragma unroll
+  for (int k = 0; k < KM; ++k) acc[k] = make_float2(0.f, 0.f);
+
+  for (int k = 0; k < nact; ++k) {
+    const int bi = k & 1;
+    if (tid == 0 && k + 1 < nact) {
+      fence_proxy_async_smem();
+      issue(k + 1, bi ^ 1);
+    }
+    uint64_t* const bar = bi ? &mbar[1] : &mbar[0];
+    uint64_t* const bar_next = bi ? &mbar[0] : &mbar[1];
+    const bool ok = mbar_wait_bounded(bar, (uint32_t)((k >> 1) & 1));
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) atomicOr(a.err, 1);
+      // let the copies of this block that may still be in flight land
+      mbar_wait_bounded(bar, (uint32_t)((k >> 1) & 1));
+      if (k + 1 < nact) mbar_wait_bounded(bar_next, (uint32_t)(((k + 1) >> 1) & 1));
+      return;
+    }
+    const int e = list[k];
+    if (tid < W) exw[tid] = a.exc[(size_t)e * a.Px + kx0 + tid];
+    const C* sg = bi ? stg1 : stg0;
+    const uint8_t* oc = bi ? occ1 : occ0;
+    // stage 0 from the staging buffer: inputs j + t*Q0 of the y-shifted line
+    for (int idx = tid; idx < Q0 * W; idx += T) {
+      const int j = idx / W, w = idx - j * W;
+      C x[R0];
+#pragma unroll
+      for (int t = 0; t < R0; ++t) {
+        int y = j + t * Q0 - a.hy;
+        if (y < 0) y += NY;
+        const int yl = y - a.oy;
+        C v = make_float2(0.f, 0.f);
+        if (yl >= 0 && yl < pny && oc[yl]) v = sg[yl * W + w];
+        x[t] = v;
+      }
+      DFT<R0, -1, C>::run(x);
+      if (j) {
+#pragma unroll
+        for (int f = 1; f < R0; ++f) x[f] = cmul(x[f], twid<-1, C>(tw, j * f));
+      }
+#pragma unroll
+      for (int f = 0; f < R0; ++f) buf[(j + f * Q0) * W + w] = x[f];
+    }
+    FastSched<NY>::template run_rest<-1>(buf, W, 1, W, tw, true);
+    __syncthreads();
+    const float kz = a.kzp[e];
+    const C* ey = bi ? ey1 : ey0;
+#pragma unroll
+    for (int kk = 0; kk < KM; ++kk) {
+      const int idx = tid + kk * T;
+      if (idx < NEL) {
+        const int p = idx / W, w = idx - p * W;
+        const int ky = kyp[p];
+        const float sv = lfxw[w] + lfy[ky];
+        const float rt = sqrtf(1.f - sv);
+        const float den = 1.f + rt;
+        const float psi = kz * sv * sv * __fdividef(0.5f, den * den);
+        float sn, cs;
+        __sincosf(psi, &sn, &cs);
+        const C h = cmul(cmul(exw[w], ey[ky]), make_float2(cs, sn));
+        acc[kk] = cadd(acc[kk], cmul(h, buf[idx]));
+      }
+    }
+    __syncthreads();
+  }
+
+  // SSB crop and inverse y-FFT input order: spectrum row ky -> i = (ky + hy) mod NY
+#pragma unroll
+  for (int kk = 0; kk < KM; ++kk) {
+    const int idx = tid + kk * T;
+    if (idx < NEL) {
+      const int p = idx / W, w = idx - p * W;
+      const int ky = kyp[p];
+      const int kx = kx0 + w;
+      if (a.spectrum) a.spectrum[(size_t)ky * a.Px + kx] = acc[kk];
+      const bool keep = kx >= a.cx1 && kx <= a.cx2 && ky >= a.cy1 && ky <= a.cy2;
+      int i = ky + a.hy;
+      if (i >= NY) i -= NY;
+      buf[i * W + w] = keep ? acc[kk] : make_float2(0.f, 0.f);
+    }
+  }
+  FastSched<NY>::template run_t<1>(buf, W, 1, W, tw, true);
+  __syncthreads();
+  for (int idx = tid; idx < pny * W; idx += T) {
+    const int yl = idx / W, w = idx - yl * W;
+    int m = a.oy + yl - a.hy;
+    if (m < 0) m += NY;
+    a.V[(size_t)yl * a.Px + kx0 + w] = cmul(buf[a.ply.perm[m] * W + w], a.shy[yl]);
+  }
+}
+
+}  // namespace oh

@@ -159,7 +159,64 @@ template <int SGN, typename C> struct DFT<30, SGN, C> {
   __device__ __forceinline__ static void run(C* x) { dft_pfa<2, 15, SGN>(x); }
 };
 
+// ---- twiddle sources: W_N^e = exp(-2 pi i e / N) ------------------------
+
+template <typename C> struct TwTable {            // full table (global or shared)
+  const C* t;
+  __device__ __forceinline__ C operator()(int e) const { return t[e]; }
+};
+template <typename C> struct TwSplit {            // W^e = W^(64 (e>>6)) * W^(e & 63)
+  const C* lo;                                    // lo[m] = W_N^m, m < 64
+  const C* hi;                                    // hi[m] = W_N^(64 m)
+  __device__ __forceinline__ C operator()(int e) const { return cmul(hi[e >> 6], lo[e & 63]); }
+};
+// fill lo/hi (shared memory) from a full table; call with all threads, then sync
+template <typename C>
+__device__ __forceinline__ void load_tw_split(C* lo, C* hi, const C* tw, int n) {
+  for (int m = threadIdx.x; m < 64; m += blockDim.x) lo[m] = m < n ? tw[m] : tw[0];
+  for (int m = threadIdx.x; m < (n + 63) / 64; m += blockDim.x) hi[m] = tw[64 * m];
+}
+template <int SGN, typename C, class TW>
+__device__ __forceinline__ C twid(const TW& tw, int e) {
+  C w = tw(e);
+  if (SGN > 0) w.y = -w.y;
+  return w;
+}
+
 // ---- one stage --------------------------------------------------------------
+
+template <int N, int R, int M, int SGN, typename C, class TW>
+__device__ __forceinline__ void fstage_t(C* buf, int nl, int ls, int es, const TW& tw, bool line_fastest) {
+  constexpr int Q = M / R;
+  constexpr int TWS = N / M;
+  constexpr int NB = N / R;
+  const int total = NB * nl;
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    int line, b;
+    if (line_fastest) { b = idx / nl; line = idx - b * nl; }
+    else { line = idx / NB; b = idx - line * NB; }
+    const int blk = b / Q, j = b - blk * Q;
+    const int base = line * ls + (blk * M + j) * es;
+    const int st = Q * es;
+    C x[R];
+#pragma unroll
+    for (int t = 0; t < R; ++t) x[t] = buf[base + t * st];
+    DFT<R, SGN, C>::run(x);
+    if (Q > 1 && j) {
+#pragma unroll
+      for (int f = 1; f < R; ++f) x[f] = cmul(x[f], twid<SGN, C>(tw, j * f * TWS));
+    }
+#pragma unroll
+    for (int t = 0; t < R; ++t) buf[base + t * st] = x[t];
+  }
+}
+
+template <int N, int M, int SGN, typename C, class TW, int R, int... Rest>
+__device__ __forceinline__ void fstages_t(C* buf, int nl, int ls, int es, const TW& tw, bool line_fastest) {
+  __syncthreads();
+  fstage_t<N, R, M, SGN>(buf, nl, ls, es, tw, line_fastest);
+  if constexpr (sizeof...(Rest) > 0) fstages_t<N, M / R, SGN, C, TW, Rest...>(buf, nl, ls, es, tw, line_fastest);
+}
 
 template <int N, int R, int M, int SGN, typename C>
 __device__ __forceinline__ void fstage(C* buf, int nl, int ls, int es, const C* __restrict__ tw,
@@ -195,16 +252,29 @@ __device__ __forceinline__ void fstages(C* buf, int nl, int ls, int es, const C*
   if constexpr (sizeof...(Rest) > 0) fstages<N, M / R, SGN, C, Rest...>(buf, nl, ls, es, tw, line_fastest);
 }
 
+template <int N, int R0, int... Rest>
+struct SchedImpl {
+  static constexpr bool ok = true;
+  static constexpr int r0 = R0;
+  template <int SGN, typename C>
+  __device__ __forceinline__ static void run(C* buf, int nl, int ls, int es, const C* tw, bool lf) {
+    fstages<N, N, SGN, C, R0, Rest...>(buf, nl, ls, es, tw, lf);
+  }
+  // all stages with a twiddle functor
+  template <int SGN, typename C, class TW>
+  __device__ __forceinline__ static void run_t(C* buf, int nl, int ls, int es, const TW& tw, bool lf) {
+    fstages_t<N, N, SGN, C, TW, R0, Rest...>(buf, nl, ls, es, tw, lf);
+  }
+  // every stage after the first (the caller ran stage 0 itself)
+  template <int SGN, typename C, class TW>
+  __device__ __forceinline__ static void run_rest(C* buf, int nl, int ls, int es, const TW& tw, bool lf) {
+    if constexpr (sizeof...(Rest) > 0) fstages_t<N, N / R0, SGN, C, TW, Rest...>(buf, nl, ls, es, tw, lf);
+  }
+};
+
 template <int N> struct FastSched { static constexpr bool ok = false; };
-#define OH_DEFINE_SCHED(n, ...)                                                   \
-  template <> struct FastSched<n> {                                               \
-    static constexpr bool ok = true;                                              \
-    template <int SGN, typename C>                                                \
-    __device__ __forceinline__ static void run(C* buf, int nl, int ls, int es,    \
-                                               const C* tw, bool lf) {            \
-      fstages<n, n, SGN, C, __VA_ARGS__>(buf, nl, ls, es, tw, lf);               \
-    }                                                                             \
-  };
+#define OH_DEFINE_SCHED(n, ...) \
+  template <> struct FastSched<n> : SchedImpl<n, __VA_ARGS__> {};
 OH_FAST_SCHEDULES(OH_DEFINE_SCHED)
 #undef OH_DEFINE_SCHED
 

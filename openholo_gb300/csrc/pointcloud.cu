@@ -9,16 +9,17 @@
 //
 // FP32 path: k r_j reaches 1e6 rad, far beyond float resolution, so the
 // phase is split exactly into FP64-reduced tables plus a small FP32 residual.
-// With r_y = sqrt((Y-y)^2 + z^2) (per point and row) and a per-point anchor
-// distance rb = sqrt(y^2 + z^2) (the SLM-centre row):
-//   k r = k dx^2/(2 rb) - k X sin tx                      table A[point][col]
-//       + k r_y        - k Y sin ty                      table B[point][row]
-//       + k dx^2 (2 rb - r - r_y) / (2 rb (r + r_y))     FP32 residual
-// since r - r_y = dx^2/(r + r_y).  The residual is evaluated without
-// cancellation as (k/(2rb)) dx^2 (-2E - dx^2/(r+r_y)) / (r+r_y) with
-// E = r_y - rb tabulated per point and row; it stays at a few rad both for
-// paraxial scenes and for strongly off-axis ones such as the KETI sample
-// (points tens of mm off-axis at 5 mm depth).
+// With a per-point anchor distance rb = sqrt(y^2 + z^2) (SLM-centre row),
+//   r_y = sqrt(dy^2 + z^2)   (per point and row),
+//   r_x = sqrt(dx^2 + rb^2)  (per point and column),
+//   k r = k (r_x - rb) - k X sin tx                  table A[point][col]
+//       + k r_y        - k Y sin ty                  table B[point][row]
+//       + k (r - r_y) - k (r_x - rb)                 FP32 residual
+// and, with E = r_y - rb (tabulated per point and row), the residual is
+// evaluated without cancellation as
+//   -k E dx^2 [(r_x + r) + (r_y + rb)] / ((r + r_y)(r_x + rb)(r_x + r)),
+// bounded by about k |E| / 2: a few rad for paraxial scenes, ~1e3 rad for
+// the strongly off-axis KETI sample over its full 1 mm SLM.
 // FP64 path: the direct formula in double precision.
 #include <cmath>
 #include <vector>
@@ -35,18 +36,18 @@ struct PCGeom {
 constexpr int kPcChunk = 32768;    // points per table chunk
 constexpr int kPcTX = 32, kPcTY = 8, kPcPts = 64;
 
-// Per point: x_j, k/(2 rb), amplitude; per point and column: A; per point
+// Per point: x_j, rb, amplitude; per point and column: A, r_x; per point
 // and row: B, r_y, E = r_y - rb.
 __global__ void pc_tables(PCGeom g, const float4* __restrict__ pts, int n, float4* __restrict__ prm,
-                          float* __restrict__ A, float* __restrict__ B, float* __restrict__ RY, float* __restrict__ E) {
+                          float* __restrict__ A, float* __restrict__ RX, float* __restrict__ B,
+                          float* __restrict__ RY, float* __restrict__ E) {
   const double two_pi = 6.283185307179586476925286766559;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int nthr = gridDim.x * blockDim.x;
   for (int j = tid; j < n; j += nthr) {
     float4 p = pts[j];
     double x = (double)p.x * g.sx, y = (double)p.y * g.sy, z = (double)p.z * g.sz + g.off;
-    double rb = sqrt(y * y + z * z);
-    prm[j] = make_float4((float)x, (float)(g.k / (2.0 * rb)), p.w, 0.f);
+    prm[j] = make_float4((float)x, (float)sqrt(y * y + z * z), p.w, 0.f);
   }
   for (long long idx = tid; idx < (long long)n * g.nx; idx += nthr) {
     int j = (int)(idx / g.nx), c = (int)(idx - (long long)j * g.nx);
@@ -55,9 +56,11 @@ __global__ void pc_tables(PCGeom g, const float4* __restrict__ pts, int n, float
     double rb = sqrt(y * y + z * z);
     double X = ((double)c + 0.5) * g.px - g.hlx;
     double dx = X - x;
-    double ph = g.k * dx * dx / (2.0 * rb) - g.k * X * g.stx;
+    double rx = sqrt(dx * dx + rb * rb);
+    double ph = g.k * (dx * dx / (rx + rb)) - g.k * X * g.stx;      // k (r_x - rb) - k X sin tx
     ph -= two_pi * rint(ph / two_pi);
     A[idx] = (float)ph;
+    RX[idx] = (float)rx;
   }
   for (long long idx = tid; idx < (long long)n * g.ny; idx += nthr) {
     int j = (int)(idx / g.ny), r = (int)(idx - (long long)j * g.ny);
@@ -77,11 +80,13 @@ __global__ void pc_tables(PCGeom g, const float4* __restrict__ pts, int n, float
 
 // One thread per pixel of a 32x8 tile; points streamed through shared memory.
 __global__ void __launch_bounds__(kPcTX * kPcTY) pc_direct_f32(PCGeom g, const float4* __restrict__ prm,
-                                                              const float* __restrict__ A, const float* __restrict__ B,
-                                                              const float* __restrict__ RY, const float* __restrict__ E,
-                                                              int n, float2* __restrict__ field,
-                                                              float* __restrict__ fringe, int accumulate_field) {
+                                                              const float* __restrict__ A, const float* __restrict__ RX,
+                                                              const float* __restrict__ B, const float* __restrict__ RY,
+                                                              const float* __restrict__ E, int n,
+                                                              float2* __restrict__ field, float* __restrict__ fringe,
+                                                              int accumulate_field) {
   __shared__ float sA[kPcPts][kPcTX];
+  __shared__ float sX[kPcPts][kPcTX];
   __shared__ float sB[kPcPts][kPcTY];
   __shared__ float sR[kPcPts][kPcTY];
   __shared__ float sE[kPcPts][kPcTY];
@@ -89,6 +94,7 @@ __global__ void __launch_bounds__(kPcTX * kPcTY) pc_direct_f32(PCGeom g, const f
   const int tx = threadIdx.x % kPcTX, ty = threadIdx.x / kPcTX;
   const int col = blockIdx.x * kPcTX + tx, row = blockIdx.y * kPcTY + ty;
   const float X = (float)(((double)col + 0.5) * g.px - g.hlx);
+  const float nk = (float)(-g.k);
   const float inv2pi = 0.15915494309189533577f, two_pi = 6.28318530717958647692f;
   float re = 0.f, im = 0.f;
   for (int j0 = 0; j0 < n; j0 += kPcPts) {
@@ -97,7 +103,9 @@ __global__ void __launch_bounds__(kPcTX * kPcTY) pc_direct_f32(PCGeom g, const f
     for (int i = threadIdx.x; i < cnt * kPcTX; i += blockDim.x) {
       int j = i / kPcTX, c = i - j * kPcTX;
       int cc = blockIdx.x * kPcTX + c;
-      sA[j][c] = cc < g.nx ? A[(size_t)(j0 + j) * g.nx + cc] : 0.f;
+      size_t o = (size_t)(j0 + j) * g.nx + cc;
+      sA[j][c] = cc < g.nx ? A[o] : 0.f;
+      sX[j][c] = cc < g.nx ? RX[o] : 1.f;
     }
     for (int i = threadIdx.x; i < cnt * kPcTY; i += blockDim.x) {
       int j = i / kPcTY, r = i - j * kPcTY;
@@ -114,11 +122,12 @@ __global__ void __launch_bounds__(kPcTX * kPcTY) pc_direct_f32(PCGeom g, const f
       const float4 p = sP[j];
       const float dx = X - p.x;
       const float dx2 = dx * dx;
-      const float ry = sR[j][ty];
+      const float ry = sR[j][ty], rx = sX[j][tx];
       const float r = sqrtf(fmaf(ry, ry, dx2));
-      const float inv = __fdividef(1.f, r + ry);
-      const float u = fmaf(-2.f, sE[j][ty], -dx2 * inv);
-      float ph = sA[j][tx] + sB[j][ty] + p.y * dx2 * u * inv;
+      const float num = (rx + r) + (ry + p.y);
+      const float den = (r + ry) * (rx + p.y) * (rx + r);
+      const float rem = nk * sE[j][ty] * dx2 * __fdividef(num, den);
+      float ph = sA[j][tx] + sB[j][ty] + rem;
       ph = fmaf(-two_pi, rintf(ph * inv2pi), ph);
       float sn, cs;
       __sincosf(ph, &sn, &cs);
@@ -207,21 +216,22 @@ oh_status pointcloud_enqueue(oh_ctx* ctx, int prec, const oh_pc_params* p, const
   }
   const int chunk = std::min(n, kPcChunk);
   void* ptr;
-  OH_TRY(scratch(ctx, "pc.tables", (size_t)chunk * (sizeof(float4) + sizeof(float) * (p->nx + 3 * (size_t)p->ny)) + 1024, &ptr));
+  OH_TRY(scratch(ctx, "pc.tables", (size_t)chunk * (sizeof(float4) + sizeof(float) * (2 * (size_t)p->nx + 3 * (size_t)p->ny)) + 1024, &ptr));
   float4* prm = (float4*)ptr;
   float* A = (float*)(prm + chunk);
-  float* B = A + (size_t)chunk * p->nx;
+  float* RX = A + (size_t)chunk * p->nx;
+  float* B = RX + (size_t)chunk * p->nx;
   float* RY = B + (size_t)chunk * p->ny;
   float* E = RY + (size_t)chunk * p->ny;
   for (int j0 = 0; j0 < n; j0 += chunk) {
     const int cnt = std::min(chunk, n - j0);
     {
       KernelTimer kt(ctx, "pc_tables", st);
-      pc_tables<<<1024, 256, 0, st>>>(g, pts + j0, cnt, prm, A, B, RY, E);
+      pc_tables<<<1024, 256, 0, st>>>(g, pts + j0, cnt, prm, A, RX, B, RY, E);
       OH_LAUNCH_CHECK();
     }
     KernelTimer kt(ctx, "pc_direct_f32", st);
-    pc_direct_f32<<<grid, kPcTX * kPcTY, 0, st>>>(g, prm, A, B, RY, E, cnt, (float2*)field, (float*)fringe, j0 > 0);
+    pc_direct_f32<<<grid, kPcTX * kPcTY, 0, st>>>(g, prm, A, RX, B, RY, E, cnt, (float2*)field, (float*)fringe, j0 > 0);
     OH_LAUNCH_CHECK();
   }
   return OH_OK;

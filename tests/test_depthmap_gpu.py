@@ -65,6 +65,22 @@ def test_depthmap_vs_oracle(ctx, dev, pad, precision):
     assert rel(fr, ref_fr) < tol
 
 
+@pytest.mark.parametrize("shape,pad,L", [((540, 960), 2, 12), ((512, 512), 2, 8), ((1080, 1920), 1, 6)])
+def test_fast_lengths_vs_oracle(ctx, dev, shape, pad, L):
+    """FFT grids with compile-time schedules (1920x1080, 1024x1024): the
+    bulk-copy pipelined column pass and the scheduled row/output passes."""
+    ny, nx = shape
+    img, depth = scenes.depthmap_scene(61, ny, nx)
+    p = dm.make_params(pnx=nx, pny=ny, num_of_depth=L, pad=pad, phase_mode=dm.OH_PHASE_SEEDED, seed=4)
+    fr, field = run(ctx, dev, img, depth, p, None, "fp32", want_field=True)
+    ref_fr, ref_field, _ = odm.generate(img, depth, oparams(p), phase=scenes.seeded_phase(4, ny, nx))
+    assert rel(field, ref_field) < TOL32
+    assert rel(fr, ref_fr) < TOL32
+    from openholo_gb300._lib import lib
+    import ctypes
+    assert lib().oh_ctx_device_status(ctx.handle, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)) == 0
+
+
 def test_reference_mode_matches_oracle(ctx, dev):
     """pad = 1, constant rand phase, viewing-window transform: the reference's own configuration."""
     ny, nx, L = 60, 96, 16
