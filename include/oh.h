@@ -184,6 +184,30 @@ oh_status oh_pointcloud_host(oh_ctx* ctx, oh_precision prec,
                              int n_points, void* field_host, void* fringe_host,
                              void* stream);
 
+/* Allocation-free point-cloud summation (FP32).  This entry point has no
+ * counterpart in the reference.  It exists for callers that cannot allocate
+ * device memory once they are running: an SLM or display loop working under
+ * a fixed device-memory budget, or a host framework that owns every device
+ * allocation through its own pool, where a cudaMalloc inside the library
+ * would synchronise the device or fail.  It takes no context and calls no
+ * cudaMalloc, cudaFree or other allocating routine: its working tables live
+ * in a file-scope device array of OH_PC_NOALLOC_SCRATCH_BYTES (16 MiB) that
+ * every GPU loading the library holds until the process exits.
+ *   - Limit: fields with 2*nx + 3*ny <= 65532 (at least 64 points per table
+ *     chunk); larger fields are rejected with OH_ERR_UNSUPPORTED_SIZE.  Any
+ *     number of points is accepted (processed in chunks).
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress) with that device current; make that first call
+ *     before any stream capture.
+ *   - Every call shares the one array and leaves the last call's tables in
+ *     it; calls that overlap on the GPU (different streams or host threads)
+ *     race on it.  Outputs are written in full (field) or accumulated
+ *     (fringe, as oh_pointcloud does), so no state needs clearing.
+ * Arguments and results are those of oh_pointcloud with OH_FP32. */
+#define OH_PC_NOALLOC_SCRATCH_BYTES (16u << 20)
+oh_status oh_pointcloud_noalloc(const oh_pc_params* p, const float* xyza, int n_points,
+                                void* field_out, void* fringe_out, void* stream);
+
 /* ---- WRP ------------------------------------------------------------------ */
 typedef struct oh_wrp_params {
   int    nx, ny;          /* WRP / hologram grid */

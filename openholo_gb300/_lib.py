@@ -83,6 +83,7 @@ SIGNATURES = {
     "oh_depthmap_levels": (_i, [C.POINTER(DepthmapParams), _vp, _vp]),
     "oh_pointcloud": (_i, [_vp, _i, C.POINTER(PcParams), _vp, _i, _vp, _vp, _vp]),
     "oh_pointcloud_host": (_i, [_vp, _i, C.POINTER(PcParams), _vp, _i, _vp, _vp, _vp]),
+    "oh_pointcloud_noalloc": (_i, [C.POINTER(PcParams), _vp, _i, _vp, _vp, _vp]),
     "oh_wrp_accumulate": (_i, [_vp, _i, C.POINTER(WrpParams), _vp, _i, _vp, _vp]),
     "oh_fresnel_propagate": (_i, [_vp, _i, _i, _i, _d, _d, _d, _vp, _vp]),
     "oh_encode": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp]),

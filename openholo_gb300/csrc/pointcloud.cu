@@ -22,6 +22,7 @@
 // the strongly off-axis KETI sample over its full 1 mm SLM.
 // FP64 path: the direct formula in double precision.
 #include <cmath>
+#include <mutex>
 #include <vector>
 #include "context.h"
 #include "fft_kernels.cuh"
@@ -237,11 +238,83 @@ oh_status pointcloud_enqueue(oh_ctx* ctx, int prec, const oh_pc_params* p, const
   return OH_OK;
 }
 
+// ---- allocation-free variant -------------------------------------------------
+// Scratch for oh_pointcloud_noalloc: the per-chunk phase tables live in this
+// file-scope device array (held by every GPU that loads the library).  Host
+// code must not use the symbol as a device address; set-up below looks the
+// address up once per device with cudaGetSymbolAddress.
+constexpr size_t kNoAllocScratchBytes = (size_t)OH_PC_NOALLOC_SCRATCH_BYTES;
+constexpr int kNoAllocMinChunk = 64;
+static __device__ __align__(256) unsigned char g_pc_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_ptr[kMaxDevices] = {nullptr};
+
+// Device address of the scratch array on the current device (first call on
+// a device does the lookup).
+static oh_status noalloc_scratch(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) return fail(OH_ERR_INVALID_ARG, "device index above the supported maximum");
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_pc_noalloc_scratch);
+    if (e != cudaSuccess || !p) return cuda_fail(e == cudaSuccess ? cudaErrorInvalidSymbol : e, "cudaGetSymbolAddress(point-cloud scratch)");
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return OH_OK;
+}
+
 }  // namespace oh
 
 using namespace oh;
 
 extern "C" {
+
+oh_status oh_pointcloud_noalloc(const oh_pc_params* p, const float* xyza, int n_points, void* field_out,
+                                void* fringe_out, void* stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  OH_TRY(validate_pc(p, n_points));
+  if (!field_out && !fringe_out) return fail(OH_ERR_INVALID_ARG, "need field_out or fringe_out");
+  if (n_points > 0 && !xyza) return fail(OH_ERR_INVALID_ARG, "null points");
+  // one chunk of tables needs 16 B + 4 B x (2 nx + 3 ny) per point
+  const size_t per_point = sizeof(float4) + sizeof(float) * (2 * (size_t)p->nx + 3 * (size_t)p->ny);
+  if (per_point * kNoAllocMinChunk > kNoAllocScratchBytes)
+    return fail(OH_ERR_UNSUPPORTED_SIZE, "oh_pointcloud_noalloc: field " + std::to_string(p->nx) + "x" + std::to_string(p->ny) +
+                                             " needs more than the fixed scratch of " + std::to_string(kNoAllocScratchBytes) +
+                                             " bytes (limit: 2*nx + 3*ny <= " +
+                                             std::to_string((kNoAllocScratchBytes / kNoAllocMinChunk - sizeof(float4)) / sizeof(float)) + ")");
+  void* base = nullptr;
+  OH_TRY(noalloc_scratch(&base));
+  PCGeom g = make_geom(p);
+  dim3 grid((p->nx + kPcTX - 1) / kPcTX, (p->ny + kPcTY - 1) / kPcTY);
+  const float4* pts = reinterpret_cast<const float4*>(xyza);
+  if (n_points == 0) {
+    if (field_out) OH_CUDA_TRY(cudaMemsetAsync(field_out, 0, (size_t)p->nx * p->ny * sizeof(float2), st));
+    return OH_OK;
+  }
+  const int chunk = (int)std::min<size_t>((size_t)n_points, kNoAllocScratchBytes / per_point);
+  float4* prm = (float4*)base;
+  float* A = (float*)(prm + chunk);
+  float* RX = A + (size_t)chunk * p->nx;
+  float* B = RX + (size_t)chunk * p->nx;
+  float* RY = B + (size_t)chunk * p->ny;
+  float* E = RY + (size_t)chunk * p->ny;
+  for (int j0 = 0; j0 < n_points; j0 += chunk) {
+    const int cnt = std::min(chunk, n_points - j0);
+    pc_tables<<<1024, 256, 0, st>>>(g, pts + j0, cnt, prm, A, RX, B, RY, E);
+    OH_LAUNCH_CHECK();
+    pc_direct_f32<<<grid, kPcTX * kPcTY, 0, st>>>(g, prm, A, RX, B, RY, E, cnt, (float2*)field_out, (float*)fringe_out,
+                                                  j0 > 0);
+    OH_LAUNCH_CHECK();
+  }
+  return OH_OK;
+}
+
 
 oh_status oh_pointcloud(oh_ctx* ctx, oh_precision prec, const oh_pc_params* p, const float* xyza, int n_points,
                         void* field_out, void* fringe_out, void* stream) {
