@@ -66,6 +66,8 @@ struct DMArgs {
   C* ey;                 // [entries][Py] exp(i alpha fy^2)       (fp32 path)
   R* lfx;                // [Px] (lambda fx)^2
   R* lfy;                // [Py] (lambda fy)^2
+  R* lfyp;               // [Py] (lambda fy)^2 in FFT storage order (fast column pass)
+  int ey_perm;           // 1: ey rows stored in FFT storage order (fast column pass)
   C* shy;                // [pny] y shift phase / (Px*Py)
   C* shx;                // [pnx] x shift phase
   int* slot_any;         // [uslots]
@@ -117,6 +119,12 @@ __global__ void dm_setup(DMArgs<R> a, DMSetup s) {
     double fy = (1.0 / (2.0 * a.ppy)) - (1.0 / a.ssy) - (1.0 / a.ssy) * (double)y;
     double l = a.lambda * fy;
     a.lfy[y] = (R)(l * l);
+    // storage position p of the column FFT output holds spectrum row ky(p)
+    int ky = a.ply.iperm[y] + a.hy;
+    if (ky >= a.Py) ky -= a.Py;
+    double fyp = (1.0 / (2.0 * a.ppy)) - (1.0 / a.ssy) - (1.0 / a.ssy) * (double)ky;
+    double lp = a.lambda * fyp;
+    a.lfyp[y] = (R)(lp * lp);
   }
   if constexpr (sizeof(R) == 4) {
     // separable paraxial factors exp(i pi lambda z' f^2), reduced in double
@@ -129,6 +137,10 @@ __global__ void dm_setup(DMArgs<R> a, DMSetup s) {
     }
     for (int idx = tid; idx < s.n_entries * a.Py; idx += nthr) {
       int e = idx / a.Py, y = idx - e * a.Py;
+      if (a.ey_perm) {
+        y = a.ply.iperm[y] + a.hy;
+        if (y >= a.Py) y -= a.Py;
+      }
       double fy = (1.0 / (2.0 * a.ppy)) - (1.0 / a.ssy) - (1.0 / a.ssy) * (double)y;
       double2 v = cexp_reduced(pi * a.lambda * s.zp[e] * fy * fy);
       a.ey[idx] = mk((R)v.x, (R)v.y);
@@ -207,18 +219,42 @@ __global__ void __launch_bounds__(256) dm_row_pass(DMArgs<R> a) {
       if (present) a.slot_any[u] = 1;
     }
     if (!present) continue;
-    // shifted, zero-padded source line: a[j] = u[(j - hx) mod Px]
-    for (int j = threadIdx.x; j < a.Px; j += blockDim.x) {
-      int x = j - a.hx; if (x < 0) x += a.Px;
-      const int c = x - a.ox;
-      C val = mk((R)0, (R)0);
-      if (c >= 0 && c < a.pnx && li[c] == u) val = v[c];
-      buf[j] = val;
-    }
     if constexpr (NX > 0) {
-      FastSched<NX>::template run_t<-1>(buf, 1, a.Px, 1, TwSplit<C>{twlo, twhi}, false);
+      // stage 0 straight from the source row: inputs j + t*Q0 of the
+      // x-shifted, zero-padded line a[j] = u[(j - hx) mod Px]
+      constexpr int R0 = FastSched<NX>::r0;
+      constexpr int Q0 = NX / R0;
+      const TwSplit<C> tw{twlo, twhi};
+      for (int j = threadIdx.x; j < Q0; j += blockDim.x) {
+        C x[R0];
+#pragma unroll
+        for (int t = 0; t < R0; ++t) {
+          int xx = j + t * Q0 - a.hx;
+          if (xx < 0) xx += NX;
+          const int c = xx - a.ox;
+          C val = mk((R)0, (R)0);
+          if (c >= 0 && c < a.pnx && li[c] == u) val = v[c];
+          x[t] = val;
+        }
+        DFT<R0, -1, C>::run(x);
+        if (j) {
+#pragma unroll
+          for (int f = 1; f < R0; ++f) x[f] = cmul(x[f], twid<-1, C>(tw, j * f));
+        }
+#pragma unroll
+        for (int f = 0; f < R0; ++f) buf[j + f * Q0] = x[f];
+      }
+      FastSched<NX>::template run_rest<-1>(buf, 1, a.Px, 1, tw, false);
       __syncthreads();
     } else {
+      // shifted, zero-padded source line: a[j] = u[(j - hx) mod Px]
+      for (int j = threadIdx.x; j < a.Px; j += blockDim.x) {
+        int x = j - a.hx; if (x < 0) x += a.Px;
+        const int c = x - a.ox;
+        C val = mk((R)0, (R)0);
+        if (c >= 0 && c < a.pnx && li[c] == u) val = v[c];
+        buf[j] = val;
+      }
       block_fft<-1>(buf, 1, a.Px, 1, a.plx, false);
     }
     C* dst = a.Rbuf + (size_t)u * a.nstrips * a.pny * a.W;
@@ -532,6 +568,7 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   }
   if (W == 0) return fail(OH_ERR_UNSUPPORTED_SIZE, "padded column length " + std::to_string(a.Py) + " too long for the column pass");
   a.W = W; a.nstrips = a.Px / W;
+  a.ey_perm = Wfast ? 1 : 0;
   const size_t smem_col = Wfast ? (size_t)col_layout(a.Py, a.pny, W, occ_stride, su.n_entries).total
                                 : (size_t)W * a.Py * sizeof(C) + W * (sizeof(C) + sizeof(R)) + (size_t)a.Py * sizeof(int);
   const size_t smem_row = (size_t)a.Px * sizeof(C) + (size_t)a.pnx * sizeof(C) + (size_t)((a.pnx + 7) & ~7) * sizeof(int16_t) +
@@ -550,13 +587,13 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   auto carve = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; };
   size_t o_lut = carve(256 * sizeof(int16_t)), o_use = carve(nE * sizeof(int16_t)), o_kz = carve(nE * sizeof(R)),
          o_cst = carve(nE * sizeof(C)), o_exc = carve(prec ? 0 : nE * a.Px * sizeof(C)),
-         o_ey = carve(prec ? 0 : nE * a.Py * sizeof(C)), o_lfx = carve(a.Px * sizeof(R)), o_lfy = carve(a.Py * sizeof(R)),
+         o_ey = carve(prec ? 0 : nE * a.Py * sizeof(C)), o_lfx = carve(a.Px * sizeof(R)), o_lfy = carve(a.Py * sizeof(R)), o_lfyp = carve(a.Py * sizeof(R)),
          o_shy = carve(a.pny * sizeof(C)), o_shx = carve(a.pnx * sizeof(C)), o_any = carve(nU * sizeof(int));
   OH_TRY(scratch(ctx, "dm.tables", off, &ptr));
   char* base = (char*)ptr;
   a.lut = (int16_t*)(base + o_lut); a.uslot_of_entry = (int16_t*)(base + o_use); a.kzp = (R*)(base + o_kz);
   a.cst = (C*)(base + o_cst); a.exc = (C*)(base + o_exc); a.ey = (C*)(base + o_ey);
-  a.lfx = (R*)(base + o_lfx); a.lfy = (R*)(base + o_lfy); a.shy = (C*)(base + o_shy); a.shx = (C*)(base + o_shx);
+  a.lfx = (R*)(base + o_lfx); a.lfy = (R*)(base + o_lfy); a.lfyp = (R*)(base + o_lfyp); a.shy = (C*)(base + o_shy); a.shx = (C*)(base + o_shx);
   a.slot_any = (int*)(base + o_any);
   a.fringe = (R*)fringe; a.field = (C*)field; a.spectrum = (C*)spectrum;
 
@@ -585,10 +622,10 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
         if constexpr (NY > 0) {
           auto launch = [&](auto wc) {
             constexpr int WW = decltype(wc)::value;
-            cudaError_t e = cudaFuncSetAttribute(dm_col_fast<NY, WW, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col);
+            cudaError_t e = cudaFuncSetAttribute(dm_col_fast<NY, WW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col);
             if (e != cudaSuccess) { rs = cuda_fail(e, "cudaFuncSetAttribute(dm_col_fast)"); return; }
             KernelTimer kt(ctx, "dm_col_pass", st);
-            dm_col_fast<NY, WW, 512><<<a.nstrips, 512, smem_col, st>>>(a);
+            dm_col_fast<NY, WW><<<a.nstrips, ColCfg<NY, WW>::T, smem_col, st>>>(a);
             note_launch();
             if ((e = cudaGetLastError()) != cudaSuccess) rs = cuda_fail(e, "dm_col_fast launch");
           };

@@ -90,13 +90,25 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* b, uint32_t parity) 
 __device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
-template <int NY, int W, int T>
-__global__ void __launch_bounds__(T) dm_col_fast(DMArgs<float> a) {
+// Threads per block for a strip of W columns: one thread per last-stage
+// butterfly (NY/RL per column), two when that would exceed 768 threads.
+template <int NY, int W> struct ColCfg {
+  static constexpr int RL = FastSched<NY>::rlast;
+  static constexpr int NBL = (NY / RL) * W;          // last-stage butterflies in the strip
+  static constexpr int KB = NBL > 768 ? 2 : 1;        // butterflies per thread
+  static constexpr int T = ((NBL + KB - 1) / KB + 31) / 32 * 32;
+};
+
+template <int NY, int W>
+__global__ void __launch_bounds__(ColCfg<NY, W>::T) dm_col_fast(DMArgs<float> a) {
   typedef float2 C;
+  typedef ColCfg<NY, W> CF;
+  constexpr int T = CF::T;
   constexpr int R0 = FastSched<NY>::r0;
+  constexpr int RL = CF::RL;
+  constexpr int KB = CF::KB;
   constexpr int Q0 = NY / R0;
-  constexpr int NEL = NY * W;
-  constexpr int KM = (NEL + T - 1) / T;
+  static_assert(FastSched<NY>::nstages == 3, "fast column pass expects a three-stage schedule");
   extern __shared__ __align__(128) unsigned char smem[];
   const ColLayout Lo = col_layout(NY, a.pny, W, a.occ_stride, a.n_entries);
   C* buf = reinterpret_cast<C*>(smem + Lo.buf);
@@ -107,7 +119,7 @@ __global__ void __launch_bounds__(T) dm_col_fast(DMArgs<float> a) {
   C* const ey1 = reinterpret_cast<C*>(smem + Lo.ey1);
   uint8_t* const occ0 = smem + Lo.occ0;
   uint8_t* const occ1 = smem + Lo.occ1;
-  float* lfy = reinterpret_cast<float*>(smem + Lo.lfy);
+  float* lfyp = reinterpret_cast<float*>(smem + Lo.lfy);     // storage order
   int16_t* kyp = reinterpret_cast<int16_t*>(smem + Lo.kyp);
   C* twlo = reinterpret_cast<C*>(smem + Lo.twlo);
   C* twhi = reinterpret_cast<C*>(smem + Lo.twhi);
@@ -135,7 +147,7 @@ __global__ void __launch_bounds__(T) dm_col_fast(DMArgs<float> a) {
     int ky = a.ply.iperm[p] + a.hy;
     if (ky >= NY) ky -= NY;
     kyp[p] = (int16_t)ky;
-    lfy[p] = a.lfy[p];
+    lfyp[p] = a.lfyp[p];
   }
   if (tid < W) lfxw[tid] = a.lfx[kx0 + tid];
   __syncthreads();
@@ -155,9 +167,13 @@ __global__ void __launch_bounds__(T) dm_col_fast(DMArgs<float> a) {
   };
   if (tid == 0 && nact > 0) issue(0, 0);
 
-  C acc[KM];
+  // accumulators: last-stage butterfly bb = tid + kb*T of the strip (bb = b*W + w),
+  // outputs f at storage position p = b*RL + f of line w
+  C acc[KB][RL];
 #pragma unroll
-  for (int k = 0; k < KM; ++k) acc[k] = make_float2(0.f, 0.f);
+  for (int kb = 0; kb < KB; ++kb)
+#pragma unroll
+    for (int f = 0; f < RL; ++f) acc[kb][f] = make_float2(0.f, 0.f);
 
   for (int k = 0; k < nact; ++k) {
     const int bi = k & 1;
@@ -200,24 +216,35 @@ __global__ void __launch_bounds__(T) dm_col_fast(DMArgs<float> a) {
 #pragma unroll
       for (int f = 0; f < R0; ++f) buf[(j + f * Q0) * W + w] = x[f];
     }
-    FastSched<NY>::template run_rest<-1>(buf, W, 1, W, tw, true);
+    FastSched<NY>::template run_middle<-1>(buf, W, 1, W, tw, true);
     __syncthreads();
+    // last stage (stride 1, no twiddles) fused with the transfer-function
+    // multiply-accumulate
     const float kz = a.kzp[e];
-    const C* ey = bi ? ey1 : ey0;
+    const C* ey = bi ? ey1 : ey0;            // storage order
 #pragma unroll
-    for (int kk = 0; kk < KM; ++kk) {
-      const int idx = tid + kk * T;
-      if (idx < NEL) {
-        const int p = idx / W, w = idx - p * W;
-        const int ky = kyp[p];
-        const float sv = lfxw[w] + lfy[ky];
-        const float rt = sqrtf(1.f - sv);
-        const float den = 1.f + rt;
-        const float psi = kz * sv * sv * __fdividef(0.5f, den * den);
-        float sn, cs;
-        __sincosf(psi, &sn, &cs);
-        const C h = cmul(cmul(exw[w], ey[ky]), make_float2(cs, sn));
-        acc[kk] = cadd(acc[kk], cmul(h, buf[idx]));
+    for (int kb = 0; kb < KB; ++kb) {
+      const int bb = tid + kb * T;
+      if (bb < CF::NBL) {
+        const int b = bb / W, w = bb - b * W;
+        C x[RL];
+#pragma unroll
+        for (int f = 0; f < RL; ++f) x[f] = buf[(b * RL + f) * W + w];
+        DFT<RL, -1, C>::run(x);
+        const C ex = exw[w];
+        const float lx = lfxw[w];
+#pragma unroll
+        for (int f = 0; f < RL; ++f) {
+          const int p = b * RL + f;
+          const float sv = lx + lfyp[p];
+          const float rt = sqrtf(1.f - sv);
+          const float den = 1.f + rt;
+          const float psi = kz * sv * sv * __fdividef(0.5f, den * den);
+          float sn, cs;
+          __sincosf(psi, &sn, &cs);
+          const C h = cmul(cmul(ex, ey[p]), make_float2(cs, sn));
+          acc[kb][f] = cadd(acc[kb][f], cmul(h, x[f]));
+        }
       }
     }
     __syncthreads();
@@ -225,17 +252,20 @@ __global__ void __launch_bounds__(T) dm_col_fast(DMArgs<float> a) {
 
   // SSB crop and inverse y-FFT input order: spectrum row ky -> i = (ky + hy) mod NY
 #pragma unroll
-  for (int kk = 0; kk < KM; ++kk) {
-    const int idx = tid + kk * T;
-    if (idx < NEL) {
-      const int p = idx / W, w = idx - p * W;
-      const int ky = kyp[p];
+  for (int kb = 0; kb < KB; ++kb) {
+    const int bb = tid + kb * T;
+    if (bb < CF::NBL) {
+      const int b = bb / W, w = bb - b * W;
       const int kx = kx0 + w;
-      if (a.spectrum) a.spectrum[(size_t)ky * a.Px + kx] = acc[kk];
-      const bool keep = kx >= a.cx1 && kx <= a.cx2 && ky >= a.cy1 && ky <= a.cy2;
-      int i = ky + a.hy;
-      if (i >= NY) i -= NY;
-      buf[i * W + w] = keep ? acc[kk] : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int f = 0; f < RL; ++f) {
+        const int ky = kyp[b * RL + f];
+        if (a.spectrum) a.spectrum[(size_t)ky * a.Px + kx] = acc[kb][f];
+        const bool keep = kx >= a.cx1 && kx <= a.cx2 && ky >= a.cy1 && ky <= a.cy2;
+        int i = ky + a.hy;
+        if (i >= NY) i -= NY;
+        buf[i * W + w] = keep ? acc[kb][f] : make_float2(0.f, 0.f);
+      }
     }
   }
   FastSched<NY>::template run_t<1>(buf, W, 1, W, tw, true);

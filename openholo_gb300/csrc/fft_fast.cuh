@@ -252,10 +252,31 @@ __device__ __forceinline__ void fstages(C* buf, int nl, int ls, int es, const C*
   if constexpr (sizeof...(Rest) > 0) fstages<N, M / R, SGN, C, Rest...>(buf, nl, ls, es, tw, line_fastest);
 }
 
+// every stage of the list except the last one (block size M at entry)
+template <int N, int M, int SGN, typename C, class TW, int R, int... Rest>
+__device__ __forceinline__ void fstages_but_last(C* buf, int nl, int ls, int es, const TW& tw, bool line_fastest) {
+  if constexpr (sizeof...(Rest) > 0) {
+    __syncthreads();
+    fstage_t<N, R, M, SGN>(buf, nl, ls, es, tw, line_fastest);
+    fstages_but_last<N, M / R, SGN, C, TW, Rest...>(buf, nl, ls, es, tw, line_fastest);
+  }
+}
+
+template <int... Rs> struct LastOf;
+template <int R> struct LastOf<R> { static constexpr int value = R; };
+template <int R, int... Rs> struct LastOf<R, Rs...> { static constexpr int value = LastOf<Rs...>::value; };
+
 template <int N, int R0, int... Rest>
 struct SchedImpl {
   static constexpr bool ok = true;
   static constexpr int r0 = R0;
+  static constexpr int nstages = 1 + (int)sizeof...(Rest);
+  static constexpr int rlast = LastOf<R0, Rest...>::value;
+  // stages 1 .. S-2 (the caller runs stage 0 and the last stage itself)
+  template <int SGN, typename C, class TW>
+  __device__ __forceinline__ static void run_middle(C* buf, int nl, int ls, int es, const TW& tw, bool lf) {
+    if constexpr (sizeof...(Rest) > 0) fstages_but_last<N, N / R0, SGN, C, TW, Rest...>(buf, nl, ls, es, tw, lf);
+  }
   template <int SGN, typename C>
   __device__ __forceinline__ static void run(C* buf, int nl, int ls, int es, const C* tw, bool lf) {
     fstages<N, N, SGN, C, R0, Rest...>(buf, nl, ls, es, tw, lf);
