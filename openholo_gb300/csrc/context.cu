@@ -39,6 +39,7 @@ CallScope::~CallScope() {
 oh_status scratch(oh_ctx* ctx, const char* name, size_t bytes, void** out) {
   auto& b = ctx->scratch[name];
   if (b.bytes < bytes) {
+    ctx->dm_setup_key.clear();          // cached tables may live in a buffer being replaced
     if (b.p) {
       cudaError_t e = cudaDeviceSynchronize();
       if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceSynchronize (scratch growth)");
@@ -258,6 +259,7 @@ oh_status oh_ctx_release_scratch(oh_ctx* ctx) {
   cudaDeviceSynchronize();
   for (auto& kv : ctx->scratch) cudaFree(kv.second.p);
   ctx->scratch.clear();
+  ctx->dm_setup_key.clear();
   cudaSetDevice(prev);
   return OH_OK;
 }

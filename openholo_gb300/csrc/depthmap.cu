@@ -79,6 +79,7 @@ struct DMArgs {
   C* spectrum;           // [Py][Px] or null
   int sig_x, sig_y;
   int occ_stride;        // bytes per layer row of occ (multiple of 16)
+  int xs;                // 1: R and V columns are in the row FFT's storage order (fast passes), 0: kx order
   int* err;              // device error word (bounded waits that ran out)
   FFTPlan plx, ply;
 };
@@ -258,10 +259,18 @@ __global__ void __launch_bounds__(256) dm_row_pass(DMArgs<R> a) {
       block_fft<-1>(buf, 1, a.Px, 1, a.plx, false);
     }
     C* dst = a.Rbuf + (size_t)u * a.nstrips * a.pny * a.W;
-    for (int kx = threadIdx.x; kx < a.Px; kx += blockDim.x) {
-      int m = kx - a.hx; if (m < 0) m += a.Px;       // S[kx] = A[(kx - hx) mod Px]
-      const int s = kx / a.W, w = kx - s * a.W;
-      dst[((size_t)s * a.pny + r) * a.W + w] = buf[a.plx.perm[m]];
+    if (a.xs) {
+      // storage order: column p of the strip layout is FFT output position p
+      for (int p = threadIdx.x; p < a.Px; p += blockDim.x) {
+        const int s = p / a.W, w = p - s * a.W;
+        dst[((size_t)s * a.pny + r) * a.W + w] = buf[p];
+      }
+    } else {
+      for (int kx = threadIdx.x; kx < a.Px; kx += blockDim.x) {
+        int m = kx - a.hx; if (m < 0) m += a.Px;       // S[kx] = A[(kx - hx) mod Px]
+        const int s = kx / a.W, w = kx - s * a.W;
+        dst[((size_t)s * a.pny + r) * a.W + w] = buf[a.plx.perm[m]];
+      }
     }
     __syncthreads();
   }
@@ -378,9 +387,19 @@ __global__ void __launch_bounds__(256) dm_out_pass(DMArgs<R> a) {
   const int yl = blockIdx.x;
   const C* row = a.V + (size_t)yl * a.Px;
   if constexpr (NX > 0) load_tw_split(twlo, twhi, static_cast<const C*>(a.plx.tw), NX);
-  for (int j = threadIdx.x; j < a.Px; j += blockDim.x) {
-    int kx = j - a.hx; if (kx < 0) kx += a.Px;
-    buf[j] = row[kx];
+  if (a.xs) {
+    // V column p holds spectrum column kx = (iperm[p] + hx) mod Px; the
+    // inverse line wants it at j = (kx + hx) mod Px
+    for (int p = threadIdx.x; p < a.Px; p += blockDim.x) {
+      int kx = a.plx.iperm[p] + a.hx; if (kx >= a.Px) kx -= a.Px;
+      int j = kx + a.hx; if (j >= a.Px) j -= a.Px;
+      buf[j] = row[p];
+    }
+  } else {
+    for (int j = threadIdx.x; j < a.Px; j += blockDim.x) {
+      int kx = j - a.hx; if (kx < 0) kx += a.Px;
+      buf[j] = row[kx];
+    }
   }
   if constexpr (NX > 0) {
     FastSched<NX>::template run_t<1>(buf, 1, a.Px, 1, TwSplit<C>{twlo, twhi}, false);
@@ -569,6 +588,9 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   if (W == 0) return fail(OH_ERR_UNSUPPORTED_SIZE, "padded column length " + std::to_string(a.Py) + " too long for the column pass");
   a.W = W; a.nstrips = a.Px / W;
   a.ey_perm = Wfast ? 1 : 0;
+  bool fastx = false;
+  with_fast_n(a.Px, [&](auto nc) { fastx = decltype(nc)::value > 0; });
+  a.xs = (prec == 0 && fastx && Wfast) ? 1 : 0;
   const size_t smem_col = Wfast ? (size_t)col_layout(a.Py, a.pny, W, occ_stride, su.n_entries).total
                                 : (size_t)W * a.Py * sizeof(C) + W * (sizeof(C) + sizeof(R)) + (size_t)a.Py * sizeof(int);
   const size_t smem_row = (size_t)a.Px * sizeof(C) + (size_t)a.pnx * sizeof(C) + (size_t)((a.pnx + 7) & ~7) * sizeof(int16_t) +
@@ -598,9 +620,31 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   a.fringe = (R*)fringe; a.field = (C*)field; a.spectrum = (C*)spectrum;
 
   {
-    KernelTimer kt(ctx, prec ? "dm_setup_f64" : "dm_setup", st);
-    dm_setup<R><<<64, 256, 0, st>>>(a, su);
-    OH_LAUNCH_CHECK();
+    // the tables depend only on the parameters: rebuild them when those (or
+    // the scratch buffer holding them) change, else only reset the per-frame
+    // layer flags
+    struct Key {
+      DMSetup su;
+      int prec, pnx, pny, Px, Py, sig_x, sig_y, ey_perm;
+      double ppx, ppy, lambda;
+      const void* tables;
+      const void* iperm;
+    } key;
+    std::memset(&key, 0, sizeof(key));
+    key.su = su;
+    key.prec = prec; key.pnx = a.pnx; key.pny = a.pny; key.Px = a.Px; key.Py = a.Py;
+    key.sig_x = a.sig_x; key.sig_y = a.sig_y; key.ey_perm = a.ey_perm;
+    key.ppx = a.ppx; key.ppy = a.ppy; key.lambda = a.lambda;
+    key.tables = base; key.iperm = a.ply.iperm;
+    std::string ks(reinterpret_cast<const char*>(&key), sizeof(key));
+    if (ks == ctx->dm_setup_key) {
+      OH_CUDA_TRY(cudaMemsetAsync(a.slot_any, 0, nU * sizeof(int), st));
+    } else {
+      KernelTimer kt(ctx, prec ? "dm_setup_f64" : "dm_setup", st);
+      dm_setup<R><<<64, 256, 0, st>>>(a, su);
+      OH_LAUNCH_CHECK();
+      ctx->dm_setup_key = ks;
+    }
   }
   // the FP32 path uses the compile-time FFT schedules; FP64 the generic engine
   oh_status rs = OH_OK;

@@ -125,6 +125,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T) dm_col_fast(DMArgs<float> a)
   C* twhi = reinterpret_cast<C*>(smem + Lo.twhi);
   C* exw = reinterpret_cast<C*>(smem + Lo.exw);
   float* lfxw = reinterpret_cast<float*>(smem + Lo.lfxw);
+  __shared__ int kxw[8];          // spectrum column of each strip column
   int16_t* list = reinterpret_cast<int16_t*>(smem + Lo.list);
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + Lo.mbar);
   __shared__ int s_nact;
@@ -149,7 +150,14 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T) dm_col_fast(DMArgs<float> a)
     kyp[p] = (int16_t)ky;
     lfyp[p] = a.lfyp[p];
   }
-  if (tid < W) lfxw[tid] = a.lfx[kx0 + tid];
+  if (tid < W) {
+    // strip column kx0 + w is either spectrum column kx0 + w or, when the row
+    // pass stored its output in FFT storage order, column iperm + hx
+    int kx = kx0 + tid;
+    if (a.xs) { kx = a.plx.iperm[kx0 + tid] + a.hx; if (kx >= a.Px) kx -= a.Px; }
+    kxw[tid] = kx;
+    lfxw[tid] = a.lfx[kx];
+  }
   __syncthreads();
   const int nact = s_nact;
   const TwSplit<C> tw{twlo, twhi};
@@ -192,7 +200,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T) dm_col_fast(DMArgs<float> a)
       return;
     }
     const int e = list[k];
-    if (tid < W) exw[tid] = a.exc[(size_t)e * a.Px + kx0 + tid];
+    if (tid < W) exw[tid] = a.exc[(size_t)e * a.Px + kxw[tid]];
     const C* sg = bi ? stg1 : stg0;
     const uint8_t* oc = bi ? occ1 : occ0;
     // stage 0 from the staging buffer: inputs j + t*Q0 of the y-shifted line
@@ -256,7 +264,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T) dm_col_fast(DMArgs<float> a)
     const int bb = tid + kb * T;
     if (bb < CF::NBL) {
       const int b = bb / W, w = bb - b * W;
-      const int kx = kx0 + w;
+      const int kx = kxw[w];
 #pragma unroll
       for (int f = 0; f < RL; ++f) {
         const int ky = kyp[b * RL + f];

@@ -182,6 +182,23 @@ def test_host_entry_point_matches_device(ctx, dev):
     assert np.array_equal(fr_dev, fr_host)
 
 
+def test_table_cache_across_parameter_changes(ctx, dev):
+    """Frames with alternating parameters give the same results as fresh runs
+    (the per-layer tables are cached per parameter set)."""
+    ny, nx = 540, 960
+    img, depth = scenes.depthmap_scene(5, ny, nx)
+    pa = dm.make_params(pnx=nx, pny=ny, num_of_depth=12, phase_mode=dm.OH_PHASE_SEEDED, seed=1)
+    pb = dm.make_params(pnx=nx, pny=ny, num_of_depth=9, near=0.2, far=0.4, phase_mode=dm.OH_PHASE_SEEDED, seed=1)
+    a1 = run(ctx, dev, img, depth, pa)
+    b1 = run(ctx, dev, img, depth, pb)
+    a2 = run(ctx, dev, img, depth, pa)
+    a3 = run(ctx, dev, img, depth, pa)
+    assert np.array_equal(a1, a2) and np.array_equal(a2, a3)
+    assert not np.array_equal(a1, b1)
+    ref_b = odm.generate(img, depth, oparams(pb), phase=scenes.seeded_phase(1, ny, nx))[0]
+    assert rel(b1, ref_b) < TOL32
+
+
 def test_invalid_arguments_raise(ctx, dev):
     img = torch.zeros((8, 8), dtype=torch.uint8, device=dev)
     with pytest.raises(OhError):
