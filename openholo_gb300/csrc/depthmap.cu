@@ -80,6 +80,7 @@ struct DMArgs {
   int sig_x, sig_y;
   int occ_stride;        // bytes per layer row of occ (multiple of 16)
   int xs;                // 1: R and V columns are in the row FFT's storage order (fast passes), 0: kx order
+  int hzx, hzy;          // 1: 2x padding with a radix-16 first stage (stage-0 inputs 4..11 are zero)
   int* err;              // device error word (bounded waits that ran out)
   FFTPlan plx, ply;
 };
@@ -228,19 +229,34 @@ __global__ void __launch_bounds__(256) dm_row_pass(DMArgs<R> a) {
       const TwSplit<C> tw{twlo, twhi};
       for (int j = threadIdx.x; j < Q0; j += blockDim.x) {
         C x[R0];
+        if (R0 == 16 && a.hzx) {
+          // 2x padding: inputs t = 4..11 fall in the zero columns
 #pragma unroll
-        for (int t = 0; t < R0; ++t) {
-          int xx = j + t * Q0 - a.hx;
-          if (xx < 0) xx += NX;
-          const int c = xx - a.ox;
-          C val = mk((R)0, (R)0);
-          if (c >= 0 && c < a.pnx && li[c] == u) val = v[c];
-          x[t] = val;
+          for (int t = 0; t < R0; ++t) {
+            if (t >= 4 && t < 12) { x[t] = mk((R)0, (R)0); continue; }
+            int xx = j + t * Q0 - a.hx;
+            if (xx < 0) xx += NX;
+            const int c = xx - a.ox;
+            x[t] = li[c] == u ? v[c] : mk((R)0, (R)0);
+          }
+          dft16_halfzero<-1>(x);
+        } else {
+#pragma unroll
+          for (int t = 0; t < R0; ++t) {
+            int xx = j + t * Q0 - a.hx;
+            if (xx < 0) xx += NX;
+            const int c = xx - a.ox;
+            C val = mk((R)0, (R)0);
+            if (c >= 0 && c < a.pnx && li[c] == u) val = v[c];
+            x[t] = val;
+          }
+          DFT<R0, -1, C>::run(x);
         }
-        DFT<R0, -1, C>::run(x);
         if (j) {
+          C wp[R0];
+          twiddle_powers<R0, -1>(tw, j, wp);
 #pragma unroll
-          for (int f = 1; f < R0; ++f) x[f] = cmul(x[f], twid<-1, C>(tw, j * f));
+          for (int f = 1; f < R0; ++f) x[f] = cmul(x[f], wp[f]);
         }
 #pragma unroll
         for (int f = 0; f < R0; ++f) buf[j + f * Q0] = x[f];
@@ -591,6 +607,11 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   bool fastx = false;
   with_fast_n(a.Px, [&](auto nc) { fastx = decltype(nc)::value > 0; });
   a.xs = (prec == 0 && fastx && Wfast) ? 1 : 0;
+  int r0x = 0, r0y = 0;
+  with_fast_n(a.Px, [&](auto nc) { if constexpr (decltype(nc)::value > 0) r0x = FastSched<decltype(nc)::value>::r0; });
+  with_fast_n(a.Py, [&](auto nc) { if constexpr (decltype(nc)::value > 0) r0y = FastSched<decltype(nc)::value>::r0; });
+  a.hzx = (p->pad == 2 && r0x == 16 && (a.Px % 16) == 0 && a.ox * 4 == a.Px && a.hx * 2 == a.Px) ? 1 : 0;
+  a.hzy = (p->pad == 2 && r0y == 16 && (a.Py % 16) == 0 && a.oy * 4 == a.Py && a.hy * 2 == a.Py) ? 1 : 0;
   const size_t smem_col = Wfast ? (size_t)col_layout(a.Py, a.pny, W, occ_stride, su.n_entries).total
                                 : (size_t)W * a.Py * sizeof(C) + W * (sizeof(C) + sizeof(R)) + (size_t)a.Py * sizeof(int);
   const size_t smem_row = (size_t)a.Px * sizeof(C) + (size_t)a.pnx * sizeof(C) + (size_t)((a.pnx + 7) & ~7) * sizeof(int16_t) +

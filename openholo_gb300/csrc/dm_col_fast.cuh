@@ -25,7 +25,7 @@
 namespace oh {
 
 struct ColLayout {
-  int buf, stg0, stg1, ey0, ey1, occ0, occ1, lfy, kyp, twlo, twhi, exw, lfxw, list, mbar, total;
+  int buf, stg0, stg1, ey0, ey1, occ0, occ1, g, kyp, twlo, twhi, exw, lfxw, list, mbar, total;
 };
 
 __host__ __device__ inline int col_take(int* o, int bytes) {
@@ -44,7 +44,7 @@ __host__ __device__ inline ColLayout col_layout(int Py, int pny, int W, int occ_
   L.ey1 = col_take(&o, Py * 8);
   L.occ0 = col_take(&o, occ_stride);
   L.occ1 = col_take(&o, occ_stride);
-  L.lfy = col_take(&o, Py * 4);
+  L.g = col_take(&o, Py * W * 4);
   L.kyp = col_take(&o, Py * 2);
   L.twlo = col_take(&o, 64 * 8);
   L.twhi = col_take(&o, ((Py + 63) / 64) * 8);
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T) dm_col_fast(DMArgs<float> a)
   C* const ey1 = reinterpret_cast<C*>(smem + Lo.ey1);
   uint8_t* const occ0 = smem + Lo.occ0;
   uint8_t* const occ1 = smem + Lo.occ1;
-  float* lfyp = reinterpret_cast<float*>(smem + Lo.lfy);     // storage order
+  float* gsm = reinterpret_cast<float*>(smem + Lo.g);        // per element, buffer order
   int16_t* kyp = reinterpret_cast<int16_t*>(smem + Lo.kyp);
   C* twlo = reinterpret_cast<C*>(smem + Lo.twlo);
   C* twhi = reinterpret_cast<C*>(smem + Lo.twhi);
@@ -148,7 +148,6 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T) dm_col_fast(DMArgs<float> a)
     int ky = a.ply.iperm[p] + a.hy;
     if (ky >= NY) ky -= NY;
     kyp[p] = (int16_t)ky;
-    lfyp[p] = a.lfyp[p];
   }
   if (tid < W) {
     // strip column kx0 + w is either spectrum column kx0 + w or, when the row
@@ -157,6 +156,15 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T) dm_col_fast(DMArgs<float> a)
     if (a.xs) { kx = a.plx.iperm[kx0 + tid] + a.hx; if (kx >= a.Px) kx -= a.Px; }
     kxw[tid] = kx;
     lfxw[tid] = a.lfx[kx];
+  }
+  __syncthreads();
+  // layer-independent part of the angular-spectrum residual phase:
+  // psi = k z' g,  g = s^2 / (2 (1 + sqrt(1 - s))^2),  s = (lambda fx)^2 + (lambda fy)^2
+  for (int idx = tid; idx < NY * W; idx += T) {
+    const int p = idx / W, w = idx - p * W;
+    const float sv = lfxw[w] + a.lfyp[p];
+    const float den = 1.f + sqrtf(1.f - sv);
+    gsm[idx] = sv * sv * __fdividef(0.5f, den * den);
   }
   __syncthreads();
   const int nact = s_nact;
@@ -207,19 +215,34 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T) dm_col_fast(DMArgs<float> a)
     for (int idx = tid; idx < Q0 * W; idx += T) {
       const int j = idx / W, w = idx - j * W;
       C x[R0];
+      if (R0 == 16 && a.hzy) {
+        // 2x padding: inputs t = 4..11 are rows of the zero band
 #pragma unroll
-      for (int t = 0; t < R0; ++t) {
-        int y = j + t * Q0 - a.hy;
-        if (y < 0) y += NY;
-        const int yl = y - a.oy;
-        C v = make_float2(0.f, 0.f);
-        if (yl >= 0 && yl < pny && oc[yl]) v = sg[yl * W + w];
-        x[t] = v;
+        for (int t = 0; t < R0; ++t) {
+          if (t >= 4 && t < 12) { x[t] = make_float2(0.f, 0.f); continue; }
+          int y = j + t * Q0 - a.hy;
+          if (y < 0) y += NY;
+          const int yl = y - a.oy;
+          x[t] = oc[yl] ? sg[yl * W + w] : make_float2(0.f, 0.f);
+        }
+        dft16_halfzero<-1>(x);
+      } else {
+#pragma unroll
+        for (int t = 0; t < R0; ++t) {
+          int y = j + t * Q0 - a.hy;
+          if (y < 0) y += NY;
+          const int yl = y - a.oy;
+          C v = make_float2(0.f, 0.f);
+          if (yl >= 0 && yl < pny && oc[yl]) v = sg[yl * W + w];
+          x[t] = v;
+        }
+        DFT<R0, -1, C>::run(x);
       }
-      DFT<R0, -1, C>::run(x);
       if (j) {
+        C wp[R0];
+        twiddle_powers<R0, -1>(tw, j, wp);
 #pragma unroll
-        for (int f = 1; f < R0; ++f) x[f] = cmul(x[f], twid<-1, C>(tw, j * f));
+        for (int f = 1; f < R0; ++f) x[f] = cmul(x[f], wp[f]);
       }
 #pragma unroll
       for (int f = 0; f < R0; ++f) buf[(j + f * Q0) * W + w] = x[f];
@@ -240,14 +263,10 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T) dm_col_fast(DMArgs<float> a)
         for (int f = 0; f < RL; ++f) x[f] = buf[(b * RL + f) * W + w];
         DFT<RL, -1, C>::run(x);
         const C ex = exw[w];
-        const float lx = lfxw[w];
 #pragma unroll
         for (int f = 0; f < RL; ++f) {
           const int p = b * RL + f;
-          const float sv = lx + lfyp[p];
-          const float rt = sqrtf(1.f - sv);
-          const float den = 1.f + rt;
-          const float psi = kz * sv * sv * __fdividef(0.5f, den * den);
+          const float psi = kz * gsm[p * W + w];
           float sn, cs;
           __sincosf(psi, &sn, &cs);
           const C h = cmul(cmul(ex, ey[p]), make_float2(cs, sn));

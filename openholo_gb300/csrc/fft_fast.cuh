@@ -183,6 +183,47 @@ __device__ __forceinline__ C twid(const TW& tw, int e) {
   return w;
 }
 
+// Twiddles W^(e f), f = 1..R-1, from two fetches (W^e, W^4e) and products:
+// W^(4a+b) = (W^4e)^a (W^e)^b; a few ulp of error for R <= 32.
+template <int R, int SGN, typename C, class TW>
+__device__ __forceinline__ void twiddle_powers(const TW& tw, int e, C* w) {
+  w[1] = twid<SGN, C>(tw, e);
+  if constexpr (R > 2) w[2] = cmul(w[1], w[1]);
+  if constexpr (R > 3) w[3] = cmul(w[2], w[1]);
+  if constexpr (R > 4) {
+    w[4] = twid<SGN, C>(tw, 4 * e);
+#pragma unroll
+    for (int f = 5; f < R; ++f) w[f] = cmul(w[f - 4], w[4]);
+  }
+}
+
+// Forward/inverse DFT16 whose inputs 4..11 are zero (stage 0 of a 2x
+// zero-padded line): inner length-4 DFTs over n1 see only n1 = 0 and 3.
+template <int SGN, typename C>
+__device__ __forceinline__ void dft16_halfzero(C* x) {
+  C a[16];
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) {
+    const C x0 = x[n2], x3 = x[n2 + 12];
+    // y_k = x0 + x3 * W4^(3k) = x0 + x3 * (-SGN i)^k
+    const C ix3 = cmul_i<-SGN>(x3);
+    C v[4];
+    v[0] = cadd(x0, x3);
+    v[1] = cadd(x0, ix3);
+    v[2] = csub(x0, x3);
+    v[3] = csub(x0, ix3);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) a[n2 * 4 + k1] = wmul<16, SGN>(v[k1], n2 * k1);
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    C v[4] = {a[k1], a[4 + k1], a[8 + k1], a[12 + k1]};
+    dft4<SGN>(v[0], v[1], v[2], v[3]);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) x[k1 + 4 * k2] = v[k2];
+  }
+}
+
 // ---- one stage --------------------------------------------------------------
 
 template <int N, int R, int M, int SGN, typename C, class TW>
@@ -203,8 +244,10 @@ __device__ __forceinline__ void fstage_t(C* buf, int nl, int ls, int es, const T
     for (int t = 0; t < R; ++t) x[t] = buf[base + t * st];
     DFT<R, SGN, C>::run(x);
     if (Q > 1 && j) {
+      C w[R];
+      twiddle_powers<R, SGN>(tw, j * TWS, w);
 #pragma unroll
-      for (int f = 1; f < R; ++f) x[f] = cmul(x[f], twid<SGN, C>(tw, j * f * TWS));
+      for (int f = 1; f < R; ++f) x[f] = cmul(x[f], w[f]);
     }
 #pragma unroll
     for (int t = 0; t < R; ++t) buf[base + t * st] = x[t];
