@@ -25,6 +25,7 @@
 // The 2x zero-padding (pad = 2) never materialises: padded rows are skipped
 // and padded columns are zeros written straight into shared memory.
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -588,7 +589,11 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   bool fastlen = false;
   with_fast_n(a.Py, [&](auto nc) { fastlen = decltype(nc)::value > 0; });
   if (prec == 0 && fastlen) {
+    // strip width: 4 (one block per SM) unless overridden by OH_DM_COL_W
+    int want = 0;
+    if (const char* ev = std::getenv("OH_DM_COL_W")) want = std::atoi(ev);
     for (int cand : {4, 2}) {
+      if (want && cand != want) continue;
       if (a.Px % cand) continue;
       if ((size_t)col_layout(a.Py, a.pny, cand, occ_stride, su.n_entries).total <= smax) { Wfast = cand; break; }
     }
@@ -688,6 +693,8 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
           auto launch = [&](auto wc) {
             constexpr int WW = decltype(wc)::value;
             cudaError_t e = cudaFuncSetAttribute(dm_col_fast<NY, WW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col);
+            if (e == cudaSuccess)
+              e = cudaFuncSetAttribute(dm_col_fast<NY, WW>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
             if (e != cudaSuccess) { rs = cuda_fail(e, "cudaFuncSetAttribute(dm_col_fast)"); return; }
             KernelTimer kt(ctx, "dm_col_pass", st);
             dm_col_fast<NY, WW><<<a.nstrips, ColCfg<NY, WW>::T, smem_col, st>>>(a);

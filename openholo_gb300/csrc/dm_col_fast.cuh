@@ -25,7 +25,7 @@
 namespace oh {
 
 struct ColLayout {
-  int buf, stg0, stg1, ey0, ey1, occ0, occ1, g, kyp, twlo, twhi, exw, lfxw, list, mbar, total;
+  int buf, stg, ey0, ey1, occ, g, kyp, twlo, twhi, exw, lfxw, list, mbar, total;
 };
 
 __host__ __device__ inline int col_take(int* o, int bytes) {
@@ -38,12 +38,10 @@ __host__ __device__ inline ColLayout col_layout(int Py, int pny, int W, int occ_
   ColLayout L;
   int o = 0;
   L.buf = col_take(&o, Py * W * 8);
-  L.stg0 = col_take(&o, pny * W * 8);
-  L.stg1 = col_take(&o, pny * W * 8);
+  L.stg = col_take(&o, pny * W * 8);
   L.ey0 = col_take(&o, Py * 8);
   L.ey1 = col_take(&o, Py * 8);
-  L.occ0 = col_take(&o, occ_stride);
-  L.occ1 = col_take(&o, occ_stride);
+  L.occ = col_take(&o, occ_stride);
   L.g = col_take(&o, Py * W * 4);
   L.kyp = col_take(&o, Py * 2);
   L.twlo = col_take(&o, 64 * 8);
@@ -51,7 +49,7 @@ __host__ __device__ inline ColLayout col_layout(int Py, int pny, int W, int occ_
   L.exw = col_take(&o, W * 8);
   L.lfxw = col_take(&o, W * 4);
   L.list = col_take(&o, n_entries * 2 + 2);
-  L.mbar = col_take(&o, 16);
+  L.mbar = col_take(&o, 24);
   L.total = o;
   return L;
 }
@@ -97,10 +95,11 @@ template <int NY, int W> struct ColCfg {
   static constexpr int NBL = (NY / RL) * W;          // last-stage butterflies in the strip
   static constexpr int KB = NBL > 768 ? 2 : 1;        // butterflies per thread
   static constexpr int T = ((NBL + KB - 1) / KB + 31) / 32 * 32;
+  static constexpr int MINB = W <= 2 ? 2 : 1;          // narrow strips: two blocks per SM
 };
 
 template <int NY, int W>
-__global__ void __launch_bounds__(ColCfg<NY, W>::T) dm_col_fast(DMArgs<float> a) {
+__global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_fast(DMArgs<float> a) {
   typedef float2 C;
   typedef ColCfg<NY, W> CF;
   constexpr int T = CF::T;
@@ -112,14 +111,11 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T) dm_col_fast(DMArgs<float> a)
   extern __shared__ __align__(128) unsigned char smem[];
   const ColLayout Lo = col_layout(NY, a.pny, W, a.occ_stride, a.n_entries);
   C* buf = reinterpret_cast<C*>(smem + Lo.buf);
-  // staging buffers are selected with conditionals (no dynamically indexed local arrays)
-  C* const stg0 = reinterpret_cast<C*>(smem + Lo.stg0);
-  C* const stg1 = reinterpret_cast<C*>(smem + Lo.stg1);
-  C* const ey0 = reinterpret_cast<C*>(smem + Lo.ey0);
+  C* const stg = reinterpret_cast<C*>(smem + Lo.stg);            // row-pass strip of the layer (single buffer)
+  uint8_t* const occ = smem + Lo.occ;                             // its row flags
+  C* const ey0 = reinterpret_cast<C*>(smem + Lo.ey0);            // Ey rows, double buffered
   C* const ey1 = reinterpret_cast<C*>(smem + Lo.ey1);
-  uint8_t* const occ0 = smem + Lo.occ0;
-  uint8_t* const occ1 = smem + Lo.occ1;
-  float* gsm = reinterpret_cast<float*>(smem + Lo.g);        // per element, buffer order
+  float* gsm = reinterpret_cast<float*>(smem + Lo.g);            // per element, buffer order
   int16_t* kyp = reinterpret_cast<int16_t*>(smem + Lo.kyp);
   C* twlo = reinterpret_cast<C*>(smem + Lo.twlo);
   C* twhi = reinterpret_cast<C*>(smem + Lo.twhi);
@@ -127,7 +123,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T) dm_col_fast(DMArgs<float> a)
   float* lfxw = reinterpret_cast<float*>(smem + Lo.lfxw);
   __shared__ int kxw[8];          // spectrum column of each strip column
   int16_t* list = reinterpret_cast<int16_t*>(smem + Lo.list);
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + Lo.mbar);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + Lo.mbar);  // [0] strip+flags, [1],[2] Ey
   __shared__ int s_nact;
 
   const int tid = threadIdx.x;
@@ -137,6 +133,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T) dm_col_fast(DMArgs<float> a)
   if (tid == 0) {
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
+    mbar_init(&mbar[2], 1);
     fence_mbar_init();
     int n = 0;
     for (int e = 0; e < a.n_entries; ++e)
@@ -166,22 +163,23 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T) dm_col_fast(DMArgs<float> a)
     const float den = 1.f + sqrtf(1.f - sv);
     gsm[idx] = sv * sv * __fdividef(0.5f, den * den);
   }
-  __syncthreads();
   const int nact = s_nact;
   const TwSplit<C> tw{twlo, twhi};
   const uint32_t strip_bytes = (uint32_t)(pny * W * 8);
-  const uint32_t layer_bytes = strip_bytes + (uint32_t)a.occ_stride + (uint32_t)(NY * 8);
 
-  auto issue = [&](int k, int bi) {
-    const int e = list[k];
-    const int u = a.uslot_of_entry[e];
-    uint64_t* bar = bi ? &mbar[1] : &mbar[0];
-    mbar_expect_tx(bar, layer_bytes);
-    bulk_g2s(bi ? stg1 : stg0, a.Rbuf + ((size_t)u * a.nstrips + s) * pny * W, strip_bytes, bar);
-    bulk_g2s(bi ? occ1 : occ0, a.occ + (size_t)u * a.occ_stride, (uint32_t)a.occ_stride, bar);
-    bulk_g2s(bi ? ey1 : ey0, a.ey + (size_t)e * NY, (uint32_t)(NY * 8), bar);
+  auto issue_strip = [&](int k) {
+    const int u = a.uslot_of_entry[list[k]];
+    mbar_expect_tx(&mbar[0], strip_bytes + (uint32_t)a.occ_stride);
+    bulk_g2s(stg, a.Rbuf + ((size_t)u * a.nstrips + s) * pny * W, strip_bytes, &mbar[0]);
+    bulk_g2s(occ, a.occ + (size_t)u * a.occ_stride, (uint32_t)a.occ_stride, &mbar[0]);
   };
-  if (tid == 0 && nact > 0) issue(0, 0);
+  auto issue_ey = [&](int k) {
+    const int e = list[k];
+    uint64_t* bar = (k & 1) ? &mbar[2] : &mbar[1];
+    mbar_expect_tx(bar, (uint32_t)(NY * 8));
+    bulk_g2s((k & 1) ? ey1 : ey0, a.ey + (size_t)e * NY, (uint32_t)(NY * 8), bar);
+  };
+  if (tid == 0 && nact > 0) { issue_strip(0); issue_ey(0); }
 
   // accumulators: last-stage butterfly bb = tid + kb*T of the strip (bb = b*W + w),
   // outputs f at storage position p = b*RL + f of line w
@@ -192,25 +190,25 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T) dm_col_fast(DMArgs<float> a)
     for (int f = 0; f < RL; ++f) acc[kb][f] = make_float2(0.f, 0.f);
 
   for (int k = 0; k < nact; ++k) {
-    const int bi = k & 1;
-    if (tid == 0 && k + 1 < nact) {
-      fence_proxy_async_smem();
-      issue(k + 1, bi ^ 1);
-    }
-    uint64_t* const bar = bi ? &mbar[1] : &mbar[0];
-    uint64_t* const bar_next = bi ? &mbar[0] : &mbar[1];
-    const bool ok = mbar_wait_bounded(bar, (uint32_t)((k >> 1) & 1));
+    // one barrier: layer k's strip and Ey have landed, and the previous
+    // layer's last stage no longer reads the work buffer
+    uint64_t* const bar_e = (k & 1) ? &mbar[2] : &mbar[1];
+    bool ok = mbar_wait_bounded(&mbar[0], (uint32_t)(k & 1));
+    ok = ok && mbar_wait_bounded(bar_e, (uint32_t)((k >> 1) & 1));
     if (__syncthreads_or(!ok)) {
       if (tid == 0) atomicOr(a.err, 1);
-      // let the copies of this block that may still be in flight land
-      mbar_wait_bounded(bar, (uint32_t)((k >> 1) & 1));
-      if (k + 1 < nact) mbar_wait_bounded(bar_next, (uint32_t)(((k + 1) >> 1) & 1));
+      // let this block's copies still in flight land before leaving
+      mbar_wait_bounded(&mbar[0], (uint32_t)(k & 1));
+      mbar_wait_bounded(bar_e, (uint32_t)((k >> 1) & 1));
       return;
+    }
+    if (tid == 0 && k + 1 < nact) {
+      // Ey buffer (k+1)&1 was last read by layer k-1, finished before the barrier
+      fence_proxy_async_smem();
+      issue_ey(k + 1);
     }
     const int e = list[k];
     if (tid < W) exw[tid] = a.exc[(size_t)e * a.Px + kxw[tid]];
-    const C* sg = bi ? stg1 : stg0;
-    const uint8_t* oc = bi ? occ1 : occ0;
     // stage 0 from the staging buffer: inputs j + t*Q0 of the y-shifted line
     for (int idx = tid; idx < Q0 * W; idx += T) {
       const int j = idx / W, w = idx - j * W;
@@ -223,7 +221,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T) dm_col_fast(DMArgs<float> a)
           int y = j + t * Q0 - a.hy;
           if (y < 0) y += NY;
           const int yl = y - a.oy;
-          x[t] = oc[yl] ? sg[yl * W + w] : make_float2(0.f, 0.f);
+          x[t] = occ[yl] ? stg[yl * W + w] : make_float2(0.f, 0.f);
         }
         dft16_halfzero<-1>(x);
       } else {
@@ -233,7 +231,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T) dm_col_fast(DMArgs<float> a)
           if (y < 0) y += NY;
           const int yl = y - a.oy;
           C v = make_float2(0.f, 0.f);
-          if (yl >= 0 && yl < pny && oc[yl]) v = sg[yl * W + w];
+          if (yl >= 0 && yl < pny && occ[yl]) v = stg[yl * W + w];
           x[t] = v;
         }
         DFT<R0, -1, C>::run(x);
@@ -247,12 +245,21 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T) dm_col_fast(DMArgs<float> a)
 #pragma unroll
       for (int f = 0; f < R0; ++f) buf[(j + f * Q0) * W + w] = x[f];
     }
-    FastSched<NY>::template run_middle<-1>(buf, W, 1, W, tw, true);
+    // middle stage(s); the leading barrier also frees the strip buffer
+    __syncthreads();
+    if (tid == 0 && k + 1 < nact) {
+      fence_proxy_async_smem();
+      issue_strip(k + 1);
+    }
+    {
+      constexpr int R1 = FastSched<NY>::r1;
+      fstage_t<NY, R1, NY / R0, -1>(buf, W, 1, W, tw, true);
+    }
     __syncthreads();
     // last stage (stride 1, no twiddles) fused with the transfer-function
     // multiply-accumulate
     const float kz = a.kzp[e];
-    const C* ey = bi ? ey1 : ey0;            // storage order
+    const C* ey = (k & 1) ? ey1 : ey0;            // storage order
 #pragma unroll
     for (int kb = 0; kb < KB; ++kb) {
       const int bb = tid + kb * T;
@@ -274,8 +281,8 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T) dm_col_fast(DMArgs<float> a)
         }
       }
     }
-    __syncthreads();
   }
+  __syncthreads();
 
   // SSB crop and inverse y-FFT input order: spectrum row ky -> i = (ky + hy) mod NY
 #pragma unroll

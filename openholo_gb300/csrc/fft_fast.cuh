@@ -305,6 +305,9 @@ __device__ __forceinline__ void fstages_but_last(C* buf, int nl, int ls, int es,
   }
 }
 
+template <int D, int... Rs> struct FirstOr { static constexpr int value = D; };
+template <int D, int R, int... Rs> struct FirstOr<D, R, Rs...> { static constexpr int value = R; };
+
 template <int... Rs> struct LastOf;
 template <int R> struct LastOf<R> { static constexpr int value = R; };
 template <int R, int... Rs> struct LastOf<R, Rs...> { static constexpr int value = LastOf<Rs...>::value; };
@@ -313,6 +316,7 @@ template <int N, int R0, int... Rest>
 struct SchedImpl {
   static constexpr bool ok = true;
   static constexpr int r0 = R0;
+  static constexpr int r1 = FirstOr<1, Rest...>::value;
   static constexpr int nstages = 1 + (int)sizeof...(Rest);
   static constexpr int rlast = LastOf<R0, Rest...>::value;
   // stages 1 .. S-2 (the caller runs stage 0 and the last stage itself)
