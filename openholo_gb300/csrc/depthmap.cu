@@ -177,58 +177,74 @@ __device__ __forceinline__ void sincos_r(R x, R* s, R* c);
 template <> __device__ __forceinline__ void sincos_r<float>(float x, float* s, float* c) { sincosf(x, s, c); }
 template <> __device__ __forceinline__ void sincos_r<double>(double x, double* s, double* c) { sincos(x, s, c); }
 
+// Two image rows per block: their layer lines are transformed as a pair and
+// stored together, so each strip receives 2*W contiguous complex values
+// (a full 32-byte sector for W = 2).
+constexpr int kRowPair = 2;
+
 template <typename R, int NX>
-__global__ void __launch_bounds__(256) dm_row_pass(DMArgs<R> a) {
+__global__ void __launch_bounds__(512) dm_row_pass(DMArgs<R> a) {
   typedef typename cplx_of<R>::type C;
   extern __shared__ unsigned char smem_raw[];
-  C* buf = reinterpret_cast<C*>(smem_raw);
-  C* v = buf + a.Px;
-  int16_t* li = reinterpret_cast<int16_t*>(v + a.pnx);
-  uint32_t* mask = reinterpret_cast<uint32_t*>(li + ((a.pnx + 7) & ~7));   // keeps 16-byte alignment
-  C* twlo = reinterpret_cast<C*>(mask + 8);          // 64 + ceil(Px/64) twiddles (fast path)
+  const int Px = a.Px, pnx = a.pnx;
+  const int lip = (pnx + 7) & ~7;                       // keeps 16-byte alignment
+  C* buf = reinterpret_cast<C*>(smem_raw);              // [2][Px]
+  C* v = buf + 2 * Px;                                  // [2][pnx] source values
+  int16_t* li = reinterpret_cast<int16_t*>(v + 2 * pnx);   // [2][lip] layer slot per pixel
+  uint32_t* mask = reinterpret_cast<uint32_t*>(li + 2 * lip);   // [2][8] layers present per row
+  C* twlo = reinterpret_cast<C*>(mask + 16);            // 64 + ceil(Px/64) twiddles (fast path)
   C* twhi = twlo + 64;
-  const int r = blockIdx.x;
-  const int nwords = (a.n_uslots + 31) >> 5;
-  for (int i = threadIdx.x; i < nwords; i += blockDim.x) mask[i] = 0u;
+  const int r0 = blockIdx.x * kRowPair;
+  const int nrows = min(kRowPair, a.pny - r0);
+  for (int i = threadIdx.x; i < 16; i += blockDim.x) mask[i] = 0u;
   if constexpr (NX > 0) load_tw_split(twlo, twhi, static_cast<const C*>(a.plx.tw), NX);
   __syncthreads();
-  const size_t rowoff = (size_t)r * a.pnx;
-  for (int c = threadIdx.x; c < a.pnx; c += blockDim.x) {
-    const uint8_t g = a.img[rowoff + c];
-    const int u = g > 0 ? (int)a.lut[a.depth[rowoff + c]] : -1;
-    li[c] = (int16_t)u;
+  for (int idx = threadIdx.x; idx < kRowPair * pnx; idx += blockDim.x) {
+    const int l = idx / pnx, c = idx - l * pnx;
+    int u = -1;
     C val = mk((R)0, (R)0);
-    if (u >= 0) {
-      const R amp = (R)g / (R)255;
-      if (a.phase_mode == OH_PHASE_REFERENCE) {
-        val = mk(amp, (R)0);
-      } else {
-        R ph;
-        if (a.phase_mode == OH_PHASE_ARRAY) ph = (R)a.phase[rowoff + c];
-        else ph = (R)u24_at(a.seed, rowoff + c) * (R)6.283185307179586476925;
-        R sn, cs;
-        sincos_r<R>(ph, &sn, &cs);
-        val = mk(amp * cs, amp * sn);
+    if (l < nrows) {
+      const size_t off = (size_t)(r0 + l) * pnx + c;
+      const uint8_t g = a.img[off];
+      u = g > 0 ? (int)a.lut[a.depth[off]] : -1;
+      if (u >= 0) {
+        const R amp = (R)g / (R)255;
+        if (a.phase_mode == OH_PHASE_REFERENCE) {
+          val = mk(amp, (R)0);
+        } else {
+          R ph;
+          if (a.phase_mode == OH_PHASE_ARRAY) ph = (R)a.phase[off];
+          else ph = (R)u24_at(a.seed, off) * (R)6.283185307179586476925;
+          R sn, cs;
+          sincos_r<R>(ph, &sn, &cs);
+          val = mk(amp * cs, amp * sn);
+        }
+        atomicOr(&mask[l * 8 + (u >> 5)], 1u << (u & 31));
       }
-      atomicOr(&mask[u >> 5], 1u << (u & 31));
     }
-    v[c] = val;
+    li[l * lip + c] = (int16_t)u;
+    v[l * pnx + c] = val;
   }
   __syncthreads();
   for (int u = 0; u < a.n_uslots; ++u) {
-    const bool present = (mask[u >> 5] >> (u & 31)) & 1u;
-    if (threadIdx.x == 0) {
-      a.occ[(size_t)u * a.occ_stride + r] = present ? 1 : 0;
-      if (present) a.slot_any[u] = 1;
+    const bool p0 = (mask[u >> 5] >> (u & 31)) & 1u;
+    const bool p1 = (mask[8 + (u >> 5)] >> (u & 31)) & 1u;
+    if (threadIdx.x < nrows) {
+      const bool pr = threadIdx.x == 0 ? p0 : p1;
+      a.occ[(size_t)u * a.occ_stride + r0 + threadIdx.x] = pr ? 1 : 0;
     }
-    if (!present) continue;
+    if (!(p0 || p1)) continue;
+    if (threadIdx.x == 0) a.slot_any[u] = 1;
     if constexpr (NX > 0) {
-      // stage 0 straight from the source row: inputs j + t*Q0 of the
+      // stage 0 straight from the source rows: inputs j + t*Q0 of each
       // x-shifted, zero-padded line a[j] = u[(j - hx) mod Px]
       constexpr int R0 = FastSched<NX>::r0;
       constexpr int Q0 = NX / R0;
       const TwSplit<C> tw{twlo, twhi};
-      for (int j = threadIdx.x; j < Q0; j += blockDim.x) {
+      for (int idx = threadIdx.x; idx < kRowPair * Q0; idx += blockDim.x) {
+        const int l = idx / Q0, j = idx - l * Q0;
+        const int16_t* lil = li + l * lip;
+        const C* vl = v + l * pnx;
         C x[R0];
         if (R0 == 16 && a.hzx) {
           // 2x padding: inputs t = 4..11 fall in the zero columns
@@ -238,7 +254,7 @@ __global__ void __launch_bounds__(256) dm_row_pass(DMArgs<R> a) {
             int xx = j + t * Q0 - a.hx;
             if (xx < 0) xx += NX;
             const int c = xx - a.ox;
-            x[t] = li[c] == u ? v[c] : mk((R)0, (R)0);
+            x[t] = lil[c] == u ? vl[c] : mk((R)0, (R)0);
           }
           dft16_halfzero<-1>(x);
         } else {
@@ -248,7 +264,7 @@ __global__ void __launch_bounds__(256) dm_row_pass(DMArgs<R> a) {
             if (xx < 0) xx += NX;
             const int c = xx - a.ox;
             C val = mk((R)0, (R)0);
-            if (c >= 0 && c < a.pnx && li[c] == u) val = v[c];
+            if (c >= 0 && c < pnx && lil[c] == u) val = vl[c];
             x[t] = val;
           }
           DFT<R0, -1, C>::run(x);
@@ -259,35 +275,40 @@ __global__ void __launch_bounds__(256) dm_row_pass(DMArgs<R> a) {
 #pragma unroll
           for (int f = 1; f < R0; ++f) x[f] = cmul(x[f], wp[f]);
         }
+        C* bl = buf + l * Px;
 #pragma unroll
-        for (int f = 0; f < R0; ++f) buf[j + f * Q0] = x[f];
+        for (int f = 0; f < R0; ++f) bl[j + f * Q0] = x[f];
       }
-      FastSched<NX>::template run_rest<-1>(buf, 1, a.Px, 1, tw, false);
+      FastSched<NX>::template run_rest<-1>(buf, kRowPair, Px, 1, tw, false);
       __syncthreads();
     } else {
-      // shifted, zero-padded source line: a[j] = u[(j - hx) mod Px]
-      for (int j = threadIdx.x; j < a.Px; j += blockDim.x) {
-        int x = j - a.hx; if (x < 0) x += a.Px;
+      // shifted, zero-padded source lines: a[j] = u[(j - hx) mod Px]
+      for (int idx = threadIdx.x; idx < kRowPair * Px; idx += blockDim.x) {
+        const int l = idx / Px, j = idx - l * Px;
+        int x = j - a.hx; if (x < 0) x += Px;
         const int c = x - a.ox;
         C val = mk((R)0, (R)0);
-        if (c >= 0 && c < a.pnx && li[c] == u) val = v[c];
-        buf[j] = val;
+        if (c >= 0 && c < pnx && li[l * lip + c] == u) val = v[l * pnx + c];
+        buf[idx] = val;
       }
-      block_fft<-1>(buf, 1, a.Px, 1, a.plx, false);
+      block_fft<-1>(buf, kRowPair, Px, 1, a.plx, false);
     }
+    // store: strip s holds rows r0, r0+1 contiguously -> 2*W values per strip
     C* dst = a.Rbuf + (size_t)u * a.nstrips * a.pny * a.W;
-    if (a.xs) {
-      // storage order: column p of the strip layout is FFT output position p
-      for (int p = threadIdx.x; p < a.Px; p += blockDim.x) {
-        const int s = p / a.W, w = p - s * a.W;
-        dst[((size_t)s * a.pny + r) * a.W + w] = buf[p];
+    const int W = a.W;
+    for (int idx = threadIdx.x; idx < nrows * Px; idx += blockDim.x) {
+      const int s = idx / (nrows * W);
+      const int rem = idx - s * nrows * W;
+      const int l = rem / W, w = rem - l * W;
+      const int col = s * W + w;                         // strip column
+      C val;
+      if (a.xs) {
+        val = buf[l * Px + col];                         // FFT storage order
+      } else {
+        int m = col - a.hx; if (m < 0) m += Px;          // S[kx] = A[(kx - hx) mod Px]
+        val = buf[l * Px + a.plx.perm[m]];
       }
-    } else {
-      for (int kx = threadIdx.x; kx < a.Px; kx += blockDim.x) {
-        int m = kx - a.hx; if (m < 0) m += a.Px;       // S[kx] = A[(kx - hx) mod Px]
-        const int s = kx / a.W, w = kx - s * a.W;
-        dst[((size_t)s * a.pny + r) * a.W + w] = buf[a.plx.perm[m]];
-      }
+      dst[((size_t)s * a.pny + r0 + l) * W + w] = val;
     }
     __syncthreads();
   }
@@ -619,8 +640,9 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   a.hzy = (p->pad == 2 && r0y == 16 && (a.Py % 16) == 0 && a.oy * 4 == a.Py && a.hy * 2 == a.Py) ? 1 : 0;
   const size_t smem_col = Wfast ? (size_t)col_layout(a.Py, a.pny, W, occ_stride, su.n_entries).total
                                 : (size_t)W * a.Py * sizeof(C) + W * (sizeof(C) + sizeof(R)) + (size_t)a.Py * sizeof(int);
-  const size_t smem_row = (size_t)a.Px * sizeof(C) + (size_t)a.pnx * sizeof(C) + (size_t)((a.pnx + 7) & ~7) * sizeof(int16_t) +
-                          8 * sizeof(uint32_t) + (64 + (size_t)(a.Px + 63) / 64) * sizeof(C);
+  const size_t smem_row = kRowPair * ((size_t)a.Px * sizeof(C) + (size_t)a.pnx * sizeof(C) +
+                                      (size_t)((a.pnx + 7) & ~7) * sizeof(int16_t)) +
+                          16 * sizeof(uint32_t) + (64 + (size_t)(a.Px + 63) / 64) * sizeof(C);
   const size_t smem_out = (size_t)a.Px * sizeof(C) + (64 + (size_t)(a.Px + 63) / 64) * sizeof(C);
   if (smem_row > smax || smem_out > smax) return fail(OH_ERR_UNSUPPORTED_SIZE, "padded row length " + std::to_string(a.Px) + " exceeds shared memory");
 
@@ -679,7 +701,7 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
     cudaError_t e = cudaFuncSetAttribute(dm_row_pass<R, NX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_row);
     if (e != cudaSuccess) { rs = cuda_fail(e, "cudaFuncSetAttribute(dm_row_pass)"); return; }
     KernelTimer kt(ctx, prec ? "dm_row_pass_f64" : "dm_row_pass", st);
-    dm_row_pass<R, NX><<<a.pny, 256, smem_row, st>>>(a);
+    dm_row_pass<R, NX><<<(a.pny + kRowPair - 1) / kRowPair, 512, smem_row, st>>>(a);
     note_launch();
     e = cudaGetLastError();
     if (e != cudaSuccess) rs = cuda_fail(e, "dm_row_pass launch");
