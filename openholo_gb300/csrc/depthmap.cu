@@ -50,7 +50,7 @@ template <typename R>
 struct DMArgs {
   typedef typename cplx_of<R>::type C;
   int pnx, pny, Px, Py, ox, oy, hx, hy;
-  int W, nstrips, n_entries, n_uslots;
+  int W, lw, nstrips, n_entries, n_uslots;     // lw = log2(W)
   int cx1, cx2, cy1, cy2;            // SSB crop window on the (padded) spectrum
   double ppx, ppy, ssx, ssy, lambda, k;
   const uint8_t* img;
@@ -294,13 +294,15 @@ __global__ void __launch_bounds__(512) dm_row_pass(DMArgs<R> a) {
       block_fft<-1>(buf, kRowPair, Px, 1, a.plx, false);
     }
     // store: strip s holds rows r0, r0+1 contiguously -> 2*W values per strip
+    // (W is a power of two: index split with shifts)
     C* dst = a.Rbuf + (size_t)u * a.nstrips * a.pny * a.W;
-    const int W = a.W;
+    const int W = a.W, lw = a.lw;
     for (int idx = threadIdx.x; idx < nrows * Px; idx += blockDim.x) {
-      const int s = idx / (nrows * W);
-      const int rem = idx - s * nrows * W;
-      const int l = rem / W, w = rem - l * W;
-      const int col = s * W + w;                         // strip column
+      const int w = idx & (W - 1);
+      const int t = idx >> lw;
+      const int l = nrows == 2 ? (t & 1) : 0;
+      const int s = nrows == 2 ? (t >> 1) : t;
+      const int col = (s << lw) + w;                     // strip column
       C val;
       if (a.xs) {
         val = buf[l * Px + col];                         // FFT storage order
@@ -629,6 +631,7 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   }
   if (W == 0) return fail(OH_ERR_UNSUPPORTED_SIZE, "padded column length " + std::to_string(a.Py) + " too long for the column pass");
   a.W = W; a.nstrips = a.Px / W;
+  a.lw = W == 8 ? 3 : W == 4 ? 2 : W == 2 ? 1 : 0;
   a.ey_perm = Wfast ? 1 : 0;
   bool fastx = false;
   with_fast_n(a.Px, [&](auto nc) { fastx = decltype(nc)::value > 0; });
