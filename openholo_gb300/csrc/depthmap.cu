@@ -612,10 +612,11 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   bool fastlen = false;
   with_fast_n(a.Py, [&](auto nc) { fastlen = decltype(nc)::value > 0; });
   if (prec == 0 && fastlen) {
-    // strip width: 4 (one block per SM) unless overridden by OH_DM_COL_W
+    // strip width: 2 (two blocks per SM) when it fits, else 4; OH_DM_COL_W
+    // forces one of them
     int want = 0;
     if (const char* ev = std::getenv("OH_DM_COL_W")) want = std::atoi(ev);
-    for (int cand : {4, 2}) {
+    for (int cand : {2, 4}) {
       if (want && cand != want) continue;
       if (a.Px % cand) continue;
       if ((size_t)col_layout(a.Py, a.pny, cand, occ_stride, su.n_entries).total <= smax) { Wfast = cand; break; }
