@@ -58,20 +58,73 @@ def load_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi sampled every 200 ms while the timed region runs."""
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    """SM clock and throttle reasons sampled while the timed region runs.
+
+    Polls NVML through ctypes every 2 ms (reads only); falls back to
+    nvidia-smi at 200 ms when NVML cannot be loaded."""
+    # NVML clocks-event reason bits
+    REASONS = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown", 0x20: "sw_thermal_slowdown", 0x4: "sw_power_cap"}
 
     def __init__(self, gpu: int):
         self.gpu = gpu
+        self.samples = []
+        self.stop = None
+        self.max_mhz = None
         self.proc = None
-        self.path = Path(tempfile.gettempdir()) / f"oh_clocks_{os.getpid()}.csv"
+
+    def _nvml(self):
+        import ctypes as C
+        for name in ("libnvidia-ml.so.1", "libnvidia-ml.so"):
+            try:
+                lib = C.CDLL(name)
+                break
+            except OSError:
+                lib = None
+        if lib is None or lib.nvmlInit_v2() != 0:
+            return None
+        h = C.c_void_p()
+        bus = None
+        try:
+            import torch
+            pr = torch.cuda.get_device_properties(self.gpu)
+            bus = "%08x:%02x:%02x.0" % (getattr(pr, "pci_domain_id"), getattr(pr, "pci_bus_id"),
+                                        getattr(pr, "pci_device_id"))
+        except Exception:
+            bus = None
+        if bus is None or lib.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), C.byref(h)) != 0:
+            if lib.nvmlDeviceGetHandleByIndex_v2(self.gpu, C.byref(h)) != 0:
+                return None
+        return lib, h
 
     def __enter__(self):
+        import threading
+        import ctypes as C
+        nv = self._nvml()
+        if nv is not None:
+            lib, h = nv
+            mx = C.c_uint()
+            if lib.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx)) == 0:
+                self.max_mhz = mx.value
+            self.stop = threading.Event()
+
+            def run():
+                clk = C.c_uint()
+                rs = C.c_ulonglong()
+                get_r = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                    lib.nvmlDeviceGetCurrentClocksThrottleReasons
+                while not self.stop.is_set():
+                    if lib.nvmlDeviceGetClockInfo(h, 1, C.byref(clk)) == 0 and get_r(h, C.byref(rs)) == 0:
+                        self.samples.append((clk.value, rs.value))
+                    time.sleep(0.002)
+            self.thread = threading.Thread(target=run, daemon=True)
+            self.thread.start()
+            return self
         try:
+            self.path = Path(tempfile.gettempdir()) / f"oh_clocks_{os.getpid()}.csv"
             self.fh = open(self.path, "w")
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=clocks.sm,clocks.max.sm,"
+                                          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                                          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
                                           "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
                                          stderr=subprocess.DEVNULL)
         except Exception:
@@ -79,37 +132,34 @@ class ClockSampler:
         return self
 
     def __exit__(self, *a):
+        if self.stop is not None:
+            self.stop.set()
+            self.thread.join(timeout=2)
         if self.proc is not None:
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
-        try:
             self.fh.close()
-        except Exception:
-            pass
+            for ln in self.path.read_text().splitlines():
+                f = [x.strip() for x in ln.split(",")]
+                if len(f) >= 6 and f[0].replace(".", "").isdigit():
+                    bits = sum(b for b, x in zip((0x8, 0x40, 0x20, 0x4), f[2:6]) if x.lower() == "active")
+                    self.samples.append((float(f[0]), bits))
+                    self.max_mhz = float(f[1]) if f[1].replace(".", "").isdigit() else self.max_mhz
+            try:
+                self.path.unlink()
+            except Exception:
+                pass
 
     def summary(self):
-        if self.proc is None or not self.path.exists():
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        rows = []
-        for ln in self.path.read_text().splitlines():
-            f = [x.strip() for x in ln.split(",")]
-            if len(f) >= 9:
-                rows.append(f)
-        try:
-            self.path.unlink()
-        except Exception:
-            pass
-        if not rows:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": ["no samples"], "samples": 0}
+        reasons = sorted({name for _, r in self.samples for bit, name in self.REASONS.items() if r & bit})
+        return {"sm_mhz": statistics.median(c for c, _ in self.samples), "sm_max_mhz": self.max_mhz,
+                "reasons": reasons, "samples": len(self.samples),
+                "source": "nvml" if self.stop is not None else "nvidia-smi"}
 
 
 def dist_setup():
@@ -206,6 +256,74 @@ def plain_gpu_path(img_t, depth_t, zt, lut, torch):
         h = torch.fft.fftshift(torch.fft.ifft2(torch.fft.fftshift(Uc)))[oy:oy + NY, ox:ox + NX]
         return (h * shy[:, None]).real
     return frame
+
+
+def secondary_measurements(ctx, dev, torch, reps=5):
+    """The other operators at their own workloads (seeded synthetic inputs):
+    config 1, point-cloud Fresnel/R-S sum 1024x1024 x 5000 points + phase-only
+    encoding; config 3, WRP (200,000 points, 64x64 windows) + zero-padded
+    Fresnel propagation to 3840x2160 at 3.74 um + phase-only encoding."""
+    import ctypes as C
+    from openholo_gb300 import _lib, scenes
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    out = {}
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    # config 1
+    n, nx, ny = 5000, 1024, 1024
+    pts = torch.from_numpy(scenes.pointcloud_scene(11, n).astype(np.float32)).to(dev)
+    p = _lib.PcParams(1.0, 1.0, 1.0, 0.0, 8e-6, 8e-6, nx, ny, 532e-9, 0.0, 0.0)
+    f32 = torch.empty((ny, nx), dtype=torch.complex64, device=dev)
+    u8 = torch.empty((ny, nx), dtype=torch.uint8, device=dev)
+
+    def pc():
+        _lib.call("oh_pointcloud", ctx.handle, 0, C.byref(p), C.c_void_p(pts.data_ptr()), n,
+                  C.c_void_p(f32.data_ptr()), None, st)
+        _lib.call("oh_encode", ctx.handle, 0, 9, nx, ny, C.c_void_p(f32.data_ptr()), C.c_void_p(u8.data_ptr()), st)
+    ms = timed(pc)
+    f64 = torch.empty((ny, nx), dtype=torch.complex128, device=dev)
+    _lib.call("oh_pointcloud", ctx.handle, 1, C.byref(p), C.c_void_p(pts.data_ptr()), n,
+              C.c_void_p(f64.data_ptr()), None, st)
+    torch.cuda.synchronize()
+    err = float(torch.linalg.norm(f32.to(torch.complex128) - f64) / torch.linalg.norm(f64))
+    out["pointcloud_1024x1024_5000pts"] = {"ms_per_hologram": ms, "holograms_per_s": 1000.0 / ms,
+                                           "point_pixel_terms_per_s": n * nx * ny / (ms / 1000.0),
+                                           "rel_err_vs_fp64": err, "dtype": "f32 (FP64-reduced phase tables)"}
+    del f64
+    # config 3
+    npts, hx, hy, dp, lam = 200_000, 3840, 2160, 3.74e-6, 532e-9
+    xyz = scenes.wrp_scene(12, npts)
+    z_wrp = float(xyz[:, 2].min()) - 5e-3
+    t_xyz = torch.from_numpy(xyz).to(dev)
+    wrp = torch.zeros((hy, hx), dtype=torch.complex64, device=dev)
+    hol = torch.empty((hy, hx), dtype=torch.uint8, device=dev)
+    wp = _lib.WrpParams(hx, hy, dp, lam, z_wrp, 32)
+
+    def wrp_frame():
+        wrp.zero_()
+        _lib.call("oh_wrp_accumulate", ctx.handle, 0, C.byref(wp), C.c_void_p(t_xyz.data_ptr()), npts,
+                  C.c_void_p(wrp.data_ptr()), st)
+        _lib.call("oh_fresnel_propagate", ctx.handle, 0, hx, hy, dp, lam, z_wrp, C.c_void_p(wrp.data_ptr()), st)
+        _lib.call("oh_encode", ctx.handle, 0, 9, hx, hy, C.c_void_p(wrp.data_ptr()), C.c_void_p(hol.data_ptr()), st)
+    ctx.set_timing(True)
+    ctx.read_timing(reset=True)
+    ms3 = timed(wrp_frame)
+    kt = ctx.read_timing(reset=True)
+    ctx.set_timing(False)
+    out["wrp_200k_64x64_fresnel_3840x2160"] = {"ms_per_hologram": ms3, "holograms_per_s": 1000.0 / ms3,
+                                               "kernels_ms": {k: v[0] / (reps + 1) for k, v in kt.items()},
+                                               "dtype": "f32"}
+    return out
 
 
 def main():
@@ -327,6 +445,11 @@ def main():
            "clocks": clocks}
 
     if rank == 0 and world == 1 and not args.no_baselines:
+        try:
+            out["other_operators"] = secondary_measurements(ctx, dev, torch)
+        except Exception as e:  # pragma: no cover
+            out["other_operators"] = {"error": str(e)[:300]}
+        torch.cuda.empty_cache()
         # accuracy of this frame against the FP64 path (pinned to the oracle in tests)
         f64 = dm.generate(ctx, p, d_img, d_depth, precision="fp64")
         torch.cuda.synchronize()

@@ -40,6 +40,7 @@ oh_status scratch(oh_ctx* ctx, const char* name, size_t bytes, void** out) {
   auto& b = ctx->scratch[name];
   if (b.bytes < bytes) {
     ctx->dm_setup_key.clear();          // cached tables may live in a buffer being replaced
+    ctx->fresnel_key.clear();
     if (b.p) {
       cudaError_t e = cudaDeviceSynchronize();
       if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceSynchronize (scratch growth)");
@@ -260,6 +261,7 @@ oh_status oh_ctx_release_scratch(oh_ctx* ctx) {
   for (auto& kv : ctx->scratch) cudaFree(kv.second.p);
   ctx->scratch.clear();
   ctx->dm_setup_key.clear();
+  ctx->fresnel_key.clear();
   cudaSetDevice(prev);
   return OH_OK;
 }

@@ -17,6 +17,7 @@ struct oh_ctx {
   cudaEvent_t last_done = nullptr;   // recorded at the end of every call
   int* dev_err = nullptr;             // set by kernels whose bounded waits ran out
   std::string dm_setup_key;           // parameters of the depth-map tables now in scratch
+  std::string fresnel_key;            // parameters of the Fresnel spectrum in scratch "fr.B"
   struct Buf { void* p = nullptr; size_t bytes = 0; };
   std::map<std::string, Buf> scratch;
   struct PlanBufs { oh::FFTPlan plan; void* tw = nullptr; int* perm = nullptr; int* iperm = nullptr; };

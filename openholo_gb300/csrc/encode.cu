@@ -72,6 +72,7 @@ static oh_status reduce(oh_ctx* ctx, const void* in, size_t n, int op, const R* 
   void* ptr;
   OH_TRY(scratch(ctx, slot, sizeof(R) * 2 * nb, &ptr));
   *red = (R*)ptr;
+  KernelTimer kt(ctx, "reduce", st);
   reduce_partial<R><<<nb, 256, 0, st>>>(in, n, op, refp, *red);
   OH_LAUNCH_CHECK();
   reduce_final<R><<<1, 256, 0, st>>>(*red, nb);
@@ -211,6 +212,7 @@ static oh_status run_encode(oh_ctx* ctx, int kind, int nx, int ny, const void* f
     OH_TRY(reduce<R>(ctx, field, n, RED_MAX_NI, red1, &red2, st, "enc.red2"));
   }
   if (kind == OH_ENC_PHASE_ONLY_U8) OH_TRY(reduce<R>(ctx, field, n, RED_MAX_PHASE, (const R*)nullptr, &red1, st, "enc.red1"));
+  KernelTimer kt(ctx, "encode_map", st);
   encode_map<R><<<grid, 256, 0, st>>>(kind, nx, ny, (const C*)field, red1, red2, out);
   OH_LAUNCH_CHECK();
   return OH_OK;

@@ -146,26 +146,40 @@ static oh_status run_fresnel(oh_ctx* ctx, int nx, int ny, double dp, double lamb
   void* pa;
   void* pb;
   OH_TRY(scratch(ctx, "fr.a", n2 * sizeof(C), &pa));
-  // cached transfer function: key stored beside the buffer
+  // one cached transfer-function spectrum per context, keyed by its parameters
   char key[160];
-  std::snprintf(key, sizeof(key), "fr.B:%d:%d:%d:%.17g:%.17g:%.17g", prec, NX, NY, dp, lambda, z);
-  auto it = ctx->scratch.find(key);
-  bool have = it != ctx->scratch.end() && it->second.bytes >= n2 * sizeof(C);
-  OH_TRY(scratch(ctx, key, n2 * sizeof(C), &pb));
+  std::snprintf(key, sizeof(key), "%d:%d:%d:%.17g:%.17g:%.17g", prec, NX, NY, dp, lambda, z);
+  void* prev_b = nullptr;
+  {
+    auto it = ctx->scratch.find("fr.B");
+    if (it != ctx->scratch.end()) prev_b = it->second.p;
+  }
+  OH_TRY(scratch(ctx, "fr.B", n2 * sizeof(C), &pb));
+  const bool have = prev_b == pb && ctx->fresnel_key == key;
+  ctx->fresnel_key = key;
   const int grid = 152 * 8;
   if (!have) {
     fresnel_kernel_sample<R><<<grid, 256, 0, st>>>(NX, NY, dp, lambda, z, (C*)pb);
     OH_LAUNCH_CHECK();
     OH_TRY(fft2d_enqueue(ctx, prec, NX, NY, pb, pb, nullptr, -1, 0, 0, st));
   }
-  fresnel_pad<R><<<grid, 256, 0, st>>>(nx, ny, (const C*)field, (C*)pa);
-  OH_LAUNCH_CHECK();
+  {
+    KernelTimer kt(ctx, "fresnel_pad", st);
+    fresnel_pad<R><<<grid, 256, 0, st>>>(nx, ny, (const C*)field, (C*)pa);
+    OH_LAUNCH_CHECK();
+  }
   OH_TRY(fft2d_enqueue(ctx, prec, NX, NY, pa, pa, nullptr, -1, 0, 0, st));
-  cmul_inplace<R><<<grid, 256, 0, st>>>(n2, (C*)pa, (const C*)pb);
-  OH_LAUNCH_CHECK();
+  {
+    KernelTimer kt(ctx, "fresnel_mul", st);
+    cmul_inplace<R><<<grid, 256, 0, st>>>(n2, (C*)pa, (const C*)pb);
+    OH_LAUNCH_CHECK();
+  }
   OH_TRY(fft2d_enqueue(ctx, prec, NX, NY, pa, pa, nullptr, 1, 0, 1, st));
-  fresnel_crop<R><<<grid, 256, 0, st>>>(nx, ny, (const C*)pa, (C*)field);
-  OH_LAUNCH_CHECK();
+  {
+    KernelTimer kt(ctx, "fresnel_crop", st);
+    fresnel_crop<R><<<grid, 256, 0, st>>>(nx, ny, (const C*)pa, (C*)field);
+    OH_LAUNCH_CHECK();
+  }
   return OH_OK;
 }
 
@@ -186,6 +200,7 @@ oh_status oh_wrp_accumulate(oh_ctx* ctx, oh_precision prec, const oh_wrp_params*
   if (n_points == 0) return OH_OK;
   WRPGeom g{p->nx, p->ny, p->pitch, p->lambda, p->z_wrp, p->window};
   const int grid = std::min(n_points, 152 * 32);
+  KernelTimer kt(ctx, "wrp_accumulate", st);
   if (prec == OH_FP64) wrp_accumulate_kernel<double><<<grid, 256, 0, st>>>(g, xyz, n_points, (double2*)wrp);
   else wrp_accumulate_kernel<float><<<grid, 256, 0, st>>>(g, xyz, n_points, (float2*)wrp);
   OH_LAUNCH_CHECK();

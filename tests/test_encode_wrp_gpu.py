@@ -102,3 +102,17 @@ def test_fresnel_point_focus(ctx):
     torch.cuda.synchronize()
     back = np.abs(t.cpu().numpy())
     assert np.unravel_index(np.argmax(back), back.shape) == (n // 2, n // 2)
+
+
+def test_fresnel_spectrum_cache_follows_distance(ctx):
+    """Alternating propagation distances reuse one cached spectrum slot
+    correctly (results equal the oracle for each distance)."""
+    ny, nx = 48, 64
+    U = field_sample(ny, nx, 3)
+    dp, lam = 8e-6, 532e-9
+    for z in (0.02, 0.035, 0.02):
+        t = torch.from_numpy(U).cuda()
+        _lib.call("oh_fresnel_propagate", ctx.handle, 1, nx, ny, dp, lam, z, C.c_void_p(t.data_ptr()), S())
+        torch.cuda.synchronize()
+        ref = owrp.fresnel_conv(U, dp, lam, z)
+        assert np.linalg.norm(t.cpu().numpy() - ref) <= 1e-10 * np.linalg.norm(ref), z
