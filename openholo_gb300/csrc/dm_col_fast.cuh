@@ -39,8 +39,8 @@ __host__ __device__ inline ColLayout col_layout(int Py, int pny, int W, int occ_
   int o = 0;
   L.buf = col_take(&o, Py * W * 8);
   L.stg = col_take(&o, pny * W * 8);
-  L.ey0 = col_take(&o, Py * 8);
-  L.ey1 = col_take(&o, Py * 8);
+  L.ey0 = col_take(&o, Py * 4);
+  L.ey1 = col_take(&o, Py * 4);
   L.occ = col_take(&o, occ_stride);
   L.g = col_take(&o, Py * W * 4);
   L.kyp = col_take(&o, Py * 2);
@@ -113,8 +113,8 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
   C* buf = reinterpret_cast<C*>(smem + Lo.buf);
   C* const stg = reinterpret_cast<C*>(smem + Lo.stg);            // row-pass strip of the layer (single buffer)
   uint8_t* const occ = smem + Lo.occ;                             // its row flags
-  C* const ey0 = reinterpret_cast<C*>(smem + Lo.ey0);            // Ey rows, double buffered
-  C* const ey1 = reinterpret_cast<C*>(smem + Lo.ey1);
+  float* const ey0 = reinterpret_cast<float*>(smem + Lo.ey0);    // Ey phase rows, double buffered
+  float* const ey1 = reinterpret_cast<float*>(smem + Lo.ey1);
   float* gsm = reinterpret_cast<float*>(smem + Lo.g);            // per element, buffer order
   int16_t* kyp = reinterpret_cast<int16_t*>(smem + Lo.kyp);
   C* twlo = reinterpret_cast<C*>(smem + Lo.twlo);
@@ -176,8 +176,8 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
   auto issue_ey = [&](int k) {
     const int e = list[k];
     uint64_t* bar = (k & 1) ? &mbar[2] : &mbar[1];
-    mbar_expect_tx(bar, (uint32_t)(NY * 8));
-    bulk_g2s((k & 1) ? ey1 : ey0, a.ey + (size_t)e * NY, (uint32_t)(NY * 8), bar);
+    mbar_expect_tx(bar, (uint32_t)(NY * 4));
+    bulk_g2s((k & 1) ? ey1 : ey0, a.eth + (size_t)e * NY, (uint32_t)(NY * 4), bar);
   };
   if (tid == 0 && nact > 0) { issue_strip(0); issue_ey(0); }
 
@@ -208,7 +208,8 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
       issue_ey(k + 1);
     }
     const int e = list[k];
-    if (tid < W) exw[tid] = a.exc[(size_t)e * a.Px + kxw[tid]];
+    // the row pass already applied C * Ex when it stored in storage order
+    if (tid < W) exw[tid] = a.xs ? make_float2(1.f, 0.f) : a.exc[(size_t)e * a.Px + kxw[tid]];
     // stage 0 from the staging buffer: inputs j + t*Q0 of the y-shifted line
     for (int idx = tid; idx < Q0 * W; idx += T) {
       const int j = idx / W, w = idx - j * W;
@@ -259,7 +260,8 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
     // last stage (stride 1, no twiddles) fused with the transfer-function
     // multiply-accumulate
     const float kz = a.kzp[e];
-    const C* ey = (k & 1) ? ey1 : ey0;            // storage order
+    const float* eth = (k & 1) ? ey1 : ey0;       // storage order
+    const float inv2pi = 0.15915494309189533577f, two_pi = 6.28318530717958647692f;
 #pragma unroll
     for (int kb = 0; kb < KB; ++kb) {
       const int bb = tid + kb * T;
@@ -273,10 +275,12 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
 #pragma unroll
         for (int f = 0; f < RL; ++f) {
           const int p = b * RL + f;
-          const float psi = kz * gsm[p * W + w];
+          // H / (C Ex) = exp(i (pi lambda z' fy^2 + k z' g)), both parts reduced
+          float ph = fmaf(kz, gsm[p * W + w], eth[p]);
+          ph = fmaf(-two_pi, rintf(ph * inv2pi), ph);
           float sn, cs;
-          __sincosf(psi, &sn, &cs);
-          const C h = cmul(cmul(ex, ey[p]), make_float2(cs, sn));
+          __sincosf(ph, &sn, &cs);
+          const C h = a.xs ? make_float2(cs, sn) : cmul(ex, make_float2(cs, sn));
           acc[kb][f] = cadd(acc[kb][f], cmul(h, x[f]));
         }
       }

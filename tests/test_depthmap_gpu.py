@@ -65,10 +65,12 @@ def test_depthmap_vs_oracle(ctx, dev, pad, precision):
     assert rel(fr, ref_fr) < tol
 
 
-@pytest.mark.parametrize("shape,pad,L", [((540, 960), 2, 12), ((512, 512), 2, 8), ((1080, 1920), 1, 6)])
+@pytest.mark.parametrize("shape,pad,L", [((540, 960), 2, 12), ((512, 512), 2, 8), ((1080, 1920), 1, 6),
+                                         ((540, 500), 2, 7)])
 def test_fast_lengths_vs_oracle(ctx, dev, shape, pad, L):
     """FFT grids with compile-time schedules (1920x1080, 1024x1024): the
-    bulk-copy pipelined column pass and the scheduled row/output passes."""
+    bulk-copy pipelined column pass and the scheduled row/output passes; and
+    a generic row length (1000) with a scheduled column length (1080)."""
     ny, nx = shape
     img, depth = scenes.depthmap_scene(61, ny, nx)
     p = dm.make_params(pnx=nx, pny=ny, num_of_depth=L, pad=pad, phase_mode=dm.OH_PHASE_SEEDED, seed=4)
