@@ -44,7 +44,6 @@ struct DMSetup {
   double zp[kMaxEntries];            // z' of each render entry
   double cre[kMaxEntries], cim[kMaxEntries];   // per-entry complex constant
   int16_t lut[256];                  // depth byte -> unique slot (-1: none)
-  int16_t entry_of_uslot[kMaxEntries];   // first render entry of each unique slot
 };
 
 template <typename R>
@@ -65,7 +64,6 @@ struct DMArgs {
   R* kzp;                // k*z' per entry
   C* cst;                // per-entry constant
   C* exc;                // [entries][Px] cst*exp(i alpha fx^2)   (fp32 path)
-  C* excp;               // [uslots][Px] the same factor in x-FFT storage order (fast passes)
   R* eth;                // [entries][Py] phase alpha fy^2 reduced to [-pi, pi], y storage order (fast passes)
   C* ey;                 // [entries][Py] exp(i alpha fy^2)       (fp32 path)
   R* lfx;                // [Px] (lambda fx)^2
@@ -140,19 +138,6 @@ __global__ void dm_setup(DMArgs<R> a, DMSetup s) {
       double2 v = cexp_reduced(pi * a.lambda * s.zp[e] * fx * fx);
       double2 c = make_double2(s.cre[e], s.cim[e]);
       a.exc[idx] = mk((R)(c.x * v.x - c.y * v.y), (R)(c.x * v.y + c.y * v.x));
-    }
-    if (a.xs) {
-      // C * exp(i alpha fx^2) per unique slot, at x-FFT storage position p
-      for (int idx = tid; idx < s.n_uslots * a.Px; idx += nthr) {
-        int u = idx / a.Px, p = idx - u * a.Px;
-        int e = s.entry_of_uslot[u];
-        int x = a.plx.iperm[p] + a.hx;
-        if (x >= a.Px) x -= a.Px;
-        double fx = (-1.0 / (2.0 * a.ppx)) + (1.0 / a.ssx) * (double)x;
-        double2 v = cexp_reduced(pi * a.lambda * s.zp[e] * fx * fx);
-        double2 c = make_double2(s.cre[e], s.cim[e]);
-        a.excp[idx] = mk((R)(c.x * v.x - c.y * v.y), (R)(c.x * v.y + c.y * v.x));
-      }
     }
     if (a.ey_perm) {
       const double two_pi = 6.283185307179586476925286766559;
@@ -332,10 +317,7 @@ __global__ void __launch_bounds__(512) dm_row_pass(DMArgs<R> a) {
       const int col = (s << lw) + w;                     // strip column
       C val;
       if (a.xs) {
-        // FFT storage order, times this level's C * exp(i alpha fx^2)
-        // (constant along y, so it commutes with the column transform)
-        if constexpr (sizeof(R) == 4) val = cmul(buf[l * Px + col], a.excp[(size_t)u * Px + col]);
-        else val = buf[l * Px + col];
+        val = buf[l * Px + col];                         // FFT storage order
       } else {
         int m = col - a.hx; if (m < 0) m += Px;          // S[kx] = A[(kx - hx) mod Px]
         val = buf[l * Px + a.plx.perm[m]];
@@ -581,11 +563,7 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   std::vector<int> uslot_of_dtr(nd + 1, -1);
   for (size_t e = 0; e < render.size(); ++e) {
     int d = render[e];
-    if (uslot_of_dtr[d] < 0) {
-      su.entry_of_uslot[udtr.size()] = (int16_t)e;
-      uslot_of_dtr[d] = (int)udtr.size();
-      udtr.push_back(d);
-    }
+    if (uslot_of_dtr[d] < 0) { uslot_of_dtr[d] = (int)udtr.size(); udtr.push_back(d); }
     su.uslot_of_entry[e] = (int16_t)uslot_of_dtr[d];
     const double z = L.ztrans[d - 1];
     su.zp[e] = z;
@@ -696,13 +674,13 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   size_t o_lut = carve(256 * sizeof(int16_t)), o_use = carve(nE * sizeof(int16_t)), o_kz = carve(nE * sizeof(R)),
          o_cst = carve(nE * sizeof(C)), o_exc = carve(prec ? 0 : nE * a.Px * sizeof(C)),
          o_ey = carve(prec ? 0 : nE * a.Py * sizeof(C)),
-         o_excp = carve(a.xs ? nU * a.Px * sizeof(C) : 0), o_eth = carve(a.ey_perm ? nE * a.Py * sizeof(R) : 0), o_lfx = carve(a.Px * sizeof(R)), o_lfy = carve(a.Py * sizeof(R)), o_lfyp = carve(a.Py * sizeof(R)),
+         o_eth = carve(a.ey_perm ? nE * a.Py * sizeof(R) : 0), o_lfx = carve(a.Px * sizeof(R)), o_lfy = carve(a.Py * sizeof(R)), o_lfyp = carve(a.Py * sizeof(R)),
          o_shy = carve(a.pny * sizeof(C)), o_shx = carve(a.pnx * sizeof(C)), o_any = carve(nU * sizeof(int));
   OH_TRY(scratch(ctx, "dm.tables", off, &ptr));
   char* base = (char*)ptr;
   a.lut = (int16_t*)(base + o_lut); a.uslot_of_entry = (int16_t*)(base + o_use); a.kzp = (R*)(base + o_kz);
   a.cst = (C*)(base + o_cst); a.exc = (C*)(base + o_exc); a.ey = (C*)(base + o_ey);
-  a.excp = (C*)(base + o_excp); a.eth = (R*)(base + o_eth);
+  a.eth = (R*)(base + o_eth);
   a.lfx = (R*)(base + o_lfx); a.lfy = (R*)(base + o_lfy); a.lfyp = (R*)(base + o_lfyp); a.shy = (C*)(base + o_shy); a.shx = (C*)(base + o_shx);
   a.slot_any = (int*)(base + o_any);
   a.fringe = (R*)fringe; a.field = (C*)field; a.spectrum = (C*)spectrum;

@@ -208,8 +208,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
       issue_ey(k + 1);
     }
     const int e = list[k];
-    // the row pass already applied C * Ex when it stored in storage order
-    if (tid < W) exw[tid] = a.xs ? make_float2(1.f, 0.f) : a.exc[(size_t)e * a.Px + kxw[tid]];
+    if (tid < W) exw[tid] = a.exc[(size_t)e * a.Px + kxw[tid]];
     // stage 0 from the staging buffer: inputs j + t*Q0 of the y-shifted line
     for (int idx = tid; idx < Q0 * W; idx += T) {
       const int j = idx / W, w = idx - j * W;
@@ -275,12 +274,12 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
 #pragma unroll
         for (int f = 0; f < RL; ++f) {
           const int p = b * RL + f;
-          // H / (C Ex) = exp(i (pi lambda z' fy^2 + k z' g)), both parts reduced
+          // H = C Ex exp(i (pi lambda z' fy^2 + k z' g)), both phase parts reduced
           float ph = fmaf(kz, gsm[p * W + w], eth[p]);
           ph = fmaf(-two_pi, rintf(ph * inv2pi), ph);
           float sn, cs;
           __sincosf(ph, &sn, &cs);
-          const C h = a.xs ? make_float2(cs, sn) : cmul(ex, make_float2(cs, sn));
+          const C h = cmul(ex, make_float2(cs, sn));
           acc[kb][f] = cadd(acc[kb][f], cmul(h, x[f]));
         }
       }
