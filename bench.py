@@ -333,6 +333,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-baselines", action="store_true", help="skip the CPU and plain-GPU comparison legs")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the point-cloud and WRP workloads")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup()
@@ -444,12 +445,13 @@ def main():
                         "algorithmic_bytes_per_launch": alg_bytes},
            "clocks": clocks}
 
-    if rank == 0 and world == 1 and not args.no_baselines:
+    if rank == 0 and world == 1 and not args.no_secondary:
         try:
             out["other_operators"] = secondary_measurements(ctx, dev, torch)
         except Exception as e:  # pragma: no cover
             out["other_operators"] = {"error": str(e)[:300]}
         torch.cuda.empty_cache()
+    if rank == 0 and world == 1 and not args.no_baselines:
         # accuracy of this frame against the FP64 path (pinned to the oracle in tests)
         f64 = dm.generate(ctx, p, d_img, d_depth, precision="fp64")
         torch.cuda.synchronize()

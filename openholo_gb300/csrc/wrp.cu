@@ -6,10 +6,11 @@
 //   tx = int(x/dp) + Nx/2, ty = int(y/dp) + Ny/2, and for wx, wy in [-w, w):
 //   r = sign(dz) sqrt((wx dp)^2 + (wy dp)^2 + dz^2),
 //   WRP[ty+wy][tx+wx] += (cos, sin)(k r) / (r + 0.05)   (pixels inside the plane)
-// The reference adds with a racy AddPixel (cwo.cpp:4298-4308); here every
-// contribution is an atomic float2/double2 add.  FP32 mode evaluates k r as
-// k dz (reduced mod 2 pi in double, once per point) + k rho^2/(|r| + |dz|)
-// (at most tens of rad, exact in float to ~1e-5 rad).
+// The reference adds with a racy AddPixel (cwo.cpp:4298-4308).  Here a fixed
+// window is summed race-free per 64x64 plane tile (wrp_tile*); the formula
+// window (w varies per point) is added with float2/double2 atomics.  FP32
+// evaluates k r as k dz (reduced mod 2 pi in double, once per point) +
+// k rho^2/(|r| + |dz|) (at most tens of rad, exact in float to ~1e-5 rad).
 //
 // CWO::Diffract(z, CWO_FRESNEL_CONV) (cwo.cpp:2198-2279, DiffractConv
 // FRESNEL_CONV cwo.cpp:2872-2898): zero-pad the Nx x Ny field into a
@@ -79,6 +80,219 @@ __global__ void __launch_bounds__(256) wrp_accumulate_kernel(WRPGeom g, const do
       C* dst = wrp + (size_t)Y * g.nx + X;
       atomicAdd(&dst->x, v.x);
       atomicAdd(&dst->y, v.y);
+    }
+  }
+}
+
+// ---- tiled accumulation for fixed windows ------------------------------------
+// Points are binned by the 64x64 plane tiles their window overlaps (count,
+// scan, fill); one block per tile sums its points' window pixels and adds the
+// tile to the plane once, with no global atomics.  FP64 sums in a
+// shared-memory copy of the tile; FP32 keeps each thread's pixels in
+// registers.
+constexpr int kWrpTile = 64;
+
+struct WrpPt { int tx, ty, w; float base, adz, sgn; double dz; };
+
+__device__ __forceinline__ void wrp_point(const WRPGeom& g, const double* xyz, int k, WrpPt* o) {
+  const double two_pi = 6.283185307179586476925286766559;
+  const float dpx = (float)g.dp;
+  const double kd = (double)(float)(2.0 * M_PI / g.lambda);
+  const double px = xyz[3 * k], py = xyz[3 * k + 1], pz = xyz[3 * k + 2];
+  // centres far outside the plane are clamped so that c +- w cannot overflow
+  const double lim = 1 << 29;
+  o->tx = (int)fmin(fmax(px / (double)dpx, -lim), lim) + (g.nx >> 1);
+  o->ty = (int)fmin(fmax(py / (double)dpx, -lim), lim) + (g.ny >> 1);
+  o->w = g.fixed_w;
+  const double dz = (double)(float)g.z - pz;
+  o->dz = dz;
+  o->sgn = dz > 0.0 ? 1.f : -1.f;
+  o->adz = (float)fabs(dz);
+  const double kdz = kd * fabs(dz);
+  o->base = (float)(kdz - two_pi * rint(kdz / two_pi));
+}
+
+// tile index range [t0, t1] along one axis for the window [c - w, c + w) clipped to [0, n)
+__device__ __forceinline__ bool wrp_tile_range(int c, int w, int n, int* t0, int* t1) {
+  const int lo = max(c - w, 0), hi = min(c + w, n);
+  if (lo >= hi) return false;
+  *t0 = lo / kWrpTile;
+  *t1 = (hi - 1) / kWrpTile;
+  return true;
+}
+
+__global__ void wrp_prep(WRPGeom g, const double* __restrict__ xyz, int n, WrpPt* __restrict__ pts,
+                         int* __restrict__ count, int tiles_x) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    WrpPt q;
+    wrp_point(g, xyz, k, &q);
+    pts[k] = q;
+    int x0, x1, y0, y1;
+    if (!wrp_tile_range(q.tx, q.w, g.nx, &x0, &x1) || !wrp_tile_range(q.ty, q.w, g.ny, &y0, &y1)) continue;
+    for (int ty = y0; ty <= y1; ++ty)
+      for (int tx = x0; tx <= x1; ++tx) atomicAdd(&count[ty * tiles_x + tx], 1);
+  }
+}
+
+// exclusive scan of count[0..n) into start[0..n], single block
+__global__ void wrp_scan(const int* __restrict__ count, int* __restrict__ start, int* __restrict__ cursor, int n) {
+  __shared__ int part[1024];
+  const int per = (n + blockDim.x - 1) / blockDim.x;
+  const int b = threadIdx.x * per, e = min(b + per, n);
+  int sum = 0;
+  for (int i = b; i < e; ++i) sum += count[i];
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int off = 1; off < blockDim.x; off <<= 1) {
+    int v = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int run = part[threadIdx.x] - sum;
+  for (int i = b; i < e; ++i) { start[i] = run; cursor[i] = run; run += count[i]; }
+  if (threadIdx.x == blockDim.x - 1) start[n] = part[threadIdx.x];
+}
+
+__global__ void wrp_fill(WRPGeom g, const WrpPt* __restrict__ pts, int n, int* __restrict__ cursor,
+                         int* __restrict__ list, int tiles_x) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const WrpPt q = pts[k];
+    int x0, x1, y0, y1;
+    if (!wrp_tile_range(q.tx, q.w, g.nx, &x0, &x1) || !wrp_tile_range(q.ty, q.w, g.ny, &y0, &y1)) continue;
+    for (int ty = y0; ty <= y1; ++ty)
+      for (int tx = x0; tx <= x1; ++tx) list[atomicAdd(&cursor[ty * tiles_x + tx], 1)] = k;
+  }
+}
+
+// FP64 tile: shared-memory accumulators (double atomics on shared memory).
+template <typename R>
+__global__ void __launch_bounds__(256) wrp_tile(WRPGeom g, const WrpPt* __restrict__ pts, const int* __restrict__ start,
+                                               const int* __restrict__ list, int tiles_x,
+                                               typename cplx_of<R>::type* __restrict__ wrp) {
+  typedef typename cplx_of<R>::type C;
+  __shared__ R acc_re[kWrpTile * kWrpTile];
+  __shared__ R acc_im[kWrpTile * kWrpTile];
+  const int tile = blockIdx.x;
+  const int X0 = (tile % tiles_x) * kWrpTile, Y0 = (tile / tiles_x) * kWrpTile;
+  for (int i = threadIdx.x; i < kWrpTile * kWrpTile; i += blockDim.x) { acc_re[i] = 0; acc_im[i] = 0; }
+  __syncthreads();
+  const float dpx = (float)g.dp;
+  const double kd = (double)(float)(2.0 * M_PI / g.lambda);
+  const int b = start[tile], e = start[tile + 1];
+  for (int li = b; li < e; ++li) {
+    const WrpPt q = pts[list[li]];
+    // window x range [tx - w, tx + w) intersected with this tile and the plane
+    const int xa = max(max(q.tx - q.w, X0), 0), xb = min(min(q.tx + q.w, X0 + kWrpTile), g.nx);
+    const int ya = max(max(q.ty - q.w, Y0), 0), yb = min(min(q.ty + q.w, Y0 + kWrpTile), g.ny);
+    const int wd = xb - xa, area = wd * (yb - ya);
+    for (int i = threadIdx.x; i < area; i += blockDim.x) {
+      const int yy = i / wd, xx = i - yy * wd;
+      const int X = xa + xx, Y = ya + yy;
+      const int wx = X - q.tx, wy = Y - q.ty;
+      R re, im;
+      if constexpr (sizeof(R) == 4) {
+        const float ddx = (float)wx * dpx, ddy = (float)wy * dpx;
+        const float rho2 = ddx * ddx + ddy * ddy;
+        const float ar = sqrtf(rho2 + q.adz * q.adz);
+        float ph = q.base + (float)kd * rho2 / (ar + q.adz);
+        ph = q.sgn > 0 ? ph : -ph;
+        float sn, cs;
+        sincosf(ph, &sn, &cs);
+        const float inv = 1.f / (q.sgn * ar + 0.05f);
+        re = cs * inv; im = sn * inv;
+      } else {
+        const double ddx = wx * (double)dpx, ddy = wy * (double)dpx;
+        const double r = (q.dz > 0.0 ? 1.0 : -1.0) * sqrt(ddx * ddx + ddy * ddy + q.dz * q.dz);
+        double sn, cs;
+        sincos(kd * r, &sn, &cs);
+        re = cs / (r + 0.05); im = sn / (r + 0.05);
+      }
+      const int o = (Y - Y0) * kWrpTile + (X - X0);
+      atomicAdd(&acc_re[o], re);
+      atomicAdd(&acc_im[o], im);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kWrpTile * kWrpTile; i += blockDim.x) {
+    const int X = X0 + i % kWrpTile, Y = Y0 + i / kWrpTile;
+    if (X < g.nx && Y < g.ny) {
+      C* d = wrp + (size_t)Y * g.nx + X;
+      C v = *d;
+      v.x += acc_re[i];
+      v.y += acc_im[i];
+      *d = v;
+    }
+  }
+}
+
+// One window pixel in FP32 at (squared) distance rho2 from the point's axis:
+//   k|r| = base + k rho^2 / (|r| + |dz|),   value = (cos, sin)(sgn k|r|) / (sgn |r| + 0.05)
+// with one MUFU reciprocal shared by the phase and the amplitude, and the
+// phase reduced to [-pi, pi] by a two-term Cody-Waite split of 2 pi before
+// the hardware sine/cosine (absolute error ~4e-7 on that interval).
+__device__ __forceinline__ float2 wrp_term_f32(float rho2, const WrpPt& q, float kf) {
+  const float a2 = fmaf(q.adz, q.adz, rho2);
+  const float ar = a2 * rsqrtf(a2);
+  const float s = ar + q.adz;
+  const float d = fmaf(q.sgn, ar, 0.05f);
+  const float inv = __fdividef(1.f, s * d);
+  float ph = q.base + kf * rho2 * (d * inv);
+  ph = q.sgn > 0.f ? ph : -ph;
+  const float n = rintf(ph * 0.159154943091895336f);            // 1 / (2 pi)
+  float red = fmaf(n, -6.28318548202514648f, ph);              // 2 pi rounded to float
+  red = fmaf(n, 1.74845553146951862e-7f, red);                 // 2 pi - float(2 pi)
+  float sn, cs;
+  __sincosf(red, &sn, &cs);
+  const float amp = s * inv;
+  return make_float2(cs * amp, sn * amp);
+}
+
+// FP32 tile: thread t owns column t % 64 and rows t / 64 + 4 j (j < 16) of the
+// tile and keeps their sums in registers; no shared memory, no atomics.
+__global__ void __launch_bounds__(256) wrp_tile_f32(WRPGeom g, const WrpPt* __restrict__ pts,
+                                                   const int* __restrict__ start, const int* __restrict__ list,
+                                                   int tiles_x, float2* __restrict__ wrp) {
+  constexpr int kRows = kWrpTile * kWrpTile / 256;
+  const int tile = blockIdx.x;
+  const int X0 = (tile % tiles_x) * kWrpTile, Y0 = (tile / tiles_x) * kWrpTile;
+  const int c = threadIdx.x & (kWrpTile - 1), r0 = threadIdx.x >> 6;
+  float2 acc[kRows];
+#pragma unroll
+  for (int j = 0; j < kRows; ++j) acc[j] = make_float2(0.f, 0.f);
+  const float dpx = (float)g.dp;
+  const float kf = (float)(2.0 * M_PI / g.lambda);
+  const int X = X0 + c;
+  const int b = start[tile], e = start[tile + 1];
+  for (int li = b; li < e; ++li) {
+    const WrpPt q = pts[__ldg(list + li)];
+    const int wx = X - q.tx;
+    if (wx < -q.w || wx >= q.w || X >= g.nx) continue;
+    const float ddx = (float)wx * dpx;
+    const float dx2 = ddx * ddx;
+    const int wy0 = Y0 + r0 - q.ty;                 // wy of row j is wy0 + 4 j
+    const int ylim = g.ny - Y0 - r0;               // row j inside the plane iff 4 j < ylim
+#pragma unroll
+    for (int j = 0; j < kRows; ++j) {
+      const int wy = wy0 + 4 * j;
+      if (wy >= -q.w && wy < q.w && 4 * j < ylim) {
+        const float ddy = (float)wy * dpx;
+        const float2 v = wrp_term_f32(fmaf(ddy, ddy, dx2), q, kf);
+        acc[j].x += v.x;
+        acc[j].y += v.y;
+      }
+    }
+  }
+  if (X >= g.nx) return;
+#pragma unroll
+  for (int j = 0; j < kRows; ++j) {
+    const int Y = Y0 + r0 + 4 * j;
+    if (Y < g.ny) {
+      float2* d = wrp + (size_t)Y * g.nx + X;
+      float2 v = *d;
+      v.x += acc[j].x;
+      v.y += acc[j].y;
+      *d = v;
     }
   }
 }
@@ -199,6 +413,38 @@ oh_status oh_wrp_accumulate(oh_ctx* ctx, oh_precision prec, const oh_wrp_params*
   if (n_points < 0 || (n_points > 0 && !xyz) || !wrp) return fail(OH_ERR_INVALID_ARG, "bad WRP buffers");
   if (n_points == 0) return OH_OK;
   WRPGeom g{p->nx, p->ny, p->pitch, p->lambda, p->z_wrp, p->window};
+  const int tiles_x = (p->nx + kWrpTile - 1) / kWrpTile, tiles_y = (p->ny + kWrpTile - 1) / kWrpTile;
+  const int span = p->window > 0 ? (2 * p->window + kWrpTile - 1) / kWrpTile + 1 : 0;  // tiles per axis a window touches
+  const size_t cap = (size_t)n_points * std::min(span, tiles_x) * std::min(span, tiles_y);
+  if (p->window > 0 && p->window < (1 << 28) && cap < (size_t)INT32_MAX) {
+    // fixed windows: binned, tiled accumulation
+    const int ntiles = tiles_x * tiles_y;
+    void* ptr;
+    const size_t off_cnt = ((size_t)n_points * sizeof(WrpPt) + 255) & ~(size_t)255;
+    const size_t off_start = off_cnt + (((size_t)ntiles * 4 + 255) & ~(size_t)255);
+    const size_t off_cur = off_start + (((size_t)(ntiles + 1) * 4 + 255) & ~(size_t)255);
+    const size_t off_list = off_cur + (((size_t)ntiles * 4 + 255) & ~(size_t)255);
+    OH_TRY(scratch(ctx, "wrp.bins", off_list + cap * sizeof(int), &ptr));
+    char* base = (char*)ptr;
+    WrpPt* pts = (WrpPt*)base;
+    int* cnt = (int*)(base + off_cnt);
+    int* start = (int*)(base + off_start);
+    int* cur = (int*)(base + off_cur);
+    int* list = (int*)(base + off_list);
+    KernelTimer kt(ctx, "wrp_accumulate", st);
+    OH_CUDA_TRY(cudaMemsetAsync(cnt, 0, (size_t)ntiles * 4, st));
+    const int g1 = std::min((n_points + 255) / 256, 152 * 8);
+    wrp_prep<<<g1, 256, 0, st>>>(g, xyz, n_points, pts, cnt, tiles_x);
+    OH_LAUNCH_CHECK();
+    wrp_scan<<<1, 1024, 0, st>>>(cnt, start, cur, ntiles);
+    OH_LAUNCH_CHECK();
+    wrp_fill<<<g1, 256, 0, st>>>(g, pts, n_points, cur, list, tiles_x);
+    OH_LAUNCH_CHECK();
+    if (prec == OH_FP64) wrp_tile<double><<<ntiles, 256, 0, st>>>(g, pts, start, list, tiles_x, (double2*)wrp);
+    else wrp_tile_f32<<<ntiles, 256, 0, st>>>(g, pts, start, list, tiles_x, (float2*)wrp);
+    OH_LAUNCH_CHECK();
+    return OH_OK;
+  }
   const int grid = std::min(n_points, 152 * 32);
   KernelTimer kt(ctx, "wrp_accumulate", st);
   if (prec == OH_FP64) wrp_accumulate_kernel<double><<<grid, 256, 0, st>>>(g, xyz, n_points, (double2*)wrp);
