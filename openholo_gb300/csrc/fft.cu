@@ -150,6 +150,12 @@ oh_status fft2d_enqueue(oh_ctx* ctx, int prec, int nx, int ny, const void* in, v
   return launch_fft2d<float>(ctx, nx, ny, in, out, aux, direction, shift, normalize, st);
 }
 
+oh_status fft_rows_enqueue(oh_ctx* ctx, int prec, int nx, int ny, const void* in, void* out, int direction,
+                           int normalize, cudaStream_t st) {
+  if (prec) return launch_fft_rows<double>(ctx, nx, ny, in, out, direction, normalize, st);
+  return launch_fft_rows<float>(ctx, nx, ny, in, out, direction, normalize, st);
+}
+
 int pick_strip_width(int nx, int ny, size_t esz, size_t smax) {
   // widest strip (<= 8 columns) that divides nx and fits in shared memory
   const int cands[4] = {8, 4, 2, 1};

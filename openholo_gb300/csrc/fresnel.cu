@@ -1,0 +1,452 @@
+// Fresnel-convolution propagation, CWO::Diffract(z, CWO_FRESNEL_CONV)
+// (cwo.cpp:2198-2279; DiffractConv FRESNEL_CONV cwo.cpp:2872-2898): zero-pad
+// the Nx x Ny field into a 2Nx x 2Ny grid at offset (Nx/2, Ny/2), FFT,
+// multiply by the FFT of the sampled Fresnel impulse response, inverse FFT
+// with 1/(2Nx 2Ny), crop the centre back.  The impulse response is written
+// from the mathematics
+//   h(x,y) = exp(i k z)/(i lambda z) exp(i pi (x^2+y^2)/(lambda z)) dp^2
+// (the DLL's kernel/coefficient bodies are not in the tree), sampled with its
+// origin at index (0,0) so that the convolution output is aligned with the
+// input.
+//
+// h is separable, h = C gx(x) gy(y), so its spectrum is C Hx(u) Hy(v), Hx and
+// Hy being the 1-D DFTs of the sampled chirps (computed once in FP64 and
+// cached per size, pitch, lambda and z).  In FP32, when 2Nx and 2Ny have
+// compile-time FFT schedules, three passes do the whole propagation without
+// materialising the padded grid:
+//   fr_row_fwd  x-FFT of each field row (the padded half is implicit),
+//               written as strips of two spectrum columns;
+//   fr_col      per strip: y-FFT, multiply by C Hx Hy / (4 Nx Ny), inverse
+//               y-FFT, keep the Ny cropped rows (in place in the strip);
+//   fr_row_inv  inverse x-FFT of each kept row, cropped into the field.
+// Each line enters its forward FFT rotated by half its padded length, so the
+// data fill the first and last quarters (radix-16 stage-0 butterflies see 8 of
+// 16 inputs); the rotation multiplies the spectrum by (-1)^u (and (-1)^v),
+// which the tables undo.  FP64 and other sizes run the padded-grid path:
+// pad, 2-D FFT, multiply by the cached 2-D spectrum, inverse 2-D FFT, crop.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include "context.h"
+#include "fft_kernels.cuh"
+
+namespace oh {
+
+template <typename R>
+__global__ void fresnel_pad(int nx, int ny, const typename cplx_of<R>::type* __restrict__ in,
+                            typename cplx_of<R>::type* __restrict__ out) {
+  const int NX = 2 * nx, NY = 2 * ny, ox = nx / 2, oy = ny / 2;
+  const size_t n = (size_t)NX * NY;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(i / NX), c = (int)(i - (size_t)r * NX);
+    const int rr = r - oy, cc = c - ox;
+    typename cplx_of<R>::type v = mk((R)0, (R)0);
+    if (rr >= 0 && rr < ny && cc >= 0 && cc < nx) v = in[(size_t)rr * nx + cc];
+    out[i] = v;
+  }
+}
+
+// Sampled impulse response with origin at index 0 (wrap-around coordinates).
+template <typename R>
+__global__ void fresnel_kernel_sample(int NX, int NY, double dp, double lambda, double z, typename cplx_of<R>::type* b) {
+  const double two_pi = 6.283185307179586476925286766559;
+  const double k = two_pi / lambda;
+  const size_t n = (size_t)NX * NY;
+  // exp(i k z) / (i lambda z) * dp^2
+  const double kz = k * z - two_pi * rint(k * z / two_pi);
+  double s0, c0;
+  sincos(kz, &s0, &c0);
+  const double amp = dp * dp / (lambda * z);
+  // 1/i = -i
+  const double cre = amp * s0, cim = -amp * c0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(i / NX), c = (int)(i - (size_t)r * NX);
+    const int jx = c < NX / 2 ? c : c - NX, jy = r < NY / 2 ? r : r - NY;
+    const double x = jx * dp, y = jy * dp;
+    double ph = M_PI * (x * x + y * y) / (lambda * z);
+    ph -= two_pi * rint(ph / two_pi);
+    double s, co;
+    sincos(ph, &s, &co);
+    b[i] = mk((R)(cre * co - cim * s), (R)(cre * s + cim * co));
+  }
+}
+
+template <typename R>
+__global__ void cmul_inplace(size_t n, typename cplx_of<R>::type* a, const typename cplx_of<R>::type* b) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) a[i] = cmul(a[i], b[i]);
+}
+
+template <typename R>
+__global__ void fresnel_crop(int nx, int ny, const typename cplx_of<R>::type* __restrict__ in, typename cplx_of<R>::type* __restrict__ out) {
+  const int NX = 2 * nx, ox = nx / 2, oy = ny / 2;
+  const size_t n = (size_t)nx * ny;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(i / nx), c = (int)(i - (size_t)r * nx);
+    out[i] = in[(size_t)(r + oy) * NX + c + ox];
+  }
+}
+
+template <typename R>
+static oh_status run_fresnel_grid(oh_ctx* ctx, int nx, int ny, double dp, double lambda, double z, void* field, cudaStream_t st) {
+  typedef typename cplx_of<R>::type C;
+  const int prec = sizeof(R) == 8 ? 1 : 0;
+  const int NX = 2 * nx, NY = 2 * ny;
+  const size_t n2 = (size_t)NX * NY;
+  void* pa;
+  void* pb;
+  OH_TRY(scratch(ctx, "fr.a", n2 * sizeof(C), &pa));
+  // one cached transfer-function spectrum per context, keyed by its parameters
+  char key[160];
+  std::snprintf(key, sizeof(key), "%d:%d:%d:%.17g:%.17g:%.17g", prec, NX, NY, dp, lambda, z);
+  void* prev_b = nullptr;
+  {
+    auto it = ctx->scratch.find("fr.B");
+    if (it != ctx->scratch.end()) prev_b = it->second.p;
+  }
+  OH_TRY(scratch(ctx, "fr.B", n2 * sizeof(C), &pb));
+  const bool have = prev_b == pb && ctx->fresnel_key == key;
+  ctx->fresnel_key = key;
+  const int grid = 152 * 8;
+  if (!have) {
+    fresnel_kernel_sample<R><<<grid, 256, 0, st>>>(NX, NY, dp, lambda, z, (C*)pb);
+    OH_LAUNCH_CHECK();
+    OH_TRY(fft2d_enqueue(ctx, prec, NX, NY, pb, pb, nullptr, -1, 0, 0, st));
+  }
+  {
+    KernelTimer kt(ctx, "fresnel_pad", st);
+    fresnel_pad<R><<<grid, 256, 0, st>>>(nx, ny, (const C*)field, (C*)pa);
+    OH_LAUNCH_CHECK();
+  }
+  OH_TRY(fft2d_enqueue(ctx, prec, NX, NY, pa, pa, nullptr, -1, 0, 0, st));
+  {
+    KernelTimer kt(ctx, "fresnel_mul", st);
+    cmul_inplace<R><<<grid, 256, 0, st>>>(n2, (C*)pa, (const C*)pb);
+    OH_LAUNCH_CHECK();
+  }
+  OH_TRY(fft2d_enqueue(ctx, prec, NX, NY, pa, pa, nullptr, 1, 0, 1, st));
+  {
+    KernelTimer kt(ctx, "fresnel_crop", st);
+    fresnel_crop<R><<<grid, 256, 0, st>>>(nx, ny, (const C*)pa, (C*)field);
+    OH_LAUNCH_CHECK();
+  }
+  return OH_OK;
+}
+
+
+
+// ---- separable three-pass path (FP32) -------------------------------------
+
+constexpr int kFrW = 2;      // spectrum columns per strip
+
+struct FrArgs {
+  int nx, ny;                // field size; the padded grid is 2nx x 2ny
+  float2* field;             // read by fr_row_fwd, written by fr_row_inv
+  float2* R;                 // strips [2nx / kFrW][ny][kFrW]
+  const float2* twx;         // plan twiddles of the two lengths
+  const float2* twy;
+  const int* perm_x;
+  const int* iperm_x;
+  const int* perm_y;
+  const int* iperm_y;
+  const float2* hxs;         // C (-1)^u Hx(u) at x-FFT storage position
+  const float2* hys;         // (-1)^v Hy(v) / (4 nx ny), natural order
+};
+
+__host__ __device__ constexpr int fr_tw_entries(int n) { return 64 + (n + 63) / 64; }
+
+// Two rows per block: x-FFT of the padded row, stored as column strips.
+template <int NX>
+__global__ void __launch_bounds__(512) fr_row_fwd(FrArgs a) {
+  typedef float2 C;
+  extern __shared__ __align__(16) unsigned char smem[];
+  C* buf = reinterpret_cast<C*>(smem);
+  C* twlo = buf + 2 * NX;
+  C* twhi = twlo + 64;
+  constexpr int Q = NX / 4;                        // = nx / 2
+  const int r0 = 2 * blockIdx.x;
+  load_tw_split(twlo, twhi, a.twx, NX);
+  const C* src = a.field + (size_t)r0 * a.nx;
+  for (int idx = threadIdx.x; idx < 2 * NX; idx += blockDim.x) {
+    const int l = idx / NX, p = idx - l * NX;
+    // rotated line: position p holds field column p - 3Q (p >= 3Q) or p + Q (p < Q)
+    int c = -1;
+    if (p >= 3 * Q) c = p - 3 * Q;
+    else if (p < Q) c = p + Q;
+    buf[idx] = c >= 0 ? src[(size_t)l * a.nx + c] : make_float2(0.f, 0.f);
+  }
+  const TwSplit<C> tw{twlo, twhi};
+  FastSched<NX>::template run_t<-1>(buf, 2, NX, 1, tw, false);
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < 2 * NX; idx += blockDim.x) {
+    const int w = idx % kFrW, l = (idx / kFrW) & 1, s = idx / (2 * kFrW);
+    a.R[((size_t)s * a.ny + r0 + l) * kFrW + w] = buf[l * NX + s * kFrW + w];
+  }
+}
+
+template <int NY> struct FrColCfg {
+  static constexpr int R0 = FastSched<NY>::r0;
+  static constexpr int RL = FastSched<NY>::rlast;
+  static constexpr int NBL = (NY / RL) * kFrW;        // last-stage butterflies in the strip
+  static constexpr int KB = NBL > 768 ? 2 : 1;         // butterflies per thread
+  static constexpr int T = ((NBL + KB - 1) / KB + 31) / 32 * 32;
+  // two blocks per SM when two strips fit in shared memory
+  static constexpr int MINB = (NY * kFrW + fr_tw_entries(NY)) * 8 <= 113 * 1024 ? 2 : 1;
+};
+
+// One strip of kFrW spectrum columns per block: y-FFT, transfer function,
+// inverse y-FFT, crop; the result overwrites the strip.
+template <int NY>
+__global__ void __launch_bounds__(FrColCfg<NY>::T, FrColCfg<NY>::MINB) fr_col(FrArgs a) {
+  typedef float2 C;
+  typedef FrColCfg<NY> CF;
+  constexpr int W = kFrW, T = CF::T, R0 = CF::R0, RL = CF::RL, KB = CF::KB;
+  constexpr int Q0 = NY / R0, QY = NY / 4;
+  static_assert(FastSched<NY>::nstages == 3, "three-stage schedule expected");
+  static_assert(R0 % 4 == 0, "stage-0 radix must split the line into quarters");
+  extern __shared__ __align__(16) unsigned char smem[];
+  C* buf = reinterpret_cast<C*>(smem);               // [NY][W]
+  C* twlo = buf + NY * W;
+  C* twhi = twlo + 64;
+  __shared__ C hxw[W];
+  const int tid = threadIdx.x, s = blockIdx.x, ny = a.ny;
+  C* strip = a.R + (size_t)s * ny * W;
+  load_tw_split(twlo, twhi, a.twy, NY);
+  if (tid < W) hxw[tid] = a.hxs[s * W + tid];
+  __syncthreads();
+  const TwSplit<C> tw{twlo, twhi};
+  // stage 0 from global memory; rotated line: positions [QY, 3QY) are zero,
+  // position p < QY holds row p + QY, p >= 3QY holds row p - 3QY
+  for (int idx = tid; idx < Q0 * W; idx += T) {
+    const int j = idx / W, w = idx - j * W;
+    C x[R0];
+#pragma unroll
+    for (int t = 0; t < R0; ++t) {
+      const int p = j + t * Q0;
+      if (t < R0 / 4) x[t] = strip[(p + QY) * W + w];
+      else if (t >= 3 * R0 / 4) x[t] = strip[(p - 3 * QY) * W + w];
+      else x[t] = make_float2(0.f, 0.f);
+    }
+    if constexpr (R0 == 16) dft16_halfzero<-1>(x);
+    else DFT<R0, -1, C>::run(x);
+    if (j) {
+      C wp[R0];
+      twiddle_powers<R0, -1>(tw, j, wp);
+#pragma unroll
+      for (int f = 1; f < R0; ++f) x[f] = cmul(x[f], wp[f]);
+    }
+#pragma unroll
+    for (int f = 0; f < R0; ++f) buf[(j + f * Q0) * W + w] = x[f];
+  }
+  __syncthreads();
+  fstage_t<NY, FastSched<NY>::r1, NY / R0, -1>(buf, W, 1, W, tw, true);
+  __syncthreads();
+  // last stage (stride 1, no twiddles) and the transfer function, in registers
+  C acc[KB][RL];
+#pragma unroll
+  for (int kb = 0; kb < KB; ++kb) {
+    const int bb = tid + kb * T;
+    if (bb < CF::NBL) {
+      const int b = bb / W, w = bb - b * W;
+      C x[RL];
+#pragma unroll
+      for (int f = 0; f < RL; ++f) x[f] = buf[(b * RL + f) * W + w];
+      DFT<RL, -1, C>::run(x);
+      const C hx = hxw[w];
+#pragma unroll
+      for (int f = 0; f < RL; ++f) {
+        const int v = __ldg(a.iperm_y + b * RL + f);
+        acc[kb][f] = cmul(x[f], cmul(hx, __ldg(a.hys + v)));
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int kb = 0; kb < KB; ++kb) {
+    const int bb = tid + kb * T;
+    if (bb < CF::NBL) {
+      const int b = bb / W, w = bb - b * W;
+#pragma unroll
+      for (int f = 0; f < RL; ++f) buf[__ldg(a.iperm_y + b * RL + f) * W + w] = acc[kb][f];
+    }
+  }
+  FastSched<NY>::template run_t<1>(buf, W, 1, W, tw, true);
+  __syncthreads();
+  // crop: output row r is the inverse transform's sample QY + r
+  for (int idx = tid; idx < ny * W; idx += T) {
+    const int r = idx / W, w = idx - r * W;
+    strip[idx] = buf[__ldg(a.perm_y + QY + r) * W + w];
+  }
+}
+
+// Two rows per block: gather the row from the strips into natural frequency
+// order, inverse x-FFT, crop into the field.
+template <int NX>
+__global__ void __launch_bounds__(512) fr_row_inv(FrArgs a) {
+  typedef float2 C;
+  extern __shared__ __align__(16) unsigned char smem[];
+  C* buf = reinterpret_cast<C*>(smem);
+  C* twlo = buf + 2 * NX;
+  C* twhi = twlo + 64;
+  constexpr int Q = NX / 4;
+  const int r0 = 2 * blockIdx.x;
+  load_tw_split(twlo, twhi, a.twx, NX);
+  for (int idx = threadIdx.x; idx < 2 * NX; idx += blockDim.x) {
+    const int w = idx % kFrW, l = (idx / kFrW) & 1, s = idx / (2 * kFrW);
+    const int p = s * kFrW + w;
+    buf[l * NX + __ldg(a.iperm_x + p)] = a.R[((size_t)s * a.ny + r0 + l) * kFrW + w];
+  }
+  const TwSplit<C> tw{twlo, twhi};
+  FastSched<NX>::template run_t<1>(buf, 2, NX, 1, tw, false);
+  __syncthreads();
+  float2* dst = a.field + (size_t)r0 * a.nx;
+  const int nx = a.nx;
+  for (int idx = threadIdx.x; idx < 2 * nx; idx += blockDim.x) {
+    const int l = idx / nx, c = idx - l * nx;
+    dst[(size_t)l * nx + c] = buf[l * NX + __ldg(a.perm_x + Q + c)];
+  }
+}
+
+// exp(i pi x^2 / (lambda z)) at x = j dp, j = i (i < n/2) or i - n
+__global__ void fr_chirp(int n, double dp, double lambda, double z, double2* g) {
+  const double two_pi = 6.283185307179586476925286766559;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int j = i < n / 2 ? i : i - n;
+    const double x = j * dp;
+    double ph = M_PI * x * x / (lambda * z);
+    ph -= two_pi * rint(ph / two_pi);
+    double s, c;
+    sincos(ph, &s, &c);
+    g[i] = make_double2(c, s);
+  }
+}
+
+__global__ void fr_tables(int NX, int NY, const double2* __restrict__ Hx, const double2* __restrict__ Hy,
+                          const int* __restrict__ iperm_x, double cre, double cim, double scale,
+                          float2* __restrict__ hxs, float2* __restrict__ hys) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NX + NY; i += gridDim.x * blockDim.x) {
+    if (i < NX) {
+      const int u = iperm_x[i];
+      const double sg = (u & 1) ? -1.0 : 1.0;
+      const double2 h = Hx[u];
+      hxs[i] = make_float2((float)(sg * (cre * h.x - cim * h.y)), (float)(sg * (cre * h.y + cim * h.x)));
+    } else {
+      const int v = i - NX;
+      const double sg = (v & 1) ? -scale : scale;
+      hys[v] = make_float2((float)(sg * Hy[v].x), (float)(sg * Hy[v].y));
+    }
+  }
+}
+
+typedef void (*FrKernel)(FrArgs);
+
+// The three kernels for padded lengths NX = 2nx, NY = 2ny, or false.
+static bool fr_pick(int NX, int NY, FrKernel* fwd, FrKernel* col, FrKernel* inv, int* col_threads) {
+  *fwd = *col = *inv = nullptr;
+  with_fast_n(NX, [&](auto nc) {
+    constexpr int N = decltype(nc)::value;
+    if constexpr (N > 0) { *fwd = fr_row_fwd<N>; *inv = fr_row_inv<N>; }
+  });
+  with_fast_n(NY, [&](auto nc) {
+    constexpr int N = decltype(nc)::value;
+    if constexpr (N > 0) { *col = fr_col<N>; *col_threads = FrColCfg<N>::T; }
+  });
+  return *fwd && *col && *inv;
+}
+
+static oh_status run_fresnel_separable(oh_ctx* ctx, int nx, int ny, double dp, double lambda, double z,
+                                       float2* field, FrKernel fwd, FrKernel col, FrKernel inv, int col_threads,
+                                       cudaStream_t st) {
+  const int NX = 2 * nx, NY = 2 * ny;
+  FFTPlan px, py;
+  OH_TRY(get_plan(ctx, NX, 0, &px));
+  OH_TRY(get_plan(ctx, NY, 0, &py));
+  // cached tables: FP64 chirps / spectra, then the FP32 factors
+  const size_t tab_bytes = (size_t)(NX + NY) * (sizeof(double2) + sizeof(float2));
+  char key[160];
+  std::snprintf(key, sizeof(key), "sep:%d:%d:%.17g:%.17g:%.17g", NX, NY, dp, lambda, z);
+  void* prev = nullptr;
+  {
+    auto it = ctx->scratch.find("fr.tab");
+    if (it != ctx->scratch.end()) prev = it->second.p;
+  }
+  void* tab;
+  OH_TRY(scratch(ctx, "fr.tab", tab_bytes, &tab));
+  double2* gx = static_cast<double2*>(tab);
+  double2* gy = gx + NX;
+  float2* hxs = reinterpret_cast<float2*>(gy + NY);
+  float2* hys = hxs + NX;
+  if (!(prev == tab && ctx->fresnel_key == key)) {
+    ctx->fresnel_key = key;
+    fr_chirp<<<(NX + 255) / 256, 256, 0, st>>>(NX, dp, lambda, z, gx);
+    OH_LAUNCH_CHECK();
+    fr_chirp<<<(NY + 255) / 256, 256, 0, st>>>(NY, dp, lambda, z, gy);
+    OH_LAUNCH_CHECK();
+    OH_TRY(fft_rows_enqueue(ctx, 1, NX, 1, gx, gx, -1, 0, st));
+    OH_TRY(fft_rows_enqueue(ctx, 1, NY, 1, gy, gy, -1, 0, st));
+    const double two_pi = 6.283185307179586476925286766559;
+    const double k = two_pi / lambda;
+    const double kz = k * z - two_pi * std::rint(k * z / two_pi);
+    const double amp = dp * dp / (lambda * z);
+    fr_tables<<<(NX + NY + 255) / 256, 256, 0, st>>>(NX, NY, gx, gy, px.iperm, amp * std::sin(kz),
+                                                      -amp * std::cos(kz), 1.0 / ((double)NX * (double)NY), hxs, hys);
+    OH_LAUNCH_CHECK();
+  }
+  void* rbuf;
+  OH_TRY(scratch(ctx, "fr.R", (size_t)ny * NX * sizeof(float2), &rbuf));
+  FrArgs a{nx, ny, field, static_cast<float2*>(rbuf), static_cast<const float2*>(px.tw),
+           static_cast<const float2*>(py.tw), px.perm, px.iperm, py.perm, py.iperm, hxs, hys};
+  const int srow = (2 * NX + fr_tw_entries(NX)) * (int)sizeof(float2);
+  const int scol = (NY * kFrW + fr_tw_entries(NY)) * (int)sizeof(float2);
+  OH_CUDA_TRY(cudaFuncSetAttribute(fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, srow));
+  OH_CUDA_TRY(cudaFuncSetAttribute(inv, cudaFuncAttributeMaxDynamicSharedMemorySize, srow));
+  OH_CUDA_TRY(cudaFuncSetAttribute(col, cudaFuncAttributeMaxDynamicSharedMemorySize, scol));
+  {
+    KernelTimer kt(ctx, "fresnel_row_fwd", st);
+    fwd<<<ny / 2, 512, srow, st>>>(a);
+    OH_LAUNCH_CHECK();
+  }
+  {
+    KernelTimer kt(ctx, "fresnel_col", st);
+    col<<<NX / kFrW, col_threads, scol, st>>>(a);
+    OH_LAUNCH_CHECK();
+  }
+  {
+    KernelTimer kt(ctx, "fresnel_row_inv", st);
+    inv<<<ny / 2, 512, srow, st>>>(a);
+    OH_LAUNCH_CHECK();
+  }
+  return OH_OK;
+}
+
+template <typename R>
+static oh_status run_fresnel(oh_ctx* ctx, int nx, int ny, double dp, double lambda, double z, void* field,
+                             cudaStream_t st) {
+  if constexpr (sizeof(R) == 4) {
+    FrKernel fwd, col, inv;
+    int ct = 0;
+    const bool even = nx % 2 == 0 && ny % 2 == 0;
+    if (even && !getenv("OH_FRESNEL_GRID") && fr_pick(2 * nx, 2 * ny, &fwd, &col, &inv, &ct) &&
+        (size_t)(2 * (2 * nx) + fr_tw_entries(2 * nx)) * sizeof(float2) <= max_smem_per_block())
+      return run_fresnel_separable(ctx, nx, ny, dp, lambda, z, static_cast<float2*>(field), fwd, col, inv, ct, st);
+  }
+  return run_fresnel_grid<R>(ctx, nx, ny, dp, lambda, z, field, st);
+}
+
+}  // namespace oh
+
+using namespace oh;
+
+extern "C" {
+
+oh_status oh_fresnel_propagate(oh_ctx* ctx, oh_precision prec, int nx, int ny, double pitch, double lambda, double z,
+                               void* field, void* stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  CallScope cs(ctx, st);
+  OH_TRY(cs.status());
+  if (nx < 1 || ny < 1 || !field || !(pitch > 0) || !(lambda > 0) || z == 0.0)
+    return fail(OH_ERR_INVALID_ARG, "bad Fresnel propagation arguments");
+  if (prec == OH_FP64) return run_fresnel<double>(ctx, nx, ny, pitch, lambda, z, field, st);
+  return run_fresnel<float>(ctx, nx, ny, pitch, lambda, z, field, st);
+}
+
+}  // extern "C"
