@@ -208,6 +208,45 @@ oh_status oh_pointcloud_host(oh_ctx* ctx, oh_precision prec,
 oh_status oh_pointcloud_noalloc(const oh_pc_params* p, const float* xyza, int n_points,
                                 void* field_out, void* fringe_out, void* stream);
 
+/* ---- point-light-source summation (cwoPLS) -------------------------------
+ * The per-pixel point sums of CWO++'s cwoPLS class
+ * (OpenHolo_WRP/openwrp_console_ver 1.0/cwo/src/cwoPLS.cpp), pixel (i, j):
+ *   dx = (j - nx/2) dst_px + dst_ox - (x_k + src_ox)
+ *   dy = (i - ny/2) dst_py + dst_oy - (y_k + src_oy),   dz = z_k + z
+ *   OH_PLS_HUYGENS     (cwoPLS.cpp:316-368)  U = sum_k exp(i (k r + ph)) / r
+ *   OH_PLS_FRESNEL     (cwoPLS.cpp:370-424)  U = sum_k exp(i (k (dx^2+dy^2)/(2 dz) + ph))
+ *   OH_PLS_CGH_FRESNEL (cwoPLS.cpp:472-520)  I = sum_k cos(k (dx^2+dy^2)/(2 dz) + ph)
+ * (nx/2 = nx >> 1).  Points use the cwoObjPoint layout (cwo_lib.h:469-474).
+ * The reference ignores the amplitude a_k; use_amplitude = 1 multiplies each
+ * term by it.  out is written (not accumulated): complex [ny][nx] for
+ * HUYGENS/FRESNEL, real [ny][nx] for CGH_FRESNEL; oh_c64/float for OH_FP32,
+ * oh_c128/double for OH_FP64.
+ * Engines (FP32): FRESNEL and CGH_FRESNEL factor into x and y phase tables,
+ * U = e^{i ph} Ey^T diag(a) Ex, a complex matrix product over the points;
+ * OH_PLS_ENGINE_AUTO runs it on the tensor cores where available (BF16
+ * operands split into high and low parts, three products, FP32 accumulation;
+ * relative error ~1e-5), OH_PLS_ENGINE_GEMM on the CUDA cores in FP32,
+ * OH_PLS_ENGINE_DIRECT evaluates every term.  HUYGENS is always direct. */
+typedef struct oh_pls_point { float a_re, a_im; float x, y, z; } oh_pls_point;
+typedef enum oh_pls_mode { OH_PLS_HUYGENS = 0, OH_PLS_FRESNEL = 1, OH_PLS_CGH_FRESNEL = 2 } oh_pls_mode;
+typedef enum oh_pls_engine {
+  OH_PLS_ENGINE_AUTO = 0, OH_PLS_ENGINE_DIRECT = 1, OH_PLS_ENGINE_GEMM = 2, OH_PLS_ENGINE_TENSOR = 3
+} oh_pls_engine;
+typedef struct oh_pls_params {
+  int    nx, ny;
+  double dst_px, dst_py;    /* GetDstPx/GetDstPy: hologram pitch */
+  double dst_ox, dst_oy;    /* GetDstOx/GetDstOy: hologram offset */
+  double src_ox, src_oy;    /* GetOx/GetOy: point offset */
+  double lambda;
+  double z;                 /* added to every point's z */
+  double phase;             /* ph, radians */
+  int    mode;              /* oh_pls_mode */
+  int    use_amplitude;
+  int    engine;            /* oh_pls_engine */
+} oh_pls_params;
+oh_status oh_pls(oh_ctx* ctx, oh_precision prec, const oh_pls_params* p,
+                 const oh_pls_point* pts, int n_points, void* out, void* stream);
+
 /* ---- WRP ------------------------------------------------------------------ */
 typedef struct oh_wrp_params {
   int    nx, ny;          /* WRP / hologram grid */

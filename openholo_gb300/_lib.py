@@ -61,6 +61,18 @@ _i = C.c_int
 _d = C.c_double
 
 # name -> (restype, argtypes); every symbol declared in include/oh.h
+class PlsParams(C.Structure):
+    """oh_pls_params (include/oh.h)."""
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("dst_px", C.c_double), ("dst_py", C.c_double),
+                ("dst_ox", C.c_double), ("dst_oy", C.c_double), ("src_ox", C.c_double), ("src_oy", C.c_double),
+                ("lambda_", C.c_double), ("z", C.c_double), ("phase", C.c_double), ("mode", C.c_int),
+                ("use_amplitude", C.c_int), ("engine", C.c_int)]
+
+
+PLS_HUYGENS, PLS_FRESNEL, PLS_CGH_FRESNEL = 0, 1, 2
+PLS_ENGINE_AUTO, PLS_ENGINE_DIRECT, PLS_ENGINE_GEMM, PLS_ENGINE_TENSOR = 0, 1, 2, 3
+
+
 SIGNATURES = {
     "oh_ctx_create": (_i, [C.POINTER(_vp), _i]),
     "oh_ctx_destroy": (_i, [_vp]),
@@ -86,6 +98,7 @@ SIGNATURES = {
     "oh_pointcloud_noalloc": (_i, [C.POINTER(PcParams), _vp, _i, _vp, _vp, _vp]),
     "oh_wrp_accumulate": (_i, [_vp, _i, C.POINTER(WrpParams), _vp, _i, _vp, _vp]),
     "oh_fresnel_propagate": (_i, [_vp, _i, _i, _i, _d, _d, _d, _vp, _vp]),
+    "oh_pls": (_i, [_vp, _i, C.POINTER(PlsParams), _vp, _i, _vp, _vp]),
     "oh_encode": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp]),
     "oh_normalize_u8": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _vp]),
 }

@@ -96,3 +96,20 @@ def wrp_scene(seed: int, n: int = 200_000, box=(10e-3, 10e-3, 2e-3), zc=0.2):
     pts[:, 1] = (u[:, 1] - 0.5) * box[1]
     pts[:, 2] = zc + (u[:, 2] - 0.5) * box[2]
     return pts
+
+
+def pls_scene(seed: int, n: int = 5000, xy_half=2e-3, z_range=(0.10, 0.12), amplitude=True):
+    """(n, 5) float32 cwoObjPoint records (a_re, a_im, x, y, z): x, y uniform in
+    [-xy_half, xy_half), z uniform in z_range, a = |a| e^{i phi} with |a| in
+    [0, 1) and phi in [0, 2 pi) (a = 1 when amplitude is False)."""
+    u = uniform(seed, 5, 5 * n).reshape(n, 5)
+    pts = np.empty((n, 5), dtype=np.float32)
+    if amplitude:
+        pts[:, 0] = u[:, 0] * np.cos(2 * np.pi * u[:, 1])
+        pts[:, 1] = u[:, 0] * np.sin(2 * np.pi * u[:, 1])
+    else:
+        pts[:, 0], pts[:, 1] = 1.0, 0.0
+    pts[:, 2] = (u[:, 2] * 2 - 1) * xy_half
+    pts[:, 3] = (u[:, 3] * 2 - 1) * xy_half
+    pts[:, 4] = z_range[0] + u[:, 4] * (z_range[1] - z_range[0])
+    return pts
