@@ -258,18 +258,23 @@ def plain_gpu_path(img_t, depth_t, zt, lut, torch):
     return frame
 
 
-def secondary_measurements(ctx, dev, torch, reps=5):
+SECONDARY_OPS = ("pointcloud", "pls", "wrp")
+
+
+def secondary_measurements(ctx, dev, torch, reps=5, ops=SECONDARY_OPS, warmup=1):
     """The other operators at their own workloads (seeded synthetic inputs):
-    config 1, point-cloud Fresnel/R-S sum 1024x1024 x 5000 points + phase-only
-    encoding; config 3, WRP (200,000 points, 64x64 windows) + zero-padded
-    Fresnel propagation to 3840x2160 at 3.74 um + phase-only encoding."""
+    pointcloud: KETI exact-r sum 1024x1024 x 5000 points + phase-only encoding;
+    pls: the same shape through the paraxial cwoPLS::Fresnel sum (tensor-core
+    and CUDA-core engines); wrp: WRP (200,000 points, 64x64 windows) +
+    zero-padded Fresnel propagation to 3840x2160 at 3.74 um + phase-only
+    encoding.  Each is timed over `reps` calls after `warmup` calls."""
     import ctypes as C
-    from openholo_gb300 import _lib, scenes
     st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     out = {}
 
     def timed(fn):
-        fn()
+        for _ in range(warmup):
+            fn()
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
@@ -279,8 +284,19 @@ def secondary_measurements(ctx, dev, torch, reps=5):
         torch.cuda.synchronize()
         return a.elapsed_time(b) / reps
 
-    # config 1
     n, nx, ny = 5000, 1024, 1024
+    if "pointcloud" in ops:
+        _sec_pointcloud(ctx, dev, torch, st, timed, out, n, nx, ny)
+    if "pls" in ops:
+        _sec_pls(ctx, dev, torch, st, timed, out, n, nx, ny, reps + warmup)
+    if "wrp" in ops:
+        _sec_wrp(ctx, dev, torch, st, timed, out, reps + warmup)
+    return out
+
+
+def _sec_pointcloud(ctx, dev, torch, st, timed, out, n, nx, ny):
+    import ctypes as C
+    from openholo_gb300 import _lib, scenes
     pts = torch.from_numpy(scenes.pointcloud_scene(11, n).astype(np.float32)).to(dev)
     p = _lib.PcParams(1.0, 1.0, 1.0, 0.0, 8e-6, 8e-6, nx, ny, 532e-9, 0.0, 0.0)
     f32 = torch.empty((ny, nx), dtype=torch.complex64, device=dev)
@@ -300,7 +316,39 @@ def secondary_measurements(ctx, dev, torch, reps=5):
                                            "point_pixel_terms_per_s": n * nx * ny / (ms / 1000.0),
                                            "rel_err_vs_fp64": err, "dtype": "f32 (FP64-reduced phase tables)"}
     del f64
-    # config 3
+
+
+def _sec_pls(ctx, dev, torch, st, timed, out, n, nx, ny, calls):
+    import ctypes as C
+    from openholo_gb300 import _lib, scenes
+    pls_pts = torch.from_numpy(scenes.pls_scene(11, n)).to(dev)
+    pls_out = torch.empty((ny, nx), dtype=torch.complex64, device=dev)
+    pls_res = {}
+    for eng_name, eng in (("tensor", _lib.PLS_ENGINE_TENSOR), ("cuda_core_gemm", _lib.PLS_ENGINE_GEMM)):
+        pp = _lib.PlsParams(nx, ny, 8e-6, 8e-6, 0.0, 0.0, 0.0, 0.0, 532e-9, 0.0, 0.0, _lib.PLS_FRESNEL, 1, eng)
+
+        def pls_frame(pp=pp):
+            _lib.call("oh_pls", ctx.handle, 0, C.byref(pp), C.c_void_p(pls_pts.data_ptr()), n,
+                      C.c_void_p(pls_out.data_ptr()), st)
+        ctx.set_timing(True)
+        ctx.read_timing(reset=True)
+        ms_p = timed(pls_frame)
+        kt = ctx.read_timing(reset=True)
+        ctx.set_timing(False)
+        pls_res[eng_name] = {"ms_per_hologram": ms_p,
+                             "kernels_ms": {k: v[0] / calls for k, v in kt.items()}}
+    tc_ms = pls_res["tensor"]["kernels_ms"].get("pls_tc_gemm")
+    if tc_ms:
+        useful = 8.0 * nx * ny * n          # complex multiply-adds as real flops, counted once
+        pls_res["tensor"]["gemm_useful_tflops"] = useful / (tc_ms * 1e-3) / 1e12
+        pls_res["tensor"]["gemm_issued_tflops"] = 3 * 2.0 * ny * (2 * nx) * (2 * n) / (tc_ms * 1e-3) / 1e12
+    out["pls_fresnel_1024x1024_5000pts"] = pls_res
+    del pls_out
+
+
+def _sec_wrp(ctx, dev, torch, st, timed, out, calls):
+    import ctypes as C
+    from openholo_gb300 import _lib, scenes
     npts, hx, hy, dp, lam = 200_000, 3840, 2160, 3.74e-6, 532e-9
     xyz = scenes.wrp_scene(12, npts)
     z_wrp = float(xyz[:, 2].min()) - 5e-3
@@ -321,9 +369,8 @@ def secondary_measurements(ctx, dev, torch, reps=5):
     kt = ctx.read_timing(reset=True)
     ctx.set_timing(False)
     out["wrp_200k_64x64_fresnel_3840x2160"] = {"ms_per_hologram": ms3, "holograms_per_s": 1000.0 / ms3,
-                                               "kernels_ms": {k: v[0] / (reps + 1) for k, v in kt.items()},
+                                               "kernels_ms": {k: v[0] / calls for k, v in kt.items()},
                                                "dtype": "f32"}
-    return out
 
 
 def main():
@@ -334,11 +381,22 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-baselines", action="store_true", help="skip the CPU and plain-GPU comparison legs")
     ap.add_argument("--no-secondary", action="store_true", help="skip the point-cloud and WRP workloads")
+    ap.add_argument("--op", choices=SECONDARY_OPS, default=None,
+                    help="time one secondary workload alone (steps calls after warmup) and print its line")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.op:
+        import torch
+        from openholo_gb300 import Context
+        torch.cuda.set_device(local)
+        res = secondary_measurements(Context(local), torch.device("cuda", local), torch, reps=args.steps,
+                                     ops=(args.op,), warmup=args.warmup)
+        if rank == 0:
+            print(json.dumps({"op": args.op, "steps": args.steps, "warmup": args.warmup, **res}), flush=True)
         return
 
     import torch

@@ -39,8 +39,10 @@ CallScope::~CallScope() {
 oh_status scratch(oh_ctx* ctx, const char* name, size_t bytes, void** out) {
   auto& b = ctx->scratch[name];
   if (b.bytes < bytes) {
-    ctx->dm_setup_key.clear();          // cached tables may live in a buffer being replaced
-    ctx->fresnel_key.clear();
+    // the cached tables of a buffer being replaced are gone
+    const std::string nm(name);
+    if (nm == "dm.tables") ctx->dm_setup_key.clear();
+    if (nm == "fr.B" || nm == "fr.tab") ctx->fresnel_key.clear();
     if (b.p) {
       cudaError_t e = cudaDeviceSynchronize();
       if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceSynchronize (scratch growth)");

@@ -360,6 +360,9 @@ static oh_status run_fresnel_separable(oh_ctx* ctx, int nx, int ny, double dp, d
   FFTPlan px, py;
   OH_TRY(get_plan(ctx, NX, 0, &px));
   OH_TRY(get_plan(ctx, NY, 0, &py));
+  // strip buffer first: growing the scratch arena drops every cached key
+  void* rbuf;
+  OH_TRY(scratch(ctx, "fr.R", (size_t)ny * NX * sizeof(float2), &rbuf));
   // cached tables: FP64 chirps / spectra, then the FP32 factors
   const size_t tab_bytes = (size_t)(NX + NY) * (sizeof(double2) + sizeof(float2));
   char key[160];
@@ -391,8 +394,6 @@ static oh_status run_fresnel_separable(oh_ctx* ctx, int nx, int ny, double dp, d
                                                       -amp * std::cos(kz), 1.0 / ((double)NX * (double)NY), hxs, hys);
     OH_LAUNCH_CHECK();
   }
-  void* rbuf;
-  OH_TRY(scratch(ctx, "fr.R", (size_t)ny * NX * sizeof(float2), &rbuf));
   FrArgs a{nx, ny, field, static_cast<float2*>(rbuf), static_cast<const float2*>(px.tw),
            static_cast<const float2*>(py.tw), px.perm, px.iperm, py.perm, py.iperm, hxs, hys};
   const int srow = (2 * NX + fr_tw_entries(NX)) * (int)sizeof(float2);

@@ -330,7 +330,7 @@ static oh_status run_pls(oh_ctx* ctx, int prec, const oh_pls_params* p, const oh
   PlsPt* q = static_cast<PlsPt*>(pp);
   {
     KernelTimer kt(ctx, "pls_prep", st);
-    pls_prep<<<std::min((n + 255) / 256, 152 * 8), 256, 0, st>>>(g, pts, n, q);
+    pls_prep<<<std::min((n + 63) / 64, 152 * 32), 64, 0, st>>>(g, pts, n, q);
     OH_LAUNCH_CHECK();
   }
   int engine = p->engine;

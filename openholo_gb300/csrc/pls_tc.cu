@@ -259,48 +259,64 @@ __global__ void __launch_bounds__(128, 1) pls_tc_gemm(const __grid_constant__ CU
 }
 
 // Operand tables for points [0, n): A (rows M_pad, K_pad) and B (rows N_pad,
-// K_pad), BF16 high and low parts, zero outside the data.
-__global__ void pls_tc_tables(PlsGeom g, const PlsPt* __restrict__ pts, int n, int kpad, int mpad, int npad,
-                              __nv_bfloat16* __restrict__ ahi, __nv_bfloat16* __restrict__ alo,
-                              __nv_bfloat16* __restrict__ bhi, __nv_bfloat16* __restrict__ blo) {
-  const int kp = kpad / 2;                                   // point slots
-  const long long na = (long long)mpad * kp, nb = (long long)(npad / 2) * kp;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < na + nb;
-       e += (long long)gridDim.x * blockDim.x) {
-    auto split = [](float v, __nv_bfloat16* h, __nv_bfloat16* l) {
-      const __nv_bfloat16 vh = __float2bfloat16_rn(v);
-      *h = vh;
-      *l = __float2bfloat16_rn(v - __bfloat162float(vh));
-    };
-    if (e < na) {
-      const int i = (int)(e / kp), k = (int)(e - (long long)i * kp);
+// K_pad), BF16 high and low parts, zero outside the data.  Grid: x over point
+// slots, y over A rows then B row pairs; each thread writes BF16 pairs.
+__device__ __forceinline__ void split2(float x, float y, __nv_bfloat162* hi, __nv_bfloat162* lo) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(x, y);
+  *hi = h;
+  *lo = __floats2bfloat162_rn(x - __low2float(h), y - __high2float(h));
+}
+
+constexpr int kTabRows = 16;     // table rows per thread (A rows, or B row pairs)
+
+__global__ void __launch_bounds__(256) pls_tc_tables(PlsGeom g, const PlsPt* __restrict__ pts, int n, int kpad,
+                                                     int mpad, __nv_bfloat16* __restrict__ ahi,
+                                                     __nv_bfloat16* __restrict__ alo, __nv_bfloat16* __restrict__ bhi,
+                                                     __nv_bfloat16* __restrict__ blo) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;      // point slot
+  if (k >= kpad / 2) return;
+  const int r0 = blockIdx.y * kTabRows;                      // mpad is a multiple of kTabRows
+  const bool live = k < n;
+  if (r0 < mpad) {
+    unsigned long long qa = 0, qb = 0, qg = 0;
+    int qm = 0;
+    float ar = 0.f, ai = 0.f;
+    if (live) {
+      const PlsPt& q = pts[k];
+      qa = q.ay; qb = q.by; qg = q.gy; qm = q.my; ar = q.ar; ai = q.ai;
+    }
+#pragma unroll 4
+    for (int r = r0; r < r0 + kTabRows; ++r) {
       float re = 0.f, im = 0.f;
-      if (k < n && i < g.ny) {
-        const PlsPt& q = pts[k];
+      if (live && r < g.ny) {
         float c, s;
-        pls_cis_neg(pls_turns(q.ay, q.by, q.gy, i - q.my), &c, &s);
-        re = -(q.ar * c - q.ai * s);
-        im = -(q.ar * s + q.ai * c);
+        pls_cis_neg(pls_turns(qa, qb, qg, r - qm), &c, &s);
+        re = -(ar * c - ai * s);
+        im = -(ar * s + ai * c);
       }
-      const size_t o = (size_t)i * kpad + 2 * k;
-      split(re, ahi + o, alo + o);
-      split(im, ahi + o + 1, alo + o + 1);
-    } else {
-      const long long f = e - na;
-      const int j = (int)(f / kp), k = (int)(f - (long long)j * kp);
+      const size_t o = (size_t)r * kpad + 2 * k;
+      split2(re, im, reinterpret_cast<__nv_bfloat162*>(ahi + o), reinterpret_cast<__nv_bfloat162*>(alo + o));
+    }
+  } else {
+    unsigned long long qa = 0, qb = 0, qg = 0;
+    int qm = 0;
+    if (live) {
+      const PlsPt& q = pts[k];
+      qa = q.ax; qb = q.bx; qg = q.gx; qm = q.mx;
+    }
+    const int j0 = r0 - mpad;
+#pragma unroll 4
+    for (int j = j0; j < j0 + kTabRows; ++j) {
       float re = 0.f, im = 0.f;
-      if (k < n && j < g.nx) {
-        const PlsPt& q = pts[k];
+      if (live && j < g.nx) {
         float c, s;
-        pls_cis_neg(pls_turns(q.ax, q.bx, q.gx, j - q.mx), &c, &s);
+        pls_cis_neg(pls_turns(qa, qb, qg, j - qm), &c, &s);
         re = -c;
         im = -s;
       }
       const size_t o0 = (size_t)(2 * j) * kpad + 2 * k, o1 = o0 + kpad;
-      split(re, bhi + o0, blo + o0);
-      split(-im, bhi + o0 + 1, blo + o0 + 1);
-      split(im, bhi + o1, blo + o1);
-      split(re, bhi + o1 + 1, blo + o1 + 1);
+      split2(re, -im, reinterpret_cast<__nv_bfloat162*>(bhi + o0), reinterpret_cast<__nv_bfloat162*>(blo + o0));
+      split2(im, re, reinterpret_cast<__nv_bfloat162*>(bhi + o1), reinterpret_cast<__nv_bfloat162*>(blo + o1));
     }
   }
 }
@@ -352,10 +368,11 @@ oh_status pls_tensor_enqueue(oh_ctx* ctx, const PlsGeom& g, const PlsPt* pts, in
   if (major != 10 || minor != 3) return fail(OH_ERR_UNSUPPORTED_SIZE, "the tensor engine is built for sm_103a");
   const int mpad = (g.ny + kBM - 1) / kBM * kBM;
   const int npad = (2 * g.nx + kBN - 1) / kBN * kBN;
+  if ((mpad + npad / 2) / kTabRows > 65535) return fail(OH_ERR_UNSUPPORTED_SIZE, "field too large for the tensor engine");
   // points per chunk: tables (mpad + npad) x 2 x 2 bytes per K column, <= 512 MiB
   const size_t per_k = (size_t)(mpad + npad) * 4;
-  int chunk_pts = (int)std::min<size_t>((size_t)n, ((size_t)512 << 20) / (per_k * 2));
-  chunk_pts = std::max(32, chunk_pts / 32 * 32);
+  const size_t fit = ((size_t)512 << 20) / (per_k * 2);
+  const int chunk_pts = (size_t)n <= fit ? n : (int)std::max<size_t>(32, fit / 32 * 32);
   const int kpad_max = (std::min(chunk_pts, n) * 2 + kBK - 1) / kBK * kBK;
   void* tp;
   OH_TRY(scratch(ctx, "pls.tc", (size_t)kpad_max * per_k, &tp));
@@ -379,7 +396,8 @@ oh_status pls_tensor_enqueue(oh_ctx* ctx, const PlsGeom& g, const PlsPt* pts, in
       OH_CUDA_TRY(cudaMemsetAsync(out, 0, (size_t)g.ny * g.nx * (g.mode == OH_PLS_CGH_FRESNEL ? 4 : 8), st));
     {
       KernelTimer kt(ctx, "pls_tc_tables", st);
-      pls_tc_tables<<<152 * 8, 256, 0, st>>>(g, pts + c0, cnt, kpad, mpad, npad, ahi, alo, bhi, blo);
+      const dim3 tg((kpad / 2 + 255) / 256, (mpad + npad / 2) / kTabRows);
+      pls_tc_tables<<<tg, 256, 0, st>>>(g, pts + c0, cnt, kpad, mpad, ahi, alo, bhi, blo);
       OH_LAUNCH_CHECK();
     }
     CUtensorMap mAhi, mAlo, mBhi, mBlo;
