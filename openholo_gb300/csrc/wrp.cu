@@ -81,7 +81,15 @@ __global__ void __launch_bounds__(256) wrp_accumulate_kernel(WRPGeom g, const do
 // registers.
 constexpr int kWrpTile = 64;
 
-struct WrpPt { int tx, ty, w; float base, adz, sgn; double dz; };
+// Per point: window centre and half-width; exact-path terms (base = k|dz|
+// reduced to radians); the FP64 path's dz; and, when the window is paraxial
+// enough (series = 1), the terms of the series evaluation below.
+struct WrpPt {
+  int tx, ty, w, series;
+  float base, adz, sgn, pad0;
+  double dz;
+  float base_t, kadz_t, inv_adz2, ea, inv_a0, pad1;
+};
 
 __device__ __forceinline__ void wrp_point(const WRPGeom& g, const double* xyz, int k, WrpPt* o) {
   const double two_pi = 6.283185307179586476925286766559;
@@ -99,6 +107,24 @@ __device__ __forceinline__ void wrp_point(const WRPGeom& g, const double* xyz, i
   o->adz = (float)fabs(dz);
   const double kdz = kd * fabs(dz);
   o->base = (float)(kdz - two_pi * rint(kdz / two_pi));
+  // Series form: with u = rho^2 / dz^2 and t = sqrt(1 + u) - 1 = u (1/2 - u/8 + u^2/16) + O(5 u^4 / 128),
+  //   k|r| = k|dz| (1 + t),   1 / (sgn |r| + 0.05) = (1 / a0) (1 - e + e^2),  a0 = sgn |dz| + 0.05,
+  //   e = sgn |dz| t / a0,
+  // used when the dropped terms stay below 1e-6 rad and 1e-8 relative over the whole window.
+  const double adz = fabs(dz), sg = dz > 0.0 ? 1.0 : -1.0;
+  const double a0 = sg * adz + 0.05;
+  const double rho2max = 2.0 * (double)g.fixed_w * g.fixed_w * (double)dpx * dpx;
+  const double umax = adz > 0.0 ? rho2max / (adz * adz) : 1.0;
+  const double emax = fabs(a0) > 1e-6 ? adz * umax / (2.0 * fabs(a0)) : 1.0;
+  o->series = (adz > 0.0 && umax < 0.05 && kdz * (5.0 / 128.0) * umax * umax * umax * umax < 1e-6 &&
+               emax * emax * emax < 1e-8) ? 1 : 0;
+  const double turns = kdz / two_pi;
+  o->base_t = (float)(sg * (turns - rint(turns)));
+  o->kadz_t = (float)(sg * turns);
+  o->inv_adz2 = adz > 0.0 ? (float)(1.0 / (adz * adz)) : 0.f;
+  o->ea = fabs(a0) > 1e-6 ? (float)(sg * adz / a0) : 0.f;
+  o->inv_a0 = fabs(a0) > 1e-6 ? (float)(1.0 / a0) : 0.f;
+  o->pad0 = o->pad1 = 0.f;
 }
 
 // tile index range [t0, t1] along one axis for the window [c - w, c + w) clipped to [0, n)
@@ -245,7 +271,8 @@ __global__ void __launch_bounds__(256) wrp_tile_f32(WRPGeom g, const WrpPt* __re
   constexpr int kRows = kWrpTile * kWrpTile / 256;
   const int tile = blockIdx.x;
   const int X0 = (tile % tiles_x) * kWrpTile, Y0 = (tile / tiles_x) * kWrpTile;
-  const int c = threadIdx.x & (kWrpTile - 1), r0 = threadIdx.x >> 6;
+  // warp w owns columns 8w..8w+7 of the tile; lane l column 8w + l % 8, rows l / 8 + 4 j
+  const int c = 8 * (threadIdx.x >> 5) + (threadIdx.x & 7), r0 = (threadIdx.x & 31) >> 3;
   float2 acc[kRows];
 #pragma unroll
   for (int j = 0; j < kRows; ++j) acc[j] = make_float2(0.f, 0.f);
@@ -261,14 +288,34 @@ __global__ void __launch_bounds__(256) wrp_tile_f32(WRPGeom g, const WrpPt* __re
     const float dx2 = ddx * ddx;
     const int wy0 = Y0 + r0 - q.ty;                 // wy of row j is wy0 + 4 j
     const int ylim = g.ny - Y0 - r0;               // row j inside the plane iff 4 j < ylim
+    if (q.series) {
 #pragma unroll
-    for (int j = 0; j < kRows; ++j) {
-      const int wy = wy0 + 4 * j;
-      if (wy >= -q.w && wy < q.w && 4 * j < ylim) {
-        const float ddy = (float)wy * dpx;
-        const float2 v = wrp_term_f32(fmaf(ddy, ddy, dx2), q, kf);
-        acc[j].x += v.x;
-        acc[j].y += v.y;
+      for (int j = 0; j < kRows; ++j) {
+        const int wy = wy0 + 4 * j;
+        if (wy >= -q.w && wy < q.w && 4 * j < ylim) {
+          const float ddy = (float)wy * dpx;
+          const float u = fmaf(ddy, ddy, dx2) * q.inv_adz2;
+          const float t = u * fmaf(u, fmaf(u, 0.0625f, -0.125f), 0.5f);
+          float f = fmaf(q.kadz_t, t, q.base_t);
+          f -= rintf(f);
+          float sn, cs;
+          __sincosf(6.28318530717958647692f * f, &sn, &cs);
+          const float e = t * q.ea;
+          const float amp = q.inv_a0 * fmaf(e, e - 1.f, 1.f);
+          acc[j].x = fmaf(cs, amp, acc[j].x);
+          acc[j].y = fmaf(sn, amp, acc[j].y);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < kRows; ++j) {
+        const int wy = wy0 + 4 * j;
+        if (wy >= -q.w && wy < q.w && 4 * j < ylim) {
+          const float ddy = (float)wy * dpx;
+          const float2 v = wrp_term_f32(fmaf(ddy, ddy, dx2), q, kf);
+          acc[j].x += v.x;
+          acc[j].y += v.y;
+        }
       }
     }
   }

@@ -60,15 +60,23 @@ def test_normalize_u8(ctx, round_half):
     assert np.array_equal(out.cpu().numpy(), ref)
 
 
-@pytest.mark.parametrize("fixed_w,precision,plane", [(8, "fp64", (96, 80)), (8, "fp32", (96, 80)), (0, "fp64", (96, 80)),
-                                                    (40, "fp32", (300, 170)), (40, "fp64", (300, 170)),
-                                                    (3, "fp32", (257, 129))])
-def test_wrp_accumulate(ctx, fixed_w, precision, plane):
-    # windows straddle 64x64 tiles and the plane's edges; some centres lie outside the plane
+@pytest.mark.parametrize("fixed_w,precision,plane,gap", [(8, "fp64", (96, 80), 0.4e-3), (8, "fp32", (96, 80), 0.4e-3),
+                                                        (0, "fp64", (96, 80), 0.4e-3),
+                                                        (40, "fp32", (300, 170), 0.4e-3),
+                                                        (40, "fp64", (300, 170), 0.4e-3),
+                                                        (3, "fp32", (257, 129), 0.4e-3),
+                                                        (24, "fp32", (300, 170), 5e-3),
+                                                        (24, "fp32", (300, 170), -5e-3)])
+def test_wrp_accumulate(ctx, fixed_w, precision, plane, gap):
+    # windows straddle 64x64 tiles and the plane's edges; some centres lie outside the plane.
+    # gap 5 mm (either side of the points) makes the FP32 windows paraxial enough for the series form.
     nx, ny = plane
     pts = scenes.wrp_scene(4, 200 if nx < 100 else 1500, box=(nx * 9e-6, ny * 9e-6, 0.2e-3), zc=0.01)
     dp, lam = 8e-6, 532e-9
-    z = 0.01 - 0.1e-3 - 0.4e-3 if fixed_w else 0.012   # formula mode: dz ~ 2 mm -> w ~ 15
+    if gap > 0:
+        z = 0.01 - 0.1e-3 - gap if fixed_w else 0.012   # dz < 0; formula mode: dz ~ 2 mm -> w ~ 15
+    else:
+        z = 0.01 + 0.1e-3 - gap                         # plane on the other side of the points (dz > 0)
     p = WrpParams(nx, ny, dp, lam, z, fixed_w)
     tp = torch.from_numpy(pts).cuda()
     cdt = torch.complex128 if precision == "fp64" else torch.complex64
