@@ -258,7 +258,7 @@ def plain_gpu_path(img_t, depth_t, zt, lut, torch):
     return frame
 
 
-SECONDARY_OPS = ("pointcloud", "pls", "wrp")
+SECONDARY_OPS = ("pointcloud", "pls", "wrp", "batch")
 
 
 def secondary_measurements(ctx, dev, torch, reps=5, ops=SECONDARY_OPS, warmup=1):
@@ -291,7 +291,58 @@ def secondary_measurements(ctx, dev, torch, reps=5, ops=SECONDARY_OPS, warmup=1)
         _sec_pls(ctx, dev, torch, st, timed, out, n, nx, ny, reps + warmup)
     if "wrp" in ops:
         _sec_wrp(ctx, dev, torch, st, timed, out, reps + warmup)
+    if "batch" in ops:
+        _sec_batch(ctx, dev, torch, out, reps, warmup)
     return out
+
+
+BATCH_FRAMES, BATCH_SEED = 64, 4
+
+
+def batch_workload():
+    """64 frames: side s from {512, 768, 1024, 1536, 2048}, layers 8..64 and
+    wavelength from {450, 532, 633} nm, drawn from SplitMix64 stream 9 of
+    seed 4; square frames, 2x pad, seeded per-pixel phase, FP32."""
+    from openholo_gb300 import scenes
+    u = scenes.uniform(BATCH_SEED, 9, 3 * BATCH_FRAMES).reshape(BATCH_FRAMES, 3)
+    sides = [512, 768, 1024, 1536, 2048]
+    lams = [450e-9, 532e-9, 633e-9]
+    return [(sides[int(a * 5)], 8 + int(b * 57), lams[int(c * 3)]) for a, b, c in u]
+
+
+def _sec_batch(ctx, dev, torch, out, reps, warmup):
+    from openholo_gb300 import depthmap as dm, launch_count, scenes
+    work = batch_workload()
+    scene = {}
+    frames = []
+    for i, (side, L, lam) in enumerate(work):
+        if side not in scene:
+            img, depth = scenes.depthmap_scene(SCENE_SEED + side, side, side)
+            scene[side] = (torch.from_numpy(img).to(dev), torch.from_numpy(depth).to(dev))
+        p = dm.make_params(pnx=side, pny=side, num_of_depth=L, lam=lam, pad=2, phase_mode=dm.OH_PHASE_SEEDED,
+                           seed=PHASE_SEED + i)
+        frames.append((p, scene[side][0], scene[side][1],
+                       torch.empty((side, side), dtype=torch.float32, device=dev)))
+    model = sum(L * 32 * (2 * side) ** 2 + 32 * (2 * side) ** 2 + 2 * side * side for side, L, _ in work)
+    stream = torch.cuda.Stream(device=dev)
+    with torch.cuda.stream(stream):
+        for _ in range(max(2, warmup)):
+            dm.generate_batch(ctx, frames, graph=True)
+        stream.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n0 = launch_count()
+        a.record(stream)
+        for _ in range(reps):
+            dm.generate_batch(ctx, frames, graph=True)
+        b.record(stream)
+        stream.synchronize()
+    ms = a.elapsed_time(b) / reps
+    out["batch_64_frames_mixed"] = {
+        "ms_per_batch": ms, "frames_per_s": BATCH_FRAMES * 1000.0 / ms,
+        "model_bytes_per_batch": model, "model_gbs": model / (ms * 1e-3) / 1e9,
+        "kernels_per_batch": (launch_count() - n0) / reps,
+        "what": "64 depth-map frames in one CUDA-graph launch: side 512-2048 px, 8-64 layers, 450/532/633 nm, "
+                "2x pad, FP32; model bytes = sum over frames of L*32*Np + 32*Np + 2N"}
 
 
 def _sec_pointcloud(ctx, dev, torch, st, timed, out, n, nx, ny):

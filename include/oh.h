@@ -151,6 +151,30 @@ oh_status oh_depthmap_generate_host(oh_ctx* ctx, oh_precision prec,
                                     const uint8_t* depth_host,
                                     const float* phase_host,
                                     void* fringe_host, void* stream);
+/* Batch of depth-map frames (frames differ in size, layer count, wavelength
+ * and every other parameter).  No reference counterpart: the reference
+ * generates one frame per call.  Each frame is what oh_depthmap_generate
+ * computes for the same arguments (fringe required, field nullable), in
+ * array order on `stream`; the scratch is sized once for the largest frame.
+ * flags OH_BATCH_GRAPH: the first call with a given frame array (parameters
+ * and buffer addresses) runs the frames and also captures them into a CUDA
+ * graph; later calls with an identical array launch that graph, reading
+ * whatever the input buffers then hold.  Graph mode needs a stream other
+ * than the legacy default stream and must not be called while the caller is
+ * capturing `stream`; otherwise the frames run without a graph. */
+typedef struct oh_depthmap_frame {
+  oh_depthmap_params params;
+  const uint8_t* img;       /* device [pny][pnx] */
+  const uint8_t* depth;     /* device [pny][pnx] */
+  const float*   phase;     /* device, OH_PHASE_ARRAY only */
+  void*          fringe;    /* device [pny][pnx] float (FP32) / double (FP64) */
+  void*          field;     /* nullable */
+} oh_depthmap_frame;
+#define OH_BATCH_GRAPH 1u
+oh_status oh_depthmap_generate_batch(oh_ctx* ctx, oh_precision prec,
+                                     const oh_depthmap_frame* frames, int n_frames,
+                                     unsigned flags, void* stream);
+
 /* Layer index per depth byte (256 entries, 0 = no layer), exactly the
  * reference's binning (change_depth_quan_*, HologramGenerator_CPU.cpp:74-103)
  * and the z' of each level (dlevel_transform_).  z_out holds num_of_depth

@@ -40,6 +40,15 @@ class DepthmapParams(C.Structure):
     ]
 
 
+class DepthmapFrame(C.Structure):
+    """oh_depthmap_frame (include/oh.h)."""
+    _fields_ = [("params", DepthmapParams), ("img", C.c_void_p), ("depth", C.c_void_p), ("phase", C.c_void_p),
+                ("fringe", C.c_void_p), ("field", C.c_void_p)]
+
+
+BATCH_GRAPH = 1
+
+
 class PcParams(C.Structure):
     """oh_pc_params (include/oh.h), field order of OphSpec."""
     _fields_ = [
@@ -99,6 +108,7 @@ SIGNATURES = {
     "oh_wrp_accumulate": (_i, [_vp, _i, C.POINTER(WrpParams), _vp, _i, _vp, _vp]),
     "oh_fresnel_propagate": (_i, [_vp, _i, _i, _i, _d, _d, _d, _vp, _vp]),
     "oh_pls": (_i, [_vp, _i, C.POINTER(PlsParams), _vp, _i, _vp, _vp]),
+    "oh_depthmap_generate_batch": (_i, [_vp, _i, C.POINTER(DepthmapFrame), _i, C.c_uint, _vp]),
     "oh_encode": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp]),
     "oh_normalize_u8": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _vp]),
 }

@@ -13,6 +13,7 @@ static std::atomic<uint64_t> g_launches{0};
 static thread_local std::string t_last_error;
 
 void note_launch(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
+uint64_t launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
 void set_error(const std::string& msg) { t_last_error = msg; }
 oh_status fail(oh_status s, const std::string& msg) { t_last_error = msg; return s; }
 oh_status cuda_fail(cudaError_t e, const char* what) {
@@ -36,9 +37,17 @@ CallScope::~CallScope() {
   if (prev_dev_ >= 0 && ctx_ && prev_dev_ != ctx_->device) cudaSetDevice(prev_dev_);
 }
 
+void drop_graphs(oh_ctx* ctx) {
+  for (auto& kv : ctx->graphs)
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+  ctx->graphs.clear();
+}
+
 oh_status scratch(oh_ctx* ctx, const char* name, size_t bytes, void** out) {
   auto& b = ctx->scratch[name];
   if (b.bytes < bytes) {
+    // captured depth-map graphs address the buffer being replaced
+    if (b.p && std::string(name).compare(0, 3, "dm.") == 0) drop_graphs(ctx);
     // the cached tables of a buffer being replaced are gone
     const std::string nm(name);
     if (nm == "dm.tables") ctx->dm_setup_key.clear();
@@ -235,6 +244,7 @@ oh_status oh_ctx_destroy(oh_ctx* ctx) {
   cudaGetDevice(&prev);
   cudaSetDevice(ctx->device);
   cudaDeviceSynchronize();
+  drop_graphs(ctx);
   for (auto& kv : ctx->scratch) cudaFree(kv.second.p);
   for (auto& kv : ctx->plans) { cudaFree(kv.second.tw); cudaFree(kv.second.perm); cudaFree(kv.second.iperm); }
   for (auto& m : ctx->marks) { cudaEventDestroy(m.a); cudaEventDestroy(m.b); }
@@ -260,6 +270,7 @@ oh_status oh_ctx_release_scratch(oh_ctx* ctx) {
   cudaGetDevice(&prev);
   cudaSetDevice(ctx->device);
   cudaDeviceSynchronize();
+  drop_graphs(ctx);
   for (auto& kv : ctx->scratch) cudaFree(kv.second.p);
   ctx->scratch.clear();
   ctx->dm_setup_key.clear();

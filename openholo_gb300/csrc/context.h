@@ -18,6 +18,10 @@ struct oh_ctx {
   int* dev_err = nullptr;             // set by kernels whose bounded waits ran out
   std::string dm_setup_key;           // parameters of the depth-map tables now in scratch
   std::string fresnel_key;            // parameters of the Fresnel spectrum in scratch "fr.B"
+  bool force_dm_setup = false;        // rebuild the depth-map tables even when cached (graph capture)
+  // captured depth-map batches: key -> executable graph and the table key it leaves behind
+  struct Graph { cudaGraphExec_t exec = nullptr; std::string dm_key; int launches = 0; };
+  std::map<std::string, Graph> graphs;
   struct Buf { void* p = nullptr; size_t bytes = 0; };
   std::map<std::string, Buf> scratch;
   struct PlanBufs { oh::FFTPlan plan; void* tw = nullptr; int* perm = nullptr; int* iperm = nullptr; };
@@ -52,6 +56,9 @@ class CallScope {
 // Returns a device buffer of at least `bytes` under `name`, growing it if
 // needed (growth synchronises the device before freeing the old buffer).
 oh_status scratch(oh_ctx* ctx, const char* name, size_t bytes, void** out);
+
+// Destroys every captured graph (they hold scratch addresses).
+void drop_graphs(oh_ctx* ctx);
 
 // Plan for length n in precision prec (0 = fp32, 1 = fp64); built on first
 // use.  Fails with OH_ERR_UNSUPPORTED_SIZE when n cannot be factored.

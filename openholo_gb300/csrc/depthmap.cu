@@ -542,10 +542,15 @@ static oh_status validate(const oh_depthmap_params* p) {
   return OH_OK;
 }
 
+// Scratch bytes one frame needs: R strips, V rows, occupancy flags, tables.
+struct DMScratch { size_t R, V, occ, tables; };
+
+// Enqueues one frame.  With sizes_only set, computes the frame's scratch
+// needs into it and returns without allocating or launching anything.
 template <typename R, int KMAX>
 static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const uint8_t* img,
                               const uint8_t* depth, const float* phase, void* fringe, void* field,
-                              void* spectrum, cudaStream_t st) {
+                              void* spectrum, cudaStream_t st, DMScratch* sizes_only = nullptr) {
   typedef typename cplx_of<R>::type C;
   const int prec = sizeof(R) == 8 ? 1 : 0;
   Levels L;
@@ -665,9 +670,8 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   // scratch
   void* ptr;
   const size_t nE = su.n_entries, nU = su.n_uslots;
-  OH_TRY(scratch(ctx, "dm.R", nU * a.pny * (size_t)a.Px * sizeof(C), &ptr)); a.Rbuf = (C*)ptr;
-  OH_TRY(scratch(ctx, "dm.V", (size_t)a.pny * a.Px * sizeof(C), &ptr)); a.V = (C*)ptr;
-  OH_TRY(scratch(ctx, "dm.occ", nU * (size_t)occ_stride + 16, &ptr)); a.occ = (uint8_t*)ptr;
+  const size_t bytes_R = nU * a.pny * (size_t)a.Px * sizeof(C), bytes_V = (size_t)a.pny * a.Px * sizeof(C),
+               bytes_occ = nU * (size_t)occ_stride + 16;
   // small tables share one buffer
   size_t off = 0;
   auto carve = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; };
@@ -676,6 +680,13 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
          o_ey = carve(prec ? 0 : nE * a.Py * sizeof(C)),
          o_eth = carve(a.ey_perm ? nE * a.Py * sizeof(R) : 0), o_lfx = carve(a.Px * sizeof(R)), o_lfy = carve(a.Py * sizeof(R)), o_lfyp = carve(a.Py * sizeof(R)),
          o_shy = carve(a.pny * sizeof(C)), o_shx = carve(a.pnx * sizeof(C)), o_any = carve(nU * sizeof(int));
+  if (sizes_only) {
+    *sizes_only = DMScratch{bytes_R, bytes_V, bytes_occ, off};
+    return OH_OK;
+  }
+  OH_TRY(scratch(ctx, "dm.R", bytes_R, &ptr)); a.Rbuf = (C*)ptr;
+  OH_TRY(scratch(ctx, "dm.V", bytes_V, &ptr)); a.V = (C*)ptr;
+  OH_TRY(scratch(ctx, "dm.occ", bytes_occ, &ptr)); a.occ = (uint8_t*)ptr;
   OH_TRY(scratch(ctx, "dm.tables", off, &ptr));
   char* base = (char*)ptr;
   a.lut = (int16_t*)(base + o_lut); a.uslot_of_entry = (int16_t*)(base + o_use); a.kzp = (R*)(base + o_kz);
@@ -703,7 +714,7 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
     key.ppx = a.ppx; key.ppy = a.ppy; key.lambda = a.lambda;
     key.tables = base; key.iperm = a.ply.iperm;
     std::string ks(reinterpret_cast<const char*>(&key), sizeof(key));
-    if (ks == ctx->dm_setup_key) {
+    if (ks == ctx->dm_setup_key && !ctx->force_dm_setup) {
       OH_CUDA_TRY(cudaMemsetAsync(a.slot_any, 0, nU * sizeof(int), st));
     } else {
       KernelTimer kt(ctx, prec ? "dm_setup_f64" : "dm_setup", st);
@@ -815,6 +826,96 @@ oh_status oh_depthmap_generate(oh_ctx* ctx, oh_precision prec, const oh_depthmap
   if (p->phase_mode == OH_PHASE_ARRAY && !phase) return fail(OH_ERR_INVALID_ARG, "OH_PHASE_ARRAY needs a phase array");
   if (prec == OH_FP64) return run_depthmap<double, 18>(ctx, p, img, depth, phase, fringe_out, field_out, spectrum_out, st);
   return run_depthmap<float, 36>(ctx, p, img, depth, phase, fringe_out, field_out, spectrum_out, st);
+}
+
+oh_status oh_depthmap_generate_batch(oh_ctx* ctx, oh_precision prec, const oh_depthmap_frame* frames, int n,
+                                     unsigned flags, void* stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  CallScope cs(ctx, st);
+  OH_TRY(cs.status());
+  if (n < 0 || (n > 0 && !frames)) return fail(OH_ERR_INVALID_ARG, "bad frame array");
+  if (flags & ~OH_BATCH_GRAPH) return fail(OH_ERR_INVALID_ARG, "unknown batch flags");
+  for (int i = 0; i < n; ++i) {
+    const oh_depthmap_frame& f = frames[i];
+    OH_TRY(validate(&f.params));
+    if (!f.img || !f.depth || !f.fringe)
+      return fail(OH_ERR_INVALID_ARG, "frame " + std::to_string(i) + ": img, depth and fringe are required");
+    if (f.params.phase_mode == OH_PHASE_ARRAY && !f.phase)
+      return fail(OH_ERR_INVALID_ARG, "frame " + std::to_string(i) + ": OH_PHASE_ARRAY needs a phase array");
+  }
+  if (n == 0) return OH_OK;
+  const bool fp64 = prec == OH_FP64;
+  auto run_all = [&](DMScratch* sizes) -> oh_status {
+    for (int i = 0; i < n; ++i) {
+      const oh_depthmap_frame& f = frames[i];
+      DMScratch* sz = sizes ? sizes + i : nullptr;
+      if (fp64) OH_TRY((run_depthmap<double, 18>(ctx, &f.params, f.img, f.depth, f.phase, f.fringe, f.field, nullptr, st, sz)));
+      else OH_TRY((run_depthmap<float, 36>(ctx, &f.params, f.img, f.depth, f.phase, f.fringe, f.field, nullptr, st, sz)));
+    }
+    return OH_OK;
+  };
+  // size the scratch once for the largest frame
+  std::vector<DMScratch> sz(n);
+  OH_TRY(run_all(sz.data()));
+  DMScratch mx{0, 0, 0, 0};
+  for (const DMScratch& z : sz) {
+    mx.R = std::max(mx.R, z.R); mx.V = std::max(mx.V, z.V);
+    mx.occ = std::max(mx.occ, z.occ); mx.tables = std::max(mx.tables, z.tables);
+  }
+  void* ptr;
+  OH_TRY(scratch(ctx, "dm.R", mx.R, &ptr));
+  OH_TRY(scratch(ctx, "dm.V", mx.V, &ptr));
+  OH_TRY(scratch(ctx, "dm.occ", mx.occ, &ptr));
+  OH_TRY(scratch(ctx, "dm.tables", mx.tables, &ptr));
+  bool graph = (flags & OH_BATCH_GRAPH) && st != nullptr;
+  if (graph) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    OH_CUDA_TRY(cudaStreamIsCapturing(st, &cap));
+    graph = cap == cudaStreamCaptureStatusNone;
+  }
+  if (!graph) return run_all(nullptr);
+  // key: precision and the whole frame array (parameters, buffer addresses,
+  // render-depth lists)
+  std::string key = std::to_string((int)fp64) + ":" + std::to_string(n) + ":";
+  key.append(reinterpret_cast<const char*>(frames), (size_t)n * sizeof(oh_depthmap_frame));
+  for (int i = 0; i < n; ++i)
+    if (frames[i].params.render_depth)
+      key.append(reinterpret_cast<const char*>(frames[i].params.render_depth),
+                 (size_t)frames[i].params.n_render_depth * sizeof(int));
+  auto it = ctx->graphs.find(key);
+  if (it != ctx->graphs.end()) {
+    OH_CUDA_TRY(cudaGraphLaunch(it->second.exec, st));
+    note_launch(it->second.launches);           // kernels inside the graph
+    ctx->dm_setup_key = it->second.dm_key;    // the tables the graph leaves in scratch
+    return OH_OK;
+  }
+  OH_TRY(run_all(nullptr));                   // this call's frames
+  if (ctx->graphs.size() >= 16) drop_graphs(ctx);
+  // capture the same launches for the next calls: tables are rebuilt inside
+  // the graph for every frame, timing events are left out
+  const bool timing = ctx->timing;
+  ctx->timing = false;
+  ctx->force_dm_setup = true;
+  cudaGraph_t g = nullptr;
+  oh_status rs = OH_OK;
+  const uint64_t l0 = launches_so_far();
+  cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) rs = cuda_fail(e, "cudaStreamBeginCapture");
+  else {
+    rs = run_all(nullptr);
+    e = cudaStreamEndCapture(st, &g);
+    if (rs == OH_OK && e != cudaSuccess) rs = cuda_fail(e, "cudaStreamEndCapture");
+  }
+  ctx->timing = timing;
+  ctx->force_dm_setup = false;
+  if (rs == OH_OK) {
+    cudaGraphExec_t ex = nullptr;
+    e = cudaGraphInstantiate(&ex, g, 0);
+    if (e != cudaSuccess) rs = cuda_fail(e, "cudaGraphInstantiate");
+    else ctx->graphs[key] = oh_ctx::Graph{ex, ctx->dm_setup_key, (int)(launches_so_far() - l0)};
+  }
+  if (g) cudaGraphDestroy(g);
+  return rs;
 }
 
 oh_status oh_depthmap_generate_host(oh_ctx* ctx, oh_precision prec, const oh_depthmap_params* p,

@@ -32,6 +32,8 @@ template <int SGN, typename C> __host__ __device__ __forceinline__ C cmul_i(C a)
 
 // Launch accounting (read through oh_kernel_launch_count()).
 void note_launch(int n = 1);
+// Kernels launched by this library so far (all threads).
+uint64_t launches_so_far();
 
 // Per-thread last-error message.
 void set_error(const std::string& msg);

@@ -74,6 +74,27 @@ def generate(ctx: _lib.Context, p: DepthmapParams, img, depth, phase=None, preci
     return fringe
 
 
+def generate_batch(ctx: _lib.Context, frames, precision="fp32", graph=False, stream=None):
+    """Run a list of frames in one call (oh_depthmap_generate_batch).  Each
+    entry is (params, img, depth, fringe) or (params, img, depth, fringe,
+    phase) with device tensors; fringe receives the result.  graph=True
+    captures the batch into a CUDA graph on the first call and replays it on
+    later calls with the same frames (same parameters and tensors)."""
+    prec = OH_FP64 if precision == "fp64" else OH_FP32
+    arr = (_lib.DepthmapFrame * len(frames))()
+    for i, fr in enumerate(frames):
+        p, img, depth, fringe = fr[:4]
+        phase = fr[4] if len(fr) > 4 else None
+        arr[i].params = p
+        arr[i].img = img.data_ptr()
+        arr[i].depth = depth.data_ptr()
+        arr[i].phase = phase.data_ptr() if phase is not None else None
+        arr[i].fringe = fringe.data_ptr()
+        arr[i].field = None
+    _lib.call("oh_depthmap_generate_batch", ctx.handle, prec, arr, len(frames),
+              _lib.BATCH_GRAPH if graph else 0, _stream_ptr(stream))
+
+
 def generate_host(ctx: _lib.Context, p: DepthmapParams, img: np.ndarray, depth: np.ndarray,
                   phase: np.ndarray | None = None, precision="fp32", out: np.ndarray | None = None, stream=None):
     """Host buffers in and out (oh_depthmap_generate_host)."""

@@ -66,11 +66,13 @@ def test_depthmap_vs_oracle(ctx, dev, pad, precision):
 
 
 @pytest.mark.parametrize("shape,pad,L", [((540, 960), 2, 12), ((512, 512), 2, 8), ((1080, 1920), 1, 6),
-                                         ((540, 500), 2, 7)])
+                                         ((540, 500), 2, 7), ((768, 768), 2, 5), ((384, 1536), 2, 4),
+                                         ((1024, 1024), 2, 4), ((384, 2048), 2, 3), ((2048, 384), 2, 3),
+                                         ((1536, 256), 2, 3)])
 def test_fast_lengths_vs_oracle(ctx, dev, shape, pad, L):
-    """FFT grids with compile-time schedules (1920x1080, 1024x1024): the
-    bulk-copy pipelined column pass and the scheduled row/output passes; and
-    a generic row length (1000) with a scheduled column length (1080)."""
+    """FFT grids with compile-time schedules (padded lengths 1024 to 4096):
+    the bulk-copy pipelined column pass and the scheduled row/output passes,
+    each paired with a generic length on the other axis where possible."""
     ny, nx = shape
     img, depth = scenes.depthmap_scene(61, ny, nx)
     p = dm.make_params(pnx=nx, pny=ny, num_of_depth=L, pad=pad, phase_mode=dm.OH_PHASE_SEEDED, seed=4)
