@@ -232,6 +232,20 @@ oh_status oh_pointcloud_host(oh_ctx* ctx, oh_precision prec,
 oh_status oh_pointcloud_noalloc(const oh_pc_params* p, const float* xyza, int n_points,
                                 void* field_out, void* fringe_out, void* stream);
 
+/* ---- propagation in the MATLAB tools' forms --------------------------------
+ * OH_PROP_FRESNEL_TF (FresnelPropagation.m:1-16): ifft2(fft2(U) .* H) with
+ *   H = exp(i k z) exp(-i pi lambda z (fx^2 + fy^2)) on the FFT-ordered grid; no padding.
+ * OH_PROP_AS_BANDLIMITED (fn_FresnelPropagation_as.m:1-48): 2x zero pad with
+ *   the field at (round(ny/2)-1, round(nx/2)-1), centred FFT, angular-spectrum
+ *   kernel exp(i 2 pi z sqrt(1/lambda^2 - a^2 - b^2)) with the Matsushima band
+ *   limit, centred inverse FFT, crop.
+ * In place on field [ny][nx] (oh_c64 for OH_FP32, oh_c128 for OH_FP64). */
+#define OH_PROP_FRESNEL_TF 0
+#define OH_PROP_AS_BANDLIMITED 1
+oh_status oh_propagate(oh_ctx* ctx, oh_precision prec, int method, int nx, int ny,
+                       double dx, double dy, double z, double lambda,
+                       void* field, void* stream);
+
 /* ---- point-light-source summation (cwoPLS) -------------------------------
  * The per-pixel point sums of CWO++'s cwoPLS class
  * (OpenHolo_WRP/openwrp_console_ver 1.0/cwo/src/cwoPLS.cpp), pixel (i, j):
@@ -284,6 +298,15 @@ typedef struct oh_wrp_params {
 oh_status oh_wrp_accumulate(oh_ctx* ctx, oh_precision prec,
                             const oh_wrp_params* p, const double* xyz,
                             int n_points, void* wrp, void* stream);
+/* MATLAB fn_wrp (fn_wrp.m:13-36): per point an odd N x N window,
+ * N = round(|lambda dz / pitch^2 / 2| + 0.5) * 2 - 1, dz = z_wrp - z, of
+ * exp(i phase[k]) exp(i k r) / r (r signed with dz, no +0.05), centred at
+ * (round(x/pitch) + (res-1)/2, round(y/pitch) + (res-1)/2) (1-based, first
+ * index along x), added into holo [res][res] (caller zeroes it).  phase
+ * (radians, nullable = 0) replaces MATLAB's rand * 2 pi.  Points are double3. */
+oh_status oh_wrp_matlab(oh_ctx* ctx, oh_precision prec, int res, double pitch, double lambda,
+                        double z_wrp, const double* xyz, const double* phase, int n_points,
+                        void* holo, void* stream);
 /* CWO::Diffract(z, CWO_FRESNEL_CONV) with the default zero-pad expansion
  * (cwo.cpp:2198-2279, 2872-2898), in place on field [ny][nx]. */
 oh_status oh_fresnel_propagate(oh_ctx* ctx, oh_precision prec, int nx, int ny,

@@ -47,6 +47,7 @@ class DepthmapFrame(C.Structure):
 
 
 BATCH_GRAPH = 1
+PROP_FRESNEL_TF, PROP_AS_BANDLIMITED = 0, 1
 
 
 class PcParams(C.Structure):
@@ -108,6 +109,8 @@ SIGNATURES = {
     "oh_wrp_accumulate": (_i, [_vp, _i, C.POINTER(WrpParams), _vp, _i, _vp, _vp]),
     "oh_fresnel_propagate": (_i, [_vp, _i, _i, _i, _d, _d, _d, _vp, _vp]),
     "oh_pls": (_i, [_vp, _i, C.POINTER(PlsParams), _vp, _i, _vp, _vp]),
+    "oh_propagate": (_i, [_vp, _i, _i, _i, _i, _d, _d, _d, _d, _vp, _vp]),
+    "oh_wrp_matlab": (_i, [_vp, _i, _i, _d, _d, _d, _vp, _vp, _i, _vp, _vp]),
     "oh_depthmap_generate_batch": (_i, [_vp, _i, C.POINTER(DepthmapFrame), _i, C.c_uint, _vp]),
     "oh_encode": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp]),
     "oh_normalize_u8": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _vp]),

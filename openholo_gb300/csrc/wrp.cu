@@ -333,6 +333,76 @@ __global__ void __launch_bounds__(256) wrp_tile_f32(WRPGeom g, const WrpPt* __re
   }
 }
 
+// ---- MATLAB fn_wrp (fn_wrp.m:13-36, WRP_matlab_ver 1.0) ----------------------
+// Per point: dz = z_wrp - z, N = round(|lambda dz / dp^2 / 2| + 0.5) * 2 - 1
+// (odd), centre (round(x/dp) + (res-1)/2, round(y/dp) + (res-1)/2) (MATLAB
+// 1-based), sub-hologram exp(i phase) exp(i k r) / r with r = sign(dz)
+// sqrt(dz^2 + xr^2 + yr^2) over the N x N offsets (a - (N-1)/2) dp; the
+// first index follows x.  Window pixels outside the res x res plane are
+// dropped; points with dz = 0 (r = 0) are skipped.  Each block takes whole
+// points and adds the part of the window inside the plane with atomics.
+struct WrpMGeom { int res; double dp, lambda, z; };
+
+__device__ __forceinline__ double mround(double x) { return x < 0 ? -floor(-x + 0.5) : floor(x + 0.5); }
+
+template <typename R>
+__global__ void __launch_bounds__(256) wrp_matlab_kernel(WrpMGeom g, const double* __restrict__ xyz,
+                                                        const double* __restrict__ phase, int n,
+                                                        typename cplx_of<R>::type* __restrict__ holo) {
+  const double two_pi = 6.283185307179586476925286766559;
+  const double k = two_pi / g.lambda;
+  const long long res = g.res;
+  for (int o = blockIdx.x; o < n; o += gridDim.x) {
+    const double px = xyz[3 * o], py = xyz[3 * o + 1], pz = xyz[3 * o + 2];
+    const double dz = g.z - pz;
+    if (dz == 0.0) continue;
+    const double nd = mround(fabs(g.lambda * dz / (g.dp * g.dp) / 2.0) + 0.5) * 2.0 - 1.0;
+    if (!(nd >= 1.0) || nd > 4.0e9) continue;
+    const long long N = (long long)nd;
+    const double lim = 4.0e18;
+    const long long cx = (long long)fmin(fmax(mround(px / g.dp), -lim), lim) + (res - 1) / 2;
+    const long long cy = (long long)fmin(fmax(mround(py / g.dp), -lim), lim) + (res - 1) / 2;
+    // plane row i takes window row a = i + a0, a in [0, N)
+    const long long a0 = (N + 1) / 2 - cx, b0 = (N + 1) / 2 - cy;
+    const long long i_lo = a0 < 0 ? -a0 : 0, i_hi = N - a0 < res ? N - a0 : res;
+    const long long j_lo = b0 < 0 ? -b0 : 0, j_hi = N - b0 < res ? N - b0 : res;
+    if (i_lo >= i_hi || j_lo >= j_hi) continue;
+    const int h = (int)(i_hi - i_lo), w = (int)(j_hi - j_lo);
+    const double ph0 = phase ? phase[o] : 0.0;
+    const double sg = dz > 0.0 ? 1.0 : -1.0, adz = fabs(dz);
+    const long long half = (N - 1) / 2;
+    // FP32: sign(dz) k |r| + ph = sign(dz) (k|dz| + k rho^2 / (|r| + |dz|)) + ph, constant part reduced in FP64
+    double base = sg * k * adz + ph0;
+    base -= two_pi * rint(base / two_pi);
+    const float basef = (float)base, kf = (float)k, adzf = (float)adz, sgf = (float)sg, dpf = (float)g.dp;
+    for (int e = threadIdx.x; e < h * w; e += blockDim.x) {
+      const int ii = e / w, jj = e - ii * w;
+      const long long i = i_lo + ii, j = j_lo + jj;
+      const long long a = i + a0 - half, b = j + b0 - half;      // offsets from the window centre
+      typename cplx_of<R>::type v;
+      if constexpr (sizeof(R) == 8) {
+        const double xr = (double)a * g.dp, yr = (double)b * g.dp;
+        const double r = sg * sqrt(dz * dz + xr * xr + yr * yr);
+        double sn, cs;
+        sincos(k * r + ph0, &sn, &cs);
+        v = mk(cs / r, sn / r);
+      } else {
+        const float xr = (float)a * dpf, yr = (float)b * dpf;
+        const float rho2 = fmaf(xr, xr, yr * yr);
+        const float ar = sqrtf(fmaf(adzf, adzf, rho2));
+        float ph = fmaf(sgf * kf, rho2 / (ar + adzf), basef);
+        float sn, cs;
+        sincosf(ph, &sn, &cs);
+        const float inv = sgf / ar;
+        v = mk(cs * inv, sn * inv);
+      }
+      typename cplx_of<R>::type* d = holo + i * res + j;
+      atomicAdd(&d->x, v.x);
+      atomicAdd(&d->y, v.y);
+    }
+  }
+}
+
 }  // namespace oh
 
 using namespace oh;
@@ -385,6 +455,23 @@ oh_status oh_wrp_accumulate(oh_ctx* ctx, oh_precision prec, const oh_wrp_params*
   KernelTimer kt(ctx, "wrp_accumulate", st);
   if (prec == OH_FP64) wrp_accumulate_kernel<double><<<grid, 256, 0, st>>>(g, xyz, n_points, (double2*)wrp);
   else wrp_accumulate_kernel<float><<<grid, 256, 0, st>>>(g, xyz, n_points, (float2*)wrp);
+  OH_LAUNCH_CHECK();
+  return OH_OK;
+}
+
+oh_status oh_wrp_matlab(oh_ctx* ctx, oh_precision prec, int res, double pitch, double lambda, double z_wrp,
+                        const double* xyz, const double* phase, int n_points, void* holo, void* stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  CallScope cs(ctx, st);
+  OH_TRY(cs.status());
+  if (res < 1 || !(pitch > 0) || !(lambda > 0)) return fail(OH_ERR_INVALID_ARG, "bad fn_wrp parameters");
+  if (n_points < 0 || (n_points > 0 && !xyz) || !holo) return fail(OH_ERR_INVALID_ARG, "bad fn_wrp buffers");
+  if (n_points == 0) return OH_OK;
+  WrpMGeom g{res, pitch, lambda, z_wrp};
+  KernelTimer kt(ctx, "wrp_matlab", st);
+  const int grid = std::min(n_points, 152 * 16);
+  if (prec == OH_FP64) wrp_matlab_kernel<double><<<grid, 256, 0, st>>>(g, xyz, phase, n_points, (double2*)holo);
+  else wrp_matlab_kernel<float><<<grid, 256, 0, st>>>(g, xyz, phase, n_points, (float2*)holo);
   OH_LAUNCH_CHECK();
   return OH_OK;
 }

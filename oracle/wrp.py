@@ -37,3 +37,43 @@ def fresnel_tf(field, dx, dy, z, lam):
     yi = np.concatenate([np.arange(0, (ny - 1) // 2 + 1), np.arange(-((ny + 2) // 2) + 1, 0)]) * fy
     H = np.exp(1j * k * z) * np.exp(-1j * np.pi * lam * z * (xi[None, :] ** 2 + yi[:, None] ** 2))
     return np.fft.ifft2(np.fft.fft2(field) * H)
+
+
+def _mround(x):
+    """MATLAB round: halves away from zero."""
+    return np.sign(x) * np.floor(np.abs(x) + 0.5)
+
+
+def fn_wrp_window(obj, lam, dp, res, z_wrp, phase=None):
+    """fn_wrp.m:13-36 (WRP_matlab_ver 1.0): the sub-hologram loop, with the
+    per-point random phase given explicitly (phase[k] radians, MATLAB draws
+    rand*2*pi).  obj: (n, 3) x, y, z.  Returns the res x res complex WRP,
+    first index following x as in the MATLAB source.  The padded `temp` array
+    of the source is reproduced; sub-holograms that MATLAB could not place
+    (negative indices) are clipped to the plane instead."""
+    obj = np.asarray(obj, dtype=np.float64)
+    k = 2 * np.pi / lam
+    z = z_wrp - obj[:, 2]
+    N = (_mround(np.abs(lam * z / dp ** 2 / 2) + 0.5) * 2 - 1).astype(np.int64)
+    cx = _mround(obj[:, 0] / dp).astype(np.int64) + (res - 1) // 2      # 1-based MATLAB index
+    cy = _mround(obj[:, 1] / dp).astype(np.int64) + (res - 1) // 2
+    holo = np.zeros((res, res), np.complex128)
+    for o in range(obj.shape[0]):
+        n = int(N[o])
+        t = (np.arange(n) - (n - 1) / 2) * dp
+        x_run, y_run = np.meshgrid(t, t, indexing="ij")             # rows follow x
+        r = np.sign(z[o]) * np.sqrt(z[o] ** 2 + y_run ** 2 + x_run ** 2)
+        ph = 0.0 if phase is None else phase[o]
+        sub = np.exp(1j * ph) * np.exp(1j * k * r) / r
+        # hologram row i (0-based) takes sub row a = i + (n + 1) / 2 - cx
+        a0 = (n + 1) // 2 - cx[o]
+        b0 = (n + 1) // 2 - cy[o]
+        for i in range(res):
+            a = i + a0
+            if a < 0 or a >= n:
+                continue
+            jb = np.arange(res)
+            b = jb + b0
+            ok = (b >= 0) & (b < n)
+            holo[i, jb[ok]] += sub[a, b[ok]]
+    return holo

@@ -12,6 +12,7 @@ from openholo_gb300._lib import WrpParams
 from oracle import depthmap as odm
 from oracle import encoding as oenc
 from oracle import pointcloud as opc
+from oracle import propagation as oprop
 from oracle import wrp as owrp
 
 pytestmark = pytest.mark.gpu
@@ -145,3 +146,56 @@ def test_fresnel_spectrum_cache_follows_distance(ctx):
         torch.cuda.synchronize()
         ref = owrp.fresnel_conv(U, dp, lam, z)
         assert np.linalg.norm(t.cpu().numpy() - ref) <= 1e-10 * np.linalg.norm(ref), z
+
+
+@pytest.mark.parametrize("shape,dx,dy,z,lam", [((48, 64), 8e-6, 8e-6, 0.05, 532e-9),       # band limit active
+                                               ((33, 45), 6e-6, 9e-6, -0.02, 633e-9),      # odd sizes, z < 0
+                                               ((40, 40), 0.2e-6, 0.2e-6, 2e-6, 532e-9)])  # evanescent region
+def test_propagate_as_bandlimited(ctx, shape, dx, dy, z, lam):
+    ny, nx = shape
+    U = field_sample(ny, nx, 11)
+    ref = oprop.as_bandlimited(U, dx, dy, z, lam)
+    for precision, tol in (("fp64", 1e-10), ("fp32", 1e-5)):
+        t = torch.from_numpy(U).to(torch.complex128 if precision == "fp64" else torch.complex64).cuda()
+        _lib.call("oh_propagate", ctx.handle, 1 if precision == "fp64" else 0, _lib.PROP_AS_BANDLIMITED, nx, ny,
+                  dx, dy, z, lam, C.c_void_p(t.data_ptr()), S())
+        torch.cuda.synchronize()
+        got = t.cpu().numpy()
+        assert np.linalg.norm(got - ref) <= tol * np.linalg.norm(ref), precision
+
+
+@pytest.mark.parametrize("shape,z", [((48, 64), 0.05), ((33, 45), -0.03), ((540, 960), 0.05)])
+def test_propagate_fresnel_tf(ctx, shape, z):
+    ny, nx = shape
+    U = field_sample(ny, nx, 12)
+    dx, dy, lam = 8e-6, 6e-6, 532e-9
+    ref = owrp.fresnel_tf(U, dx, dy, z, lam)
+    for precision, tol in (("fp64", 1e-10), ("fp32", 1e-5)):
+        t = torch.from_numpy(U).to(torch.complex128 if precision == "fp64" else torch.complex64).cuda()
+        _lib.call("oh_propagate", ctx.handle, 1 if precision == "fp64" else 0, _lib.PROP_FRESNEL_TF, nx, ny,
+                  dx, dy, z, lam, C.c_void_p(t.data_ptr()), S())
+        torch.cuda.synchronize()
+        assert np.linalg.norm(t.cpu().numpy() - ref) <= tol * np.linalg.norm(ref), precision
+
+
+@pytest.mark.parametrize("res,precision", [(65, "fp64"), (65, "fp32"), (64, "fp32")])
+def test_wrp_matlab_window(ctx, res, precision):
+    """fn_wrp.m: odd centred windows, random phase given per point, 1/r; some
+    windows run off the plane."""
+    dp, lam, z_wrp = 10e-6, 532e-9, 5e-3
+    u = scenes.uniform(21, 3, 40 * 4).reshape(40, 4)
+    obj = np.empty((40, 3))
+    obj[:, 0] = (u[:, 0] - 0.5) * res * dp * 1.2
+    obj[:, 1] = (u[:, 1] - 0.5) * res * dp * 1.2
+    obj[:, 2] = 1e-3 + u[:, 2] * 2e-3
+    phase = u[:, 3] * 2 * np.pi
+    ref = owrp.fn_wrp_window(obj, lam, dp, res, z_wrp, phase)
+    cdt = torch.complex128 if precision == "fp64" else torch.complex64
+    holo = torch.zeros((res, res), dtype=cdt, device="cuda")
+    t_obj = torch.from_numpy(obj).cuda()
+    t_ph = torch.from_numpy(phase).cuda()
+    _lib.call("oh_wrp_matlab", ctx.handle, 1 if precision == "fp64" else 0, res, dp, lam, z_wrp,
+              C.c_void_p(t_obj.data_ptr()), C.c_void_p(t_ph.data_ptr()), 40, C.c_void_p(holo.data_ptr()), S())
+    torch.cuda.synchronize()
+    tol = 1e-10 if precision == "fp64" else 1e-5
+    assert np.linalg.norm(holo.cpu().numpy() - ref) <= tol * np.linalg.norm(ref)

@@ -176,3 +176,16 @@ def test_library_levels_transform(lib_built):
     _, z = dm.levels(p)
     op = odm.DMParams(num_of_depth=8, near=0.2, far=0.7, transform_viewing_window=1, field_lens=1.0)
     assert np.array_equal(z, np.array(odm.transformed_levels(op)))
+
+
+def test_as_bandlimited_oracle_limits():
+    """The band-limited AS restatement: z -> 0 returns the input (the kernel is
+    1 inside the band); a plane wave along the axis keeps its amplitude."""
+    from oracle import propagation as oprop
+    rng = np.random.default_rng(3)
+    U = rng.standard_normal((24, 30)) + 1j * rng.standard_normal((24, 30))
+    out = oprop.as_bandlimited(U, 8e-6, 8e-6, 0.0, 532e-9)
+    assert np.abs(out - U).max() < 1e-12 * np.abs(U).max()
+    plane = np.ones((32, 32), np.complex128)
+    out = oprop.as_bandlimited(plane, 8e-6, 8e-6, 1e-3, 532e-9)
+    assert abs(abs(out[16, 16]) - 1.0) < 0.05
