@@ -85,6 +85,19 @@ def test_fast_lengths_vs_oracle(ctx, dev, shape, pad, L):
     assert lib().oh_ctx_device_status(ctx.handle, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)) == 0
 
 
+@pytest.mark.parametrize("sig", [(1, 0), (-1, -1), (1, 1), (0, 0), (0, -1)])
+def test_fast_path_ssb_crops(ctx, dev, sig):
+    """FP32 scheduled lengths with every single-sideband crop: the column pass
+    skips the transfer-function work of cropped spectrum samples."""
+    ny, nx = 540, 960
+    img, depth = scenes.depthmap_scene(71, ny, nx)
+    p = dm.make_params(pnx=nx, pny=ny, num_of_depth=5, pad=2, sig_location=sig, phase_mode=dm.OH_PHASE_SEEDED,
+                       seed=9)
+    fr = run(ctx, dev, img, depth, p, None, "fp32")
+    ref_fr = odm.generate(img, depth, oparams(p), phase=scenes.seeded_phase(9, ny, nx))[0]
+    assert rel(fr, ref_fr) < TOL32
+
+
 def test_reference_mode_matches_oracle(ctx, dev):
     """pad = 1, constant rand phase, viewing-window transform: the reference's own configuration."""
     ny, nx, L = 60, 96, 16
