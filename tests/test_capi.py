@@ -89,3 +89,18 @@ def test_null_arguments_rejected_without_gpu(lib_built):
     L = lib_built
     assert L.oh_depthmap_levels(None, None, None) == 1
     assert L.oh_ctx_create(None, 0) == 1
+
+
+def test_library_resolves_its_own_symbols(lib_built):
+    """Every undefined dynamic symbol of the library comes from the system
+    libraries (versioned glibc / libstdc++ / libgcc entries or weak ones): a
+    library-internal function declared in the wrong namespace would show up
+    here as an unversioned undefined symbol."""
+    import shutil
+    import subprocess
+    if not shutil.which("nm"):
+        pytest.skip("nm not available")
+    from openholo_gb300 import build as B
+    out = subprocess.run(["nm", "-D", "--undefined-only", str(B.LIB)], capture_output=True, text=True).stdout
+    bad = [ln for ln in out.splitlines() if ln.split() and ln.split()[0] == "U" and "@" not in ln]
+    assert not bad, bad[:10]
