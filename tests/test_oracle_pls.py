@@ -45,3 +45,23 @@ def test_huygens_paraxial_limit():
     k = 2 * np.pi / lam
     ratio = h * 0.5 / np.exp(1j * k * 0.5) / f
     assert np.abs(ratio - 1).max() < 1e-3
+
+
+def test_texdep_single_equals_convolution():
+    """cwoTexDep::WRP(z) oracle: the per-texel scatter equals the 2-D
+    convolution of the texture with the separable zone-plate window (the
+    identity the GPU kernel is built on)."""
+    from scipy.signal import convolve2d
+    from oracle import texdep as otd
+    rng = np.random.default_rng(4)
+    tex = (rng.random((20, 26)) * 256).astype(np.uint8)
+    z, px, py, lam = 1.2e-3, 8e-6, 6e-6, 532e-9
+    w = otd.half_width(z, lam, px)
+    k = 2 * np.pi / float(np.float32(lam))
+    off = np.arange(-w, w)
+    kern = np.exp(1j * k * (z + ((off[None, :] * float(np.float32(px))) ** 2 +
+                                 (off[:, None] * float(np.float32(py))) ** 2) / (2 * z)))
+    full = convolve2d(tex.astype(np.complex128), kern)     # output index = texel + (off + w)
+    conv = full[w:w + 20, w:w + 26]
+    ref = otd.wrp_single(tex, px, py, lam, z)
+    assert np.abs(conv - ref).max() < 1e-9 * np.abs(ref).max()
