@@ -307,6 +307,28 @@ oh_status oh_wrp_accumulate(oh_ctx* ctx, oh_precision prec,
 oh_status oh_wrp_matlab(oh_ctx* ctx, oh_precision prec, int res, double pitch, double lambda,
                         double z_wrp, const double* xyz, const double* phase, int n_points,
                         void* holo, void* stream);
+/* Texture/depth WRP, cwoTexDep::WRP (cwoTexDep.cpp:29-136).  tex, dep:
+ * uint8 [ny][nx] on the device (dep nullable); field [ny][nx] accumulated
+ * (oh_c64 for OH_FP32, oh_c128 for OH_FP64).
+ *   OH_TEXDEP_SINGLE: WRP(z), full zone plates of half-width
+ *     int(|z| tan(asin(lambda/(2 px))) / px); r = z + rho^2 / (2 z).
+ *   OH_TEXDEP_RANGE: WRP(z, dz_step, {range_lo, range_hi}), texels with dep in
+ *     [lo, hi), dz = z + (hi - dep) dz_step, half zone plates (wy < 0) of
+ *     half-width int(int(...) / 1.4), r = rho^2 / (2 dz).  dep_from_texture = 1
+ *     reproduces the reference, which takes dep from the texture value when
+ *     a depth image is given (0 without one); 0 reads dep from the depth image. */
+#define OH_TEXDEP_SINGLE 0
+#define OH_TEXDEP_RANGE 1
+typedef struct oh_texdep_params {
+  int    nx, ny;
+  double px, py, lambda;
+  double z, dz_step;
+  int    range_lo, range_hi;
+  int    dep_from_texture;
+} oh_texdep_params;
+oh_status oh_texdep_wrp(oh_ctx* ctx, oh_precision prec, int mode, const oh_texdep_params* p,
+                        const uint8_t* tex, const uint8_t* dep, void* field, void* stream);
+
 /* CWO::Diffract(z, CWO_FRESNEL_CONV) with the default zero-pad expansion
  * (cwo.cpp:2198-2279, 2872-2898), in place on field [ny][nx]. */
 oh_status oh_fresnel_propagate(oh_ctx* ctx, oh_precision prec, int nx, int ny,

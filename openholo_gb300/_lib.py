@@ -83,6 +83,16 @@ PLS_HUYGENS, PLS_FRESNEL, PLS_CGH_FRESNEL = 0, 1, 2
 PLS_ENGINE_AUTO, PLS_ENGINE_DIRECT, PLS_ENGINE_GEMM, PLS_ENGINE_TENSOR = 0, 1, 2, 3
 
 
+class TexdepParams(C.Structure):
+    """oh_texdep_params (include/oh.h)."""
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("px", C.c_double), ("py", C.c_double), ("lambda_", C.c_double),
+                ("z", C.c_double), ("dz_step", C.c_double), ("range_lo", C.c_int), ("range_hi", C.c_int),
+                ("dep_from_texture", C.c_int)]
+
+
+TEXDEP_SINGLE, TEXDEP_RANGE = 0, 1
+
+
 SIGNATURES = {
     "oh_ctx_create": (_i, [C.POINTER(_vp), _i]),
     "oh_ctx_destroy": (_i, [_vp]),
@@ -111,6 +121,7 @@ SIGNATURES = {
     "oh_pls": (_i, [_vp, _i, C.POINTER(PlsParams), _vp, _i, _vp, _vp]),
     "oh_propagate": (_i, [_vp, _i, _i, _i, _i, _d, _d, _d, _d, _vp, _vp]),
     "oh_wrp_matlab": (_i, [_vp, _i, _i, _d, _d, _d, _vp, _vp, _i, _vp, _vp]),
+    "oh_texdep_wrp": (_i, [_vp, _i, _i, C.POINTER(TexdepParams), _vp, _vp, _vp, _vp]),
     "oh_depthmap_generate_batch": (_i, [_vp, _i, C.POINTER(DepthmapFrame), _i, C.c_uint, _vp]),
     "oh_encode": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp]),
     "oh_normalize_u8": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _vp]),
