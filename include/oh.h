@@ -182,6 +182,27 @@ oh_status oh_depthmap_generate_batch(oh_ctx* ctx, oh_precision prec,
 oh_status oh_depthmap_levels(const oh_depthmap_params* p, int16_t lut_out[256],
                              double* z_out);
 
+/* Eye-model reconstruction of a fringe (HologramGenerator::ReconstructImage,
+ * HologramGenerator_CPU.cpp:414-614), one frame: propagation to the eye pupil
+ * through the field lens, eye position shift, eye lens focused at
+ * focus_distance with its anti-aliasing and pupil masks, propagation to the
+ * retina; out = magnitude [pny/s][pnx/s] (s = pixel_scale, the reference's
+ * test_pixel_number_scale).  fringe: real [pny][pnx] (float / double), read as
+ * the first (pnx/s)(pny/s) values in row-major order as the reference does.
+ * A focus or eye-position sweep is one call per value. */
+typedef struct oh_eye_params {
+  int    pnx, pny;             /* SLM pixels (before scaling) */
+  double ppx, ppy;             /* SLM pitch */
+  double lambda;
+  double field_lens;           /* FIELD_LENS */
+  int    pixel_scale;          /* test_pixel_number_scale (>= 1) */
+  double eye_length, eye_pupil_diameter;
+  double eye_center_x, eye_center_y;
+  double focus_distance;
+} oh_eye_params;
+oh_status oh_reconstruct_eye(oh_ctx* ctx, oh_precision prec, const oh_eye_params* p,
+                             const void* fringe, void* out, void* stream);
+
 /* ---- point cloud -----------------------------------------------------------
  * Field order mirrors OphSpec (ophgen_pointcloud.h:45-70). */
 typedef struct oh_pc_params {

@@ -93,6 +93,14 @@ class TexdepParams(C.Structure):
 TEXDEP_SINGLE, TEXDEP_RANGE = 0, 1
 
 
+class EyeParams(C.Structure):
+    """oh_eye_params (include/oh.h)."""
+    _fields_ = [("pnx", C.c_int), ("pny", C.c_int), ("ppx", C.c_double), ("ppy", C.c_double),
+                ("lambda_", C.c_double), ("field_lens", C.c_double), ("pixel_scale", C.c_int),
+                ("eye_length", C.c_double), ("eye_pupil_diameter", C.c_double), ("eye_center_x", C.c_double),
+                ("eye_center_y", C.c_double), ("focus_distance", C.c_double)]
+
+
 SIGNATURES = {
     "oh_ctx_create": (_i, [C.POINTER(_vp), _i]),
     "oh_ctx_destroy": (_i, [_vp]),
@@ -122,6 +130,7 @@ SIGNATURES = {
     "oh_propagate": (_i, [_vp, _i, _i, _i, _i, _d, _d, _d, _d, _vp, _vp]),
     "oh_wrp_matlab": (_i, [_vp, _i, _i, _d, _d, _d, _vp, _vp, _i, _vp, _vp]),
     "oh_texdep_wrp": (_i, [_vp, _i, _i, C.POINTER(TexdepParams), _vp, _vp, _vp, _vp]),
+    "oh_reconstruct_eye": (_i, [_vp, _i, C.POINTER(EyeParams), _vp, _vp, _vp]),
     "oh_depthmap_generate_batch": (_i, [_vp, _i, C.POINTER(DepthmapFrame), _i, C.c_uint, _vp]),
     "oh_encode": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp]),
     "oh_normalize_u8": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _vp]),

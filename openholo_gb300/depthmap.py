@@ -158,3 +158,22 @@ class HologramGenerator:
         returns u255_fringe_ (real fringe before uint8 normalisation)."""
         self.u255_fringe_ = generate_host(self.ctx, self.params_, img, depth, precision=self.precision)
         return self.u255_fringe_
+
+
+def reconstruct_eye(ctx: _lib.Context, fringe, pnx: int, pny: int, ppx: float, ppy: float, lam: float,
+                    field_lens: float, eye_length: float, pupil_diameter: float, eye_center=(0.0, 0.0),
+                    focus_distance: float = 0.5, pixel_scale: int = 1, precision="fp64", stream=None):
+    """Eye-model reconstruction of a fringe (HologramGenerator::ReconstructImage,
+    one frame; oh_reconstruct_eye).  fringe: device tensor [pny][pnx] (real).
+    Returns the retina-plane magnitude [pny/s][pnx/s].  A focus sweep is one
+    call per focus distance."""
+    import torch
+    prec = OH_FP64 if precision == "fp64" else OH_FP32
+    dt = torch.float64 if prec == OH_FP64 else torch.float32
+    f = fringe.to(dt).contiguous()
+    out = torch.empty((pny // pixel_scale, pnx // pixel_scale), dtype=dt, device=f.device)
+    p = _lib.EyeParams(pnx, pny, ppx, ppy, lam, field_lens, pixel_scale, eye_length, pupil_diameter,
+                       eye_center[0], eye_center[1], focus_distance)
+    _lib.call("oh_reconstruct_eye", ctx.handle, prec, C.byref(p), C.c_void_p(f.data_ptr()),
+              C.c_void_p(out.data_ptr()), _stream_ptr(stream))
+    return out
