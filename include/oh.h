@@ -182,6 +182,18 @@ oh_status oh_depthmap_generate_batch(oh_ctx* ctx, oh_precision prec,
 oh_status oh_depthmap_levels(const oh_depthmap_params* p, int16_t lut_out[256],
                              double* z_out);
 
+/* Light field to complex field (fn_convertLightField2ComplexField.m:1-11,
+ * LF-CGH): view (s, t) of the light field, times exp(i phase), becomes the
+ * centred 2-D FFT (fftshift(fft2(ifftshift(.))), fn_myfft2.m) in block rows
+ * t nv.., columns s nu.. of field [nt*nv][ns*nu] (oh_c64 for OH_FP32, oh_c128
+ * for OH_FP64).  lf and phase: float [nt][ns][nv][nu] on the device; phase in
+ * radians replaces MATLAB's 2*pi*rand, or is NULL for the seeded generator
+ * 2 pi u24(seed, index) (SplitMix64, the same generator as the depth map's
+ * seeded phase). */
+oh_status oh_lightfield_to_field(oh_ctx* ctx, oh_precision prec, int nu, int nv, int ns, int nt,
+                                 const float* lf, const float* phase, uint64_t seed,
+                                 void* field, void* stream);
+
 /* Eye-model reconstruction of a fringe (HologramGenerator::ReconstructImage,
  * HologramGenerator_CPU.cpp:414-614), one frame: propagation to the eye pupil
  * through the field lens, eye position shift, eye lens focused at

@@ -131,6 +131,7 @@ SIGNATURES = {
     "oh_wrp_matlab": (_i, [_vp, _i, _i, _d, _d, _d, _vp, _vp, _i, _vp, _vp]),
     "oh_texdep_wrp": (_i, [_vp, _i, _i, C.POINTER(TexdepParams), _vp, _vp, _vp, _vp]),
     "oh_reconstruct_eye": (_i, [_vp, _i, C.POINTER(EyeParams), _vp, _vp, _vp]),
+    "oh_lightfield_to_field": (_i, [_vp, _i, _i, _i, _i, _i, _vp, _vp, C.c_uint64, _vp, _vp]),
     "oh_depthmap_generate_batch": (_i, [_vp, _i, C.POINTER(DepthmapFrame), _i, C.c_uint, _vp]),
     "oh_encode": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp]),
     "oh_normalize_u8": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _vp]),

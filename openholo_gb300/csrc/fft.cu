@@ -150,6 +150,34 @@ oh_status fft2d_enqueue(oh_ctx* ctx, int prec, int nx, int ny, const void* in, v
   return launch_fft2d<float>(ctx, nx, ny, in, out, aux, direction, shift, normalize, st);
 }
 
+template <typename R>
+static oh_status launch_fft_cols(oh_ctx* ctx, int nx, int ny, void* data, int direction, int normalize,
+                                 cudaStream_t st) {
+  typedef typename cplx_of<R>::type C;
+  const int prec = sizeof(R) == 8 ? 1 : 0;
+  FFTPlan py;
+  OH_TRY(get_plan(ctx, ny, prec, &py));
+  const int W = pick_strip_width(nx, ny, sizeof(C), max_smem_per_block());
+  if (W == 0) return fail(OH_ERR_UNSUPPORTED_SIZE, "column length " + std::to_string(ny) + " exceeds shared memory");
+  const size_t scol = (size_t)W * ny * sizeof(C);
+  const R scale = normalize ? (R)(1.0 / (double)ny) : (R)1;
+  if (direction < 0) {
+    OH_CUDA_TRY(cudaFuncSetAttribute(fft_cols_kernel<R, -1, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scol));
+    fft_cols_kernel<R, -1, 0><<<nx / W, 512, scol, st>>>(static_cast<C*>(data), nullptr, nx, ny, W, 0, scale, py);
+  } else {
+    OH_CUDA_TRY(cudaFuncSetAttribute(fft_cols_kernel<R, 1, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scol));
+    fft_cols_kernel<R, 1, 0><<<nx / W, 512, scol, st>>>(static_cast<C*>(data), nullptr, nx, ny, W, 0, scale, py);
+  }
+  OH_LAUNCH_CHECK();
+  return OH_OK;
+}
+
+oh_status fft_cols_enqueue(oh_ctx* ctx, int prec, int nx, int ny, void* data, int direction, int normalize,
+                           cudaStream_t st) {
+  if (prec) return launch_fft_cols<double>(ctx, nx, ny, data, direction, normalize, st);
+  return launch_fft_cols<float>(ctx, nx, ny, data, direction, normalize, st);
+}
+
 oh_status fft_rows_enqueue(oh_ctx* ctx, int prec, int nx, int ny, const void* in, void* out, int direction,
                            int normalize, cudaStream_t st) {
   if (prec) return launch_fft_rows<double>(ctx, nx, ny, in, out, direction, normalize, st);

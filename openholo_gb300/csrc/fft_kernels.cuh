@@ -14,6 +14,11 @@ oh_status fft2d_enqueue(oh_ctx* ctx, int prec, int nx, int ny, const void* in, v
 oh_status fft_rows_enqueue(oh_ctx* ctx, int prec, int nx, int ny, const void* in, void* out, int direction,
                            int normalize, cudaStream_t st);
 
+// Enqueue in-place transforms of the nx columns (length ny) of a [ny][nx]
+// array (no shift).
+oh_status fft_cols_enqueue(oh_ctx* ctx, int prec, int nx, int ny, void* data, int direction, int normalize,
+                           cudaStream_t st);
+
 // Widest column strip (8, 4, 2 or 1 columns) dividing nx whose ny-long
 // complex lines fit in smax bytes of shared memory; 0 if none fits.
 int pick_strip_width(int nx, int ny, size_t esz, size_t smax);
