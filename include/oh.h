@@ -182,6 +182,22 @@ oh_status oh_depthmap_generate_batch(oh_ctx* ctx, oh_precision prec,
 oh_status oh_depthmap_levels(const oh_depthmap_params* p, int16_t lut_out[256],
                              double* z_out);
 
+/* Triangle-mesh hologram by analytic angular spectra (OpenHolo_MeshCGH,
+ * fn_genH.m:1-53 with fn_AS_shading.m or, continuous != 0, fn_AS_continuous.m
+ * and fn_FindVertexNormalVector.m).  tris: host array [n][9] of vertex
+ * coordinates (x1 y1 z1 x2 y2 z2 x3 y3 z3, metres); back-facing triangles
+ * (normal z <= 0) contribute nothing.  field: device oh_c128 [ny][nx], the
+ * hologram fftshift(fft2(fftshift(G))); spectrum (nullable): the summed
+ * angular spectrum G.  FP64 only; pitches must exceed the wavelength. */
+typedef struct oh_mesh_params {
+  int    nx, ny;
+  double dx, dy, lambda;
+  double illu[3];           /* shadingParam.illu */
+  int    continuous;        /* shadingParam.con */
+} oh_mesh_params;
+oh_status oh_mesh_hologram(oh_ctx* ctx, const oh_mesh_params* p, const double* tris, int n_tris,
+                           void* field, void* spectrum, void* stream);
+
 /* Light field to complex field (fn_convertLightField2ComplexField.m:1-11,
  * LF-CGH): view (s, t) of the light field, times exp(i phase), becomes the
  * centred 2-D FFT (fftshift(fft2(ifftshift(.))), fn_myfft2.m) in block rows

@@ -101,6 +101,12 @@ class EyeParams(C.Structure):
                 ("eye_center_y", C.c_double), ("focus_distance", C.c_double)]
 
 
+class MeshParams(C.Structure):
+    """oh_mesh_params (include/oh.h)."""
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("dx", C.c_double), ("dy", C.c_double), ("lambda_", C.c_double),
+                ("illu", C.c_double * 3), ("continuous", C.c_int)]
+
+
 SIGNATURES = {
     "oh_ctx_create": (_i, [C.POINTER(_vp), _i]),
     "oh_ctx_destroy": (_i, [_vp]),
@@ -132,6 +138,7 @@ SIGNATURES = {
     "oh_texdep_wrp": (_i, [_vp, _i, _i, C.POINTER(TexdepParams), _vp, _vp, _vp, _vp]),
     "oh_reconstruct_eye": (_i, [_vp, _i, C.POINTER(EyeParams), _vp, _vp, _vp]),
     "oh_lightfield_to_field": (_i, [_vp, _i, _i, _i, _i, _i, _vp, _vp, C.c_uint64, _vp, _vp]),
+    "oh_mesh_hologram": (_i, [_vp, C.POINTER(MeshParams), _vp, _i, _vp, _vp, _vp]),
     "oh_depthmap_generate_batch": (_i, [_vp, _i, C.POINTER(DepthmapFrame), _i, C.c_uint, _vp]),
     "oh_encode": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp]),
     "oh_normalize_u8": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _vp]),

@@ -113,3 +113,37 @@ def pls_scene(seed: int, n: int = 5000, xy_half=2e-3, z_range=(0.10, 0.12), ampl
     pts[:, 3] = (u[:, 3] * 2 - 1) * xy_half
     pts[:, 4] = z_range[0] + u[:, 4] * (z_range[1] - z_range[0])
     return pts
+
+
+def mesh_scene(seed: int, cells: int = 5, size: float = 170e-6, z0: float = 0.1, relief: float = 20e-6,
+               back_facing: int = 2):
+    """(n, 9) triangles of a seeded height field z = z0 + relief * h(x, y) over
+    a cells x cells grid of the given size, two triangles per cell ordered so
+    that their normals face +z (shared vertices are bit-identical), followed
+    by `back_facing` flipped copies of the first triangles (shifted by `size`
+    in x) and one triangle lying in a plane parallel to the hologram."""
+    u = uniform(seed, 6, (cells + 1) ** 2).reshape(cells + 1, cells + 1)
+    xs = (np.arange(cells + 1) / cells - 0.5) * size
+    Z = z0 + relief * (u - 0.5)
+    tris = []
+    for j in range(cells):
+        for i in range(cells):
+            a = (xs[i], xs[j], Z[j, i])
+            b = (xs[i + 1], xs[j], Z[j, i + 1])
+            c = (xs[i], xs[j + 1], Z[j + 1, i])
+            d = (xs[i + 1], xs[j + 1], Z[j + 1, i + 1])
+            for tri in ((a, c, b), (b, c, d)):
+                v1, v2, v3 = (np.array(t) for t in tri)
+                if np.cross(v2 - v3, v1 - v3)[2] <= 0:
+                    v2, v3 = v3, v2
+                tris.append(np.concatenate([v1, v2, v3]))
+    for k in range(back_facing):
+        # moved off the mesh: a back-facing copy sharing vertices with its
+        # original would cancel their averaged normals (0/0 in continuous shading)
+        t = tris[k].reshape(3, 3) + np.array([size, 0.0, 0.0])
+        tris.append(t[[0, 2, 1]].reshape(-1))
+    flat = np.array([[0.0, 0.0, z0], [0.0, 0.3 * size, z0], [0.3 * size, 0.0, z0]])
+    if np.cross(flat[1] - flat[2], flat[0] - flat[2])[2] <= 0:
+        flat = flat[[0, 2, 1]]
+    tris.append(flat.reshape(-1))
+    return np.array(tris, dtype=np.float64)
