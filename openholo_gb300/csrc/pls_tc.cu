@@ -12,8 +12,8 @@
 // FP32 (relative error ~1e-5).
 //
 // Kernel: one CTA per 128 x 256 tile of C (and per K split), 4 warps.
-// Thread 0 loads K-slices of 64 (Ahi, Alo, Bhi, Blo: 96 KB, two stages) with
-// TMA (128-byte swizzle); thread 32 issues tcgen05.mma (M=128, N=256, K=16,
+// Thread 0 loads K-slices of 32 (Ahi, Alo, Bhi, Blo: 48 KB, four stages) with
+// TMA (64-byte swizzle); thread 32 issues tcgen05.mma (M=128, N=256, K=16,
 // BF16 -> FP32 in 256 TMEM columns) and releases each stage with
 // tcgen05.commit; all four warps then read the accumulator with tcgen05.ld
 // (warp w owns TMEM lanes 32w..32w+31) and store (or, with K splits, add)
@@ -29,10 +29,10 @@ namespace oh {
 
 namespace {
 
-constexpr int kBM = 128, kBN = 256, kBK = 64, kStages = 2;
-constexpr int kTileA = kBM * kBK * 2;                 // 16 KB
-constexpr int kTileB = kBN * kBK * 2;                 // 32 KB
-constexpr int kStageBytes = 2 * kTileA + 2 * kTileB;  // 96 KB
+constexpr int kBM = 128, kBN = 256, kBK = 32, kStages = 4;
+constexpr int kTileA = kBM * kBK * 2;                 // 8 KB
+constexpr int kTileB = kBN * kBK * 2;                 // 16 KB
+constexpr int kStageBytes = 2 * kTileA + 2 * kTileB;  // 48 KB
 constexpr int kTmemCols = 256;
 constexpr int kSmemBytes = kStages * kStageBytes + 1024 /*alignment*/ + 256 /*barriers*/;
 constexpr long long kWaitCycles = 2000000000LL;       // ~1 s at 2 GHz
@@ -70,15 +70,15 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
-// Shared-memory matrix descriptor: K-major tile with 128-byte swizzle,
-// 8-row atoms 1024 bytes apart (SBO), version 1, layout SWIZZLE_128B.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+// Shared-memory matrix descriptor: K-major tile with 64-byte swizzle (rows of
+// kBK = 32 BF16), 8-row atoms 512 bytes apart (SBO), version 1, layout SWIZZLE_64B.
+__device__ __forceinline__ uint64_t sw_desc(uint32_t saddr) {
   uint64_t d = 0;
   d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
   d |= (uint64_t)1 << 16;                 // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;       // stride byte offset
+  d |= (uint64_t)((8 * kBK * 2) >> 4) << 32;   // stride byte offset: 8 rows
   d |= (uint64_t)1 << 46;                 // descriptor version
-  d |= (uint64_t)2 << 61;                 // SWIZZLE_128B
+  d |= (uint64_t)4 << 61;                 // SWIZZLE_64B
   return d;
 }
 
@@ -116,6 +116,7 @@ struct TcArgs {
   int mode;         // OH_PLS_FRESNEL (complex out) or OH_PLS_CGH_FRESNEL (real out)
   int rows, cols;   // C extent: Ny x 2 Nx
   int atomic;       // add into out (K splits or point chunks)
+  int vec4;         // out rows start on 16-byte boundaries (base aligned, cols % 4 == 0)
   float* out;
   int* err;
 };
@@ -193,8 +194,8 @@ __global__ void __launch_bounds__(128, 1) pls_tc_gemm(const __grid_constant__ CU
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint64_t ah = sw128_desc(su32(sA(s, 0))), al = sw128_desc(su32(sA(s, 1)));
-      const uint64_t bh = sw128_desc(su32(sB(s, 0))), bl = sw128_desc(su32(sB(s, 1)));
+      const uint64_t ah = sw_desc(su32(sA(s, 0))), al = sw_desc(su32(sA(s, 1)));
+      const uint64_t bh = sw_desc(su32(sB(s, 0))), bl = sw_desc(su32(sB(s, 1)));
 #pragma unroll
       for (int kk = 0; kk < kBK / 16; ++kk) {
         const uint64_t adv = (uint64_t)((kk * 32) >> 4);     // 16 BF16 = 32 bytes along K
@@ -232,12 +233,21 @@ __global__ void __launch_bounds__(128, 1) pls_tc_gemm(const __grid_constant__ CU
           }
         } else {
           float* dst = a.out + (size_t)row * a.cols + col0;
+          if (a.atomic && a.vec4 && col0 + 32 <= a.cols) {
+            // 16-byte aligned rows: vector reductions
 #pragma unroll
-          for (int q = 0; q < 32; ++q) {
-            if (col0 + q < a.cols) {
-              const float v = __uint_as_float(r[q]);
-              if (a.atomic) atomicAdd(dst + q, v);
-              else dst[q] = v;
+            for (int q = 0; q < 32; q += 4)
+              asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst + q), "f"(__uint_as_float(r[q])),
+                           "f"(__uint_as_float(r[q + 1])), "f"(__uint_as_float(r[q + 2])), "f"(__uint_as_float(r[q + 3]))
+                           : "memory");
+          } else {
+#pragma unroll
+            for (int q = 0; q < 32; ++q) {
+              if (col0 + q < a.cols) {
+                const float v = __uint_as_float(r[q]);
+                if (a.atomic) atomicAdd(dst + q, v);
+                else dst[q] = v;
+              }
             }
           }
         }
@@ -350,7 +360,7 @@ oh_status make_map(CUtensorMap* m, void* ptr, int kpad, int rows, int box_rows) 
   const cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
   const cuuint32_t estr[2] = {1, 1};
   const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ptr, dims, strides, box, estr,
-                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(OH_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
   return OH_OK;
@@ -389,8 +399,22 @@ oh_status pls_tensor_enqueue(oh_ctx* ctx, const PlsGeom& g, const PlsPt* pts, in
     const int cnt = std::min(chunk_pts, n - c0);
     const int kpad = (cnt * 2 + kBK - 1) / kBK * kBK;
     const int kb_total = kpad / kBK;
-    // K splits to fill the SMs (each split keeps at least 8 K blocks)
-    const int splits = std::max(1, std::min(152 / std::max(1, tiles), kb_total / 8));
+    // K splits: the fewest that fill the SMs' waves to 95 % (each split keeps
+    // at least 8 K blocks), else the best filling
+    int splits = 1;
+    {
+      int sms = 152;
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      const int smax = std::max(1, kb_total / 8);
+      double best = -1.0;
+      for (int sp = 1; sp <= std::min(smax, 32); ++sp) {
+        const long long ctas = (long long)tiles * sp;
+        const long long waves = (ctas + sms - 1) / sms;
+        const double eff = (double)ctas / (double)(waves * sms);
+        if (eff > best + 1e-9) { best = eff; splits = sp; }
+        if (eff >= 0.95) break;
+      }
+    }
     if (splits > 1) atomic = true;
     if (atomic && c0 == 0)
       OH_CUDA_TRY(cudaMemsetAsync(out, 0, (size_t)g.ny * g.nx * (g.mode == OH_PLS_CGH_FRESNEL ? 4 : 8), st));
@@ -405,7 +429,8 @@ oh_status pls_tensor_enqueue(oh_ctx* ctx, const PlsGeom& g, const PlsPt* pts, in
     OH_TRY(make_map(&mAlo, alo, kpad, mpad, kBM));
     OH_TRY(make_map(&mBhi, bhi, kpad, npad, kBN));
     OH_TRY(make_map(&mBlo, blo, kpad, npad, kBN));
-    TcArgs a{kb_total, splits, g.mode, g.ny, 2 * g.nx, atomic ? 1 : 0, static_cast<float*>(out), err};
+    const int vec4 = ((reinterpret_cast<uintptr_t>(out) & 15) == 0 && ((2 * g.nx) & 3) == 0) ? 1 : 0;
+    TcArgs a{kb_total, splits, g.mode, g.ny, 2 * g.nx, atomic ? 1 : 0, vec4, static_cast<float*>(out), err};
     KernelTimer kt(ctx, "pls_tc_gemm", st);
     pls_tc_gemm<<<dim3(npad / kBN, mpad / kBM, splits), 128, kSmemBytes, st>>>(mAhi, mAlo, mBhi, mBlo, a);
     OH_LAUNCH_CHECK();
