@@ -84,6 +84,13 @@ struct DMArgs {
   int xs;                // 1: R and V columns are in the row FFT's storage order (fast passes), 0: kx order
   int hzx, hzy;          // 1: 2x padding with a radix-16 first stage (stage-0 inputs 4..11 are zero)
   int* err;              // device error word (bounded waits that ran out)
+  // evenly spaced layers (fast column pass): step dz = z'_e - z'_(e-1) of the
+  // render entries; D = Dx(fx) Dy(fy) exp(-i k dz g) per spectrum element
+  int horner;
+  float kdz_pi;          // k dz / pi
+  double dz;
+  C* dxh;                // [Px] exp(-i pi lambda dz fx^2)
+  C* dyh;                // [Py] exp(-i pi lambda dz fy^2), y storage order
   FFTPlan plx, ply;
 };
 
@@ -138,6 +145,20 @@ __global__ void dm_setup(DMArgs<R> a, DMSetup s) {
       double2 v = cexp_reduced(pi * a.lambda * s.zp[e] * fx * fx);
       double2 c = make_double2(s.cre[e], s.cim[e]);
       a.exc[idx] = mk((R)(c.x * v.x - c.y * v.y), (R)(c.x * v.y + c.y * v.x));
+    }
+    if (a.horner) {
+      for (int x = tid; x < a.Px; x += nthr) {
+        double fx = (-1.0 / (2.0 * a.ppx)) + (1.0 / a.ssx) * (double)x;
+        double2 v = cexp_reduced(-pi * a.lambda * a.dz * fx * fx);
+        a.dxh[x] = mk((R)v.x, (R)v.y);
+      }
+      for (int p = tid; p < a.Py; p += nthr) {
+        int y = a.ply.iperm[p] + a.hy;
+        if (y >= a.Py) y -= a.Py;
+        double fy = (1.0 / (2.0 * a.ppy)) - (1.0 / a.ssy) - (1.0 / a.ssy) * (double)y;
+        double2 v = cexp_reduced(-pi * a.lambda * a.dz * fy * fy);
+        a.dyh[p] = mk((R)v.x, (R)v.y);
+      }
     }
     if (a.ey_perm) {
       const double two_pi = 6.283185307179586476925286766559;
@@ -629,15 +650,8 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   bool fastlen = false;
   with_fast_n(a.Py, [&](auto nc) { fastlen = decltype(nc)::value > 0; });
   if (prec == 0 && fastlen) {
-    // strip width: 2 (two blocks per SM) when it fits, else 4; OH_DM_COL_W
-    // forces one of them
-    int want = 0;
-    if (const char* ev = std::getenv("OH_DM_COL_W")) want = std::atoi(ev);
-    for (int cand : {2, 4}) {
-      if (want && cand != want) continue;
-      if (a.Px % cand) continue;
-      if ((size_t)col_layout(a.Py, a.pny, cand, occ_stride, su.n_entries).total <= smax) { Wfast = cand; break; }
-    }
+    // strips of two spectrum columns (two blocks per SM)
+    if (a.Px % 2 == 0 && (size_t)col_layout(a.Py, a.pny, 2, occ_stride, su.n_entries).total <= smax) Wfast = 2;
   }
   int W = Wfast;
   if (W == 0) {
@@ -651,6 +665,24 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   a.W = W; a.nstrips = a.Px / W;
   a.lw = W == 8 ? 3 : W == 4 ? 2 : W == 2 ? 1 : 0;
   a.ey_perm = Wfast ? 1 : 0;
+  // Render entries evenly spaced in z' with one entry constant: the fast
+  // column pass accumulates with the layer-step recurrence (the transfer
+  // function is exp(i z' Phi(fx, fy)) times that constant, so consecutive
+  // entries differ by the factor exp(-i dz Phi)).  OH_DM_LAYER_STEP=0 keeps
+  // the per-layer evaluation.
+  a.horner = 0;
+  if (Wfast && su.n_entries >= 2) {
+    const char* ev = std::getenv("OH_DM_LAYER_STEP");
+    const int n = su.n_entries;
+    const double dz = (su.zp[n - 1] - su.zp[0]) / (n - 1);
+    const double k = 2.0 * M_PI / p->lambda;
+    bool even = dz != 0.0 && !(ev && std::atoi(ev) == 0);
+    for (int e = 0; e < n && even; ++e) {
+      if (std::fabs(su.zp[e] - (su.zp[0] + e * dz)) * k > 1e-7) even = false;
+      if (std::fabs(su.cre[e] - su.cre[0]) > 1e-12 || std::fabs(su.cim[e] - su.cim[0]) > 1e-12) even = false;
+    }
+    if (even) { a.horner = 1; a.dz = dz; a.kdz_pi = (float)(k * dz / M_PI); }
+  }
   bool fastx = false;
   with_fast_n(a.Px, [&](auto nc) { fastx = decltype(nc)::value > 0; });
   a.xs = (prec == 0 && fastx && Wfast) ? 1 : 0;
@@ -679,7 +711,8 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
          o_cst = carve(nE * sizeof(C)), o_exc = carve(prec ? 0 : nE * a.Px * sizeof(C)),
          o_ey = carve(prec ? 0 : nE * a.Py * sizeof(C)),
          o_eth = carve(a.ey_perm ? nE * a.Py * sizeof(R) : 0), o_lfx = carve(a.Px * sizeof(R)), o_lfy = carve(a.Py * sizeof(R)), o_lfyp = carve(a.Py * sizeof(R)),
-         o_shy = carve(a.pny * sizeof(C)), o_shx = carve(a.pnx * sizeof(C)), o_any = carve(nU * sizeof(int));
+         o_shy = carve(a.pny * sizeof(C)), o_shx = carve(a.pnx * sizeof(C)), o_any = carve(nU * sizeof(int)),
+         o_dxh = carve(a.horner ? a.Px * sizeof(C) : 0), o_dyh = carve(a.horner ? a.Py * sizeof(C) : 0);
   if (sizes_only) {
     *sizes_only = DMScratch{bytes_R, bytes_V, bytes_occ, off};
     return OH_OK;
@@ -694,6 +727,8 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   a.eth = (R*)(base + o_eth);
   a.lfx = (R*)(base + o_lfx); a.lfy = (R*)(base + o_lfy); a.lfyp = (R*)(base + o_lfyp); a.shy = (C*)(base + o_shy); a.shx = (C*)(base + o_shx);
   a.slot_any = (int*)(base + o_any);
+  a.dxh = a.horner ? (C*)(base + o_dxh) : nullptr;
+  a.dyh = a.horner ? (C*)(base + o_dyh) : nullptr;
   a.fringe = (R*)fringe; a.field = (C*)field; a.spectrum = (C*)spectrum;
 
   {
@@ -702,7 +737,7 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
     // layer flags
     struct Key {
       DMSetup su;
-      int prec, pnx, pny, Px, Py, sig_x, sig_y, ey_perm;
+      int prec, pnx, pny, Px, Py, sig_x, sig_y, ey_perm, horner;
       double ppx, ppy, lambda;
       const void* tables;
       const void* iperm;
@@ -710,7 +745,7 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
     std::memset(&key, 0, sizeof(key));
     key.su = su;
     key.prec = prec; key.pnx = a.pnx; key.pny = a.pny; key.Px = a.Px; key.Py = a.Py;
-    key.sig_x = a.sig_x; key.sig_y = a.sig_y; key.ey_perm = a.ey_perm;
+    key.sig_x = a.sig_x; key.sig_y = a.sig_y; key.ey_perm = a.ey_perm; key.horner = a.horner;
     key.ppx = a.ppx; key.ppy = a.ppy; key.lambda = a.lambda;
     key.tables = base; key.iperm = a.ply.iperm;
     std::string ks(reinterpret_cast<const char*>(&key), sizeof(key));
@@ -741,19 +776,17 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
       with_fast_n(a.Py, [&](auto nc) {
         constexpr int NY = decltype(nc)::value;
         if constexpr (NY > 0) {
-          auto launch = [&](auto wc) {
-            constexpr int WW = decltype(wc)::value;
-            cudaError_t e = cudaFuncSetAttribute(dm_col_fast<NY, WW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col);
-            if (e == cudaSuccess)
-              e = cudaFuncSetAttribute(dm_col_fast<NY, WW>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+          auto launch = [&](auto kern) {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col);
+            if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
             if (e != cudaSuccess) { rs = cuda_fail(e, "cudaFuncSetAttribute(dm_col_fast)"); return; }
             KernelTimer kt(ctx, "dm_col_pass", st);
-            dm_col_fast<NY, WW><<<a.nstrips, ColCfg<NY, WW>::T, smem_col, st>>>(a);
+            kern<<<a.nstrips, ColCfg<NY, 2>::T, smem_col, st>>>(a);
             note_launch();
             if ((e = cudaGetLastError()) != cudaSuccess) rs = cuda_fail(e, "dm_col_fast launch");
           };
-          if (Wfast == 4) launch(std::integral_constant<int, 4>{});
-          else launch(std::integral_constant<int, 2>{});
+          if (a.horner) launch(dm_col_fast<NY, 2, true>);
+          else launch(dm_col_fast<NY, 2, false>);
         }
       });
       OH_TRY(rs);

@@ -12,7 +12,11 @@
 //      then the remaining stages in place, twiddles from a two-level
 //      shared-memory table;
 //   3. multiplies by the layer's transfer function and accumulates into
-//      registers (fixed element ownership across layers).
+//      registers (fixed element ownership across layers).  When the layers
+//      are evenly spaced in z' (H_l = H_last D^(last - l) with one step factor
+//      D per element), step 3 is the recurrence acc = acc D + x instead, with
+//      no per-layer Ey row and no per-layer sine/cosine, and the last layer's
+//      H is applied once in the epilogue.
 // The epilogue applies the SSB crop, the inverse y-FFT and the y shift phase
 // and writes the pny output rows of the strip.
 //
@@ -39,10 +43,13 @@ __host__ __device__ inline ColLayout col_layout(int Py, int pny, int W, int occ_
   int o = 0;
   L.buf = col_take(&o, Py * W * 8);
   L.stg = col_take(&o, pny * W * 8);
-  L.ey0 = col_take(&o, Py * 4);
-  L.ey1 = col_take(&o, Py * 4);
+  // one region holds either the residual phase g (float per element) and the
+  // two Ey rows, or the layer-step factor D (float2 per element)
+  const int gb = (Py * W * 4 + 127) & ~127, eb = (Py * 4 + 127) & ~127;
+  L.g = col_take(&o, gb + 2 * eb > Py * W * 8 ? gb + 2 * eb : Py * W * 8);
+  L.ey0 = L.g + gb;
+  L.ey1 = L.ey0 + eb;
   L.occ = col_take(&o, occ_stride);
-  L.g = col_take(&o, Py * W * 4);
   L.kyp = col_take(&o, Py * 2);
   L.twlo = col_take(&o, 64 * 8);
   L.twhi = col_take(&o, ((Py + 63) / 64) * 8);
@@ -98,7 +105,8 @@ template <int NY, int W> struct ColCfg {
   static constexpr int MINB = W <= 2 ? 2 : 1;          // narrow strips: two blocks per SM
 };
 
-template <int NY, int W>
+// STEP: evenly spaced layers, accumulated with the layer-step recurrence.
+template <int NY, int W, bool STEP>
 __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_fast(DMArgs<float> a) {
   typedef float2 C;
   typedef ColCfg<NY, W> CF;
@@ -156,12 +164,23 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
   }
   __syncthreads();
   // layer-independent part of the angular-spectrum residual phase:
-  // psi = k z' g,  g = s^2 / (2 (1 + sqrt(1 - s))^2),  s = (lambda fx)^2 + (lambda fy)^2
+  // psi = k z' g,  g = s^2 / (2 (1 + sqrt(1 - s))^2),  s = (lambda fx)^2 + (lambda fy)^2.
+  // With the layer-step recurrence the region holds instead the step factor
+  // D = H(z' - dz) / H(z') = Dx(fx) Dy(fy) exp(-i k dz g).
+  constexpr bool horner = STEP;
+  C* const dsm = reinterpret_cast<C*>(smem + Lo.g);
   for (int idx = tid; idx < NY * W; idx += T) {
     const int p = idx / W, w = idx - p * W;
     const float sv = lfxw[w] + a.lfyp[p];
     const float den = 1.f + sqrtf(1.f - sv);
-    gsm[idx] = sv * sv * __fdividef(0.5f, den * den);
+    const float g = sv * sv * __fdividef(0.5f, den * den);
+    if constexpr (horner) {
+      float sn, cs;
+      sincospif(-a.kdz_pi * g, &sn, &cs);
+      dsm[idx] = cmul(cmul(a.dxh[kxw[w]], a.dyh[p]), make_float2(cs, sn));
+    } else {
+      gsm[idx] = g;
+    }
   }
   const int nact = s_nact;
   const TwSplit<C> tw{twlo, twhi};
@@ -179,7 +198,10 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
     mbar_expect_tx(bar, (uint32_t)(NY * 4));
     bulk_g2s((k & 1) ? ey1 : ey0, a.eth + (size_t)e * NY, (uint32_t)(NY * 4), bar);
   };
-  if (tid == 0 && nact > 0) { issue_strip(0); issue_ey(0); }
+  if (tid == 0 && nact > 0) {
+    issue_strip(0);
+    if (!horner) issue_ey(0);
+  }
 
   // accumulators: last-stage butterfly bb = tid + kb*T of the strip (bb = b*W + w),
   // outputs f at storage position p = b*RL + f of line w
@@ -194,21 +216,36 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
     // layer's last stage no longer reads the work buffer
     uint64_t* const bar_e = (k & 1) ? &mbar[2] : &mbar[1];
     bool ok = mbar_wait_bounded(&mbar[0], (uint32_t)(k & 1));
-    ok = ok && mbar_wait_bounded(bar_e, (uint32_t)((k >> 1) & 1));
+    ok = ok && (horner || mbar_wait_bounded(bar_e, (uint32_t)((k >> 1) & 1)));
     if (__syncthreads_or(!ok)) {
       if (tid == 0) atomicOr(a.err, 1);
       // let this block's copies still in flight land before leaving
       mbar_wait_bounded(&mbar[0], (uint32_t)(k & 1));
-      mbar_wait_bounded(bar_e, (uint32_t)((k >> 1) & 1));
+      if (!horner) mbar_wait_bounded(bar_e, (uint32_t)((k >> 1) & 1));
       return;
     }
-    if (tid == 0 && k + 1 < nact) {
+    if (tid == 0 && k + 1 < nact && !horner) {
       // Ey buffer (k+1)&1 was last read by layer k-1, finished before the barrier
       fence_proxy_async_smem();
       issue_ey(k + 1);
     }
     const int e = list[k];
-    if (tid < W) exw[tid] = a.exc[(size_t)e * a.Px + kxw[tid]];
+    if (tid < W && !horner) exw[tid] = a.exc[(size_t)e * a.Px + kxw[tid]];
+    const int gap = k ? e - list[k - 1] : 1;
+    if constexpr (horner) {
+      // layers without pixels since the previous one: acc D^(gap - 1)
+      for (int r = 1; r < gap; ++r) {
+#pragma unroll
+        for (int kb = 0; kb < KB; ++kb) {
+          const int bb = tid + kb * T;
+          if (bb < CF::NBL) {
+            const int b = bb / W, w = bb - b * W;
+#pragma unroll
+            for (int f = 0; f < RL; ++f) acc[kb][f] = cmul(acc[kb][f], dsm[(b * RL + f) * W + w]);
+          }
+        }
+      }
+    }
     // stage 0 from the staging buffer: inputs j + t*Q0 of the y-shifted line
     for (int idx = tid; idx < Q0 * W; idx += T) {
       const int j = idx / W, w = idx - j * W;
@@ -257,7 +294,9 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
     }
     __syncthreads();
     // last stage (stride 1, no twiddles) fused with the transfer-function
-    // multiply-accumulate
+    // multiply-accumulate: either acc += H x per layer, or the recurrence
+    // acc = acc D^gap + x over the evenly spaced layers (H of the last layer
+    // applied once in the epilogue)
     const float kz = a.kzp[e];
     const float* eth = (k & 1) ? ey1 : ey0;       // storage order
     const float inv2pi = 0.15915494309189533577f, two_pi = 6.28318530717958647692f;
@@ -270,6 +309,15 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
 #pragma unroll
         for (int f = 0; f < RL; ++f) x[f] = buf[(b * RL + f) * W + w];
         DFT<RL, -1, C>::run(x);
+        if constexpr (horner) {
+#pragma unroll
+          for (int f = 0; f < RL; ++f) {
+            const C d = dsm[(b * RL + f) * W + w];
+            const C t = acc[kb][f];
+            acc[kb][f] = make_float2(fmaf(t.x, d.x, fmaf(-t.y, d.y, x[f].x)), fmaf(t.x, d.y, fmaf(t.y, d.x, x[f].y)));
+          }
+          continue;
+        }
         const C ex = exw[w];
 #pragma unroll
         for (int f = 0; f < RL; ++f) {
@@ -286,6 +334,34 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
     }
   }
   __syncthreads();
+
+  // recurrence: apply the last layer's transfer function
+  //   H = C Ex exp(i (pi lambda z' fy^2 + k z' g)), as in the per-layer form
+  if (horner && nact > 0) {
+    const int e = list[nact - 1];
+    const float kz = a.kzp[e];
+    const float inv2pi = 0.15915494309189533577f, two_pi = 6.28318530717958647692f;
+#pragma unroll
+    for (int kb = 0; kb < KB; ++kb) {
+      const int bb = tid + kb * T;
+      if (bb < CF::NBL) {
+        const int b = bb / W, w = bb - b * W;
+        const C ex = a.exc[(size_t)e * a.Px + kxw[w]];
+#pragma unroll
+        for (int f = 0; f < RL; ++f) {
+          const int p = b * RL + f;
+          const float sv = lfxw[w] + a.lfyp[p];
+          const float den = 1.f + sqrtf(1.f - sv);
+          const float g = sv * sv * __fdividef(0.5f, den * den);
+          float ph = fmaf(kz, g, a.eth[(size_t)e * NY + p]);
+          ph = fmaf(-two_pi, rintf(ph * inv2pi), ph);
+          float sn, cs;
+          __sincosf(ph, &sn, &cs);
+          acc[kb][f] = cmul(acc[kb][f], cmul(ex, make_float2(cs, sn)));
+        }
+      }
+    }
+  }
 
   // SSB crop and inverse y-FFT input order: spectrum row ky -> i = (ky + hy) mod NY
 #pragma unroll

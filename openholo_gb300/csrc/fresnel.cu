@@ -132,11 +132,14 @@ static oh_status run_fresnel_grid(oh_ctx* ctx, int nx, int ny, double dp, double
   return OH_OK;
 }
 
-
-
 // ---- separable three-pass path (FP32) -------------------------------------
 
 constexpr int kFrW = 2;      // spectrum columns per strip
+// Rows per block of the two row passes (measured at 3840x2160: the forward
+// pass is faster with two rows per 512-thread block, the inverse with one row
+// per 256-thread block, where its gather latency hides across more blocks).
+constexpr int kFrFwdRows = 2;
+constexpr int kFrInvRows = 1;
 
 struct FrArgs {
   int nx, ny;                // field size; the padded grid is 2nx x 2ny
@@ -154,19 +157,19 @@ struct FrArgs {
 
 __host__ __device__ constexpr int fr_tw_entries(int n) { return 64 + (n + 63) / 64; }
 
-// Two rows per block: x-FFT of the padded row, stored as column strips.
-template <int NX>
-__global__ void __launch_bounds__(512) fr_row_fwd(FrArgs a) {
+// ROWS rows per block: x-FFT of the padded row, stored as column strips.
+template <int NX, int ROWS>
+__global__ void __launch_bounds__(256 * ROWS) fr_row_fwd(FrArgs a) {
   typedef float2 C;
   extern __shared__ __align__(16) unsigned char smem[];
   C* buf = reinterpret_cast<C*>(smem);
-  C* twlo = buf + 2 * NX;
+  C* twlo = buf + ROWS * NX;
   C* twhi = twlo + 64;
   constexpr int Q = NX / 4;                        // = nx / 2
-  const int r0 = 2 * blockIdx.x;
+  const int r0 = ROWS * blockIdx.x;
   load_tw_split(twlo, twhi, a.twx, NX);
   const C* src = a.field + (size_t)r0 * a.nx;
-  for (int idx = threadIdx.x; idx < 2 * NX; idx += blockDim.x) {
+  for (int idx = threadIdx.x; idx < ROWS * NX; idx += blockDim.x) {
     const int l = idx / NX, p = idx - l * NX;
     // rotated line: position p holds field column p - 3Q (p >= 3Q) or p + Q (p < Q)
     int c = -1;
@@ -175,10 +178,10 @@ __global__ void __launch_bounds__(512) fr_row_fwd(FrArgs a) {
     buf[idx] = c >= 0 ? src[(size_t)l * a.nx + c] : make_float2(0.f, 0.f);
   }
   const TwSplit<C> tw{twlo, twhi};
-  FastSched<NX>::template run_t<-1>(buf, 2, NX, 1, tw, false);
+  FastSched<NX>::template run_t<-1>(buf, ROWS, NX, 1, tw, false);
   __syncthreads();
-  for (int idx = threadIdx.x; idx < 2 * NX; idx += blockDim.x) {
-    const int w = idx % kFrW, l = (idx / kFrW) & 1, s = idx / (2 * kFrW);
+  for (int idx = threadIdx.x; idx < ROWS * NX; idx += blockDim.x) {
+    const int w = idx % kFrW, l = (idx / kFrW) % ROWS, s = idx / (ROWS * kFrW);
     a.R[((size_t)s * a.ny + r0 + l) * kFrW + w] = buf[l * NX + s * kFrW + w];
   }
 }
@@ -278,29 +281,29 @@ __global__ void __launch_bounds__(FrColCfg<NY>::T, FrColCfg<NY>::MINB) fr_col(Fr
   }
 }
 
-// Two rows per block: gather the row from the strips into natural frequency
+// ROWS rows per block: gather the row from the strips into natural frequency
 // order, inverse x-FFT, crop into the field.
-template <int NX>
-__global__ void __launch_bounds__(512) fr_row_inv(FrArgs a) {
+template <int NX, int ROWS>
+__global__ void __launch_bounds__(256 * ROWS) fr_row_inv(FrArgs a) {
   typedef float2 C;
   extern __shared__ __align__(16) unsigned char smem[];
   C* buf = reinterpret_cast<C*>(smem);
-  C* twlo = buf + 2 * NX;
+  C* twlo = buf + ROWS * NX;
   C* twhi = twlo + 64;
   constexpr int Q = NX / 4;
-  const int r0 = 2 * blockIdx.x;
+  const int r0 = ROWS * blockIdx.x;
   load_tw_split(twlo, twhi, a.twx, NX);
-  for (int idx = threadIdx.x; idx < 2 * NX; idx += blockDim.x) {
-    const int w = idx % kFrW, l = (idx / kFrW) & 1, s = idx / (2 * kFrW);
+  for (int idx = threadIdx.x; idx < ROWS * NX; idx += blockDim.x) {
+    const int w = idx % kFrW, l = (idx / kFrW) % ROWS, s = idx / (ROWS * kFrW);
     const int p = s * kFrW + w;
     buf[l * NX + __ldg(a.iperm_x + p)] = a.R[((size_t)s * a.ny + r0 + l) * kFrW + w];
   }
   const TwSplit<C> tw{twlo, twhi};
-  FastSched<NX>::template run_t<1>(buf, 2, NX, 1, tw, false);
+  FastSched<NX>::template run_t<1>(buf, ROWS, NX, 1, tw, false);
   __syncthreads();
   float2* dst = a.field + (size_t)r0 * a.nx;
   const int nx = a.nx;
-  for (int idx = threadIdx.x; idx < 2 * nx; idx += blockDim.x) {
+  for (int idx = threadIdx.x; idx < ROWS * nx; idx += blockDim.x) {
     const int l = idx / nx, c = idx - l * nx;
     dst[(size_t)l * nx + c] = buf[l * NX + __ldg(a.perm_x + Q + c)];
   }
@@ -344,7 +347,7 @@ static bool fr_pick(int NX, int NY, FrKernel* fwd, FrKernel* col, FrKernel* inv,
   *fwd = *col = *inv = nullptr;
   with_fast_n(NX, [&](auto nc) {
     constexpr int N = decltype(nc)::value;
-    if constexpr (N > 0) { *fwd = fr_row_fwd<N>; *inv = fr_row_inv<N>; }
+    if constexpr (N > 0) { *fwd = fr_row_fwd<N, kFrFwdRows>; *inv = fr_row_inv<N, kFrInvRows>; }
   });
   with_fast_n(NY, [&](auto nc) {
     constexpr int N = decltype(nc)::value;
@@ -396,14 +399,15 @@ static oh_status run_fresnel_separable(oh_ctx* ctx, int nx, int ny, double dp, d
   }
   FrArgs a{nx, ny, field, static_cast<float2*>(rbuf), static_cast<const float2*>(px.tw),
            static_cast<const float2*>(py.tw), px.perm, px.iperm, py.perm, py.iperm, hxs, hys};
-  const int srow = (2 * NX + fr_tw_entries(NX)) * (int)sizeof(float2);
+  const int sfwd = (kFrFwdRows * NX + fr_tw_entries(NX)) * (int)sizeof(float2);
+  const int sinv = (kFrInvRows * NX + fr_tw_entries(NX)) * (int)sizeof(float2);
   const int scol = (NY * kFrW + fr_tw_entries(NY)) * (int)sizeof(float2);
-  OH_CUDA_TRY(cudaFuncSetAttribute(fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, srow));
-  OH_CUDA_TRY(cudaFuncSetAttribute(inv, cudaFuncAttributeMaxDynamicSharedMemorySize, srow));
+  OH_CUDA_TRY(cudaFuncSetAttribute(fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, sfwd));
+  OH_CUDA_TRY(cudaFuncSetAttribute(inv, cudaFuncAttributeMaxDynamicSharedMemorySize, sinv));
   OH_CUDA_TRY(cudaFuncSetAttribute(col, cudaFuncAttributeMaxDynamicSharedMemorySize, scol));
   {
     KernelTimer kt(ctx, "fresnel_row_fwd", st);
-    fwd<<<ny / 2, 512, srow, st>>>(a);
+    fwd<<<ny / kFrFwdRows, 256 * kFrFwdRows, sfwd, st>>>(a);
     OH_LAUNCH_CHECK();
   }
   {
@@ -413,7 +417,7 @@ static oh_status run_fresnel_separable(oh_ctx* ctx, int nx, int ny, double dp, d
   }
   {
     KernelTimer kt(ctx, "fresnel_row_inv", st);
-    inv<<<ny / 2, 512, srow, st>>>(a);
+    inv<<<ny / kFrInvRows, 256 * kFrInvRows, sinv, st>>>(a);
     OH_LAUNCH_CHECK();
   }
   return OH_OK;
@@ -427,7 +431,7 @@ static oh_status run_fresnel(oh_ctx* ctx, int nx, int ny, double dp, double lamb
     int ct = 0;
     const bool even = nx % 2 == 0 && ny % 2 == 0;
     if (even && !getenv("OH_FRESNEL_GRID") && fr_pick(2 * nx, 2 * ny, &fwd, &col, &inv, &ct) &&
-        (size_t)(2 * (2 * nx) + fr_tw_entries(2 * nx)) * sizeof(float2) <= max_smem_per_block())
+        (size_t)(kFrFwdRows * (2 * nx) + fr_tw_entries(2 * nx)) * sizeof(float2) <= max_smem_per_block())
       return run_fresnel_separable(ctx, nx, ny, dp, lambda, z, static_cast<float2*>(field), fwd, col, inv, ct, st);
   }
   return run_fresnel_grid<R>(ctx, nx, ny, dp, lambda, z, field, st);

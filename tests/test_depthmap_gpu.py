@@ -190,6 +190,54 @@ def test_full_size_linearity_and_fp64_agreement(ctx, dev):
     assert rel(fa + fb, f64) < 1e-9
 
 
+def _run_layer_step(ctx, dev, img, depth, p, enabled):
+    import os
+    old = os.environ.get("OH_DM_LAYER_STEP")
+    os.environ["OH_DM_LAYER_STEP"] = "1" if enabled else "0"
+    try:
+        return run(ctx, dev, img, depth, p, None, "fp32", want_field=True)
+    finally:
+        if old is None:
+            del os.environ["OH_DM_LAYER_STEP"]
+        else:
+            os.environ["OH_DM_LAYER_STEP"] = old
+
+
+def test_layer_step_recurrence_matches_per_layer(ctx, dev):
+    """Evenly spaced layers (transform_viewing_window = 0): the column pass
+    accumulates acc = acc D + x with one step factor D per spectrum sample
+    instead of evaluating every layer's transfer function.  Both forms agree
+    with each other and with the FP64 path far inside the FP32 bound."""
+    ny, nx, L = 540, 960, 12
+    img, depth = scenes.depthmap_scene(17, ny, nx)
+    p = dm.make_params(pnx=nx, pny=ny, num_of_depth=L, pad=2, phase_mode=dm.OH_PHASE_SEEDED, seed=23)
+    _, f_step = _run_layer_step(ctx, dev, img, depth, p, True)
+    _, f_layer = _run_layer_step(ctx, dev, img, depth, p, False)
+    _, f64 = run(ctx, dev, img, depth, p, None, "fp64", want_field=True)
+    assert rel(f_step, f64) < 2e-5
+    assert rel(f_layer, f64) < 2e-5
+    assert rel(f_step, f_layer) < 2e-5
+
+
+def test_layer_step_with_empty_layers(ctx, dev):
+    """Levels without pixels between occupied ones: the recurrence applies
+    D once per skipped level (gaps of 1, 3 and 4 levels here), checked
+    against the oracle."""
+    ny, nx, L = 540, 960, 14
+    img, depth0 = scenes.depthmap_scene(29, ny, nx)
+    p = dm.make_params(pnx=nx, pny=ny, num_of_depth=L, pad=2, phase_mode=dm.OH_PHASE_SEEDED, seed=31)
+    op = oparams(p)
+    lut = odm.depth_lut(op)
+    used = [2, 3, 7, 8, 12]
+    byte_of = {lv: int(np.flatnonzero(lut == lv)[0]) for lv in used}
+    band = (depth0.astype(np.int64) * len(used)) // 256
+    depth = np.vectorize(lambda i: byte_of[used[i]])(band).astype(np.uint8)
+    assert set(np.unique(lut[depth])) == set(used)
+    _, f_step = _run_layer_step(ctx, dev, img, depth, p, True)
+    _, ref_field, _ = odm.generate(img, depth, op, phase=scenes.seeded_phase(31, ny, nx))
+    assert rel(f_step, ref_field) < 2e-5
+
+
 def test_host_entry_point_matches_device(ctx, dev):
     ny, nx = 72, 120
     img, depth = scenes.depthmap_scene(3, ny, nx)
