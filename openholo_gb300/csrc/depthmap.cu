@@ -227,10 +227,14 @@ __global__ void __launch_bounds__(512) dm_row_pass(DMArgs<R> a) {
   uint32_t* mask = reinterpret_cast<uint32_t*>(li + 2 * lip);   // [2][8] layers present per row
   C* twlo = reinterpret_cast<C*>(mask + 16);            // 64 + ceil(Px/64) twiddles (fast path)
   C* twhi = twlo + 64;
+  C* tab1 = twhi + (Px + 63) / 64;                      // stage-1 twiddle table (fast path)
   const int r0 = blockIdx.x * kRowPair;
   const int nrows = min(kRowPair, a.pny - r0);
   for (int i = threadIdx.x; i < 16; i += blockDim.x) mask[i] = 0u;
-  if constexpr (NX > 0) load_tw_split(twlo, twhi, static_cast<const C*>(a.plx.tw), NX);
+  if constexpr (NX > 0) {
+    load_tw_split(twlo, twhi, static_cast<const C*>(a.plx.tw), NX);
+    fill_stage_tab<NX, FastSched<NX>::r1, NX / FastSched<NX>::r0, -1>(tab1, static_cast<const C*>(a.plx.tw));
+  }
   __syncthreads();
   for (int idx = threadIdx.x; idx < kRowPair * pnx; idx += blockDim.x) {
     const int l = idx / pnx, c = idx - l * pnx;
@@ -312,7 +316,7 @@ __global__ void __launch_bounds__(512) dm_row_pass(DMArgs<R> a) {
 #pragma unroll
         for (int f = 0; f < R0; ++f) bl[j + f * Q0] = x[f];
       }
-      FastSched<NX>::template run_rest<-1>(buf, kRowPair, Px, 1, tw, false);
+      FastSched<NX>::template run_rest_tab<-1>(buf, kRowPair, Px, 1, tab1, tw, false);
       __syncthreads();
     } else {
       // shifted, zero-padded source lines: a[j] = u[(j - hx) mod Px]
@@ -646,12 +650,16 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   a.err = ctx->dev_err;
   // FP32 with a compile-time FFT length: bulk-copy pipelined column pass
   // (dm_col_fast) with the widest strip whose shared-memory layout fits
-  int Wfast = 0;
+  int Wfast = 0, col_tab = 0;
   bool fastlen = false;
   with_fast_n(a.Py, [&](auto nc) { fastlen = decltype(nc)::value > 0; });
   if (prec == 0 && fastlen) {
     // strips of two spectrum columns (two blocks per SM)
-    if (a.Px % 2 == 0 && (size_t)col_layout(a.Py, a.pny, 2, occ_stride, su.n_entries).total <= smax) Wfast = 2;
+    with_fast_n(a.Py, [&](auto nc) {
+      if constexpr (decltype(nc)::value > 0) col_tab = col_tab_entries<decltype(nc)::value>();
+    });
+    if (a.Px % 2 == 0 && (size_t)col_layout(a.Py, a.pny, 2, occ_stride, su.n_entries, col_tab).total <= smax)
+      Wfast = 2;
   }
   int W = Wfast;
   if (W == 0) {
@@ -691,11 +699,15 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   with_fast_n(a.Py, [&](auto nc) { if constexpr (decltype(nc)::value > 0) r0y = FastSched<decltype(nc)::value>::r0; });
   a.hzx = (p->pad == 2 && r0x == 16 && (a.Px % 16) == 0 && a.ox * 4 == a.Px && a.hx * 2 == a.Px) ? 1 : 0;
   a.hzy = (p->pad == 2 && r0y == 16 && (a.Py % 16) == 0 && a.oy * 4 == a.Py && a.hy * 2 == a.Py) ? 1 : 0;
-  const size_t smem_col = Wfast ? (size_t)col_layout(a.Py, a.pny, W, occ_stride, su.n_entries).total
+  const size_t smem_col = Wfast ? (size_t)col_layout(a.Py, a.pny, W, occ_stride, su.n_entries, col_tab).total
                                 : (size_t)W * a.Py * sizeof(C) + W * (sizeof(C) + sizeof(R)) + (size_t)a.Py * sizeof(int);
+  int row_tab = 0;
+  with_fast_n_if<sizeof(R) == 4>(a.Px, [&](auto nc) {
+    if constexpr (decltype(nc)::value > 0) row_tab = FastSched<decltype(nc)::value>::tab1_entries;
+  });
   const size_t smem_row = kRowPair * ((size_t)a.Px * sizeof(C) + (size_t)a.pnx * sizeof(C) +
                                       (size_t)((a.pnx + 7) & ~7) * sizeof(int16_t)) +
-                          16 * sizeof(uint32_t) + (64 + (size_t)(a.Px + 63) / 64) * sizeof(C);
+                          16 * sizeof(uint32_t) + (64 + (size_t)(a.Px + 63) / 64 + row_tab) * sizeof(C);
   const size_t smem_out = (size_t)a.Px * sizeof(C) + (64 + (size_t)(a.Px + 63) / 64) * sizeof(C);
   if (smem_row > smax || smem_out > smax) return fail(OH_ERR_UNSUPPORTED_SIZE, "padded row length " + std::to_string(a.Px) + " exceeds shared memory");
 

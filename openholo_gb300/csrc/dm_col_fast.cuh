@@ -29,8 +29,20 @@
 namespace oh {
 
 struct ColLayout {
-  int buf, stg, ey0, ey1, occ, g, kyp, twlo, twhi, exw, lfxw, list, mbar, total;
+  int buf, stg, ey0, ey1, occ, g, kyp, twlo, twhi, tab, exw, lfxw, list, mbar, total;
 };
+
+// Twiddle-table entries of the middle forward stage of the column FFT
+// (W^(j f) per butterfly offset j and output f: one load per twiddle instead
+// of two loads and a product), or 0 when they would take more than 8 KB.
+// (A table for stage 0 as well raises the register pressure there, where the
+// accumulators are live, into spills.)
+template <int NY>
+constexpr int col_tab_entries() {
+  constexpr int R0 = FastSched<NY>::r0, R1 = FastSched<NY>::r1;
+  constexpr int n = (NY / R0 / R1) * (R1 - 1);
+  return n * 8 <= 8192 ? n : 0;
+}
 
 __host__ __device__ inline int col_take(int* o, int bytes) {
   const int r = *o;
@@ -38,7 +50,8 @@ __host__ __device__ inline int col_take(int* o, int bytes) {
   return r;
 }
 
-__host__ __device__ inline ColLayout col_layout(int Py, int pny, int W, int occ_stride, int n_entries) {
+__host__ __device__ inline ColLayout col_layout(int Py, int pny, int W, int occ_stride, int n_entries,
+                                                int tab_entries) {
   ColLayout L;
   int o = 0;
   L.buf = col_take(&o, Py * W * 8);
@@ -53,6 +66,7 @@ __host__ __device__ inline ColLayout col_layout(int Py, int pny, int W, int occ_
   L.kyp = col_take(&o, Py * 2);
   L.twlo = col_take(&o, 64 * 8);
   L.twhi = col_take(&o, ((Py + 63) / 64) * 8);
+  L.tab = col_take(&o, tab_entries * 8);
   L.exw = col_take(&o, W * 8);
   L.lfxw = col_take(&o, W * 4);
   L.list = col_take(&o, n_entries * 2 + 2);
@@ -117,7 +131,9 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
   constexpr int Q0 = NY / R0;
   static_assert(FastSched<NY>::nstages == 3, "fast column pass expects a three-stage schedule");
   extern __shared__ __align__(128) unsigned char smem[];
-  const ColLayout Lo = col_layout(NY, a.pny, W, a.occ_stride, a.n_entries);
+  constexpr int kTab = col_tab_entries<NY>();
+  constexpr int R1 = FastSched<NY>::r1;
+  const ColLayout Lo = col_layout(NY, a.pny, W, a.occ_stride, a.n_entries, kTab);
   C* buf = reinterpret_cast<C*>(smem + Lo.buf);
   C* const stg = reinterpret_cast<C*>(smem + Lo.stg);            // row-pass strip of the layer (single buffer)
   uint8_t* const occ = smem + Lo.occ;                             // its row flags
@@ -127,6 +143,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
   int16_t* kyp = reinterpret_cast<int16_t*>(smem + Lo.kyp);
   C* twlo = reinterpret_cast<C*>(smem + Lo.twlo);
   C* twhi = reinterpret_cast<C*>(smem + Lo.twhi);
+  C* const tab1 = reinterpret_cast<C*>(smem + Lo.tab);            // stage 1: [NY/R0/R1][R1-1]
   C* exw = reinterpret_cast<C*>(smem + Lo.exw);
   float* lfxw = reinterpret_cast<float*>(smem + Lo.lfxw);
   __shared__ int kxw[8];          // spectrum column of each strip column
@@ -149,6 +166,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
     s_nact = n;
   }
   load_tw_split(twlo, twhi, static_cast<const C*>(a.ply.tw), NY);
+  if constexpr (kTab > 0) fill_stage_tab<NY, R1, NY / R0, -1>(tab1, static_cast<const C*>(a.ply.tw));
   for (int p = tid; p < NY; p += T) {
     int ky = a.ply.iperm[p] + a.hy;
     if (ky >= NY) ky -= NY;
@@ -288,10 +306,8 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
       fence_proxy_async_smem();
       issue_strip(k + 1);
     }
-    {
-      constexpr int R1 = FastSched<NY>::r1;
-      fstage_t<NY, R1, NY / R0, -1>(buf, W, 1, W, tw, true);
-    }
+    if constexpr (kTab > 0) fstage_tab<NY, R1, NY / R0, -1>(buf, W, 1, W, tab1, true);
+    else fstage_t<NY, R1, NY / R0, -1>(buf, W, 1, W, tw, true);
     __syncthreads();
     // last stage (stride 1, no twiddles) fused with the transfer-function
     // multiply-accumulate: either acc += H x per layer, or the recurrence

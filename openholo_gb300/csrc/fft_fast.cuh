@@ -254,6 +254,49 @@ __device__ __forceinline__ void fstage_t(C* buf, int nl, int ls, int es, const T
   }
 }
 
+// One stage with its twiddles from a per-stage table: tab[j (R-1) + f - 1] =
+// W^(SGN j f N/M) for butterfly offset j < M/R, output f = 1..R-1.
+template <int N, int R, int M, int SGN, typename C>
+__device__ __forceinline__ void fstage_tab(C* buf, int nl, int ls, int es, const C* __restrict__ tab,
+                                           bool line_fastest) {
+  constexpr int Q = M / R;
+  constexpr int NB = N / R;
+  const int total = NB * nl;
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    int line, b;
+    if (line_fastest) { b = idx / nl; line = idx - b * nl; }
+    else { line = idx / NB; b = idx - line * NB; }
+    const int blk = b / Q, j = b - blk * Q;
+    const int base = line * ls + (blk * M + j) * es;
+    const int st = Q * es;
+    C x[R];
+#pragma unroll
+    for (int t = 0; t < R; ++t) x[t] = buf[base + t * st];
+    DFT<R, SGN, C>::run(x);
+    if (Q > 1 && j) {
+      const C* tj = tab + j * (R - 1) - 1;
+#pragma unroll
+      for (int f = 1; f < R; ++f) x[f] = cmul(x[f], tj[f]);
+    }
+#pragma unroll
+    for (int t = 0; t < R; ++t) buf[base + t * st] = x[t];
+  }
+}
+
+// Fill a per-stage table for fstage_tab from the full table tw (W_N^e,
+// e < N); call with all threads, then sync.
+template <int N, int R, int M, int SGN, typename C>
+__device__ __forceinline__ void fill_stage_tab(C* tab, const C* __restrict__ tw) {
+  constexpr int Q = M / R;
+  constexpr int TWS = N / M;
+  for (int i = threadIdx.x; i < Q * (R - 1); i += blockDim.x) {
+    const int j = i / (R - 1), f = i - j * (R - 1) + 1;
+    C w = tw[(j * f * TWS) % N];
+    if (SGN > 0) w.y = -w.y;
+    tab[i] = w;
+  }
+}
+
 template <int N, int M, int SGN, typename C, class TW, int R, int... Rest>
 __device__ __forceinline__ void fstages_t(C* buf, int nl, int ls, int es, const TW& tw, bool line_fastest) {
   __syncthreads();
@@ -293,6 +336,15 @@ __device__ __forceinline__ void fstages(C* buf, int nl, int ls, int es, const C*
   __syncthreads();
   fstage<N, R, M, SGN>(buf, nl, ls, es, tw, line_fastest);
   if constexpr (sizeof...(Rest) > 0) fstages<N, M / R, SGN, C, Rest...>(buf, nl, ls, es, tw, line_fastest);
+}
+
+// the first stage of the list with its table twiddles, then the others
+template <int N, int M, int SGN, typename C, class TW, int R, int... Rest>
+__device__ __forceinline__ void fstages_tab_first(C* buf, int nl, int ls, int es, const C* tab, const TW& tw,
+                                                  bool line_fastest) {
+  __syncthreads();
+  fstage_tab<N, R, M, SGN>(buf, nl, ls, es, tab, line_fastest);
+  if constexpr (sizeof...(Rest) > 0) fstages_t<N, M / R, SGN, C, TW, Rest...>(buf, nl, ls, es, tw, line_fastest);
 }
 
 // every stage of the list except the last one (block size M at entry)
@@ -337,6 +389,14 @@ struct SchedImpl {
   template <int SGN, typename C, class TW>
   __device__ __forceinline__ static void run_rest(C* buf, int nl, int ls, int es, const TW& tw, bool lf) {
     if constexpr (sizeof...(Rest) > 0) fstages_t<N, N / R0, SGN, C, TW, Rest...>(buf, nl, ls, es, tw, lf);
+  }
+  // entries of the stage-1 twiddle table (fill_stage_tab<N, r1, N / r0>)
+  static constexpr int tab1_entries = (N / R0 / r1) * (r1 - 1);
+  // as run_rest, with stage 1's twiddles from its table tab1
+  template <int SGN, typename C, class TW>
+  __device__ __forceinline__ static void run_rest_tab(C* buf, int nl, int ls, int es, const C* tab1, const TW& tw,
+                                                      bool lf) {
+    if constexpr (sizeof...(Rest) > 0) fstages_tab_first<N, N / R0, SGN, C, TW, Rest...>(buf, nl, ls, es, tab1, tw, lf);
   }
 };
 
