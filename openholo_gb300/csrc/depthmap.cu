@@ -284,13 +284,13 @@ __global__ void __launch_bounds__(512) dm_row_pass(DMArgs<R> a) {
         const C* vl = v + l * pnx;
         C x[R0];
         if (R0 == 16 && a.hzx) {
-          // 2x padding: inputs t = 4..11 fall in the zero columns
+          // 2x padding: inputs t = 4..11 fall in the zero columns; with
+          // hx = NX/2 and ox = NX/4 the image column of input t is
+          // j + (t + 4) Q0 (t < 4) or j + (t - 12) Q0 (t >= 12)
 #pragma unroll
           for (int t = 0; t < R0; ++t) {
             if (t >= 4 && t < 12) { x[t] = mk((R)0, (R)0); continue; }
-            int xx = j + t * Q0 - a.hx;
-            if (xx < 0) xx += NX;
-            const int c = xx - a.ox;
+            const int c = j + (t < 4 ? t + 4 : t - 12) * Q0;
             x[t] = lil[c] == u ? vl[c] : mk((R)0, (R)0);
           }
           dft16_halfzero<-1>(x);
@@ -334,6 +334,19 @@ __global__ void __launch_bounds__(512) dm_row_pass(DMArgs<R> a) {
     // (W is a power of two: index split with shifts)
     C* dst = a.Rbuf + (size_t)u * a.nstrips * a.pny * a.W;
     const int W = a.W, lw = a.lw;
+    if (sizeof(R) == 4 && W == 2 && nrows == 2 && a.xs) {
+      // FP32, strips of two columns, FFT storage order: a thread pair moves
+      // one strip's 2 x 2 block (32 contiguous bytes, one full sector), one
+      // row each, with 16-byte accesses
+      const float4* b4 = reinterpret_cast<const float4*>(buf);
+      float4* d4 = reinterpret_cast<float4*>(dst);
+      for (int idx = threadIdx.x; idx < Px; idx += blockDim.x) {
+        const int st = idx >> 1, l = idx & 1;
+        d4[(size_t)st * a.pny + r0 + l] = b4[l * (Px / 2) + st];
+      }
+      __syncthreads();
+      continue;
+    }
     for (int idx = threadIdx.x; idx < nrows * Px; idx += blockDim.x) {
       const int w = idx & (W - 1);
       const int t = idx >> lw;

@@ -269,13 +269,13 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
       const int j = idx / W, w = idx - j * W;
       C x[R0];
       if (R0 == 16 && a.hzy) {
-        // 2x padding: inputs t = 4..11 are rows of the zero band
+        // 2x padding: inputs t = 4..11 are rows of the zero band; with
+        // hy = NY/2 and oy = NY/4 the image row of input t is
+        // j + (t + 4) Q0 (t < 4) or j + (t - 12) Q0 (t >= 12)
 #pragma unroll
         for (int t = 0; t < R0; ++t) {
           if (t >= 4 && t < 12) { x[t] = make_float2(0.f, 0.f); continue; }
-          int y = j + t * Q0 - a.hy;
-          if (y < 0) y += NY;
-          const int yl = y - a.oy;
+          const int yl = j + (t < 4 ? t + 4 : t - 12) * Q0;
           x[t] = occ[yl] ? stg[yl * W + w] : make_float2(0.f, 0.f);
         }
         dft16_halfzero<-1>(x);
