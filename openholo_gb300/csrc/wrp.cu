@@ -83,12 +83,14 @@ constexpr int kWrpTile = 64;
 
 // Per point: window centre and half-width; exact-path terms (base = k|dz|
 // reduced to radians); the FP64 path's dz; and, when the window is paraxial
-// enough (series = 1), the terms of the series evaluation below.
+// enough (series = 1), the polynomial coefficients of the series evaluation
+// below in u = rho^2 / dz^2 = (wx sx)^2 + (wy sx)^2, sx = dp / |dz|.
 struct WrpPt {
   int tx, ty, w, series;
-  float base, adz, sgn, pad0;
-  double dz;
-  float base_t, kadz_t, inv_adz2, ea, inv_a0, pad1;
+  float base, adz, sgn, sx;
+  float base_t, c1, c2, c3;          // phase in turns: base_t + u (c1 + u (c2 + u c3))
+  float a0c, a1c, a2c, pad0;         // amplitude: a0c + u (a1c + u a2c)
+  double dz, pad1;
 };
 
 __device__ __forceinline__ void wrp_point(const WRPGeom& g, const double* xyz, int k, WrpPt* o) {
@@ -108,23 +110,33 @@ __device__ __forceinline__ void wrp_point(const WRPGeom& g, const double* xyz, i
   const double kdz = kd * fabs(dz);
   o->base = (float)(kdz - two_pi * rint(kdz / two_pi));
   // Series form: with u = rho^2 / dz^2 and t = sqrt(1 + u) - 1 = u (1/2 - u/8 + u^2/16) + O(5 u^4 / 128),
-  //   k|r| = k|dz| (1 + t),   1 / (sgn |r| + 0.05) = (1 / a0) (1 - e + e^2),  a0 = sgn |dz| + 0.05,
-  //   e = sgn |dz| t / a0,
-  // used when the dropped terms stay below 1e-6 rad and 1e-8 relative over the whole window.
+  //   sgn k|r| / (2 pi) = sgn turns (1 + t),  turns = k|dz| / (2 pi),
+  //   1 / (sgn |r| + 0.05) = (1 / a0) / (1 + e),  a0 = sgn |dz| + 0.05,  e = ea t,  ea = sgn |dz| / a0,
+  //   1 / (1 + e) = 1 - ea u / 2 + (ea / 8 + ea^2 / 4) u^2 - (ea / 16 + ea^2 / 8 + ea^3 / 8) u^3 + ...,
+  // used when the dropped terms stay below 1e-6 rad (phase) and 1e-8 relative
+  // (amplitude) over the whole window.
   const double adz = fabs(dz), sg = dz > 0.0 ? 1.0 : -1.0;
   const double a0 = sg * adz + 0.05;
   const double rho2max = 2.0 * (double)g.fixed_w * g.fixed_w * (double)dpx * dpx;
   const double umax = adz > 0.0 ? rho2max / (adz * adz) : 1.0;
-  const double emax = fabs(a0) > 1e-6 ? adz * umax / (2.0 * fabs(a0)) : 1.0;
-  o->series = (adz > 0.0 && umax < 0.05 && kdz * (5.0 / 128.0) * umax * umax * umax * umax < 1e-6 &&
-               emax * emax * emax < 1e-8) ? 1 : 0;
+  const double ea = fabs(a0) > 1e-6 ? sg * adz / a0 : 0.0;
+  const double aea = fabs(ea);
+  const double u3 = umax * umax * umax;
+  o->series = (adz > 0.0 && fabs(a0) > 1e-6 && umax < 0.05 &&
+               kdz * (5.0 / 128.0) * umax * u3 < 1e-6 &&
+               (aea / 16.0 + aea * aea / 8.0 + aea * aea * aea / 8.0) * u3 < 1e-8) ? 1 : 0;
   const double turns = kdz / two_pi;
   o->base_t = (float)(sg * (turns - rint(turns)));
-  o->kadz_t = (float)(sg * turns);
-  o->inv_adz2 = adz > 0.0 ? (float)(1.0 / (adz * adz)) : 0.f;
-  o->ea = fabs(a0) > 1e-6 ? (float)(sg * adz / a0) : 0.f;
-  o->inv_a0 = fabs(a0) > 1e-6 ? (float)(1.0 / a0) : 0.f;
-  o->pad0 = o->pad1 = 0.f;
+  o->c1 = (float)(sg * turns * 0.5);
+  o->c2 = (float)(sg * turns * -0.125);
+  o->c3 = (float)(sg * turns * 0.0625);
+  o->sx = adz > 0.0 ? (float)((double)dpx / adz) : 0.f;
+  const double ia0 = fabs(a0) > 1e-6 ? 1.0 / a0 : 0.0;
+  o->a0c = (float)ia0;
+  o->a1c = (float)(-ia0 * ea * 0.5);
+  o->a2c = (float)(ia0 * (ea * 0.125 + ea * ea * 0.25));
+  o->pad0 = 0.f;
+  o->pad1 = 0.0;
 }
 
 // tile index range [t0, t1] along one axis for the window [c - w, c + w) clipped to [0, n)
@@ -284,33 +296,36 @@ __global__ void __launch_bounds__(256) wrp_tile_f32(WRPGeom g, const WrpPt* __re
     const WrpPt q = pts[__ldg(list + li)];
     const int wx = X - q.tx;
     if (wx < -q.w || wx >= q.w || X >= g.nx) continue;
-    const float ddx = (float)wx * dpx;
-    const float dx2 = ddx * ddx;
     const int wy0 = Y0 + r0 - q.ty;                 // wy of row j is wy0 + 4 j
-    const int ylim = g.ny - Y0 - r0;               // row j inside the plane iff 4 j < ylim
+    // row j is in the window and the plane iff 0 <= wy0 + 4 j + w < vlim
+    const int v0 = wy0 + q.w;
+    const int vlim = min(2 * q.w, g.ny - q.ty + q.w);
+    if (vlim <= 0) continue;
     if (q.series) {
+      const float xs = (float)wx * q.sx;
+      const float xs2 = xs * xs;
+      const float ys0 = (float)wy0 * q.sx, s4 = 4.f * q.sx;
 #pragma unroll
       for (int j = 0; j < kRows; ++j) {
-        const int wy = wy0 + 4 * j;
-        if (wy >= -q.w && wy < q.w && 4 * j < ylim) {
-          const float ddy = (float)wy * dpx;
-          const float u = fmaf(ddy, ddy, dx2) * q.inv_adz2;
-          const float t = u * fmaf(u, fmaf(u, 0.0625f, -0.125f), 0.5f);
-          float f = fmaf(q.kadz_t, t, q.base_t);
+        if ((unsigned)(v0 + 4 * j) < (unsigned)vlim) {
+          const float ys = fmaf((float)j, s4, ys0);
+          const float u = fmaf(ys, ys, xs2);
+          float f = fmaf(u, fmaf(u, fmaf(u, q.c3, q.c2), q.c1), q.base_t);
           f -= rintf(f);
           float sn, cs;
           __sincosf(6.28318530717958647692f * f, &sn, &cs);
-          const float e = t * q.ea;
-          const float amp = q.inv_a0 * fmaf(e, e - 1.f, 1.f);
+          const float amp = fmaf(u, fmaf(u, q.a2c, q.a1c), q.a0c);
           acc[j].x = fmaf(cs, amp, acc[j].x);
           acc[j].y = fmaf(sn, amp, acc[j].y);
         }
       }
     } else {
+      const float ddx = (float)wx * dpx;
+      const float dx2 = ddx * ddx;
 #pragma unroll
       for (int j = 0; j < kRows; ++j) {
         const int wy = wy0 + 4 * j;
-        if (wy >= -q.w && wy < q.w && 4 * j < ylim) {
+        if ((unsigned)(v0 + 4 * j) < (unsigned)vlim) {
           const float ddy = (float)wy * dpx;
           const float2 v = wrp_term_f32(fmaf(ddy, ddy, dx2), q, kf);
           acc[j].x += v.x;
