@@ -275,12 +275,18 @@ __device__ __forceinline__ float2 wrp_term_f32(float rho2, const WrpPt& q, float
   return make_float2(cs * amp, sn * amp);
 }
 
-// FP32 tile: thread t owns column t % 64 and rows t / 64 + 4 j (j < 16) of the
-// tile and keeps their sums in registers; no shared memory, no atomics.
+// FP32 tile: each thread owns 16 pixels of the tile (below) and keeps their
+// sums in registers; no atomics.  The tile's point records are staged in
+// shared memory in chunks of kWrpChunk.
+constexpr int kWrpChunk = 128;
+static_assert(sizeof(WrpPt) % 16 == 0, "point records are copied as float4");
+
 __global__ void __launch_bounds__(256) wrp_tile_f32(WRPGeom g, const WrpPt* __restrict__ pts,
                                                    const int* __restrict__ start, const int* __restrict__ list,
                                                    int tiles_x, float2* __restrict__ wrp) {
   constexpr int kRows = kWrpTile * kWrpTile / 256;
+  constexpr int kParts = (int)(sizeof(WrpPt) / 16);
+  __shared__ __align__(16) WrpPt sp[kWrpChunk];
   const int tile = blockIdx.x;
   const int X0 = (tile % tiles_x) * kWrpTile, Y0 = (tile / tiles_x) * kWrpTile;
   // warp w owns columns 8w..8w+7 of the tile; lane l column 8w + l % 8, rows l / 8 + 4 j
@@ -292,44 +298,62 @@ __global__ void __launch_bounds__(256) wrp_tile_f32(WRPGeom g, const WrpPt* __re
   const float kf = (float)(2.0 * M_PI / g.lambda);
   const int X = X0 + c;
   const int b = start[tile], e = start[tile + 1];
-  for (int li = b; li < e; ++li) {
-    const WrpPt q = pts[__ldg(list + li)];
-    const int wx = X - q.tx;
-    if (wx < -q.w || wx >= q.w || X >= g.nx) continue;
-    const int wy0 = Y0 + r0 - q.ty;                 // wy of row j is wy0 + 4 j
-    // row j is in the window and the plane iff 0 <= wy0 + 4 j + w < vlim
-    const int v0 = wy0 + q.w;
-    const int vlim = min(2 * q.w, g.ny - q.ty + q.w);
-    if (vlim <= 0) continue;
-    if (q.series) {
-      const float xs = (float)wx * q.sx;
-      const float xs2 = xs * xs;
-      const float ys0 = (float)wy0 * q.sx, s4 = 4.f * q.sx;
+  for (int c0 = b; c0 < e; c0 += kWrpChunk) {
+    const int nc = min(kWrpChunk, e - c0);
+    __syncthreads();                                  // the previous chunk is consumed
+    for (int i = threadIdx.x; i < nc * kParts; i += blockDim.x) {
+      const int k = i / kParts, part = i - k * kParts;
+      reinterpret_cast<float4*>(sp + k)[part] = reinterpret_cast<const float4*>(pts + __ldg(list + c0 + k))[part];
+    }
+    __syncthreads();
+    for (int li = 0; li < nc; ++li) {
+      const WrpPt& q = sp[li];
+      const int wx = X - q.tx;
+      if (wx < -q.w || wx >= q.w || X >= g.nx) continue;
+      const int wy0 = Y0 + r0 - q.ty;                 // wy of row j is wy0 + 4 j
+      // row j is in the window and the plane iff 0 <= wy0 + 4 j + w < vlim
+      const int v0 = wy0 + q.w;
+      const int vlim = min(2 * q.w, g.ny - q.ty + q.w);
+      if (vlim <= 0) continue;
+      if (q.series) {
+        const float sx = q.sx;
+        const float xs = (float)wx * sx;
+        const float xs2 = xs * xs;
+        const float ys0 = (float)wy0 * sx, s4 = 4.f * sx;
+        const float bt = q.base_t, c1 = q.c1, c2 = q.c2, c3 = q.c3, a0 = q.a0c, a1 = q.a1c, a2 = q.a2c;
+        // rows j = 8h .. 8h+7 span v0 + 32h .. v0 + 32h + 28: skip a half the window misses
 #pragma unroll
-      for (int j = 0; j < kRows; ++j) {
-        if ((unsigned)(v0 + 4 * j) < (unsigned)vlim) {
-          const float ys = fmaf((float)j, s4, ys0);
-          const float u = fmaf(ys, ys, xs2);
-          float f = fmaf(u, fmaf(u, fmaf(u, q.c3, q.c2), q.c1), q.base_t);
-          f -= rintf(f);
-          float sn, cs;
-          __sincosf(6.28318530717958647692f * f, &sn, &cs);
-          const float amp = fmaf(u, fmaf(u, q.a2c, q.a1c), q.a0c);
-          acc[j].x = fmaf(cs, amp, acc[j].x);
-          acc[j].y = fmaf(sn, amp, acc[j].y);
+        for (int h = 0; h < kRows / 8; ++h) {
+          const int vh = v0 + 32 * h;
+          if (vh + 28 < 0 || vh >= vlim) continue;
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) {
+            const int j = 8 * h + jj;
+            if ((unsigned)(vh + 4 * jj) < (unsigned)vlim) {
+              const float ys = fmaf((float)j, s4, ys0);
+              const float u = fmaf(ys, ys, xs2);
+              float f = fmaf(u, fmaf(u, fmaf(u, c3, c2), c1), bt);
+              f -= rintf(f);
+              float sn, cs;
+              __sincosf(6.28318530717958647692f * f, &sn, &cs);
+              const float amp = fmaf(u, fmaf(u, a2, a1), a0);
+              acc[j].x = fmaf(cs, amp, acc[j].x);
+              acc[j].y = fmaf(sn, amp, acc[j].y);
+            }
+          }
         }
-      }
-    } else {
-      const float ddx = (float)wx * dpx;
-      const float dx2 = ddx * ddx;
+      } else {
+        const float ddx = (float)wx * dpx;
+        const float dx2 = ddx * ddx;
 #pragma unroll
-      for (int j = 0; j < kRows; ++j) {
-        const int wy = wy0 + 4 * j;
-        if ((unsigned)(v0 + 4 * j) < (unsigned)vlim) {
-          const float ddy = (float)wy * dpx;
-          const float2 v = wrp_term_f32(fmaf(ddy, ddy, dx2), q, kf);
-          acc[j].x += v.x;
-          acc[j].y += v.y;
+        for (int j = 0; j < kRows; ++j) {
+          const int wy = wy0 + 4 * j;
+          if ((unsigned)(v0 + 4 * j) < (unsigned)vlim) {
+            const float ddy = (float)wy * dpx;
+            const float2 v = wrp_term_f32(fmaf(ddy, ddy, dx2), q, kf);
+            acc[j].x += v.x;
+            acc[j].y += v.y;
+          }
         }
       }
     }
