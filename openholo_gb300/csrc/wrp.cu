@@ -321,25 +321,26 @@ __global__ void __launch_bounds__(256) wrp_tile_f32(WRPGeom g, const WrpPt* __re
         const float xs2 = xs * xs;
         const float ys0 = (float)wy0 * sx, s4 = 4.f * sx;
         const float bt = q.base_t, c1 = q.c1, c2 = q.c2, c3 = q.c3, a0 = q.a0c, a1 = q.a1c, a2 = q.a2c;
-        // rows j = 8h .. 8h+7 span v0 + 32h .. v0 + 32h + 28: skip a half the window misses
+        // rows j = 4h .. 4h+3 span v0 + 16h .. v0 + 16h + 12: a group the window
+        // misses is skipped; the others are evaluated without branches (four
+        // independent chains) and rows outside the window get amplitude 0
 #pragma unroll
-        for (int h = 0; h < kRows / 8; ++h) {
-          const int vh = v0 + 32 * h;
-          if (vh + 28 < 0 || vh >= vlim) continue;
+        for (int h = 0; h < kRows / 4; ++h) {
+          const int vh = v0 + 16 * h;
+          if (vh + 12 < 0 || vh >= vlim) continue;
 #pragma unroll
-          for (int jj = 0; jj < 8; ++jj) {
-            const int j = 8 * h + jj;
-            if ((unsigned)(vh + 4 * jj) < (unsigned)vlim) {
-              const float ys = fmaf((float)j, s4, ys0);
-              const float u = fmaf(ys, ys, xs2);
-              float f = fmaf(u, fmaf(u, fmaf(u, c3, c2), c1), bt);
-              f -= rintf(f);
-              float sn, cs;
-              __sincosf(6.28318530717958647692f * f, &sn, &cs);
-              const float amp = fmaf(u, fmaf(u, a2, a1), a0);
-              acc[j].x = fmaf(cs, amp, acc[j].x);
-              acc[j].y = fmaf(sn, amp, acc[j].y);
-            }
+          for (int jj = 0; jj < 4; ++jj) {
+            const int j = 4 * h + jj;
+            const bool in = (unsigned)(vh + 4 * jj) < (unsigned)vlim;
+            const float ys = fmaf((float)j, s4, ys0);
+            const float u = fmaf(ys, ys, xs2);
+            float f = fmaf(u, fmaf(u, fmaf(u, c3, c2), c1), bt);
+            f -= rintf(f);
+            float sn, cs;
+            __sincosf(6.28318530717958647692f * f, &sn, &cs);
+            const float amp = in ? fmaf(u, fmaf(u, a2, a1), a0) : 0.f;
+            acc[j].x = fmaf(cs, amp, acc[j].x);
+            acc[j].y = fmaf(sn, amp, acc[j].y);
           }
         }
       } else {
