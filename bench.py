@@ -369,6 +369,20 @@ def _sec_pointcloud(ctx, dev, torch, st, timed, out, n, nx, ny):
     del f64
 
 
+def kernel_breakdown(ctx, torch, fn, calls=5):
+    """Per-kernel milliseconds per call, from the library's stream events, in
+    a separate pass (the timed pass above runs with these events off)."""
+    torch.cuda.synchronize()
+    ctx.set_timing(True)
+    ctx.read_timing(reset=True)
+    for _ in range(calls):
+        fn()
+    torch.cuda.synchronize()
+    kt = ctx.read_timing(reset=True)
+    ctx.set_timing(False)
+    return {k: v[0] / calls for k, v in kt.items()}
+
+
 def _sec_pls(ctx, dev, torch, st, timed, out, n, nx, ny, calls):
     import ctypes as C
     from openholo_gb300 import _lib, scenes
@@ -381,13 +395,8 @@ def _sec_pls(ctx, dev, torch, st, timed, out, n, nx, ny, calls):
         def pls_frame(pp=pp):
             _lib.call("oh_pls", ctx.handle, 0, C.byref(pp), C.c_void_p(pls_pts.data_ptr()), n,
                       C.c_void_p(pls_out.data_ptr()), st)
-        ctx.set_timing(True)
-        ctx.read_timing(reset=True)
         ms_p = timed(pls_frame)
-        kt = ctx.read_timing(reset=True)
-        ctx.set_timing(False)
-        pls_res[eng_name] = {"ms_per_hologram": ms_p,
-                             "kernels_ms": {k: v[0] / calls for k, v in kt.items()}}
+        pls_res[eng_name] = {"ms_per_hologram": ms_p, "kernels_ms": kernel_breakdown(ctx, torch, pls_frame)}
     tc_ms = pls_res["tensor"]["kernels_ms"].get("pls_tc_gemm")
     if tc_ms:
         useful = 8.0 * nx * ny * n          # complex multiply-adds as real flops, counted once
@@ -414,13 +423,9 @@ def _sec_wrp(ctx, dev, torch, st, timed, out, calls):
                   C.c_void_p(wrp.data_ptr()), st)
         _lib.call("oh_fresnel_propagate", ctx.handle, 0, hx, hy, dp, lam, z_wrp, C.c_void_p(wrp.data_ptr()), st)
         _lib.call("oh_encode", ctx.handle, 0, 9, hx, hy, C.c_void_p(wrp.data_ptr()), C.c_void_p(hol.data_ptr()), st)
-    ctx.set_timing(True)
-    ctx.read_timing(reset=True)
     ms3 = timed(wrp_frame)
-    kt = ctx.read_timing(reset=True)
-    ctx.set_timing(False)
     out["wrp_200k_64x64_fresnel_3840x2160"] = {"ms_per_hologram": ms3, "holograms_per_s": 1000.0 / ms3,
-                                               "kernels_ms": {k: v[0] / calls for k, v in kt.items()},
+                                               "kernels_ms": kernel_breakdown(ctx, torch, wrp_frame),
                                                "dtype": "f32"}
 
 
@@ -546,7 +551,9 @@ def main():
            "config": {"workload": WORKLOAD, "pnx": NX, "pny": NY, "layers": LAYERS, "pad": PAD,
                       "fft_grid": [PAD * NX, PAD * NY], "l2": "flushed between timed steps (512 MiB write)"},
            "e2e": {"value": world * 1000.0 / e2e_ms, "unit": "frames/s", "h2d_bytes_per_step": 2 * NX * NY,
-                   "d2h_bytes_per_step": 4 * NX * NY},
+                   "d2h_bytes_per_step": 4 * NX * NY,
+                   "call_ms": {"min": 1000.0 * min(wall), "median": 1000.0 * sorted(wall)[len(wall) // 2],
+                               "max": 1000.0 * max(wall)}},
            "gpu_launches": launches,
            "kernels_ms_per_frame": {k: v[0] / args.steps for k, v in ktimes.items()},
            "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -79,8 +79,22 @@ __global__ void pc_tables(PCGeom g, const float4* __restrict__ pts, int n, float
   }
 }
 
-// One thread per pixel of a 32x8 tile; points streamed through shared memory.
-__global__ void __launch_bounds__(kPcTX * kPcTY) pc_direct_f32(PCGeom g, const float4* __restrict__ prm,
+// A 32 x 16 pixel tile per 128-thread block: thread (tx, ty) owns column tx
+// and rows ty + 4 i (i < 4), so each point's column terms (x table, r_x, dx)
+// serve four pixels; points streamed through shared memory in chunks.
+// (2048 blocks at 1024 x 1024: about two full waves at 7 blocks per SM.)
+constexpr int kPcFTY = 4, kPcRows = 4;
+constexpr int kPcTR = kPcFTY * kPcRows;    // tile rows
+
+__device__ __forceinline__ float pc_sqrt_approx(float a) {
+  float r;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+  return r;
+}
+
+inline dim3 pc_grid_f32(int nx, int ny) { return dim3((nx + kPcTX - 1) / kPcTX, (ny + kPcTR - 1) / kPcTR); }
+
+__global__ void __launch_bounds__(kPcTX * kPcFTY) pc_direct_f32(PCGeom g, const float4* __restrict__ prm,
                                                               const float* __restrict__ A, const float* __restrict__ RX,
                                                               const float* __restrict__ B, const float* __restrict__ RY,
                                                               const float* __restrict__ E, int n,
@@ -88,16 +102,18 @@ __global__ void __launch_bounds__(kPcTX * kPcTY) pc_direct_f32(PCGeom g, const f
                                                               int accumulate_field) {
   __shared__ float sA[kPcPts][kPcTX];
   __shared__ float sX[kPcPts][kPcTX];
-  __shared__ float sB[kPcPts][kPcTY];
-  __shared__ float sR[kPcPts][kPcTY];
-  __shared__ float sE[kPcPts][kPcTY];
+  __shared__ float sB[kPcPts][kPcTR];
+  __shared__ float sR[kPcPts][kPcTR];
+  __shared__ float sE[kPcPts][kPcTR];
   __shared__ float4 sP[kPcPts];
   const int tx = threadIdx.x % kPcTX, ty = threadIdx.x / kPcTX;
-  const int col = blockIdx.x * kPcTX + tx, row = blockIdx.y * kPcTY + ty;
+  const int col = blockIdx.x * kPcTX + tx, row0 = blockIdx.y * kPcTR + ty;
   const float X = (float)(((double)col + 0.5) * g.px - g.hlx);
   const float nk = (float)(-g.k);
   const float inv2pi = 0.15915494309189533577f, two_pi = 6.28318530717958647692f;
-  float re = 0.f, im = 0.f;
+  float re[kPcRows], im[kPcRows];
+#pragma unroll
+  for (int i = 0; i < kPcRows; ++i) re[i] = im[i] = 0.f;
   for (int j0 = 0; j0 < n; j0 += kPcPts) {
     const int cnt = min(kPcPts, n - j0);
     __syncthreads();
@@ -108,9 +124,9 @@ __global__ void __launch_bounds__(kPcTX * kPcTY) pc_direct_f32(PCGeom g, const f
       sA[j][c] = cc < g.nx ? A[o] : 0.f;
       sX[j][c] = cc < g.nx ? RX[o] : 1.f;
     }
-    for (int i = threadIdx.x; i < cnt * kPcTY; i += blockDim.x) {
-      int j = i / kPcTY, r = i - j * kPcTY;
-      int rr = blockIdx.y * kPcTY + r;
+    for (int i = threadIdx.x; i < cnt * kPcTR; i += blockDim.x) {
+      int j = i / kPcTR, r = i - j * kPcTR;
+      int rr = blockIdx.y * kPcTR + r;
       size_t o = (size_t)(j0 + j) * g.ny + rr;
       sB[j][r] = rr < g.ny ? B[o] : 0.f;
       sR[j][r] = rr < g.ny ? RY[o] : 1.f;
@@ -118,31 +134,43 @@ __global__ void __launch_bounds__(kPcTX * kPcTY) pc_direct_f32(PCGeom g, const f
     }
     for (int i = threadIdx.x; i < cnt; i += blockDim.x) sP[i] = prm[j0 + i];
     __syncthreads();
-#pragma unroll 4
+#pragma unroll 2
     for (int j = 0; j < cnt; ++j) {
-      const float4 p = sP[j];
+      const float4 p = sP[j];                     // x_j, rb, amplitude
       const float dx = X - p.x;
       const float dx2 = dx * dx;
-      const float ry = sR[j][ty], rx = sX[j][tx];
-      const float r = sqrtf(fmaf(ry, ry, dx2));
-      const float num = (rx + r) + (ry + p.y);
-      const float den = (r + ry) * (rx + p.y) * (rx + r);
-      const float rem = nk * sE[j][ty] * dx2 * __fdividef(num, den);
-      float ph = sA[j][tx] + sB[j][ty] + rem;
-      ph = fmaf(-two_pi, rintf(ph * inv2pi), ph);
-      float sn, cs;
-      __sincosf(ph, &sn, &cs);
-      re = fmaf(p.z, cs, re);
-      im = fmaf(p.z, sn, im);
+      const float ndx2 = nk * dx2;
+      const float rx = sX[j][tx], a = sA[j][tx];
+      const float rxb = rx + p.y;
+#pragma unroll
+      for (int i = 0; i < kPcRows; ++i) {
+        const int r = ty + kPcFTY * i;
+        const float ry = sR[j][r];
+        const float rr = pc_sqrt_approx(fmaf(ry, ry, dx2));
+        const float num = (rx + rr) + (ry + p.y);
+        const float den = (rr + ry) * rxb * (rx + rr);
+        const float rem = ndx2 * sE[j][r] * __fdividef(num, den);
+        float ph = (a + sB[j][r]) + rem;
+        ph = fmaf(-two_pi, rintf(ph * inv2pi), ph);
+        float sn, cs;
+        __sincosf(ph, &sn, &cs);
+        re[i] = fmaf(p.z, cs, re[i]);
+        im[i] = fmaf(p.z, sn, im[i]);
+      }
     }
   }
-  if (col < g.nx && row < g.ny) {
-    const size_t o = (size_t)row * g.nx + col;
-    if (field) {
-      if (accumulate_field) { float2 f = field[o]; field[o] = make_float2(f.x + re, f.y + im); }
-      else field[o] = make_float2(re, im);
+  if (col >= g.nx) return;
+#pragma unroll
+  for (int i = 0; i < kPcRows; ++i) {
+    const int row = row0 + kPcFTY * i;
+    if (row < g.ny) {
+      const size_t o = (size_t)row * g.nx + col;
+      if (field) {
+        if (accumulate_field) { float2 f = field[o]; field[o] = make_float2(f.x + re[i], f.y + im[i]); }
+        else field[o] = make_float2(re[i], im[i]);
+      }
+      if (fringe) fringe[o] += re[i];
     }
-    if (fringe) fringe[o] += re;
   }
 }
 
@@ -232,7 +260,7 @@ oh_status pointcloud_enqueue(oh_ctx* ctx, int prec, const oh_pc_params* p, const
       OH_LAUNCH_CHECK();
     }
     KernelTimer kt(ctx, "pc_direct_f32", st);
-    pc_direct_f32<<<grid, kPcTX * kPcTY, 0, st>>>(g, prm, A, RX, B, RY, E, cnt, (float2*)field, (float*)fringe, j0 > 0);
+    pc_direct_f32<<<pc_grid_f32(p->nx, p->ny), kPcTX * kPcFTY, 0, st>>>(g, prm, A, RX, B, RY, E, cnt, (float2*)field, (float*)fringe, j0 > 0);
     OH_LAUNCH_CHECK();
   }
   return OH_OK;
@@ -308,7 +336,7 @@ oh_status oh_pointcloud_noalloc(const oh_pc_params* p, const float* xyza, int n_
     const int cnt = std::min(chunk, n_points - j0);
     pc_tables<<<1024, 256, 0, st>>>(g, pts + j0, cnt, prm, A, RX, B, RY, E);
     OH_LAUNCH_CHECK();
-    pc_direct_f32<<<grid, kPcTX * kPcTY, 0, st>>>(g, prm, A, RX, B, RY, E, cnt, (float2*)field_out, (float*)fringe_out,
+    pc_direct_f32<<<pc_grid_f32(p->nx, p->ny), kPcTX * kPcFTY, 0, st>>>(g, prm, A, RX, B, RY, E, cnt, (float2*)field_out, (float*)fringe_out,
                                                   j0 > 0);
     OH_LAUNCH_CHECK();
   }
