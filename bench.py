@@ -457,6 +457,7 @@ def main():
 
     import torch
     from openholo_gb300 import Context, depthmap as dm, launch_count, scenes
+    from openholo_gb300.shard import max_over_ranks, rank_seed
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
@@ -467,9 +468,9 @@ def main():
         pg = dist
     ctx = Context(local)
     stream = torch.cuda.current_stream()
-    img, depth = scenes.depthmap_scene(SCENE_SEED + rank, NY, NX)
+    img, depth = scenes.depthmap_scene(rank_seed(SCENE_SEED, rank), NY, NX)
     p = dm.make_params(pnx=NX, pny=NY, num_of_depth=LAYERS, pad=PAD, phase_mode=dm.OH_PHASE_SEEDED,
-                       seed=PHASE_SEED + rank)
+                       seed=rank_seed(PHASE_SEED, rank))
     d_img = torch.from_numpy(img).to(dev)
     d_depth = torch.from_numpy(depth).to(dev)
     fringe = torch.empty((NY, NX), dtype=torch.float32, device=dev)
@@ -499,10 +500,7 @@ def main():
     ktimes = ctx.read_timing(reset=True)
     clocks = clk.summary()
     total_ms = sum(a.elapsed_time(b) for a, b in ev)
-    if pg:
-        t = torch.tensor([total_ms], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, pg, dev)
     ms_step = total_ms / args.steps
     fps = world * 1000.0 / ms_step
 
@@ -522,10 +520,7 @@ def main():
         dm.generate_host(ctx, p, h_img.numpy(), h_depth.numpy(), out=h_out.numpy())
         wall.append(time.perf_counter() - t0)
     e2e_ms = 1000.0 * sum(wall) / len(wall)
-    if pg:
-        t = torch.tensor([e2e_ms], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(e2e_ms, pg, dev)
 
     # ---- roofline of the dominant kernel
     peak, peak_kind = load_peaks()
