@@ -87,6 +87,7 @@ struct DMArgs {
   // evenly spaced layers (fast column pass): step dz = z'_e - z'_(e-1) of the
   // render entries; D = Dx(fx) Dy(fy) exp(-i k dz g) per spectrum element
   int horner;
+  uint32_t fkeep;        // fast column pass: bit f set when last-stage output f can fall in the SSB crop
   float kdz_pi;          // k dz / pi
   double dz;
   C* dxh;                // [Px] exp(-i pi lambda dz fx^2)
@@ -710,6 +711,24 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   int r0x = 0, r0y = 0;
   with_fast_n(a.Px, [&](auto nc) { if constexpr (decltype(nc)::value > 0) r0x = FastSched<decltype(nc)::value>::r0; });
   with_fast_n(a.Py, [&](auto nc) { if constexpr (decltype(nc)::value > 0) r0y = FastSched<decltype(nc)::value>::r0; });
+  // Last-stage outputs of the fast column pass that can reach the SSB crop:
+  // storage position p = b RL + f holds spectrum row ky = (k_low(b) + (Py/RL) f + hy) mod Py
+  // (the last radix is the most significant output digit), k_low < Py/RL.
+  a.fkeep = 0xffffffffu;
+  if (Wfast && !spectrum) {
+    int rl = 0;
+    with_fast_n(a.Py, [&](auto nc) { if constexpr (decltype(nc)::value > 0) rl = FastSched<decltype(nc)::value>::rlast; });
+    if (rl > 0 && rl <= 32) {
+      const int q = a.Py / rl;
+      uint32_t m = 0;
+      for (int f = 0; f < rl; ++f)
+        for (int kl = 0; kl < q; ++kl) {
+          const int ky = (kl + q * f + a.hy) % a.Py;
+          if (ky >= a.cy1 && ky <= a.cy2) { m |= 1u << f; break; }
+        }
+      a.fkeep = m;
+    }
+  }
   a.hzx = (p->pad == 2 && r0x == 16 && (a.Px % 16) == 0 && a.ox * 4 == a.Px && a.hx * 2 == a.Px) ? 1 : 0;
   a.hzy = (p->pad == 2 && r0y == 16 && (a.Py % 16) == 0 && a.oy * 4 == a.Py && a.hy * 2 == a.Py) ? 1 : 0;
   const size_t smem_col = Wfast ? (size_t)col_layout(a.Py, a.pny, W, occ_stride, su.n_entries, col_tab).total

@@ -296,6 +296,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
         if constexpr (horner) {
 #pragma unroll
           for (int f = 0; f < RL; ++f) {
+            if (!((a.fkeep >> f) & 1u)) continue;         // outside the SSB crop for every b
             const C d = dsm[(b * RL + f) * W + w];
             const C t = acc[kb][f];
             acc[kb][f] = make_float2(fmaf(t.x, d.x, fmaf(-t.y, d.y, x[f].x)), fmaf(t.x, d.y, fmaf(t.y, d.x, x[f].y)));
@@ -305,6 +306,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
         const C ex = exw[w];
 #pragma unroll
         for (int f = 0; f < RL; ++f) {
+          if (!((a.fkeep >> f) & 1u)) continue;           // outside the SSB crop for every b
           const int p = b * RL + f;
           // H = C Ex exp(i (pi lambda z' fy^2 + k z' g)), both phase parts reduced
           float ph = fmaf(kz, gsm[p * W + w], eth[p]);
