@@ -500,7 +500,10 @@ __global__ void __launch_bounds__(256) dm_out_pass(DMArgs<R> a) {
   }
   for (int c = threadIdx.x; c < a.pnx; c += blockDim.x) {
     int m = a.ox + c - a.hx; if (m < 0) m += a.Px;
-    C h = buf[a.plx.perm[m]];
+    int pm;
+    if constexpr (NX > 0) pm = FastSched<NX>::perm(m);
+    else pm = a.plx.perm[m];
+    C h = buf[pm];
     if (a.sig_x != 0) h = cmul(h, a.shx[c]);
     a.fringe[(size_t)yl * a.pnx + c] = h.x;
     if (a.field) a.field[(size_t)yl * a.pnx + c] = h;

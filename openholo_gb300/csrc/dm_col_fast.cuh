@@ -373,7 +373,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
     const int yl = idx / W, w = idx - yl * W;
     int m = a.oy + yl - a.hy;
     if (m < 0) m += NY;
-    a.V[(size_t)yl * a.Px + kx0 + w] = cmul(buf[a.ply.perm[m] * W + w], a.shy[yl]);
+    a.V[(size_t)yl * a.Px + kx0 + w] = cmul(buf[FastSched<NY>::perm(m) * W + w], a.shy[yl]);
   }
 }
 

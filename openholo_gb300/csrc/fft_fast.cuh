@@ -390,6 +390,33 @@ struct SchedImpl {
   __device__ __forceinline__ static void run_rest(C* buf, int nl, int ls, int es, const TW& tw, bool lf) {
     if constexpr (sizeof...(Rest) > 0) fstages_t<N, N / R0, SGN, C, TW, Rest...>(buf, nl, ls, es, tw, lf);
   }
+  // Output order of this schedule as arithmetic (the plan's perm / iperm
+  // tables): X[k], k = f0 + r0 f1 + r0 r1 f2 + ..., sits at position
+  // sum_s f_s N / (r0 ... r_s).
+  __host__ __device__ __forceinline__ static constexpr int perm(int k) {
+    constexpr int rs[] = {R0, Rest...};
+    int pos = 0, q = N;
+#pragma unroll
+    for (int s = 0; s < nstages; ++s) {
+      q /= rs[s];
+      pos += (k % rs[s]) * q;
+      k /= rs[s];
+    }
+    return pos;
+  }
+  __host__ __device__ __forceinline__ static constexpr int iperm(int pos) {
+    constexpr int rs[] = {R0, Rest...};
+    int k = 0, mul = 1, q = N;
+#pragma unroll
+    for (int s = 0; s < nstages; ++s) {
+      q /= rs[s];
+      const int f = pos / q;
+      pos -= f * q;
+      k += f * mul;
+      mul *= rs[s];
+    }
+    return k;
+  }
   // entries of the stage-1 twiddle table (fill_stage_tab<N, r1, N / r0>)
   static constexpr int tab1_entries = (N / R0 / r1) * (r1 - 1);
   // as run_rest, with stage 1's twiddles from its table tab1

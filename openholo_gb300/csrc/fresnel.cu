@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(FrColCfg<NY>::T, FrColCfg<NY>::MINB) fr_col(Fr
       const C hx = hxw[w];
 #pragma unroll
       for (int f = 0; f < RL; ++f) {
-        const int v = __ldg(a.iperm_y + b * RL + f);
+        const int v = FastSched<NY>::iperm(b * RL + f);
         acc[kb][f] = cmul(x[f], cmul(hx, __ldg(a.hys + v)));
       }
     }
@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(FrColCfg<NY>::T, FrColCfg<NY>::MINB) fr_col(Fr
     if (bb < CF::NBL) {
       const int b = bb / W, w = bb - b * W;
 #pragma unroll
-      for (int f = 0; f < RL; ++f) buf[__ldg(a.iperm_y + b * RL + f) * W + w] = acc[kb][f];
+      for (int f = 0; f < RL; ++f) buf[FastSched<NY>::iperm(b * RL + f) * W + w] = acc[kb][f];
     }
   }
   FastSched<NY>::template run_t<1>(buf, W, 1, W, tw, true);
@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(FrColCfg<NY>::T, FrColCfg<NY>::MINB) fr_col(Fr
   // crop: output row r is the inverse transform's sample QY + r
   for (int idx = tid; idx < ny * W; idx += T) {
     const int r = idx / W, w = idx - r * W;
-    strip[idx] = buf[__ldg(a.perm_y + QY + r) * W + w];
+    strip[idx] = buf[FastSched<NY>::perm(QY + r) * W + w];
   }
 }
 
@@ -296,7 +296,7 @@ __global__ void __launch_bounds__(256 * ROWS) fr_row_inv(FrArgs a) {
   for (int idx = threadIdx.x; idx < ROWS * NX; idx += blockDim.x) {
     const int w = idx % kFrW, l = (idx / kFrW) % ROWS, s = idx / (ROWS * kFrW);
     const int p = s * kFrW + w;
-    buf[l * NX + __ldg(a.iperm_x + p)] = a.R[((size_t)s * a.ny + r0 + l) * kFrW + w];
+    buf[l * NX + FastSched<NX>::iperm(p)] = a.R[((size_t)s * a.ny + r0 + l) * kFrW + w];
   }
   const TwSplit<C> tw{twlo, twhi};
   FastSched<NX>::template run_t<1>(buf, ROWS, NX, 1, tw, false);
@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(256 * ROWS) fr_row_inv(FrArgs a) {
   const int nx = a.nx;
   for (int idx = threadIdx.x; idx < ROWS * nx; idx += blockDim.x) {
     const int l = idx / nx, c = idx - l * nx;
-    dst[(size_t)l * nx + c] = buf[l * NX + __ldg(a.perm_x + Q + c)];
+    dst[(size_t)l * nx + c] = buf[l * NX + FastSched<NX>::perm(Q + c)];
   }
 }
 
