@@ -10,7 +10,9 @@
 // window (w varies per point) is added with float2/double2 atomics.  FP32
 // evaluates k r as k dz (reduced mod 2 pi in double, once per point) +
 // k rho^2/(|r| + |dz|) (at most tens of rad, exact in float to ~1e-5 rad).
+#include <cuda_bf16.h>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include "context.h"
 #include "fft_kernels.cuh"
@@ -83,14 +85,19 @@ constexpr int kWrpTile = 64;
 
 // Per point: window centre and half-width; exact-path terms (base = k|dz|
 // reduced to radians); the FP64 path's dz; and, when the window is paraxial
-// enough (series = 1), the polynomial coefficients of the series evaluation
-// below in u = rho^2 / dz^2 = (wx sx)^2 + (wy sx)^2, sx = dp / |dz|.
+// enough (series >= 1), the polynomial coefficients of the series evaluation
+// below in u = rho^2 / dz^2 = ux + uy, ux = (wx sx)^2, uy = (wy sx)^2,
+// sx = dp / |dz|.  series = 2 marks windows that are also separable to
+// within the bounds of the tensor-core form (wrp_tc):
+//   e^{2 pi i phase} amp = a0 e^{2 pi i (base_t + fy)} Ay  e^{2 pi i fx} Ax  (1 + i kappa ux uy),
+//   f(u) = u (c1 + u (c2 + u c3)),  A(u) = 1 + u (alpha + u beta),  kappa = 2 pi 2 c2.
 struct WrpPt {
   int tx, ty, w, series;
   float base, adz, sgn, sx;
   float base_t, c1, c2, c3;          // phase in turns: base_t + u (c1 + u (c2 + u c3))
-  float a0c, a1c, a2c, pad0;         // amplitude: a0c + u (a1c + u a2c)
-  double dz, pad1;
+  float a0c, a1c, a2c, kappa;        // amplitude: a0c + u (a1c + u a2c); cross-term factor (rad)
+  double dz;
+  float alpha, beta;                 // per-axis amplitude factors: a1c / a0c, a2c / a0c
 };
 
 __device__ __forceinline__ void wrp_point(const WRPGeom& g, const double* xyz, int k, WrpPt* o) {
@@ -135,29 +142,60 @@ __device__ __forceinline__ void wrp_point(const WRPGeom& g, const double* xyz, i
   o->a0c = (float)ia0;
   o->a1c = (float)(-ia0 * ea * 0.5);
   o->a2c = (float)(ia0 * (ea * 0.125 + ea * ea * 0.25));
-  o->pad0 = 0.f;
-  o->pad1 = 0.0;
+  // separable form: the dropped terms at the window corner (ux = uy = (w sx)^2)
+  //   phase cross term to second order (kappa ux uy)^2 / 2, the c3 cross terms
+  //   2 pi 3 c3 ux uy (ux + uy), the amplitude cross term (alpha^2 - 2 beta) ux uy
+  const double two_pi_d = 6.283185307179586476925286766559;
+  const double al = -ea * 0.5, be = ea * 0.125 + ea * ea * 0.25;
+  const double kap = two_pi_d * 2.0 * (sg * turns * -0.125);
+  const double uc = adz > 0.0 ? (double)g.fixed_w * g.fixed_w * (double)dpx * dpx / (adz * adz) : 1.0;
+  const double t1 = kap * uc * uc, t2 = two_pi_d * 3.0 * fabs(sg * turns * 0.0625) * uc * uc * 2.0 * uc;
+  const double t3 = fabs(al * al - 2.0 * be) * uc * uc;
+  if (o->series && g.fixed_w > 0 && 0.5 * t1 * t1 < 3e-5 && t2 < 1e-5 && t3 < 1e-6) o->series = 2;
+  o->kappa = (float)kap;
+  o->alpha = (float)al;
+  o->beta = (float)be;
 }
 
-// tile index range [t0, t1] along one axis for the window [c - w, c + w) clipped to [0, n)
-__device__ __forceinline__ bool wrp_tile_range(int c, int w, int n, int* t0, int* t1) {
+// Two binnings share one count / start / list layout: 64 x 64 tiles for the
+// direct tile kernels (bins [0, nd)) and, for points the tensor-core form
+// takes (series == 2 and use_tc), 64-column x 128-row regions (bins
+// [nd, nd + regions)).
+constexpr int kTcW = 64, kTcH = 128;
+
+struct WrpBins {
+  int tiles_x, nd;          // direct tiles across, direct bin count
+  int regions_x;            // tensor regions across
+  int use_tc;
+};
+
+// bin index range [t0, t1] along one axis for the window [c - w, c + w) clipped to [0, n)
+__device__ __forceinline__ bool wrp_bin_range(int c, int w, int n, int size, int* t0, int* t1) {
   const int lo = max(c - w, 0), hi = min(c + w, n);
   if (lo >= hi) return false;
-  *t0 = lo / kWrpTile;
-  *t1 = (hi - 1) / kWrpTile;
+  *t0 = lo / size;
+  *t1 = (hi - 1) / size;
   return true;
 }
 
+// calls f(bin) for every bin the point's window touches
+template <class F>
+__device__ __forceinline__ void wrp_for_bins(const WRPGeom& g, const WrpBins& b, const WrpPt& q, F f) {
+  const bool tc = b.use_tc && q.series == 2;
+  const int bw = tc ? kTcW : kWrpTile, bh = tc ? kTcH : kWrpTile;
+  int x0, x1, y0, y1;
+  if (!wrp_bin_range(q.tx, q.w, g.nx, bw, &x0, &x1) || !wrp_bin_range(q.ty, q.w, g.ny, bh, &y0, &y1)) return;
+  for (int ty = y0; ty <= y1; ++ty)
+    for (int tx = x0; tx <= x1; ++tx) f(tc ? b.nd + ty * b.regions_x + tx : ty * b.tiles_x + tx);
+}
+
 __global__ void wrp_prep(WRPGeom g, const double* __restrict__ xyz, int n, WrpPt* __restrict__ pts,
-                         int* __restrict__ count, int tiles_x) {
+                         int* __restrict__ count, WrpBins bins) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     WrpPt q;
     wrp_point(g, xyz, k, &q);
     pts[k] = q;
-    int x0, x1, y0, y1;
-    if (!wrp_tile_range(q.tx, q.w, g.nx, &x0, &x1) || !wrp_tile_range(q.ty, q.w, g.ny, &y0, &y1)) continue;
-    for (int ty = y0; ty <= y1; ++ty)
-      for (int tx = x0; tx <= x1; ++tx) atomicAdd(&count[ty * tiles_x + tx], 1);
+    wrp_for_bins(g, bins, q, [&](int t) { atomicAdd(&count[t], 1); });
   }
 }
 
@@ -182,13 +220,10 @@ __global__ void wrp_scan(const int* __restrict__ count, int* __restrict__ start,
 }
 
 __global__ void wrp_fill(WRPGeom g, const WrpPt* __restrict__ pts, int n, int* __restrict__ cursor,
-                         int* __restrict__ list, int tiles_x) {
+                         int* __restrict__ list, WrpBins bins) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const WrpPt q = pts[k];
-    int x0, x1, y0, y1;
-    if (!wrp_tile_range(q.tx, q.w, g.nx, &x0, &x1) || !wrp_tile_range(q.ty, q.w, g.ny, &y0, &y1)) continue;
-    for (int ty = y0; ty <= y1; ++ty)
-      for (int tx = x0; tx <= x1; ++tx) list[atomicAdd(&cursor[ty * tiles_x + tx], 1)] = k;
+    wrp_for_bins(g, bins, q, [&](int t) { list[atomicAdd(&cursor[t], 1)] = k; });
   }
 }
 
@@ -298,6 +333,7 @@ __global__ void __launch_bounds__(256) wrp_tile_f32(WRPGeom g, const WrpPt* __re
   const float kf = (float)(2.0 * M_PI / g.lambda);
   const int X = X0 + c;
   const int b = start[tile], e = start[tile + 1];
+  if (b == e) return;                               // no window reaches this tile
   for (int c0 = b; c0 < e; c0 += kWrpChunk) {
     const int nc = min(kWrpChunk, e - c0);
     __syncthreads();                                  // the previous chunk is consumed
@@ -370,6 +406,306 @@ __global__ void __launch_bounds__(256) wrp_tile_f32(WRPGeom g, const WrpPt* __re
       v.y += acc[j].y;
       *d = v;
     }
+  }
+}
+
+// ---- tensor-core form of the fixed-window sum (series == 2 points) ---------
+// Over a 128-row x 64-column plane region, the separable windows make the sum
+//   W[y][x] = sum_p L0_p[y] R0_p[x] + L1_p[y] R1_p[x],
+//   L0 = a0 e^{2 pi i (base_t + f(uy))} A(uy),  L1 = uy L0,
+//   R0 = e^{2 pi i f(ux)} A(ux),                R1 = i kappa ux R0
+// (zero outside each window) a complex matrix product with K = 2 per point.
+// Embedded in reals as in the point-sum GEMM (K column 2k / 2k+1 = Re / Im of
+// term k; B rows 2x / 2x+1 give Re / Im of column x), C = A B^T is the
+// region's complex64 sum, M = 128, N = 128, K = 4 per point.  BF16 high and
+// low parts, three products (Ahi Bhi + Ahi Blo + Alo Bhi), FP32 in TMEM.
+//
+// One CTA per region, 256 threads.  Warps 1-7 write the operands of 8 points
+// (K = 32) per stage straight into shared memory, in the layout a TMA load
+// with 64-byte swizzle would give, then arrive on the stage's full barrier;
+// thread 0 issues tcgen05.mma (M 128, N 128, K 16) and releases stages with
+// tcgen05.commit; warps 4-7 read the accumulator (tcgen05.ld) and add the
+// region into the plane.  Waits are bounded: on timeout the CTA sets the
+// device error word, skips the add, waits for its MMAs and frees TMEM.
+namespace tcw {
+
+constexpr int kRows = kTcH, kCols = kTcW;             // region
+constexpr int kBK = 32, kPts = kBK / 4, kStages = 3;
+constexpr int kTile = 128 * kBK * 2;                   // 8 KB: 128 rows x 32 BF16
+constexpr int kStageBytes = 4 * kTile;                 // Ahi, Alo, Bhi, Blo
+constexpr int kTmemCols = 128;
+constexpr int kThreads = 256, kProducerWarps = 7;
+constexpr int kSmemBytes = kStages * kStageBytes + 1024 + 256;
+constexpr long long kWaitCycles = 2000000000LL;
+
+__device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mb_init(uint64_t* b, uint32_t n) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(n) : "memory");
+}
+__device__ __forceinline__ void mb_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
+}
+__device__ __forceinline__ bool mb_try(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(su32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mb_wait(uint64_t* b, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mb_try(b, parity)) {
+    if (clock64() - t0 > kWaitCycles) return false;
+  }
+  return true;
+}
+// K-major tile, rows of 32 BF16 (64 bytes), 64-byte swizzle, 8-row atoms 512 bytes apart
+__device__ __forceinline__ uint64_t sw_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)((8 * kBK * 2) >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)4 << 61;
+  return d;
+}
+// kind::f16, D FP32, A and B BF16, K-major, N = 128, M = 128
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(128 >> 3) << 17) |
+                            ((uint32_t)(128 >> 4) << 24);
+__device__ __forceinline__ void umma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t accum) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(accum)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Byte offset of point slot j (4 BF16 = 8 bytes) in row r of a [128][32] BF16
+// tile with 64-byte swizzle: 16-byte chunk c of the row lands at c ^ ((r >> 1) & 3).
+__device__ __forceinline__ int sw_off(int r, int j) {
+  return r * 64 + (((j >> 1) ^ ((r >> 1) & 3)) << 4) + ((j & 1) << 3);
+}
+
+// BF16 high / low parts of four values, written as 8 bytes each
+__device__ __forceinline__ void put4(unsigned char* hi, unsigned char* lo, int off, float a, float b, float c,
+                                     float d) {
+  const __nv_bfloat162 h0 = __floats2bfloat162_rn(a, b), h1 = __floats2bfloat162_rn(c, d);
+  const __nv_bfloat162 l0 = __floats2bfloat162_rn(a - __low2float(h0), b - __high2float(h0));
+  const __nv_bfloat162 l1 = __floats2bfloat162_rn(c - __low2float(h1), d - __high2float(h1));
+  uint2 vh, vl;
+  vh.x = *reinterpret_cast<const uint32_t*>(&h0);
+  vh.y = *reinterpret_cast<const uint32_t*>(&h1);
+  vl.x = *reinterpret_cast<const uint32_t*>(&l0);
+  vl.y = *reinterpret_cast<const uint32_t*>(&l1);
+  *reinterpret_cast<uint2*>(hi + off) = vh;
+  *reinterpret_cast<uint2*>(lo + off) = vl;
+}
+
+__device__ __forceinline__ float frac_turns(float f) { return f - rintf(f); }
+
+// the fields of a point record the operand builders use (held in registers)
+struct Rec {
+  int tx, ty, w;
+  float sx, base_t, c1, c2, c3, a0c, alpha, beta, kappa;
+};
+__device__ __forceinline__ Rec load_rec(const WrpPt* __restrict__ pts, const int* __restrict__ list, int k, int e) {
+  Rec r;
+  if (k < e) {
+    const WrpPt* q = pts + __ldg(list + k);
+    r.tx = q->tx; r.ty = q->ty; r.w = q->w;
+    r.sx = q->sx; r.base_t = q->base_t; r.c1 = q->c1; r.c2 = q->c2; r.c3 = q->c3;
+    r.a0c = q->a0c; r.alpha = q->alpha; r.beta = q->beta; r.kappa = q->kappa;
+  } else {
+    r.tx = r.ty = 0; r.w = 0;                       // empty slot: every item writes zeros
+    r.sx = r.base_t = r.c1 = r.c2 = r.c3 = r.a0c = r.alpha = r.beta = r.kappa = 0.f;
+  }
+  return r;
+}
+
+}  // namespace tcw
+
+__global__ void __launch_bounds__(tcw::kThreads, 2) wrp_tc(WRPGeom g, const WrpPt* __restrict__ pts,
+                                                           const int* __restrict__ start,
+                                                           const int* __restrict__ list, int regions_x,
+                                                           float2* __restrict__ wrp, int* err) {
+  using namespace tcw;
+  extern __shared__ unsigned char smem_raw[];
+  const uint32_t raw = su32(smem_raw);
+  unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base + kStages * kStageBytes);
+  uint64_t* full = bars;                 // [kStages], one arrival per producer warp
+  uint64_t* empty = bars + kStages;      // [kStages], tcgen05.commit
+  uint64_t* done = bars + 2 * kStages;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kStages + 1);
+  int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int region = blockIdx.x;
+  const int X0 = (region % regions_x) * kCols, Y0 = (region / regions_x) * kRows;
+  const int b = start[region], e = start[region + 1];
+  if (b == e) return;                    // uniform: no window reaches this region
+  const int npts = e - b;
+  const int nst = (npts + kPts - 1) / kPts;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) { mb_init(&full[s], kProducerWarps); mb_init(&empty[s], 1); }
+    mb_init(done, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp >= 1) {
+    // producers: 224 threads, 1536 items per stage (A: 8 points x 128 rows,
+    // B: 8 points x 64 columns, each writing rows 2x and 2x+1).  Item i takes
+    // point slot i & 7, and 224 is a multiple of 8, so a thread always works
+    // on slot j = pt & 7: its record sits in registers, the next stage's is
+    // loaded while this stage is built.
+    const int pt = threadIdx.x - 32;
+    const int j = pt & (kPts - 1);
+    Rec q = load_rec(pts, list, b + j, e);
+    for (int it = 0; it < nst; ++it) {
+      const int s = it % kStages;
+      const uint32_t ph = (uint32_t)((it / kStages) & 1);
+      bool ok = true;
+      if (lane == 0) ok = mb_wait(&empty[s], ph ^ 1u) && !*((volatile int*)abort_flag);
+      ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+      if (!ok) {
+        if (lane == 0) atomicExch(abort_flag, 1);
+        break;
+      }
+      unsigned char* sAh = base + s * kStageBytes;
+      unsigned char* sAl = sAh + kTile;
+      unsigned char* sBh = sAh + 2 * kTile;
+      unsigned char* sBl = sAh + 3 * kTile;
+      const Rec qn = load_rec(pts, list, b + (it + 1) * kPts + j, e);
+      for (int item = pt; item < kPts * (kRows + kCols); item += kProducerWarps * 32) {
+        if (item < kPts * kRows) {
+          const int r = item >> 3;
+          float v0 = 0.f, v1 = 0.f, v2 = 0.f, v3 = 0.f;
+          {
+            const int Y = Y0 + r, wy = Y - q.ty;
+            if (Y < g.ny && wy >= -q.w && wy < q.w) {
+              const float ys = (float)wy * q.sx, uy = ys * ys;
+              const float f = frac_turns(fmaf(uy, fmaf(uy, fmaf(uy, q.c3, q.c2), q.c1), q.base_t));
+              float sn, cs;
+              __sincosf(6.28318530717958647692f * f, &sn, &cs);
+              const float amp = q.a0c * fmaf(uy, fmaf(uy, q.beta, q.alpha), 1.f);
+              v0 = amp * cs; v1 = amp * sn; v2 = uy * v0; v3 = uy * v1;
+            }
+          }
+          put4(sAh, sAl, sw_off(r, j), v0, v1, v2, v3);
+        } else {
+          const int x = (item - kPts * kRows) >> 3;
+          float r0x = 0.f, r0y = 0.f, r1x = 0.f, r1y = 0.f;
+          {
+            const int X = X0 + x, wx = X - q.tx;
+            if (X < g.nx && wx >= -q.w && wx < q.w) {
+              const float xs = (float)wx * q.sx, ux = xs * xs;
+              const float f = frac_turns(ux * fmaf(ux, fmaf(ux, q.c3, q.c2), q.c1));
+              float sn, cs;
+              __sincosf(6.28318530717958647692f * f, &sn, &cs);
+              const float amp = fmaf(ux, fmaf(ux, q.beta, q.alpha), 1.f);
+              r0x = amp * cs; r0y = amp * sn;
+              const float kx = q.kappa * ux;
+              r1x = -kx * r0y; r1y = kx * r0x;        // i kappa ux R0
+            }
+          }
+          put4(sBh, sBl, sw_off(2 * x, j), r0x, -r0y, r1x, -r1y);
+          put4(sBh, sBl, sw_off(2 * x + 1, j), r0y, r0x, r1y, r1x);
+        }
+      }
+      // generic-proxy writes -> visible to the tensor core's async proxy
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mb_arrive(&full[s]);
+      q = qn;
+    }
+  } else if (threadIdx.x == 0) {
+    // MMA issuer
+    for (int it = 0; it < nst; ++it) {
+      const int s = it % kStages;
+      const uint32_t ph = (uint32_t)((it / kStages) & 1);
+      if (!mb_wait(&full[s], ph) || *((volatile int*)abort_flag)) {
+        atomicExch(abort_flag, 1);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      unsigned char* st0 = base + s * kStageBytes;
+      const uint64_t ah = sw_desc(su32(st0)), al = sw_desc(su32(st0 + kTile));
+      const uint64_t bh = sw_desc(su32(st0 + 2 * kTile)), bl = sw_desc(su32(st0 + 3 * kTile));
+#pragma unroll
+      for (int kk = 0; kk < kBK / 16; ++kk) {
+        const uint64_t adv = (uint64_t)((kk * 32) >> 4);
+        umma(tmem, ah + adv, bh + adv, (it | kk) ? 1u : 0u);
+        umma(tmem, ah + adv, bl + adv, 1u);
+        umma(tmem, al + adv, bh + adv, 1u);
+      }
+      umma_commit(&empty[s]);
+    }
+    umma_commit(done);                   // arrives when every MMA issued above has completed
+  }
+  // epilogue: warps 4-7 own TMEM lanes 32 (warp - 4) .. + 31 = region rows
+  __syncwarp();
+  bool ok_done = true;
+  if (warp >= 4) ok_done = mb_wait(done, 0);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const bool good = __syncthreads_and(ok_done && !*((volatile int*)abort_flag));
+  if (good && warp >= 4) {
+    const int r = 32 * (warp - 4) + lane;
+    const int Y = Y0 + r;
+#pragma unroll 1
+    for (int c = 0; c < 2 * kCols / 32; ++c) {
+      uint32_t v[32];
+      tmem_ld32(tmem + ((uint32_t)(32 * (warp - 4)) << 16) + (uint32_t)(c * 32), v);
+      if (Y < g.ny) {
+        float2* dst = wrp + (size_t)Y * g.nx + X0 + 16 * c;
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          if (X0 + 16 * c + q < g.nx) {
+            float2 o = dst[q];
+            o.x += __uint_as_float(v[2 * q]);
+            o.y += __uint_as_float(v[2 * q + 1]);
+            dst[q] = o;
+          }
+        }
+      }
+    }
+  } else if (!good && threadIdx.x == 0) {
+    atomicOr(err, 4);
+  }
+  // the MMAs must have finished reading shared memory and TMEM before exit
+  if (!good && threadIdx.x == 0) mb_wait(done, 0);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
   }
 }
 
@@ -460,16 +796,34 @@ oh_status oh_wrp_accumulate(oh_ctx* ctx, oh_precision prec, const oh_wrp_params*
   if (n_points == 0) return OH_OK;
   WRPGeom g{p->nx, p->ny, p->pitch, p->lambda, p->z_wrp, p->window};
   const int tiles_x = (p->nx + kWrpTile - 1) / kWrpTile, tiles_y = (p->ny + kWrpTile - 1) / kWrpTile;
-  const int span = p->window > 0 ? (2 * p->window + kWrpTile - 1) / kWrpTile + 1 : 0;  // tiles per axis a window touches
-  const size_t cap = (size_t)n_points * std::min(span, tiles_x) * std::min(span, tiles_y);
+  const int regions_x = (p->nx + kTcW - 1) / kTcW, regions_y = (p->ny + kTcH - 1) / kTcH;
+  // bins a window touches per axis: direct tiles, tensor regions
+  const int span = p->window > 0 ? (2 * p->window + kWrpTile - 1) / kWrpTile + 1 : 0;
+  const int span_rx = p->window > 0 ? (2 * p->window + kTcW - 1) / kTcW + 1 : 0;
+  const int span_ry = p->window > 0 ? (2 * p->window + kTcH - 1) / kTcH + 1 : 0;
+  const size_t cap_d = (size_t)std::min(span, tiles_x) * std::min(span, tiles_y);
+  const size_t cap_t = (size_t)std::min(span_rx, regions_x) * std::min(span_ry, regions_y);
+  const size_t cap = (size_t)n_points * std::max(cap_d, cap_t);
   if (p->window > 0 && p->window < (1 << 28) && cap < (size_t)INT32_MAX) {
-    // fixed windows: binned, tiled accumulation
-    const int ntiles = tiles_x * tiles_y;
+    // fixed windows: binned, tiled accumulation; in FP32 the separable points
+    // go to the tensor-core form (OH_WRP_ENGINE=direct keeps every point on
+    // the direct tile kernel)
+    bool use_tc = prec != OH_FP64;
+    if (const char* ev = std::getenv("OH_WRP_ENGINE")) use_tc = use_tc && std::strcmp(ev, "direct") != 0;
+    if (use_tc) {
+      int dev = 0, major = 0, minor = 0;
+      OH_CUDA_TRY(cudaGetDevice(&dev));
+      OH_CUDA_TRY(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+      OH_CUDA_TRY(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
+      use_tc = major == 10 && minor == 3;
+    }
+    const int ntiles = tiles_x * tiles_y, nregions = regions_x * regions_y;
+    const int nbins = ntiles + (use_tc ? nregions : 0);
     void* ptr;
     const size_t off_cnt = ((size_t)n_points * sizeof(WrpPt) + 255) & ~(size_t)255;
-    const size_t off_start = off_cnt + (((size_t)ntiles * 4 + 255) & ~(size_t)255);
-    const size_t off_cur = off_start + (((size_t)(ntiles + 1) * 4 + 255) & ~(size_t)255);
-    const size_t off_list = off_cur + (((size_t)ntiles * 4 + 255) & ~(size_t)255);
+    const size_t off_start = off_cnt + (((size_t)nbins * 4 + 255) & ~(size_t)255);
+    const size_t off_cur = off_start + (((size_t)(nbins + 1) * 4 + 255) & ~(size_t)255);
+    const size_t off_list = off_cur + (((size_t)nbins * 4 + 255) & ~(size_t)255);
     OH_TRY(scratch(ctx, "wrp.bins", off_list + cap * sizeof(int), &ptr));
     char* base = (char*)ptr;
     WrpPt* pts = (WrpPt*)base;
@@ -477,18 +831,30 @@ oh_status oh_wrp_accumulate(oh_ctx* ctx, oh_precision prec, const oh_wrp_params*
     int* start = (int*)(base + off_start);
     int* cur = (int*)(base + off_cur);
     int* list = (int*)(base + off_list);
+    const WrpBins bins{tiles_x, ntiles, regions_x, use_tc ? 1 : 0};
+    if (use_tc)
+      OH_CUDA_TRY(cudaFuncSetAttribute(wrp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tcw::kSmemBytes));
     KernelTimer kt(ctx, "wrp_accumulate", st);
-    OH_CUDA_TRY(cudaMemsetAsync(cnt, 0, (size_t)ntiles * 4, st));
+    OH_CUDA_TRY(cudaMemsetAsync(cnt, 0, (size_t)nbins * 4, st));
     const int g1 = std::min((n_points + 255) / 256, 152 * 8);
-    wrp_prep<<<g1, 256, 0, st>>>(g, xyz, n_points, pts, cnt, tiles_x);
+    wrp_prep<<<g1, 256, 0, st>>>(g, xyz, n_points, pts, cnt, bins);
     OH_LAUNCH_CHECK();
-    wrp_scan<<<1, 1024, 0, st>>>(cnt, start, cur, ntiles);
+    wrp_scan<<<1, 1024, 0, st>>>(cnt, start, cur, nbins);
     OH_LAUNCH_CHECK();
-    wrp_fill<<<g1, 256, 0, st>>>(g, pts, n_points, cur, list, tiles_x);
+    wrp_fill<<<g1, 256, 0, st>>>(g, pts, n_points, cur, list, bins);
     OH_LAUNCH_CHECK();
-    if (prec == OH_FP64) wrp_tile<double><<<ntiles, 256, 0, st>>>(g, pts, start, list, tiles_x, (double2*)wrp);
-    else wrp_tile_f32<<<ntiles, 256, 0, st>>>(g, pts, start, list, tiles_x, (float2*)wrp);
-    OH_LAUNCH_CHECK();
+    if (use_tc) {
+      KernelTimer kt2(ctx, "wrp_tc", st);
+      wrp_tc<<<nregions, tcw::kThreads, tcw::kSmemBytes, st>>>(g, pts, start + ntiles, list, regions_x,
+                                                              (float2*)wrp, ctx->dev_err);
+      OH_LAUNCH_CHECK();
+    }
+    {
+      KernelTimer kt3(ctx, "wrp_tile", st);
+      if (prec == OH_FP64) wrp_tile<double><<<ntiles, 256, 0, st>>>(g, pts, start, list, tiles_x, (double2*)wrp);
+      else wrp_tile_f32<<<ntiles, 256, 0, st>>>(g, pts, start, list, tiles_x, (float2*)wrp);
+      OH_LAUNCH_CHECK();
+    }
     return OH_OK;
   }
   const int grid = std::min(n_points, 152 * 32);

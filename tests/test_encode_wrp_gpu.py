@@ -90,6 +90,84 @@ def test_wrp_accumulate(ctx, fixed_w, precision, plane, gap):
     assert np.linalg.norm(w.cpu().numpy() - ref) <= tol * np.linalg.norm(ref)
 
 
+def _wrp_run(ctx, pts, nx, ny, dp, lam, z, w, engine=None, kernels=None):
+    """One oh_wrp_accumulate call; `kernels` (a set) receives the names of the
+    library's timed kernels that ran."""
+    import os
+    p = WrpParams(nx, ny, dp, lam, z, w)
+    tp = torch.from_numpy(pts).cuda()
+    out = torch.zeros((ny, nx), dtype=torch.complex64, device="cuda")
+    old = os.environ.get("OH_WRP_ENGINE")
+    if engine:
+        os.environ["OH_WRP_ENGINE"] = engine
+    try:
+        ctx.set_timing(True)
+        ctx.read_timing(reset=True)
+        _lib.call("oh_wrp_accumulate", ctx.handle, 0, C.byref(p), C.c_void_p(tp.data_ptr()), pts.shape[0],
+                  C.c_void_p(out.data_ptr()), S())
+        torch.cuda.synchronize()
+        if kernels is not None:
+            kernels.update(ctx.read_timing(reset=True).keys())
+    finally:
+        ctx.set_timing(False)
+        if engine:
+            if old is None:
+                del os.environ["OH_WRP_ENGINE"]
+            else:
+                os.environ["OH_WRP_ENGINE"] = old
+    from openholo_gb300._lib import lib
+    assert lib().oh_ctx_device_status(ctx.handle, S()) == 0
+    return out.cpu().numpy()
+
+
+@pytest.mark.parametrize("plane,npts,w,gap", [((300, 170), 1500, 24, 5e-3), ((257, 200), 900, 32, -6e-3),
+                                             ((64, 300), 400, 16, 8e-3)])
+def test_wrp_tensor_form(ctx, plane, npts, w, gap):
+    """Fixed windows far enough from the points to be separable run as the
+    tcgen05 GEMM (BF16 hi/lo, rank-2 separable terms): against the FP64
+    oracle and against the direct FP32 tile kernel.  Windows straddle the
+    128 x 64 regions and the plane's edges; some centres lie outside."""
+    nx, ny = plane
+    dp, lam = 3.74e-6, 532e-9
+    pts = scenes.wrp_scene(8, npts, box=(nx * 4.2e-6, ny * 4.2e-6, 1e-3), zc=0.01)
+    z = 0.01 - 0.5e-3 - gap if gap > 0 else 0.01 + 0.5e-3 - gap
+    ran, ran_direct = set(), set()
+    tc = _wrp_run(ctx, pts, nx, ny, dp, lam, z, w, kernels=ran)
+    direct = _wrp_run(ctx, pts, nx, ny, dp, lam, z, w, engine="direct", kernels=ran_direct)
+    assert "wrp_tc" in ran and "wrp_tc" not in ran_direct
+    ref = opc.wrp_f64(pts, nx, ny, dp, lam, z, w)
+    assert np.linalg.norm(tc - ref) <= 5e-5 * np.linalg.norm(ref)
+    assert np.linalg.norm(tc - direct) <= 5e-5 * np.linalg.norm(ref)
+
+
+def test_wrp_tensor_and_direct_points_mixed(ctx):
+    """Points near the plane (not separable: direct kernel) and far from it
+    (tensor form) in one call: both parts land in the same plane."""
+    nx, ny, dp, lam, w = 200, 180, 3.74e-6, 532e-9, 24
+    far = scenes.wrp_scene(9, 700, box=(nx * 4.2e-6, ny * 4.2e-6, 1e-3), zc=0.01)
+    near = scenes.wrp_scene(10, 300, box=(nx * 4.2e-6, ny * 4.2e-6, 0.2e-3), zc=0.0146)
+    pts = np.concatenate([far, near])
+    z = 0.015
+    ran = set()
+    got = _wrp_run(ctx, pts, nx, ny, dp, lam, z, w, kernels=ran)
+    assert "wrp_tc" in ran
+    ref = opc.wrp_f64(pts, nx, ny, dp, lam, z, w)
+    assert np.linalg.norm(got - ref) <= 5e-5 * np.linalg.norm(ref)
+
+
+def test_wrp_tensor_form_full_size(ctx):
+    """The 200,000-point, 3840 x 2160, 64 x 64 window workload: the tensor
+    form against the direct kernel (the oracle is too slow at this size)."""
+    nx, ny, dp, lam, w = 3840, 2160, 3.74e-6, 532e-9, 32
+    pts = scenes.wrp_scene(12, 200_000)
+    z = float(pts[:, 2].min()) - 5e-3
+    ran = set()
+    tc = _wrp_run(ctx, pts, nx, ny, dp, lam, z, w, kernels=ran)
+    direct = _wrp_run(ctx, pts, nx, ny, dp, lam, z, w, engine="direct")
+    assert "wrp_tc" in ran
+    assert np.linalg.norm(tc - direct) <= 5e-5 * np.linalg.norm(direct)
+
+
 @pytest.mark.parametrize("shape", [(64, 64), (48, 80)])
 def test_fresnel_propagate(ctx, shape):
     ny, nx = shape
