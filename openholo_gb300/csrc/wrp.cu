@@ -430,7 +430,7 @@ __global__ void __launch_bounds__(256) wrp_tile_f32(WRPGeom g, const WrpPt* __re
 namespace tcw {
 
 constexpr int kRows = kTcH, kCols = kTcW;             // region
-constexpr int kBK = 32, kPts = kBK / 4, kStages = 3;
+constexpr int kBK = 32, kPts = kBK / 4, kStages = 2;
 constexpr int kTile = 128 * kBK * 2;                   // 8 KB: 128 rows x 32 BF16
 constexpr int kStageBytes = 4 * kTile;                 // Ahi, Alo, Bhi, Blo
 constexpr int kTmemCols = 128;
@@ -519,6 +519,20 @@ __device__ __forceinline__ void put4(unsigned char* hi, unsigned char* lo, int o
 
 __device__ __forceinline__ float frac_turns(float f) { return f - rintf(f); }
 
+// BF16 high / low parts of (a, b, c, d) packed as two bf16x2 words each
+struct Split4 { uint32_t h01, h23, l01, l23; };
+__device__ __forceinline__ Split4 split4(float a, float b, float c, float d) {
+  const __nv_bfloat162 h0 = __floats2bfloat162_rn(a, b), h1 = __floats2bfloat162_rn(c, d);
+  const __nv_bfloat162 l0 = __floats2bfloat162_rn(a - __low2float(h0), b - __high2float(h0));
+  const __nv_bfloat162 l1 = __floats2bfloat162_rn(c - __low2float(h1), d - __high2float(h1));
+  Split4 r;
+  r.h01 = *reinterpret_cast<const uint32_t*>(&h0);
+  r.h23 = *reinterpret_cast<const uint32_t*>(&h1);
+  r.l01 = *reinterpret_cast<const uint32_t*>(&l0);
+  r.l23 = *reinterpret_cast<const uint32_t*>(&l1);
+  return r;
+}
+
 // the fields of a point record the operand builders use (held in registers)
 struct Rec {
   int tx, ty, w;
@@ -540,7 +554,7 @@ __device__ __forceinline__ Rec load_rec(const WrpPt* __restrict__ pts, const int
 
 }  // namespace tcw
 
-__global__ void __launch_bounds__(tcw::kThreads, 2) wrp_tc(WRPGeom g, const WrpPt* __restrict__ pts,
+__global__ void __launch_bounds__(tcw::kThreads, 3) wrp_tc(WRPGeom g, const WrpPt* __restrict__ pts,
                                                            const int* __restrict__ start,
                                                            const int* __restrict__ list, int regions_x,
                                                            float2* __restrict__ wrp, int* err) {
@@ -604,40 +618,42 @@ __global__ void __launch_bounds__(tcw::kThreads, 2) wrp_tc(WRPGeom g, const WrpP
       unsigned char* sBh = sAh + 2 * kTile;
       unsigned char* sBl = sAh + 3 * kTile;
       const Rec qn = load_rec(pts, list, b + (it + 1) * kPts + j, e);
+#pragma unroll 2
       for (int item = pt; item < kPts * (kRows + kCols); item += kProducerWarps * 32) {
         if (item < kPts * kRows) {
+          // branch-free: rows outside the window get amplitude 0
           const int r = item >> 3;
-          float v0 = 0.f, v1 = 0.f, v2 = 0.f, v3 = 0.f;
-          {
-            const int Y = Y0 + r, wy = Y - q.ty;
-            if (Y < g.ny && wy >= -q.w && wy < q.w) {
-              const float ys = (float)wy * q.sx, uy = ys * ys;
-              const float f = frac_turns(fmaf(uy, fmaf(uy, fmaf(uy, q.c3, q.c2), q.c1), q.base_t));
-              float sn, cs;
-              __sincosf(6.28318530717958647692f * f, &sn, &cs);
-              const float amp = q.a0c * fmaf(uy, fmaf(uy, q.beta, q.alpha), 1.f);
-              v0 = amp * cs; v1 = amp * sn; v2 = uy * v0; v3 = uy * v1;
-            }
-          }
-          put4(sAh, sAl, sw_off(r, j), v0, v1, v2, v3);
+          const int Y = Y0 + r, wy = Y - q.ty;
+          const bool in = Y < g.ny && wy >= -q.w && wy < q.w;
+          const float ys = (float)wy * q.sx, uy = ys * ys;
+          const float f = frac_turns(fmaf(uy, fmaf(uy, fmaf(uy, q.c3, q.c2), q.c1), q.base_t));
+          float sn, cs;
+          __sincosf(6.28318530717958647692f * f, &sn, &cs);
+          const float amp = in ? q.a0c * fmaf(uy, fmaf(uy, q.beta, q.alpha), 1.f) : 0.f;
+          const float v0 = amp * cs, v1 = amp * sn;
+          put4(sAh, sAl, sw_off(r, j), v0, v1, uy * v0, uy * v1);
         } else {
           const int x = (item - kPts * kRows) >> 3;
-          float r0x = 0.f, r0y = 0.f, r1x = 0.f, r1y = 0.f;
+          const int X = X0 + x, wx = X - q.tx;
+          const int o0 = sw_off(2 * x, j), o1 = sw_off(2 * x + 1, j);
           {
-            const int X = X0 + x, wx = X - q.tx;
-            if (X < g.nx && wx >= -q.w && wx < q.w) {
-              const float xs = (float)wx * q.sx, ux = xs * xs;
-              const float f = frac_turns(ux * fmaf(ux, fmaf(ux, q.c3, q.c2), q.c1));
-              float sn, cs;
-              __sincosf(6.28318530717958647692f * f, &sn, &cs);
-              const float amp = fmaf(ux, fmaf(ux, q.beta, q.alpha), 1.f);
-              r0x = amp * cs; r0y = amp * sn;
-              const float kx = q.kappa * ux;
-              r1x = -kx * r0y; r1y = kx * r0x;        // i kappa ux R0
-            }
+            const bool in = X < g.nx && wx >= -q.w && wx < q.w;
+            const float xs = (float)wx * q.sx, ux = xs * xs;
+            const float f = frac_turns(ux * fmaf(ux, fmaf(ux, q.c3, q.c2), q.c1));
+            float sn, cs;
+            __sincosf(6.28318530717958647692f * f, &sn, &cs);
+            const float amp = in ? fmaf(ux, fmaf(ux, q.beta, q.alpha), 1.f) : 0.f;
+            const float r0x = amp * cs, r0y = amp * sn;
+            const float kx = q.kappa * ux;
+            // R1 = i kappa ux R0; row 2x: (R0x, -R0y, R1x, -R1y), row 2x+1: (R0y, R0x, R1y, R1x),
+            // from one split of (R0x, R0y, R1x, R1y) by swapping halves and flipping signs
+            const Split4 v = split4(r0x, r0y, -kx * r0y, kx * r0x);
+            const uint32_t neg_hi = 0x80000000u;             // sign of the second BF16 of a pair
+            *reinterpret_cast<uint2*>(sBh + o0) = make_uint2(v.h01 ^ neg_hi, v.h23 ^ neg_hi);
+            *reinterpret_cast<uint2*>(sBl + o0) = make_uint2(v.l01 ^ neg_hi, v.l23 ^ neg_hi);
+            *reinterpret_cast<uint2*>(sBh + o1) = make_uint2(__byte_perm(v.h01, 0, 0x1032), __byte_perm(v.h23, 0, 0x1032));
+            *reinterpret_cast<uint2*>(sBl + o1) = make_uint2(__byte_perm(v.l01, 0, 0x1032), __byte_perm(v.l23, 0, 0x1032));
           }
-          put4(sBh, sBl, sw_off(2 * x, j), r0x, -r0y, r1x, -r1y);
-          put4(sBh, sBl, sw_off(2 * x + 1, j), r0y, r0x, r1y, r1x);
         }
       }
       // generic-proxy writes -> visible to the tensor core's async proxy
