@@ -420,10 +420,12 @@ __global__ void __launch_bounds__(256) wrp_tile_f32(WRPGeom g, const WrpPt* __re
 // region's complex64 sum, M = 128, N = 128, K = 4 per point.  BF16 high and
 // low parts, three products (Ahi Bhi + Ahi Blo + Alo Bhi), FP32 in TMEM.
 //
-// One CTA per region, 256 threads.  Warps 1-7 write the operands of 8 points
+// One CTA per region, 288 threads.  Warps 0-7 write the operands of 8 points
 // (K = 32) per stage straight into shared memory, in the layout a TMA load
-// with 64-byte swizzle would give, then arrive on the stage's full barrier;
-// thread 0 issues tcgen05.mma (M 128, N 128, K 16) and releases stages with
+// with 64-byte swizzle would give, then arrive on the stage's full barrier:
+// thread t takes point slot t & 7, A rows (t >> 3) + 32 m (m < 4) and B
+// columns (t >> 3) + 32 m (m < 2), so its swizzled offsets are fixed.  Warp 8
+// issues tcgen05.mma (M 128, N 128, K 16) and releases stages with
 // tcgen05.commit; warps 4-7 read the accumulator (tcgen05.ld) and add the
 // region into the plane.  Waits are bounded: on timeout the CTA sets the
 // device error word, skips the add, waits for its MMAs and frees TMEM.
@@ -434,7 +436,7 @@ constexpr int kBK = 32, kPts = kBK / 4, kStages = 2;
 constexpr int kTile = 128 * kBK * 2;                   // 8 KB: 128 rows x 32 BF16
 constexpr int kStageBytes = 4 * kTile;                 // Ahi, Alo, Bhi, Blo
 constexpr int kTmemCols = 128;
-constexpr int kThreads = 256, kProducerWarps = 7;
+constexpr int kProducerWarps = 8, kThreads = 32 * kProducerWarps + 32;   // + the MMA warp
 constexpr int kSmemBytes = kStages * kStageBytes + 1024 + 256;
 constexpr long long kWaitCycles = 2000000000LL;
 
@@ -594,14 +596,21 @@ __global__ void __launch_bounds__(tcw::kThreads, 3) wrp_tc(WRPGeom g, const WrpP
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
-  if (warp >= 1) {
-    // producers: 224 threads, 1536 items per stage (A: 8 points x 128 rows,
-    // B: 8 points x 64 columns, each writing rows 2x and 2x+1).  Item i takes
-    // point slot i & 7, and 224 is a multiple of 8, so a thread always works
-    // on slot j = pt & 7: its record sits in registers, the next stage's is
-    // loaded while this stage is built.
-    const int pt = threadIdx.x - 32;
-    const int j = pt & (kPts - 1);
+  if (warp < kProducerWarps) {
+    // producers: point slot j, A rows rb + 32 m, B columns rb + 32 m; the
+    // record of this stage's point sits in registers, the next stage's is
+    // loaded while this stage is built
+    const int pt = threadIdx.x;
+    const int j = pt & (kPts - 1), rb = pt >> 3;
+    int offA[4], YA[4], offB0[2], offB1[2], XB[2];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) { offA[m] = sw_off(rb + 32 * m, j); YA[m] = Y0 + rb + 32 * m; }
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+      offB0[m] = sw_off(2 * (rb + 32 * m), j);
+      offB1[m] = sw_off(2 * (rb + 32 * m) + 1, j);
+      XB[m] = X0 + rb + 32 * m;
+    }
     Rec q = load_rec(pts, list, b + j, e);
     for (int it = 0; it < nst; ++it) {
       const int s = it % kStages;
@@ -618,43 +627,38 @@ __global__ void __launch_bounds__(tcw::kThreads, 3) wrp_tc(WRPGeom g, const WrpP
       unsigned char* sBh = sAh + 2 * kTile;
       unsigned char* sBl = sAh + 3 * kTile;
       const Rec qn = load_rec(pts, list, b + (it + 1) * kPts + j, e);
-#pragma unroll 2
-      for (int item = pt; item < kPts * (kRows + kCols); item += kProducerWarps * 32) {
-        if (item < kPts * kRows) {
-          // branch-free: rows outside the window get amplitude 0
-          const int r = item >> 3;
-          const int Y = Y0 + r, wy = Y - q.ty;
-          const bool in = Y < g.ny && wy >= -q.w && wy < q.w;
-          const float ys = (float)wy * q.sx, uy = ys * ys;
-          const float f = frac_turns(fmaf(uy, fmaf(uy, fmaf(uy, q.c3, q.c2), q.c1), q.base_t));
-          float sn, cs;
-          __sincosf(6.28318530717958647692f * f, &sn, &cs);
-          const float amp = in ? q.a0c * fmaf(uy, fmaf(uy, q.beta, q.alpha), 1.f) : 0.f;
-          const float v0 = amp * cs, v1 = amp * sn;
-          put4(sAh, sAl, sw_off(r, j), v0, v1, uy * v0, uy * v1);
-        } else {
-          const int x = (item - kPts * kRows) >> 3;
-          const int X = X0 + x, wx = X - q.tx;
-          const int o0 = sw_off(2 * x, j), o1 = sw_off(2 * x + 1, j);
-          {
-            const bool in = X < g.nx && wx >= -q.w && wx < q.w;
-            const float xs = (float)wx * q.sx, ux = xs * xs;
-            const float f = frac_turns(ux * fmaf(ux, fmaf(ux, q.c3, q.c2), q.c1));
-            float sn, cs;
-            __sincosf(6.28318530717958647692f * f, &sn, &cs);
-            const float amp = in ? fmaf(ux, fmaf(ux, q.beta, q.alpha), 1.f) : 0.f;
-            const float r0x = amp * cs, r0y = amp * sn;
-            const float kx = q.kappa * ux;
-            // R1 = i kappa ux R0; row 2x: (R0x, -R0y, R1x, -R1y), row 2x+1: (R0y, R0x, R1y, R1x),
-            // from one split of (R0x, R0y, R1x, R1y) by swapping halves and flipping signs
-            const Split4 v = split4(r0x, r0y, -kx * r0y, kx * r0x);
-            const uint32_t neg_hi = 0x80000000u;             // sign of the second BF16 of a pair
-            *reinterpret_cast<uint2*>(sBh + o0) = make_uint2(v.h01 ^ neg_hi, v.h23 ^ neg_hi);
-            *reinterpret_cast<uint2*>(sBl + o0) = make_uint2(v.l01 ^ neg_hi, v.l23 ^ neg_hi);
-            *reinterpret_cast<uint2*>(sBh + o1) = make_uint2(__byte_perm(v.h01, 0, 0x1032), __byte_perm(v.h23, 0, 0x1032));
-            *reinterpret_cast<uint2*>(sBl + o1) = make_uint2(__byte_perm(v.l01, 0, 0x1032), __byte_perm(v.l23, 0, 0x1032));
-          }
-        }
+      // A: branch-free, rows outside the window (or the plane) get amplitude 0
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const int wy = YA[m] - q.ty;
+        const bool in = YA[m] < g.ny && (unsigned)(wy + q.w) < (unsigned)(2 * q.w);
+        const float ys = (float)wy * q.sx, uy = ys * ys;
+        const float f = frac_turns(fmaf(uy, fmaf(uy, fmaf(uy, q.c3, q.c2), q.c1), q.base_t));
+        float sn, cs;
+        __sincosf(6.28318530717958647692f * f, &sn, &cs);
+        const float amp = in ? q.a0c * fmaf(uy, fmaf(uy, q.beta, q.alpha), 1.f) : 0.f;
+        const float v0 = amp * cs, v1 = amp * sn;
+        put4(sAh, sAl, offA[m], v0, v1, uy * v0, uy * v1);
+      }
+      // B: R1 = i kappa ux R0; row 2x: (R0x, -R0y, R1x, -R1y), row 2x+1:
+      // (R0y, R0x, R1y, R1x), from one split by swapping halves and flipping signs
+#pragma unroll
+      for (int m = 0; m < 2; ++m) {
+        const int wx = XB[m] - q.tx;
+        const bool in = XB[m] < g.nx && (unsigned)(wx + q.w) < (unsigned)(2 * q.w);
+        const float xs = (float)wx * q.sx, ux = xs * xs;
+        const float f = frac_turns(ux * fmaf(ux, fmaf(ux, q.c3, q.c2), q.c1));
+        float sn, cs;
+        __sincosf(6.28318530717958647692f * f, &sn, &cs);
+        const float amp = in ? fmaf(ux, fmaf(ux, q.beta, q.alpha), 1.f) : 0.f;
+        const float r0x = amp * cs, r0y = amp * sn;
+        const float kx = q.kappa * ux;
+        const Split4 v = split4(r0x, r0y, -kx * r0y, kx * r0x);
+        const uint32_t neg_hi = 0x80000000u;               // sign of the second BF16 of a pair
+        *reinterpret_cast<uint2*>(sBh + offB0[m]) = make_uint2(v.h01 ^ neg_hi, v.h23 ^ neg_hi);
+        *reinterpret_cast<uint2*>(sBl + offB0[m]) = make_uint2(v.l01 ^ neg_hi, v.l23 ^ neg_hi);
+        *reinterpret_cast<uint2*>(sBh + offB1[m]) = make_uint2(__byte_perm(v.h01, 0, 0x1032), __byte_perm(v.h23, 0, 0x1032));
+        *reinterpret_cast<uint2*>(sBl + offB1[m]) = make_uint2(__byte_perm(v.l01, 0, 0x1032), __byte_perm(v.l23, 0, 0x1032));
       }
       // generic-proxy writes -> visible to the tensor core's async proxy
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -662,7 +666,7 @@ __global__ void __launch_bounds__(tcw::kThreads, 3) wrp_tc(WRPGeom g, const WrpP
       if (lane == 0) mb_arrive(&full[s]);
       q = qn;
     }
-  } else if (threadIdx.x == 0) {
+  } else if (threadIdx.x == 32 * kProducerWarps) {
     // MMA issuer
     for (int it = 0; it < nst; ++it) {
       const int s = it % kStages;
@@ -688,11 +692,12 @@ __global__ void __launch_bounds__(tcw::kThreads, 3) wrp_tc(WRPGeom g, const WrpP
   }
   // epilogue: warps 4-7 own TMEM lanes 32 (warp - 4) .. + 31 = region rows
   __syncwarp();
+  const bool epi = warp >= 4 && warp < 8;
   bool ok_done = true;
-  if (warp >= 4) ok_done = mb_wait(done, 0);
+  if (epi) ok_done = mb_wait(done, 0);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const bool good = __syncthreads_and(ok_done && !*((volatile int*)abort_flag));
-  if (good && warp >= 4) {
+  if (good && epi) {
     const int r = 32 * (warp - 4) + lane;
     const int Y = Y0 + r;
 #pragma unroll 1
