@@ -114,47 +114,51 @@ __device__ __forceinline__ void wrp_point(const WRPGeom& g, const double* xyz, i
   o->dz = dz;
   o->sgn = dz > 0.0 ? 1.f : -1.f;
   o->adz = (float)fabs(dz);
+  // FP64 only for the phase reduction; the rest in FP32 (FP64 is a small
+  // fraction of FP32 throughput here)
   const double kdz = kd * fabs(dz);
-  o->base = (float)(kdz - two_pi * rint(kdz / two_pi));
+  const double turns = kdz * 0.15915494309189533576888376337251;      // k|dz| / (2 pi)
+  const double tfrac = turns - rint(turns);
+  o->base = (float)(two_pi * tfrac);
   // Series form: with u = rho^2 / dz^2 and t = sqrt(1 + u) - 1 = u (1/2 - u/8 + u^2/16) + O(5 u^4 / 128),
   //   sgn k|r| / (2 pi) = sgn turns (1 + t),  turns = k|dz| / (2 pi),
   //   1 / (sgn |r| + 0.05) = (1 / a0) / (1 + e),  a0 = sgn |dz| + 0.05,  e = ea t,  ea = sgn |dz| / a0,
   //   1 / (1 + e) = 1 - ea u / 2 + (ea / 8 + ea^2 / 4) u^2 - (ea / 16 + ea^2 / 8 + ea^3 / 8) u^3 + ...,
   // used when the dropped terms stay below 1e-6 rad (phase) and 1e-8 relative
   // (amplitude) over the whole window.
-  const double adz = fabs(dz), sg = dz > 0.0 ? 1.0 : -1.0;
-  const double a0 = sg * adz + 0.05;
-  const double rho2max = 2.0 * (double)g.fixed_w * g.fixed_w * (double)dpx * dpx;
-  const double umax = adz > 0.0 ? rho2max / (adz * adz) : 1.0;
-  const double ea = fabs(a0) > 1e-6 ? sg * adz / a0 : 0.0;
-  const double aea = fabs(ea);
-  const double u3 = umax * umax * umax;
-  o->series = (adz > 0.0 && fabs(a0) > 1e-6 && umax < 0.05 &&
-               kdz * (5.0 / 128.0) * umax * u3 < 1e-6 &&
-               (aea / 16.0 + aea * aea / 8.0 + aea * aea * aea / 8.0) * u3 < 1e-8) ? 1 : 0;
-  const double turns = kdz / two_pi;
-  o->base_t = (float)(sg * (turns - rint(turns)));
-  o->c1 = (float)(sg * turns * 0.5);
-  o->c2 = (float)(sg * turns * -0.125);
-  o->c3 = (float)(sg * turns * 0.0625);
-  o->sx = adz > 0.0 ? (float)((double)dpx / adz) : 0.f;
-  const double ia0 = fabs(a0) > 1e-6 ? 1.0 / a0 : 0.0;
-  o->a0c = (float)ia0;
-  o->a1c = (float)(-ia0 * ea * 0.5);
-  o->a2c = (float)(ia0 * (ea * 0.125 + ea * ea * 0.25));
+  const float adz = (float)fabs(dz), sg = dz > 0.0 ? 1.f : -1.f;
+  const float a0 = sg * adz + 0.05f;
+  const float rho2max = 2.f * (float)g.fixed_w * (float)g.fixed_w * dpx * dpx;
+  const float umax = adz > 0.f ? rho2max / (adz * adz) : 1.f;
+  const float ea = fabsf(a0) > 1e-6f ? sg * adz / a0 : 0.f;
+  const float aea = fabsf(ea);
+  const float u3 = umax * umax * umax;
+  const float kdzf = (float)kdz;
+  o->series = (adz > 0.f && fabsf(a0) > 1e-6f && umax < 0.05f && kdzf * (5.f / 128.f) * umax * u3 < 1e-6f &&
+               (aea / 16.f + aea * aea / 8.f + aea * aea * aea / 8.f) * u3 < 1e-8f) ? 1 : 0;
+  const float st = (float)(dz > 0.0 ? turns : -turns);               // sgn turns; the c's are its exact scalings
+  o->base_t = (float)(dz > 0.0 ? tfrac : -tfrac);
+  o->c1 = st * 0.5f;
+  o->c2 = st * -0.125f;
+  o->c3 = st * 0.0625f;
+  o->sx = adz > 0.f ? dpx / adz : 0.f;
+  const float ia0 = fabsf(a0) > 1e-6f ? 1.f / a0 : 0.f;
+  o->a0c = ia0;
+  o->a1c = -ia0 * ea * 0.5f;
+  o->a2c = ia0 * (ea * 0.125f + ea * ea * 0.25f);
   // separable form: the dropped terms at the window corner (ux = uy = (w sx)^2)
   //   phase cross term to second order (kappa ux uy)^2 / 2, the c3 cross terms
   //   2 pi 3 c3 ux uy (ux + uy), the amplitude cross term (alpha^2 - 2 beta) ux uy
-  const double two_pi_d = 6.283185307179586476925286766559;
-  const double al = -ea * 0.5, be = ea * 0.125 + ea * ea * 0.25;
-  const double kap = two_pi_d * 2.0 * (sg * turns * -0.125);
-  const double uc = adz > 0.0 ? (double)g.fixed_w * g.fixed_w * (double)dpx * dpx / (adz * adz) : 1.0;
-  const double t1 = kap * uc * uc, t2 = two_pi_d * 3.0 * fabs(sg * turns * 0.0625) * uc * uc * 2.0 * uc;
-  const double t3 = fabs(al * al - 2.0 * be) * uc * uc;
-  if (o->series && g.fixed_w > 0 && 0.5 * t1 * t1 < 3e-5 && t2 < 1e-5 && t3 < 1e-6) o->series = 2;
-  o->kappa = (float)kap;
-  o->alpha = (float)al;
-  o->beta = (float)be;
+  const float two_pi_f = 6.28318530717958647692f;
+  const float al = -ea * 0.5f, be = ea * 0.125f + ea * ea * 0.25f;
+  const float kap = two_pi_f * 2.f * o->c2;
+  const float uc = adz > 0.f ? (float)g.fixed_w * (float)g.fixed_w * dpx * dpx / (adz * adz) : 1.f;
+  const float t1 = kap * uc * uc, t2 = two_pi_f * 3.f * fabsf(o->c3) * uc * uc * 2.f * uc;
+  const float t3 = fabsf(al * al - 2.f * be) * uc * uc;
+  if (o->series && g.fixed_w > 0 && 0.5f * t1 * t1 < 3e-5f && t2 < 1e-5f && t3 < 1e-6f) o->series = 2;
+  o->kappa = kap;
+  o->alpha = al;
+  o->beta = be;
 }
 
 // Two binnings share one count / start / list layout: 64 x 64 tiles for the
