@@ -45,15 +45,15 @@ constexpr int col_tab_entries() {
   return n * 8 <= 8192 ? n : 0;
 }
 
-__host__ __device__ inline int col_take(int* o, int bytes) {
+__host__ __device__ constexpr int col_take(int* o, int bytes) {
   const int r = *o;
   *o += (bytes + 127) & ~127;
   return r;
 }
 
-__host__ __device__ inline ColLayout col_layout(int Py, int pny, int W, int occ_stride, int n_entries,
-                                                int tab_entries) {
-  ColLayout L;
+__host__ __device__ constexpr ColLayout col_layout(int Py, int pny, int W, int occ_stride, int n_entries,
+                                                   int tab_entries) {
+  ColLayout L{};
   int o = 0;
   L.buf = col_take(&o, Py * W * 8);
   L.stg = col_take(&o, pny * W * 8);
@@ -84,7 +84,11 @@ template <int NY, int W> struct ColCfg {
   static constexpr int NBL = (NY / RL) * W;          // last-stage butterflies in the strip
   static constexpr int KB = NBL > 768 ? 2 : 1;        // butterflies per thread
   static constexpr int T = ((NBL + KB - 1) / KB + 31) / 32 * 32;
-  static constexpr int MINB = W <= 2 ? 2 : 1;          // narrow strips: two blocks per SM
+  // two blocks per SM when two strips' shared memory fits (2x padding,
+  // pny = NY / 2); otherwise one, and the register cap that two would
+  // impose (spills at the longer lengths) is lifted
+  static constexpr int SMEM = col_layout(NY, NY / 2, W, ((NY / 2) + 15) & ~15, kMaxEntries, col_tab_entries<NY>()).total;
+  static constexpr int MINB = (W <= 2 && 2 * (SMEM + 1024) <= 228 * 1024) ? 2 : 1;
 };
 
 // STEP: evenly spaced layers, accumulated with the layer-step recurrence.
