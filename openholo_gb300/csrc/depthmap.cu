@@ -675,7 +675,8 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
     with_fast_n(a.Py, [&](auto nc) {
       if constexpr (decltype(nc)::value > 0) col_tab = col_tab_entries<decltype(nc)::value>();
     });
-    if (a.Px % 2 == 0 && (size_t)col_layout(a.Py, a.pny, 2, occ_stride, su.n_entries, col_tab).total <= smax)
+    if (a.Px % 2 == 0 &&
+        (size_t)col_layout(a.Py, a.pny, 2, kColStripW, false, occ_stride, su.n_entries, col_tab).total <= smax)
       Wfast = 2;
   }
   int W = Wfast;
@@ -734,8 +735,25 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   }
   a.hzx = (p->pad == 2 && r0x == 16 && (a.Px % 16) == 0 && a.ox * 4 == a.Px && a.hx * 2 == a.Px) ? 1 : 0;
   a.hzy = (p->pad == 2 && r0y == 16 && (a.Py % 16) == 0 && a.oy * 4 == a.Py && a.hy * 2 == a.Py) ? 1 : 0;
-  const size_t smem_col = Wfast ? (size_t)col_layout(a.Py, a.pny, W, occ_stride, su.n_entries, col_tab).total
-                                : (size_t)W * a.Py * sizeof(C) + W * (sizeof(C) + sizeof(R)) + (size_t)a.Py * sizeof(int);
+  // fast column pass: one-column blocks over the two-column strips where
+  // that turns one block per SM into two
+  int wcol = Wfast;
+  if (Wfast) {
+    bool narrow = false;
+    with_fast_n(a.Py, [&](auto nc) {
+      if constexpr (decltype(nc)::value > 0) narrow = col_narrow_ok<decltype(nc)::value>();
+    });
+    const bool step = a.horner != 0;
+    auto two_fit = [&](int w) {
+      return 2 * ((size_t)col_layout(a.Py, a.pny, w, kColStripW, step, occ_stride, su.n_entries, col_tab).total +
+                  1024) <= (size_t)228 * 1024;
+    };
+    const char* ev = std::getenv("OH_DM_COL_NARROW");
+    if (narrow && !(ev && std::atoi(ev) == 0) && !two_fit(2) && two_fit(1)) wcol = 1;
+  }
+  const size_t smem_col =
+      Wfast ? (size_t)col_layout(a.Py, a.pny, wcol, kColStripW, a.horner != 0, occ_stride, su.n_entries, col_tab).total
+            : (size_t)W * a.Py * sizeof(C) + W * (sizeof(C) + sizeof(R)) + (size_t)a.Py * sizeof(int);
   int row_tab = 0;
   with_fast_n_if<sizeof(R) == 4>(a.Px, [&](auto nc) {
     if constexpr (decltype(nc)::value > 0) row_tab = FastSched<decltype(nc)::value>::tab1_entries;
@@ -823,17 +841,27 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
       with_fast_n(a.Py, [&](auto nc) {
         constexpr int NY = decltype(nc)::value;
         if constexpr (NY > 0) {
-          auto launch = [&](auto kern) {
+          auto launch = [&](auto kern, int threads, int blocks) {
             cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col);
             if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
             if (e != cudaSuccess) { rs = cuda_fail(e, "cudaFuncSetAttribute(dm_col_fast)"); return; }
             KernelTimer kt(ctx, "dm_col_pass", st);
-            kern<<<a.nstrips, ColCfg<NY, 2>::T, smem_col, st>>>(a);
+            kern<<<blocks, threads, smem_col, st>>>(a);
             note_launch();
             if ((e = cudaGetLastError()) != cudaSuccess) rs = cuda_fail(e, "dm_col_fast launch");
           };
-          if (a.horner) launch(dm_col_fast<NY, 2, true>);
-          else launch(dm_col_fast<NY, 2, false>);
+          bool done = false;
+          if constexpr (col_narrow_ok<NY>()) {
+            if (wcol == 1) {
+              if (a.horner) launch(dm_col_fast<NY, 1, true>, ColCfg<NY, 1, true>::T, a.Px);
+              else launch(dm_col_fast<NY, 1, false>, ColCfg<NY, 1, false>::T, a.Px);
+              done = true;
+            }
+          }
+          if (!done) {
+            if (a.horner) launch(dm_col_fast<NY, 2, true>, ColCfg<NY, 2, true>::T, a.nstrips);
+            else launch(dm_col_fast<NY, 2, false>, ColCfg<NY, 2, false>::T, a.nstrips);
+          }
         }
       });
       OH_TRY(rs);

@@ -30,7 +30,7 @@
 namespace oh {
 
 struct ColLayout {
-  int buf, stg, ey0, ey1, occ, g, kyp, twlo, twhi, tab, exw, lfxw, list, mbar, total;
+  int buf, stg, ey0, ey1, occ, g, twlo, twhi, tab, exw, lfxw, list, mbar, total;
 };
 
 // Twiddle-table entries of the middle forward stage of the column FFT
@@ -51,20 +51,20 @@ __host__ __device__ constexpr int col_take(int* o, int bytes) {
   return r;
 }
 
-__host__ __device__ constexpr ColLayout col_layout(int Py, int pny, int W, int occ_stride, int n_entries,
-                                                   int tab_entries) {
+// W: spectrum columns a block transforms; sw: columns per strip of the row
+// pass output (the staging buffer holds a whole strip); step: the layer-step
+// variant (its region holds D, float2 per element, instead of g and two Ey rows)
+__host__ __device__ constexpr ColLayout col_layout(int Py, int pny, int W, int sw, bool step, int occ_stride,
+                                                   int n_entries, int tab_entries) {
   ColLayout L{};
   int o = 0;
   L.buf = col_take(&o, Py * W * 8);
-  L.stg = col_take(&o, pny * W * 8);
-  // one region holds either the residual phase g (float per element) and the
-  // two Ey rows, or the layer-step factor D (float2 per element)
+  L.stg = col_take(&o, pny * sw * 8);
   const int gb = (Py * W * 4 + 127) & ~127, eb = (Py * 4 + 127) & ~127;
-  L.g = col_take(&o, gb + 2 * eb > Py * W * 8 ? gb + 2 * eb : Py * W * 8);
+  L.g = col_take(&o, step ? Py * W * 8 : gb + 2 * eb);
   L.ey0 = L.g + gb;
   L.ey1 = L.ey0 + eb;
   L.occ = col_take(&o, occ_stride);
-  L.kyp = col_take(&o, Py * 2);
   L.twlo = col_take(&o, 64 * 8);
   L.twhi = col_take(&o, ((Py + 63) / 64) * 8);
   L.tab = col_take(&o, tab_entries * 8);
@@ -79,23 +79,33 @@ __host__ __device__ constexpr ColLayout col_layout(int Py, int pny, int W, int o
 
 // Threads per block for a strip of W columns: one thread per last-stage
 // butterfly (NY/RL per column), two when that would exceed 768 threads.
-template <int NY, int W> struct ColCfg {
+constexpr int kColStripW = 2;     // columns per strip of the row pass output
+
+template <int NY, int W, bool STEP> struct ColCfg {
   static constexpr int RL = FastSched<NY>::rlast;
-  static constexpr int NBL = (NY / RL) * W;          // last-stage butterflies in the strip
+  static constexpr int NBL = (NY / RL) * W;          // last-stage butterflies of the block's columns
   static constexpr int KB = NBL > 768 ? 2 : 1;        // butterflies per thread
   static constexpr int T = ((NBL + KB - 1) / KB + 31) / 32 * 32;
-  // two blocks per SM when two strips' shared memory fits (2x padding,
-  // pny = NY / 2); otherwise one, and the register cap that two would
-  // impose (spills at the longer lengths) is lifted
-  static constexpr int SMEM = col_layout(NY, NY / 2, W, ((NY / 2) + 15) & ~15, kMaxEntries, col_tab_entries<NY>()).total;
-  static constexpr int MINB = (W <= 2 && 2 * (SMEM + 1024) <= 228 * 1024) ? 2 : 1;
+  // two blocks per SM when two fit in shared memory (2x padding, pny =
+  // NY / 2); otherwise one, and the register cap that two would impose
+  // (spills at the longer lengths) is lifted
+  static constexpr int SMEM =
+      col_layout(NY, NY / 2, W, kColStripW, STEP, ((NY / 2) + 15) & ~15, kMaxEntries, col_tab_entries<NY>()).total;
+  static constexpr int MINB = 2 * (SMEM + 1024) <= 228 * 1024 ? 2 : 1;
 };
+
+// One-column blocks (W = 1) over two-column strips, for the lengths where a
+// two-column block's shared memory leaves one block per SM and the second
+// read of each strip still hits L2 (measured: 3072 faster, 4096 slower)
+template <int NY> constexpr bool col_narrow_ok() { return NY >= 3072 && NY <= 3840; }
 
 // STEP: evenly spaced layers, accumulated with the layer-step recurrence.
 template <int NY, int W, bool STEP>
-__global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_fast(DMArgs<float> a) {
+__global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::MINB) dm_col_fast(DMArgs<float> a) {
   typedef float2 C;
-  typedef ColCfg<NY, W> CF;
+  typedef ColCfg<NY, W, STEP> CF;
+  constexpr int SW = kColStripW;
+  static_assert(W == 1 || W == SW, "a block takes one column or a whole strip");
   constexpr int T = CF::T;
   constexpr int R0 = FastSched<NY>::r0;
   constexpr int RL = CF::RL;
@@ -105,14 +115,13 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int kTab = col_tab_entries<NY>();
   constexpr int R1 = FastSched<NY>::r1;
-  const ColLayout Lo = col_layout(NY, a.pny, W, a.occ_stride, a.n_entries, kTab);
+  const ColLayout Lo = col_layout(NY, a.pny, W, SW, STEP, a.occ_stride, a.n_entries, kTab);
   C* buf = reinterpret_cast<C*>(smem + Lo.buf);
   C* const stg = reinterpret_cast<C*>(smem + Lo.stg);            // row-pass strip of the layer (single buffer)
   uint8_t* const occ = smem + Lo.occ;                             // its row flags
   float* const ey0 = reinterpret_cast<float*>(smem + Lo.ey0);    // Ey phase rows, double buffered
   float* const ey1 = reinterpret_cast<float*>(smem + Lo.ey1);
   float* gsm = reinterpret_cast<float*>(smem + Lo.g);            // per element, buffer order
-  int16_t* kyp = reinterpret_cast<int16_t*>(smem + Lo.kyp);
   C* twlo = reinterpret_cast<C*>(smem + Lo.twlo);
   C* twhi = reinterpret_cast<C*>(smem + Lo.twhi);
   C* const tab1 = reinterpret_cast<C*>(smem + Lo.tab);            // stage 1: [NY/R0/R1][R1-1]
@@ -124,8 +133,9 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
   __shared__ int s_nact;
 
   const int tid = threadIdx.x;
-  const int s = blockIdx.x;
-  const int kx0 = s * W;
+  const int s = blockIdx.x / (SW / W);                // row-pass strip
+  const int csel = (blockIdx.x % (SW / W)) * W;       // first of its columns this block takes
+  const int kx0 = blockIdx.x * W;
   const int pny = a.pny;
   if (tid == 0) {
     mbar_init(&mbar[0], 1);
@@ -139,11 +149,6 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
   }
   load_tw_split(twlo, twhi, static_cast<const C*>(a.ply.tw), NY);
   if constexpr (kTab > 0) fill_stage_tab<NY, R1, NY / R0, -1>(tab1, static_cast<const C*>(a.ply.tw));
-  for (int p = tid; p < NY; p += T) {
-    int ky = a.ply.iperm[p] + a.hy;
-    if (ky >= NY) ky -= NY;
-    kyp[p] = (int16_t)ky;
-  }
   if (tid < W) {
     // strip column kx0 + w is either spectrum column kx0 + w or, when the row
     // pass stored its output in FFT storage order, column iperm + hx
@@ -174,12 +179,12 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
   }
   const int nact = s_nact;
   const TwSplit<C> tw{twlo, twhi};
-  const uint32_t strip_bytes = (uint32_t)(pny * W * 8);
+  const uint32_t strip_bytes = (uint32_t)(pny * SW * 8);
 
   auto issue_strip = [&](int k) {
     const int u = a.uslot_of_entry[list[k]];
     mbar_expect_tx(&mbar[0], strip_bytes + (uint32_t)a.occ_stride);
-    bulk_g2s(stg, a.Rbuf + ((size_t)u * a.nstrips + s) * pny * W, strip_bytes, &mbar[0]);
+    bulk_g2s(stg, a.Rbuf + ((size_t)u * a.nstrips + s) * pny * SW, strip_bytes, &mbar[0]);
     bulk_g2s(occ, a.occ + (size_t)u * a.occ_stride, (uint32_t)a.occ_stride, &mbar[0]);
   };
   auto issue_ey = [&](int k) {
@@ -248,7 +253,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
         for (int t = 0; t < R0; ++t) {
           if (t >= 4 && t < 12) { x[t] = make_float2(0.f, 0.f); continue; }
           const int yl = j + (t < 4 ? t + 4 : t - 12) * Q0;
-          x[t] = occ[yl] ? stg[yl * W + w] : make_float2(0.f, 0.f);
+          x[t] = occ[yl] ? stg[yl * SW + csel + w] : make_float2(0.f, 0.f);
         }
         dft16_halfzero<-1>(x);
       } else {
@@ -258,7 +263,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
           if (y < 0) y += NY;
           const int yl = y - a.oy;
           C v = make_float2(0.f, 0.f);
-          if (yl >= 0 && yl < pny && occ[yl]) v = stg[yl * W + w];
+          if (yl >= 0 && yl < pny && occ[yl]) v = stg[yl * SW + csel + w];
           x[t] = v;
         }
         DFT<R0, -1, C>::run(x);
@@ -362,7 +367,8 @@ __global__ void __launch_bounds__(ColCfg<NY, W>::T, ColCfg<NY, W>::MINB) dm_col_
       const int kx = kxw[w];
 #pragma unroll
       for (int f = 0; f < RL; ++f) {
-        const int ky = kyp[b * RL + f];
+        int ky = FastSched<NY>::iperm(b * RL + f) + a.hy;      // spectrum row at storage position
+        if (ky >= NY) ky -= NY;
         if (a.spectrum) a.spectrum[(size_t)ky * a.Px + kx] = acc[kb][f];
         const bool keep = kx >= a.cx1 && kx <= a.cx2 && ky >= a.cy1 && ky <= a.cy2;
         int i = ky + a.hy;
