@@ -11,14 +11,16 @@
 //
 // h is separable, h = C gx(x) gy(y), so its spectrum is C Hx(u) Hy(v), Hx and
 // Hy being the 1-D DFTs of the sampled chirps (computed once in FP64 and
-// cached per size, pitch, lambda and z).  In FP32, when 2Nx and 2Ny have
-// compile-time FFT schedules, three passes do the whole propagation without
-// materialising the padded grid:
-//   fr_row_fwd  x-FFT of each field row (the padded half is implicit),
-//               written as strips of two spectrum columns;
-//   fr_col      per strip: y-FFT, multiply by C Hx Hy / (4 Nx Ny), inverse
-//               y-FFT, keep the Ny cropped rows (in place in the strip);
-//   fr_row_inv  inverse x-FFT of each kept row, cropped into the field.
+// cached per size, pitch, lambda and z), and the padded 2-D convolution is a
+// row convolution with C gx followed by a column convolution with gy.  In
+// FP32, when 2Nx and 2Ny have compile-time FFT schedules, three kernels do
+// the propagation without materialising the padded grid:
+//   fr_rowconv         per row: x-FFT on the padded length, times C Hx,
+//                      inverse x-FFT, crop to Nx, written as strips of two
+//                      columns;
+//   fr_col             per strip: the same along y with Hy / (4 Nx Ny),
+//                      keeping the Ny cropped rows (in place in the strip);
+//   fr_strips_to_rows  strips back to the row-major field.
 // Each line enters its forward FFT rotated by half its padded length, so the
 // data fill the first and last quarters (radix-16 stage-0 butterflies see 8 of
 // 16 inputs); the rotation multiplies the spectrum by (-1)^u (and (-1)^v),
@@ -132,59 +134,21 @@ static oh_status run_fresnel_grid(oh_ctx* ctx, int nx, int ny, double dp, double
   return OH_OK;
 }
 
-// ---- separable three-pass path (FP32) -------------------------------------
+// ---- separable path (FP32) ------------------------------------------------
 
-constexpr int kFrW = 2;      // spectrum columns per strip
-// Rows per block of the two row passes (measured at 3840x2160: the forward
-// pass is faster with two rows per 512-thread block, the inverse with one row
-// per 256-thread block, where its gather latency hides across more blocks).
-constexpr int kFrFwdRows = 2;
-constexpr int kFrInvRows = 1;
+constexpr int kFrW = 2;      // columns per strip
 
 struct FrArgs {
   int nx, ny;                // field size; the padded grid is 2nx x 2ny
-  float2* field;             // read by fr_row_fwd, written by fr_row_inv
-  float2* R;                 // strips [2nx / kFrW][ny][kFrW]
+  float2* field;             // read by fr_rowconv, written by fr_strips_to_rows
+  float2* R;                 // strips [nx / kFrW][ny][kFrW]
   const float2* twx;         // plan twiddles of the two lengths
   const float2* twy;
-  const int* perm_x;
-  const int* iperm_x;
-  const int* perm_y;
-  const int* iperm_y;
   const float2* hxs;         // C (-1)^u Hx(u) at x-FFT storage position
   const float2* hys;         // (-1)^v Hy(v) / (4 nx ny), natural order
 };
 
 __host__ __device__ constexpr int fr_tw_entries(int n) { return 64 + (n + 63) / 64; }
-
-// ROWS rows per block: x-FFT of the padded row, stored as column strips.
-template <int NX, int ROWS>
-__global__ void __launch_bounds__(256 * ROWS) fr_row_fwd(FrArgs a) {
-  typedef float2 C;
-  extern __shared__ __align__(16) unsigned char smem[];
-  C* buf = reinterpret_cast<C*>(smem);
-  C* twlo = buf + ROWS * NX;
-  C* twhi = twlo + 64;
-  constexpr int Q = NX / 4;                        // = nx / 2
-  const int r0 = ROWS * blockIdx.x;
-  load_tw_split(twlo, twhi, a.twx, NX);
-  const C* src = a.field + (size_t)r0 * a.nx;
-  for (int idx = threadIdx.x; idx < ROWS * NX; idx += blockDim.x) {
-    const int l = idx / NX, p = idx - l * NX;
-    // rotated line: position p holds field column p - 3Q (p >= 3Q) or p + Q (p < Q)
-    int c = -1;
-    if (p >= 3 * Q) c = p - 3 * Q;
-    else if (p < Q) c = p + Q;
-    buf[idx] = c >= 0 ? src[(size_t)l * a.nx + c] : make_float2(0.f, 0.f);
-  }
-  const TwSplit<C> tw{twlo, twhi};
-  FastSched<NX>::template run_t<-1>(buf, ROWS, NX, 1, tw, false);
-  __syncthreads();
-  for (int idx = threadIdx.x; idx < ROWS * NX; idx += blockDim.x) {
-    const int w = idx % kFrW, l = (idx / kFrW) % ROWS, s = idx / (ROWS * kFrW);
-    a.R[((size_t)s * a.ny + r0 + l) * kFrW + w] = buf[l * NX + s * kFrW + w];
-  }
-}
 
 template <int NY> struct FrColCfg {
   static constexpr int R0 = FastSched<NY>::r0;
@@ -196,8 +160,8 @@ template <int NY> struct FrColCfg {
   static constexpr int MINB = (NY * kFrW + fr_tw_entries(NY)) * 8 <= 113 * 1024 ? 2 : 1;
 };
 
-// One strip of kFrW spectrum columns per block: y-FFT, transfer function,
-// inverse y-FFT, crop; the result overwrites the strip.
+// One strip of kFrW columns (already convolved along x) per block: y-FFT,
+// times Hy, inverse y-FFT, crop; the result overwrites the strip.
 template <int NY>
 __global__ void __launch_bounds__(FrColCfg<NY>::T, FrColCfg<NY>::MINB) fr_col(FrArgs a) {
   typedef float2 C;
@@ -210,11 +174,9 @@ __global__ void __launch_bounds__(FrColCfg<NY>::T, FrColCfg<NY>::MINB) fr_col(Fr
   C* buf = reinterpret_cast<C*>(smem);               // [NY][W]
   C* twlo = buf + NY * W;
   C* twhi = twlo + 64;
-  __shared__ C hxw[W];
   const int tid = threadIdx.x, s = blockIdx.x, ny = a.ny;
   C* strip = a.R + (size_t)s * ny * W;
   load_tw_split(twlo, twhi, a.twy, NY);
-  if (tid < W) hxw[tid] = a.hxs[s * W + tid];
   __syncthreads();
   const TwSplit<C> tw{twlo, twhi};
   // stage 0 from global memory; rotated line: positions [QY, 3QY) are zero,
@@ -254,12 +216,8 @@ __global__ void __launch_bounds__(FrColCfg<NY>::T, FrColCfg<NY>::MINB) fr_col(Fr
 #pragma unroll
       for (int f = 0; f < RL; ++f) x[f] = buf[(b * RL + f) * W + w];
       DFT<RL, -1, C>::run(x);
-      const C hx = hxw[w];
 #pragma unroll
-      for (int f = 0; f < RL; ++f) {
-        const int v = FastSched<NY>::iperm(b * RL + f);
-        acc[kb][f] = cmul(x[f], cmul(hx, __ldg(a.hys + v)));
-      }
+      for (int f = 0; f < RL; ++f) acc[kb][f] = cmul(x[f], __ldg(a.hys + FastSched<NY>::iperm(b * RL + f)));
     }
   }
   __syncthreads();
@@ -281,31 +239,80 @@ __global__ void __launch_bounds__(FrColCfg<NY>::T, FrColCfg<NY>::MINB) fr_col(Fr
   }
 }
 
-// ROWS rows per block: gather the row from the strips into natural frequency
-// order, inverse x-FFT, crop into the field.
-template <int NX, int ROWS>
-__global__ void __launch_bounds__(256 * ROWS) fr_row_inv(FrArgs a) {
+// Separable form, first pass: two rows per block, each convolved with hx on
+// the padded length (x-FFT of the rotated row, times C (-1)^u Hx(u), back to
+// natural order through registers, inverse x-FFT), cropped to nx columns and
+// stored as strips [nx / kFrW][ny][kFrW] (four threads per 32-byte sector).
+template <int NX>
+__global__ void __launch_bounds__(512) fr_rowconv(FrArgs a) {
   typedef float2 C;
+  constexpr int ROWS = 2, NT = 512;
+  constexpr int PER = (ROWS * NX + NT - 1) / NT;
   extern __shared__ __align__(16) unsigned char smem[];
   C* buf = reinterpret_cast<C*>(smem);
   C* twlo = buf + ROWS * NX;
   C* twhi = twlo + 64;
-  constexpr int Q = NX / 4;
-  const int r0 = ROWS * blockIdx.x;
+  constexpr int Q = NX / 4;                        // = nx / 2
+  const int r0 = ROWS * blockIdx.x, nx = a.nx;
   load_tw_split(twlo, twhi, a.twx, NX);
-  for (int idx = threadIdx.x; idx < ROWS * NX; idx += blockDim.x) {
-    const int w = idx % kFrW, l = (idx / kFrW) % ROWS, s = idx / (ROWS * kFrW);
-    const int p = s * kFrW + w;
-    buf[l * NX + FastSched<NX>::iperm(p)] = a.R[((size_t)s * a.ny + r0 + l) * kFrW + w];
+  const C* src = a.field + (size_t)r0 * nx;
+  for (int idx = threadIdx.x; idx < ROWS * NX; idx += NT) {
+    const int l = idx / NX, p = idx - l * NX;
+    // rotated line: position p holds field column p - 3Q (p >= 3Q) or p + Q (p < Q)
+    int c = -1;
+    if (p >= 3 * Q) c = p - 3 * Q;
+    else if (p < Q) c = p + Q;
+    buf[idx] = c >= 0 ? src[(size_t)l * nx + c] : make_float2(0.f, 0.f);
   }
   const TwSplit<C> tw{twlo, twhi};
+  FastSched<NX>::template run_t<-1>(buf, ROWS, NX, 1, tw, false);
+  __syncthreads();
+  C v[PER];
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    const int idx = threadIdx.x + i * NT;
+    if (idx < ROWS * NX) {
+      const int l = idx / NX, p = idx - l * NX;
+      v[i] = cmul(buf[idx], __ldg(a.hxs + p));
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    const int idx = threadIdx.x + i * NT;
+    if (idx < ROWS * NX) {
+      const int l = idx / NX, p = idx - l * NX;
+      buf[l * NX + FastSched<NX>::iperm(p)] = v[i];
+    }
+  }
   FastSched<NX>::template run_t<1>(buf, ROWS, NX, 1, tw, false);
   __syncthreads();
-  float2* dst = a.field + (size_t)r0 * a.nx;
-  const int nx = a.nx;
-  for (int idx = threadIdx.x; idx < ROWS * nx; idx += blockDim.x) {
-    const int l = idx / nx, c = idx - l * nx;
-    dst[(size_t)l * nx + c] = buf[l * NX + FastSched<NX>::perm(Q + c)];
+  for (int idx = threadIdx.x; idx < ROWS * nx; idx += NT) {
+    const int w = idx % kFrW, l = (idx / kFrW) % ROWS, s = idx / (ROWS * kFrW);
+    a.R[((size_t)s * a.ny + r0 + l) * kFrW + w] = buf[l * NX + FastSched<NX>::perm(Q + s * kFrW + w)];
+  }
+}
+
+// Separable form, last pass: strips [nx / kFrW][ny][kFrW] to the row-major
+// field, through a 32-row x 64-column shared-memory tile.
+__global__ void __launch_bounds__(256) fr_strips_to_rows(FrArgs a) {
+  __shared__ float2 tile[32][64 + 1];
+  const int x0 = blockIdx.x * 64, y0 = blockIdx.y * 32, nx = a.nx, ny = a.ny;
+  const int ns = nx / kFrW;
+  for (int i = threadIdx.x; i < 32 * 32; i += 256) {
+    const int s = i & 31, r = i >> 5;                 // 32 strips x 32 rows, 16 bytes each
+    const int sg = x0 / kFrW + s, y = y0 + r;
+    if (sg < ns && y < ny) {
+      const float4 v = *reinterpret_cast<const float4*>(a.R + ((size_t)sg * ny + y) * kFrW);
+      tile[r][2 * s] = make_float2(v.x, v.y);
+      tile[r][2 * s + 1] = make_float2(v.z, v.w);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 32 * 64; i += 256) {
+    const int c = i & 63, r = i >> 6;
+    const int x = x0 + c, y = y0 + r;
+    if (x < nx && y < ny) a.field[(size_t)y * nx + x] = tile[r][c];
   }
 }
 
@@ -342,23 +349,27 @@ __global__ void fr_tables(int NX, int NY, const double2* __restrict__ Hx, const 
 
 typedef void (*FrKernel)(FrArgs);
 
-// The three kernels for padded lengths NX = 2nx, NY = 2ny, or false.
-static bool fr_pick(int NX, int NY, FrKernel* fwd, FrKernel* col, FrKernel* inv, int* col_threads) {
-  *fwd = *col = *inv = nullptr;
+struct FrKernels {
+  FrKernel rowconv, col;
+  int col_threads;
+};
+
+// The kernels for padded lengths NX = 2nx, NY = 2ny, or false.
+static bool fr_pick(int NX, int NY, FrKernels* k) {
+  std::memset(k, 0, sizeof(*k));
   with_fast_n(NX, [&](auto nc) {
     constexpr int N = decltype(nc)::value;
-    if constexpr (N > 0) { *fwd = fr_row_fwd<N, kFrFwdRows>; *inv = fr_row_inv<N, kFrInvRows>; }
+    if constexpr (N > 0) k->rowconv = fr_rowconv<N>;
   });
   with_fast_n(NY, [&](auto nc) {
     constexpr int N = decltype(nc)::value;
-    if constexpr (N > 0) { *col = fr_col<N>; *col_threads = FrColCfg<N>::T; }
+    if constexpr (N > 0) { k->col = fr_col<N>; k->col_threads = FrColCfg<N>::T; }
   });
-  return *fwd && *col && *inv;
+  return k->rowconv && k->col;
 }
 
 static oh_status run_fresnel_separable(oh_ctx* ctx, int nx, int ny, double dp, double lambda, double z,
-                                       float2* field, FrKernel fwd, FrKernel col, FrKernel inv, int col_threads,
-                                       cudaStream_t st) {
+                                       float2* field, const FrKernels& k, cudaStream_t st) {
   const int NX = 2 * nx, NY = 2 * ny;
   FFTPlan px, py;
   OH_TRY(get_plan(ctx, NX, 0, &px));
@@ -398,26 +409,26 @@ static oh_status run_fresnel_separable(oh_ctx* ctx, int nx, int ny, double dp, d
     OH_LAUNCH_CHECK();
   }
   FrArgs a{nx, ny, field, static_cast<float2*>(rbuf), static_cast<const float2*>(px.tw),
-           static_cast<const float2*>(py.tw), px.perm, px.iperm, py.perm, py.iperm, hxs, hys};
-  const int sfwd = (kFrFwdRows * NX + fr_tw_entries(NX)) * (int)sizeof(float2);
-  const int sinv = (kFrInvRows * NX + fr_tw_entries(NX)) * (int)sizeof(float2);
+           static_cast<const float2*>(py.tw), hxs, hys};
   const int scol = (NY * kFrW + fr_tw_entries(NY)) * (int)sizeof(float2);
-  OH_CUDA_TRY(cudaFuncSetAttribute(fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, sfwd));
-  OH_CUDA_TRY(cudaFuncSetAttribute(inv, cudaFuncAttributeMaxDynamicSharedMemorySize, sinv));
-  OH_CUDA_TRY(cudaFuncSetAttribute(col, cudaFuncAttributeMaxDynamicSharedMemorySize, scol));
+  // rows convolved with hx and cropped to nx, then the nx / 2 strips with
+  // hy (cropped to ny in place), then strips to rows
+  const int srow = (2 * NX + fr_tw_entries(NX)) * (int)sizeof(float2);
+  OH_CUDA_TRY(cudaFuncSetAttribute(k.rowconv, cudaFuncAttributeMaxDynamicSharedMemorySize, srow));
+  OH_CUDA_TRY(cudaFuncSetAttribute(k.col, cudaFuncAttributeMaxDynamicSharedMemorySize, scol));
   {
-    KernelTimer kt(ctx, "fresnel_row_fwd", st);
-    fwd<<<ny / kFrFwdRows, 256 * kFrFwdRows, sfwd, st>>>(a);
+    KernelTimer kt(ctx, "fresnel_rowconv", st);
+    k.rowconv<<<ny / 2, 512, srow, st>>>(a);
     OH_LAUNCH_CHECK();
   }
   {
     KernelTimer kt(ctx, "fresnel_col", st);
-    col<<<NX / kFrW, col_threads, scol, st>>>(a);
+    k.col<<<nx / kFrW, k.col_threads, scol, st>>>(a);
     OH_LAUNCH_CHECK();
   }
   {
-    KernelTimer kt(ctx, "fresnel_row_inv", st);
-    inv<<<ny / kFrInvRows, 256 * kFrInvRows, sinv, st>>>(a);
+    KernelTimer kt(ctx, "fresnel_to_rows", st);
+    fr_strips_to_rows<<<dim3((nx + 63) / 64, (ny + 31) / 32), 256, 0, st>>>(a);
     OH_LAUNCH_CHECK();
   }
   return OH_OK;
@@ -427,12 +438,11 @@ template <typename R>
 static oh_status run_fresnel(oh_ctx* ctx, int nx, int ny, double dp, double lambda, double z, void* field,
                              cudaStream_t st) {
   if constexpr (sizeof(R) == 4) {
-    FrKernel fwd, col, inv;
-    int ct = 0;
+    FrKernels k;
     const bool even = nx % 2 == 0 && ny % 2 == 0;
-    if (even && !getenv("OH_FRESNEL_GRID") && fr_pick(2 * nx, 2 * ny, &fwd, &col, &inv, &ct) &&
-        (size_t)(kFrFwdRows * (2 * nx) + fr_tw_entries(2 * nx)) * sizeof(float2) <= max_smem_per_block())
-      return run_fresnel_separable(ctx, nx, ny, dp, lambda, z, static_cast<float2*>(field), fwd, col, inv, ct, st);
+    if (even && !getenv("OH_FRESNEL_GRID") && fr_pick(2 * nx, 2 * ny, &k) &&
+        (size_t)(2 * (2 * nx) + fr_tw_entries(2 * nx)) * sizeof(float2) <= max_smem_per_block())
+      return run_fresnel_separable(ctx, nx, ny, dp, lambda, z, static_cast<float2*>(field), k, st);
   }
   return run_fresnel_grid<R>(ctx, nx, ny, dp, lambda, z, field, st);
 }
