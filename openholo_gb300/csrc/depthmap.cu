@@ -216,8 +216,12 @@ template <> __device__ __forceinline__ void sincos_r<double>(double x, double* s
 // (a full 32-byte sector for W = 2).
 constexpr int kRowPair = 2;
 
+// two blocks per SM where two row pairs fit in shared memory (padded lengths
+// up to 4320); the register cap that comes with it applies only there
+template <int NX> constexpr int row_min_blocks() { return NX > 0 && NX <= 4320 ? 2 : 1; }
+
 template <typename R, int NX>
-__global__ void __launch_bounds__(512) dm_row_pass(DMArgs<R> a) {
+__global__ void __launch_bounds__(512, row_min_blocks<NX>()) dm_row_pass(DMArgs<R> a) {
   typedef typename cplx_of<R>::type C;
   extern __shared__ unsigned char smem_raw[];
   const int Px = a.Px, pnx = a.pnx;
@@ -316,6 +320,52 @@ __global__ void __launch_bounds__(512) dm_row_pass(DMArgs<R> a) {
         C* bl = buf + l * Px;
 #pragma unroll
         for (int f = 0; f < R0; ++f) bl[j + f * Q0] = x[f];
+      }
+      if constexpr (FastSched<NX>::nstages == 3 && NX / FastSched<NX>::rlast == 256) {
+        if (a.W == 2 && a.xs && nrows == 2) {
+          // middle stage, then the last stage (no twiddles) straight from
+          // registers into the strips: thread pair (2b, 2b+1) = rows r0, r0+1
+          // of butterfly b; each writes 16 bytes (storage positions p, p+1 of
+          // its row) of the same 32-byte strip sector
+          constexpr int RL = FastSched<NX>::rlast;
+          __syncthreads();
+          fstage_tab<NX, FastSched<NX>::r1, NX / FastSched<NX>::r0, -1>(buf, kRowPair, Px, 1, tab1, false);
+          __syncthreads();
+          {
+            const int b = threadIdx.x >> 1, l = threadIdx.x & 1;
+            C x[RL];
+#pragma unroll
+            for (int t = 0; t < RL; ++t) x[t] = buf[l * Px + b * RL + t];
+            DFT<RL, -1, C>::run(x);
+            float4* d4 = reinterpret_cast<float4*>(a.Rbuf + (size_t)u * a.nstrips * a.pny * 2);
+            const size_t rowoff = (size_t)r0 + l;
+            if constexpr (RL % 2 == 0) {
+#pragma unroll
+              for (int f = 0; f < RL; f += 2) {
+                const int s2 = (b * RL + f) >> 1;
+                d4[(size_t)s2 * a.pny + rowoff] = make_float4(x[f].x, x[f].y, x[f + 1].x, x[f + 1].y);
+              }
+            } else {
+              // odd RL: even b also writes (its last, b+1's first), from lane + 2
+              const C nxt0 = make_float2(__shfl_down_sync(0xffffffffu, x[0].x, 2),
+                                         __shfl_down_sync(0xffffffffu, x[0].y, 2));
+              const int f0 = b & 1;                     // first paired output
+#pragma unroll
+              for (int f = 0; f + 1 < RL; ++f) {
+                if (((f - f0) & 1) == 0 && f >= f0) {
+                  const int s2 = (b * RL + f) >> 1;
+                  d4[(size_t)s2 * a.pny + rowoff] = make_float4(x[f].x, x[f].y, x[f + 1].x, x[f + 1].y);
+                }
+              }
+              if (f0 == 0) {
+                const int s2 = (b * RL + RL - 1) >> 1;
+                d4[(size_t)s2 * a.pny + rowoff] = make_float4(x[RL - 1].x, x[RL - 1].y, nxt0.x, nxt0.y);
+              }
+            }
+          }
+          __syncthreads();
+          continue;
+        }
       }
       FastSched<NX>::template run_rest_tab<-1>(buf, kRowPair, Px, 1, tab1, tw, false);
       __syncthreads();
