@@ -44,9 +44,8 @@ __device__ __forceinline__ void dft2(C& a, C& b) {
 template <int SGN, typename C>
 __device__ __forceinline__ void dft4(C& x0, C& x1, C& x2, C& x3) {
   C t0 = cadd(x0, x2), t1 = csub(x0, x2), t2 = cadd(x1, x3), t3 = csub(x1, x3);
-  C u3 = cmul_i<SGN>(t3);   // forward: -i*t3
   x0 = cadd(t0, t2); x2 = csub(t0, t2);
-  x1 = cadd(t1, u3); x3 = csub(t1, u3);
+  x1 = cadd_i<SGN>(t1, t3); x3 = cadd_i<-SGN>(t1, t3);   // forward: t1 -/+ i t3
 }
 
 template <int SGN, typename C>
@@ -55,10 +54,9 @@ __device__ __forceinline__ void dft3(C& x0, C& x1, C& x2) {
   const R c = (R)0.86602540378443864676;   // sqrt(3)/2
   C t = cadd(x1, x2), d = csub(x1, x2);
   C y0 = cadd(x0, t);
-  C m; m.x = x0.x - (R)0.5 * t.x; m.y = x0.y - (R)0.5 * t.y;
+  C m = caxpy((R)-0.5, t, x0);
   // forward y1 = m - i c d, y2 = m + i c d
-  C icd = cmul_i<SGN>(cscale(d, c));
-  x0 = y0; x1 = cadd(m, icd); x2 = csub(m, icd);
+  x0 = y0; x1 = caxpy_i<SGN>(c, d, m); x2 = caxpy_i<-SGN>(c, d, m);
 }
 
 template <int SGN, typename C>
@@ -70,15 +68,14 @@ __device__ __forceinline__ void dft5(C& x0, C& x1, C& x2, C& x3, C& x4) {
   const R s2 = (R)0.58778525229247312917;   // sin(4pi/5)
   C a1 = cadd(x1, x4), b1 = csub(x1, x4), a2 = cadd(x2, x3), b2 = csub(x2, x3);
   C y0 = cadd(x0, cadd(a1, a2));
-  C p1, p2, q1, q2;
-  p1.x = x0.x + c1 * a1.x + c2 * a2.x; p1.y = x0.y + c1 * a1.y + c2 * a2.y;
-  p2.x = x0.x + c2 * a1.x + c1 * a2.x; p2.y = x0.y + c2 * a1.y + c1 * a2.y;
-  q1.x = s1 * b1.x + s2 * b2.x; q1.y = s1 * b1.y + s2 * b2.y;
-  q2.x = s2 * b1.x - s1 * b2.x; q2.y = s2 * b1.y - s1 * b2.y;
-  C iq1 = cmul_i<SGN>(q1), iq2 = cmul_i<SGN>(q2);   // forward: -i q
+  const C p1 = caxpy(c2, a2, caxpy(c1, a1, x0));
+  const C p2 = caxpy(c1, a2, caxpy(c2, a1, x0));
+  const C q1 = caxpy(s2, b2, cscale(b1, s1));
+  const C q2 = caxpy(-s1, b2, cscale(b1, s2));
   x0 = y0;
-  x1 = cadd(p1, iq1); x4 = csub(p1, iq1);
-  x2 = cadd(p2, iq2); x3 = csub(p2, iq2);
+  // forward: p -/+ i q
+  x1 = cadd_i<SGN>(p1, q1); x4 = cadd_i<-SGN>(p1, q1);
+  x2 = cadd_i<SGN>(p2, q2); x3 = cadd_i<-SGN>(p2, q2);
 }
 
 template <int SGN, typename C>
@@ -94,11 +91,10 @@ __device__ __forceinline__ void dft8(C* x) {
   w1.x = h; w1.y = (R)SGN * h;
   w3.x = -h; w3.y = (R)SGN * h;
   o1 = cmul(o1, w1);
-  o2 = cmul_i<SGN>(o2);
   o3 = cmul(o3, w3);
   x[0] = cadd(e0, o0); x[4] = csub(e0, o0);
   x[1] = cadd(e1, o1); x[5] = csub(e1, o1);
-  x[2] = cadd(e2, o2); x[6] = csub(e2, o2);
+  x[2] = cadd_i<SGN>(e2, o2); x[6] = cadd_i<-SGN>(e2, o2);
   x[3] = cadd(e3, o3); x[7] = csub(e3, o3);
 }
 

@@ -71,6 +71,15 @@ template <int N, int SGN, typename C>
 __device__ __forceinline__ C wmul(C a, int m) {
   typedef decltype(a.x) R;
   if (m == 0) return a;
+  if (N == 16 && (m == 2 || m == 6)) {
+    // W16^2 = h (1 + SGN i), W16^6 = -h (1 - SGN i), h = sqrt(1/2): a sum
+    // and a difference, then one real scale
+    const R h = (R)0.70710678118654752440;
+    C u;
+    if (m == 2) { u.x = a.x - (R)SGN * a.y; u.y = a.y + (R)SGN * a.x; return cscale(u, h); }
+    u.x = a.x + (R)SGN * a.y; u.y = a.y - (R)SGN * a.x;
+    return cscale(u, -h);
+  }
   R c, s;
   if (N == 16) {
     // reduce m in [1, 9] to the first quadrant: W16^m for m = 4 is -i (fwd)
@@ -206,12 +215,11 @@ __device__ __forceinline__ void dft16_halfzero(C* x) {
   for (int n2 = 0; n2 < 4; ++n2) {
     const C x0 = x[n2], x3 = x[n2 + 12];
     // y_k = x0 + x3 * W4^(3k) = x0 + x3 * (-SGN i)^k
-    const C ix3 = cmul_i<-SGN>(x3);
     C v[4];
     v[0] = cadd(x0, x3);
-    v[1] = cadd(x0, ix3);
+    v[1] = cadd_i<-SGN>(x0, x3);
     v[2] = csub(x0, x3);
-    v[3] = csub(x0, ix3);
+    v[3] = cadd_i<SGN>(x0, x3);
 #pragma unroll
     for (int k1 = 0; k1 < 4; ++k1) a[n2 * 4 + k1] = wmul<16, SGN>(v[k1], n2 * k1);
   }

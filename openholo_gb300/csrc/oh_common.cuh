@@ -25,17 +25,31 @@ template <typename C> __host__ __device__ __forceinline__ C cmulc(C a, C b) {
   C r; r.x = a.x * b.x + a.y * b.y; r.y = a.y * b.x - a.x * b.y; return r;
 }
 template <typename C, typename R> __host__ __device__ __forceinline__ C cscale(C a, R s) { C r; r.x = a.x * s; r.y = a.y * s; return r; }
+// s a + b, s real
+template <typename C, typename R> __host__ __device__ __forceinline__ C caxpy(R s, C a, C b) {
+  C r; r.x = s * a.x + b.x; r.y = s * a.y + b.y; return r;
+}
 #if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
-// FP32 complex add, subtract and real scale as one packed two-lane
+// FP32 complex add, subtract, real scale and real axpy as one packed two-lane
 // instruction each (sm_100 family); per component the rounding is that of
 // the scalar operation (a - b = a + (-1) b, the product exact)
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return __fmul2_rn(a, make_float2(s, s)); }
+__device__ __forceinline__ float2 caxpy(float s, float2 a, float2 b) { return __ffma2_rn(make_float2(s, s), a, b); }
 #endif
 // multiply by -i (forward) or +i (inverse): sgn = -1 -> -i*a, sgn = +1 -> i*a
 template <int SGN, typename C> __host__ __device__ __forceinline__ C cmul_i(C a) {
   C r; if (SGN < 0) { r.x = a.y; r.y = -a.x; } else { r.x = -a.y; r.y = a.x; } return r;
+}
+// a + cmul_i<SGN>(b) and a + s cmul_i<SGN>(b), component by component (the
+// swapped halves of b do not form a packed pair)
+template <int SGN, typename C> __host__ __device__ __forceinline__ C cadd_i(C a, C b) {
+  C r; if (SGN < 0) { r.x = a.x + b.y; r.y = a.y - b.x; } else { r.x = a.x - b.y; r.y = a.y + b.x; } return r;
+}
+template <int SGN, typename C, typename R> __host__ __device__ __forceinline__ C caxpy_i(R s, C b, C a) {
+  C r; if (SGN < 0) { r.x = a.x + s * b.y; r.y = a.y - s * b.x; } else { r.x = a.x - s * b.y; r.y = a.y + s * b.x; }
+  return r;
 }
 
 // Launch accounting (read through oh_kernel_launch_count()).
