@@ -220,14 +220,68 @@ constexpr int kRowPair = 2;
 // up to 4320); the register cap that comes with it applies only there
 template <int NX> constexpr int row_min_blocks() { return NX > 0 && NX <= 4320 ? 2 : 1; }
 
+// Shared-memory layout of the row pass's fused path (three-stage schedules
+// whose last stage has 256 butterflies per row, two rows, last stage stored
+// straight from registers): element p of row l sits at l LS + (p / M1) BS +
+// p % M1, M1 = NX / r0 (one stage-0 output block).  The block pad BS - M1
+// puts consecutive blocks Q1 = M1 / r1 bank pairs apart, so the middle
+// stage's half-warps (consecutive butterflies, across a block boundary) hit
+// 16 distinct 8-byte bank pairs; the row stride LS does the same for the last
+// stage (8 butterflies x 2 rows per half-warp).  Where no pad makes both
+// conflict free the plain layout (LS = NX, BS = M1) is kept.
+template <int NX, bool FAST = (NX > 0)> struct RowPad {
+  static constexpr bool fusable = false;
+  static constexpr int LS = NX, BS = 0, LSMAX = NX;
+};
+template <int NX> struct RowPad<NX, true> {
+  typedef FastSched<NX> S;
+  static constexpr bool fusable = S::nstages == 3 && NX / S::rlast == 256;
+  static constexpr int M1 = NX / S::r0, Q1 = M1 / S::r1, RL = S::rlast, NB1 = NX / S::r1;
+  static constexpr int BPB = M1 % RL == 0 ? M1 / RL : 0;    // last-stage butterflies per block
+  static constexpr bool conflict_free(int bs, int ls) {
+    if (BPB == 0) return false;
+    for (int h = 0; h < 2 * NB1 / 16; ++h) {          // middle stage, line-major
+      int seen = 0;
+      for (int i = 0; i < 16; ++i) {
+        const int idx = h * 16 + i, line = idx / NB1, b = idx % NB1;
+        const int e = line * ls + (b / Q1) * bs + b % Q1;
+        if (seen & (1 << (e % 16))) return false;
+        seen |= 1 << (e % 16);
+      }
+    }
+    for (int h = 0; h < 512 / 16; ++h) {              // last stage, thread pairs = rows
+      int seen = 0;
+      for (int i = 0; i < 16; ++i) {
+        const int idx = h * 16 + i, b = idx >> 1, l = idx & 1;
+        const int e = l * ls + (b / BPB) * bs + (b % BPB) * RL;
+        if (seen & (1 << (e % 16))) return false;
+        seen |= 1 << (e % 16);
+      }
+    }
+    return true;
+  }
+  static constexpr int PADB = ((Q1 - M1) % 16 + 16) % 16;
+  static constexpr int pick_ls() {
+    for (int ls = S::r0 * (M1 + PADB); ls < S::r0 * (M1 + PADB) + 16; ++ls)
+      if (conflict_free(M1 + PADB, ls)) return ls;
+    return 0;
+  }
+  static constexpr bool padded = fusable && pick_ls() > 0;
+  static constexpr int LS = padded ? pick_ls() : NX;
+  static constexpr int BS = padded ? M1 + PADB : M1;
+  static constexpr int LSMAX = LS > NX ? LS : NX;
+};
+
 template <typename R, int NX>
 __global__ void __launch_bounds__(512, row_min_blocks<NX>()) dm_row_pass(DMArgs<R> a) {
   typedef typename cplx_of<R>::type C;
   extern __shared__ unsigned char smem_raw[];
   const int Px = a.Px, pnx = a.pnx;
   const int lip = (pnx + 7) & ~7;                       // keeps 16-byte alignment
-  C* buf = reinterpret_cast<C*>(smem_raw);              // [2][Px]
-  C* v = buf + 2 * Px;                                  // [2][pnx] source values
+  typedef RowPad<NX> RP;
+  const int lsmax = NX > 0 ? RP::LSMAX : Px;
+  C* buf = reinterpret_cast<C*>(smem_raw);              // [2][lsmax]
+  C* v = buf + 2 * lsmax;                               // [2][pnx] source values
   int16_t* li = reinterpret_cast<int16_t*>(v + 2 * pnx);   // [2][lip] layer slot per pixel
   uint32_t* mask = reinterpret_cast<uint32_t*>(li + 2 * lip);   // [2][8] layers present per row
   C* twlo = reinterpret_cast<C*>(mask + 16);            // 64 + ceil(Px/64) twiddles (fast path)
@@ -235,6 +289,8 @@ __global__ void __launch_bounds__(512, row_min_blocks<NX>()) dm_row_pass(DMArgs<
   C* tab1 = twhi + (Px + 63) / 64;                      // stage-1 twiddle table (fast path)
   const int r0 = blockIdx.x * kRowPair;
   const int nrows = min(kRowPair, a.pny - r0);
+  // fused last stage + strip store, in the padded layout
+  const bool fused = RP::fusable && a.W == 2 && a.xs && nrows == 2;
   for (int i = threadIdx.x; i < 16; i += blockDim.x) mask[i] = 0u;
   if constexpr (NX > 0) {
     load_tw_split(twlo, twhi, static_cast<const C*>(a.plx.tw), NX);
@@ -283,6 +339,7 @@ __global__ void __launch_bounds__(512, row_min_blocks<NX>()) dm_row_pass(DMArgs<
       constexpr int R0 = FastSched<NX>::r0;
       constexpr int Q0 = NX / R0;
       const TwSplit<C> tw{twlo, twhi};
+      const int ls = fused ? RP::LS : Px, bs = fused ? RP::BS : Q0;
       for (int idx = threadIdx.x; idx < kRowPair * Q0; idx += blockDim.x) {
         const int l = idx / Q0, j = idx - l * Q0;
         const int16_t* lil = li + l * lip;
@@ -317,25 +374,27 @@ __global__ void __launch_bounds__(512, row_min_blocks<NX>()) dm_row_pass(DMArgs<
 #pragma unroll
           for (int f = 1; f < R0; ++f) x[f] = cmul(x[f], wp[f]);
         }
-        C* bl = buf + l * Px;
+        C* bl = buf + l * ls;
 #pragma unroll
-        for (int f = 0; f < R0; ++f) bl[j + f * Q0] = x[f];
+        for (int f = 0; f < R0; ++f) bl[j + f * bs] = x[f];
       }
-      if constexpr (FastSched<NX>::nstages == 3 && NX / FastSched<NX>::rlast == 256) {
-        if (a.W == 2 && a.xs && nrows == 2) {
+      if constexpr (RP::fusable) {
+        if (fused) {
           // middle stage, then the last stage (no twiddles) straight from
           // registers into the strips: thread pair (2b, 2b+1) = rows r0, r0+1
           // of butterfly b; each writes 16 bytes (storage positions p, p+1 of
           // its row) of the same 32-byte strip sector
           constexpr int RL = FastSched<NX>::rlast;
           __syncthreads();
-          fstage_tab<NX, FastSched<NX>::r1, NX / FastSched<NX>::r0, -1>(buf, kRowPair, Px, 1, tab1, false);
+          fstage_tab<NX, FastSched<NX>::r1, NX / FastSched<NX>::r0, -1, C, RP::BS>(buf, kRowPair, RP::LS, 1, tab1,
+                                                                                  false);
           __syncthreads();
           {
             const int b = threadIdx.x >> 1, l = threadIdx.x & 1;
             C x[RL];
+            const C* src = buf + l * RP::LS + (b / RP::BPB) * RP::BS + (b % RP::BPB) * RL;
 #pragma unroll
-            for (int t = 0; t < RL; ++t) x[t] = buf[l * Px + b * RL + t];
+            for (int t = 0; t < RL; ++t) x[t] = src[t];
             DFT<RL, -1, C>::run(x);
             float4* d4 = reinterpret_cast<float4*>(a.Rbuf + (size_t)u * a.nstrips * a.pny * 2);
             const size_t rowoff = (size_t)r0 + l;
@@ -804,11 +863,14 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   const size_t smem_col =
       Wfast ? (size_t)col_layout(a.Py, a.pny, wcol, kColStripW, a.horner != 0, occ_stride, su.n_entries, col_tab).total
             : (size_t)W * a.Py * sizeof(C) + W * (sizeof(C) + sizeof(R)) + (size_t)a.Py * sizeof(int);
-  int row_tab = 0;
+  int row_tab = 0, row_ls = a.Px;
   with_fast_n_if<sizeof(R) == 4>(a.Px, [&](auto nc) {
-    if constexpr (decltype(nc)::value > 0) row_tab = FastSched<decltype(nc)::value>::tab1_entries;
+    if constexpr (decltype(nc)::value > 0) {
+      row_tab = FastSched<decltype(nc)::value>::tab1_entries;
+      row_ls = RowPad<decltype(nc)::value>::LSMAX;
+    }
   });
-  const size_t smem_row = kRowPair * ((size_t)a.Px * sizeof(C) + (size_t)a.pnx * sizeof(C) +
+  const size_t smem_row = kRowPair * ((size_t)row_ls * sizeof(C) + (size_t)a.pnx * sizeof(C) +
                                       (size_t)((a.pnx + 7) & ~7) * sizeof(int16_t)) +
                           16 * sizeof(uint32_t) + (64 + (size_t)(a.Px + 63) / 64 + row_tab) * sizeof(C);
   const size_t smem_out = (size_t)a.Px * sizeof(C) + (64 + (size_t)(a.Px + 63) / 64) * sizeof(C);

@@ -263,8 +263,10 @@ __device__ __forceinline__ void fstage_t(C* buf, int nl, int ls, int es, const T
 }
 
 // One stage with its twiddles from a per-stage table: tab[j (R-1) + f - 1] =
-// W^(SGN j f N/M) for butterfly offset j < M/R, output f = 1..R-1.
-template <int N, int R, int M, int SGN, typename C>
+// W^(SGN j f N/M) for butterfly offset j < M/R, output f = 1..R-1.  BS is the
+// storage distance between consecutive blocks of M elements (M, or more for a
+// padded layout).
+template <int N, int R, int M, int SGN, typename C, int BS = M>
 __device__ __forceinline__ void fstage_tab(C* buf, int nl, int ls, int es, const C* __restrict__ tab,
                                            bool line_fastest) {
   constexpr int Q = M / R;
@@ -275,7 +277,7 @@ __device__ __forceinline__ void fstage_tab(C* buf, int nl, int ls, int es, const
     if (line_fastest) { b = idx / nl; line = idx - b * nl; }
     else { line = idx / NB; b = idx - line * NB; }
     const int blk = b / Q, j = b - blk * Q;
-    const int base = line * ls + (blk * M + j) * es;
+    const int base = line * ls + (blk * BS + j) * es;
     const int st = Q * es;
     C x[R];
 #pragma unroll
