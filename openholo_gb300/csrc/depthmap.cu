@@ -284,8 +284,8 @@ __global__ void __launch_bounds__(512, row_min_blocks<NX>()) dm_row_pass(DMArgs<
   C* v = buf + 2 * lsmax;                               // [2][pnx] source values
   int16_t* li = reinterpret_cast<int16_t*>(v + 2 * pnx);   // [2][lip] layer slot per pixel
   uint32_t* mask = reinterpret_cast<uint32_t*>(li + 2 * lip);   // [2][8] layers present per row
-  C* twlo = reinterpret_cast<C*>(mask + 16);            // 64 + ceil(Px/64) twiddles (fast path)
-  C* twhi = twlo + 64;
+  C* twlo = reinterpret_cast<C*>(mask + 16);            // kTwLo + ceil(Px/64) twiddles (fast path)
+  C* twhi = twlo + kTwLo;
   C* tab1 = twhi + (Px + 63) / 64;                      // stage-1 twiddle table (fast path)
   const int r0 = blockIdx.x * kRowPair;
   const int nrows = min(kRowPair, a.pny - r0);
@@ -583,7 +583,7 @@ __global__ void __launch_bounds__(256) dm_out_pass(DMArgs<R> a) {
   extern __shared__ unsigned char smem_raw[];
   C* buf = reinterpret_cast<C*>(smem_raw);
   C* twlo = buf + a.Px;
-  C* twhi = twlo + 64;
+  C* twhi = twlo + kTwLo;
   const int yl = blockIdx.x;
   const C* row = a.V + (size_t)yl * a.Px;
   if constexpr (NX > 0) load_tw_split(twlo, twhi, static_cast<const C*>(a.plx.tw), NX);
@@ -872,8 +872,8 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   });
   const size_t smem_row = kRowPair * ((size_t)row_ls * sizeof(C) + (size_t)a.pnx * sizeof(C) +
                                       (size_t)((a.pnx + 7) & ~7) * sizeof(int16_t)) +
-                          16 * sizeof(uint32_t) + (64 + (size_t)(a.Px + 63) / 64 + row_tab) * sizeof(C);
-  const size_t smem_out = (size_t)a.Px * sizeof(C) + (64 + (size_t)(a.Px + 63) / 64) * sizeof(C);
+                          16 * sizeof(uint32_t) + (kTwLo + (size_t)(a.Px + 63) / 64 + row_tab) * sizeof(C);
+  const size_t smem_out = (size_t)a.Px * sizeof(C) + (kTwLo + (size_t)(a.Px + 63) / 64) * sizeof(C);
   if (smem_row > smax || smem_out > smax) return fail(OH_ERR_UNSUPPORTED_SIZE, "padded row length " + std::to_string(a.Px) + " exceeds shared memory");
 
   // scratch

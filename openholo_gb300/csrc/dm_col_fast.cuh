@@ -41,7 +41,7 @@ struct ColLayout {
 template <int NY>
 constexpr int col_tab_entries() {
   constexpr int R0 = FastSched<NY>::r0, R1 = FastSched<NY>::r1;
-  constexpr int n = (NY / R0 / R1) * (R1 - 1);
+  constexpr int n = (NY / R0 / R1) * stage_tab_stride(R1);
   return n * 8 <= 8192 ? n : 0;
 }
 
@@ -65,7 +65,7 @@ __host__ __device__ constexpr ColLayout col_layout(int Py, int pny, int W, int s
   L.ey0 = L.g + gb;
   L.ey1 = L.ey0 + eb;
   L.occ = col_take(&o, occ_stride);
-  L.twlo = col_take(&o, 64 * 8);
+  L.twlo = col_take(&o, kTwLo * 8);
   L.twhi = col_take(&o, ((Py + 63) / 64) * 8);
   L.tab = col_take(&o, tab_entries * 8);
   L.exw = col_take(&o, W * 8);

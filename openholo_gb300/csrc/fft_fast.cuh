@@ -174,20 +174,41 @@ template <typename C> struct TwTable {            // full table (global or share
   const C* t;
   __device__ __forceinline__ C operator()(int e) const { return t[e]; }
 };
+// entries of the low table of TwSplit: W^m for m < 64, then W^(4m) for m < 16
+constexpr int kTwLo = 80;
 template <typename C> struct TwSplit {            // W^e = W^(64 (e>>6)) * W^(e & 63)
-  const C* lo;                                    // lo[m] = W_N^m, m < 64
+  const C* lo;                                    // lo[m] = W_N^m, m < 64; lo[64 + m] = W_N^(4m), m < 16
   const C* hi;                                    // hi[m] = W_N^(64 m)
   __device__ __forceinline__ C operator()(int e) const { return cmul(hi[e >> 6], lo[e & 63]); }
+  // W^(4e) = W^(64 (e>>4)) W^(4 (e & 15)): consecutive e read consecutive
+  // entries (lo[4 (e & 15)] would put 16 consecutive e on four bank pairs)
+  __device__ __forceinline__ C pow4(int e) const { return cmul(hi[e >> 4], lo[64 + (e & 15)]); }
 };
 // fill lo/hi (shared memory) from a full table; call with all threads, then sync
 template <typename C>
 __device__ __forceinline__ void load_tw_split(C* lo, C* hi, const C* tw, int n) {
-  for (int m = threadIdx.x; m < 64; m += blockDim.x) lo[m] = m < n ? tw[m] : tw[0];
+  for (int m = threadIdx.x; m < kTwLo; m += blockDim.x) {
+    const int e = m < 64 ? m : 4 * (m - 64);
+    lo[m] = e < n ? tw[e] : tw[0];
+  }
   for (int m = threadIdx.x; m < (n + 63) / 64; m += blockDim.x) hi[m] = tw[64 * m];
 }
 template <int SGN, typename C, class TW>
 __device__ __forceinline__ C twid(const TW& tw, int e) {
   C w = tw(e);
+  if (SGN > 0) w.y = -w.y;
+  return w;
+}
+// W^(4e), conjugated for SGN > 0
+template <int SGN, typename C, class TW>
+__device__ __forceinline__ C twid4(const TW& tw, int e) {
+  C w = tw(4 * e);
+  if (SGN > 0) w.y = -w.y;
+  return w;
+}
+template <int SGN, typename C>
+__device__ __forceinline__ C twid4(const TwSplit<C>& tw, int e) {
+  C w = tw.pow4(e);
   if (SGN > 0) w.y = -w.y;
   return w;
 }
@@ -200,7 +221,7 @@ __device__ __forceinline__ void twiddle_powers(const TW& tw, int e, C* w) {
   if constexpr (R > 2) w[2] = cmul(w[1], w[1]);
   if constexpr (R > 3) w[3] = cmul(w[2], w[1]);
   if constexpr (R > 4) {
-    w[4] = twid<SGN, C>(tw, 4 * e);
+    w[4] = twid4<SGN, C>(tw, e);
 #pragma unroll
     for (int f = 5; f < R; ++f) w[f] = cmul(w[f - 4], w[4]);
   }
@@ -262,8 +283,13 @@ __device__ __forceinline__ void fstage_t(C* buf, int nl, int ls, int es, const T
   }
 }
 
-// One stage with its twiddles from a per-stage table: tab[j (R-1) + f - 1] =
-// W^(SGN j f N/M) for butterfly offset j < M/R, output f = 1..R-1.  BS is the
+// Row stride of a per-stage twiddle table: R - 1 rounded up to odd, so that
+// consecutive butterflies j read from distinct shared-memory bank pairs.
+constexpr int stage_tab_stride(int R) { return (R - 1) | 1; }
+
+// One stage with its twiddles from a per-stage table: tab[j TS + f - 1] =
+// W^(SGN j f N/M) for butterfly offset j < M/R, output f = 1..R-1, TS =
+// stage_tab_stride(R).  BS is the
 // storage distance between consecutive blocks of M elements (M, or more for a
 // padded layout).
 template <int N, int R, int M, int SGN, typename C, int BS = M>
@@ -284,7 +310,7 @@ __device__ __forceinline__ void fstage_tab(C* buf, int nl, int ls, int es, const
     for (int t = 0; t < R; ++t) x[t] = buf[base + t * st];
     DFT<R, SGN, C>::run(x);
     if (Q > 1 && j) {
-      const C* tj = tab + j * (R - 1) - 1;
+      const C* tj = tab + j * stage_tab_stride(R) - 1;
 #pragma unroll
       for (int f = 1; f < R; ++f) x[f] = cmul(x[f], tj[f]);
     }
@@ -299,9 +325,10 @@ template <int N, int R, int M, int SGN, typename C>
 __device__ __forceinline__ void fill_stage_tab(C* tab, const C* __restrict__ tw) {
   constexpr int Q = M / R;
   constexpr int TWS = N / M;
-  for (int i = threadIdx.x; i < Q * (R - 1); i += blockDim.x) {
-    const int j = i / (R - 1), f = i - j * (R - 1) + 1;
-    C w = tw[(j * f * TWS) % N];
+  constexpr int TS = stage_tab_stride(R);
+  for (int i = threadIdx.x; i < Q * TS; i += blockDim.x) {
+    const int j = i / TS, f = i - j * TS + 1;
+    C w = tw[(j * (f < R ? f : 0) * TWS) % N];       // f = R: the pad entry
     if (SGN > 0) w.y = -w.y;
     tab[i] = w;
   }
@@ -428,7 +455,7 @@ struct SchedImpl {
     return k;
   }
   // entries of the stage-1 twiddle table (fill_stage_tab<N, r1, N / r0>)
-  static constexpr int tab1_entries = (N / R0 / r1) * (r1 - 1);
+  static constexpr int tab1_entries = (N / R0 / r1) * stage_tab_stride(r1);
   // as run_rest, with stage 1's twiddles from its table tab1
   template <int SGN, typename C, class TW>
   __device__ __forceinline__ static void run_rest_tab(C* buf, int nl, int ls, int es, const C* tab1, const TW& tw,

@@ -148,7 +148,7 @@ struct FrArgs {
   const float2* hys;         // (-1)^v Hy(v) / (4 nx ny), natural order
 };
 
-__host__ __device__ constexpr int fr_tw_entries(int n) { return 64 + (n + 63) / 64; }
+__host__ __device__ constexpr int fr_tw_entries(int n) { return kTwLo + (n + 63) / 64; }
 
 template <int NY> struct FrColCfg {
   static constexpr int R0 = FastSched<NY>::r0;
@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(FrColCfg<NY>::T, FrColCfg<NY>::MINB) fr_col(Fr
   extern __shared__ __align__(16) unsigned char smem[];
   C* buf = reinterpret_cast<C*>(smem);               // [NY][W]
   C* twlo = buf + NY * W;
-  C* twhi = twlo + 64;
+  C* twhi = twlo + kTwLo;
   const int tid = threadIdx.x, s = blockIdx.x, ny = a.ny;
   C* strip = a.R + (size_t)s * ny * W;
   load_tw_split(twlo, twhi, a.twy, NY);
@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(512) fr_rowconv(FrArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   C* buf = reinterpret_cast<C*>(smem);
   C* twlo = buf + ROWS * NX;
-  C* twhi = twlo + 64;
+  C* twhi = twlo + kTwLo;
   constexpr int Q = NX / 4;                        // = nx / 2
   const int r0 = ROWS * blockIdx.x, nx = a.nx;
   load_tw_split(twlo, twhi, a.twx, NX);
