@@ -283,6 +283,40 @@ __device__ __forceinline__ void fstage_t(C* buf, int nl, int ls, int es, const T
   }
 }
 
+// Adjoint (transpose) of the forward stage fstage_t<N, R, M, -1>: inputs at
+// j + f Q of each block times conj(W^(j f N/M)) for f >= 1, then DFT<R, +1>,
+// outputs back at j + t Q.  The adjoint stages, run in reverse stage order on
+// a line in the forward transform's storage order, compute its unnormalised
+// inverse DFT with the output in natural order (the forward network maps x to
+// P F x, its adjoint maps P y to F^H y = N F^-1 y).
+template <int N, int R, int M, typename C, class TW>
+__device__ __forceinline__ void fstage_adj(C* buf, int nl, int ls, int es, const TW& tw, bool line_fastest) {
+  constexpr int Q = M / R;
+  constexpr int TWS = N / M;
+  constexpr int NB = N / R;
+  const int total = NB * nl;
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    int line, b;
+    if (line_fastest) { b = idx / nl; line = idx - b * nl; }
+    else { line = idx / NB; b = idx - line * NB; }
+    const int blk = b / Q, j = b - blk * Q;
+    const int base = line * ls + (blk * M + j) * es;
+    const int st = Q * es;
+    C x[R];
+#pragma unroll
+    for (int t = 0; t < R; ++t) x[t] = buf[base + t * st];
+    if (Q > 1 && j) {
+      C w[R];
+      twiddle_powers<R, 1>(tw, j * TWS, w);
+#pragma unroll
+      for (int f = 1; f < R; ++f) x[f] = cmul(x[f], w[f]);
+    }
+    DFT<R, 1, C>::run(x);
+#pragma unroll
+    for (int t = 0; t < R; ++t) buf[base + t * st] = x[t];
+  }
+}
+
 // Row stride of a per-stage twiddle table: R - 1 rounded up to odd, so that
 // consecutive butterflies j read from distinct shared-memory bank pairs.
 constexpr int stage_tab_stride(int R) { return (R - 1) | 1; }

@@ -156,17 +156,24 @@ template <int NY> struct FrColCfg {
   static constexpr int NBL = (NY / RL) * kFrW;        // last-stage butterflies in the strip
   static constexpr int KB = NBL > 768 ? 2 : 1;         // butterflies per thread
   static constexpr int T = ((NBL + KB - 1) / KB + 31) / 32 * 32;
-  // two blocks per SM when two strips fit in shared memory
+  // two blocks per SM when two strips fit in shared memory (at 4320, 576
+  // threads x 2 blocks cap the registers at 56 with a few spills; measured
+  // still faster than 288 threads with two butterflies each)
   static constexpr int MINB = (NY * kFrW + fr_tw_entries(NY)) * 8 <= 113 * 1024 ? 2 : 1;
 };
 
 // One strip of kFrW columns (already convolved along x) per block: y-FFT,
-// times Hy, inverse y-FFT, crop; the result overwrites the strip.
+// times Hy, inverse y-FFT, crop; the result overwrites the strip.  The last
+// forward stage, Hy and the first stage of the inverse run in registers; the
+// inverse is the adjoint of the forward network (storage order in, natural
+// order out), and its last stage computes only the outputs of the crop and
+// stores them straight into the strip.
 template <int NY>
 __global__ void __launch_bounds__(FrColCfg<NY>::T, FrColCfg<NY>::MINB) fr_col(FrArgs a) {
   typedef float2 C;
   typedef FrColCfg<NY> CF;
   constexpr int W = kFrW, T = CF::T, R0 = CF::R0, RL = CF::RL, KB = CF::KB;
+  constexpr int R1 = FastSched<NY>::r1;
   constexpr int Q0 = NY / R0, QY = NY / 4;
   static_assert(FastSched<NY>::nstages == 3, "three-stage schedule expected");
   static_assert(R0 % 4 == 0, "stage-0 radix must split the line into quarters");
@@ -174,8 +181,8 @@ __global__ void __launch_bounds__(FrColCfg<NY>::T, FrColCfg<NY>::MINB) fr_col(Fr
   C* buf = reinterpret_cast<C*>(smem);               // [NY][W]
   C* twlo = buf + NY * W;
   C* twhi = twlo + kTwLo;
-  const int tid = threadIdx.x, s = blockIdx.x, ny = a.ny;
-  C* strip = a.R + (size_t)s * ny * W;
+  const int tid = threadIdx.x, s = blockIdx.x;
+  C* strip = a.R + (size_t)s * a.ny * W;
   load_tw_split(twlo, twhi, a.twy, NY);
   __syncthreads();
   const TwSplit<C> tw{twlo, twhi};
@@ -203,10 +210,9 @@ __global__ void __launch_bounds__(FrColCfg<NY>::T, FrColCfg<NY>::MINB) fr_col(Fr
     for (int f = 0; f < R0; ++f) buf[(j + f * Q0) * W + w] = x[f];
   }
   __syncthreads();
-  fstage_t<NY, FastSched<NY>::r1, NY / R0, -1>(buf, W, 1, W, tw, true);
+  fstage_t<NY, R1, NY / R0, -1>(buf, W, 1, W, tw, true);
   __syncthreads();
-  // last stage (stride 1, no twiddles) and the transfer function, in registers
-  C acc[KB][RL];
+  // last forward stage (stride 1, no twiddles), Hy, first inverse stage
 #pragma unroll
   for (int kb = 0; kb < KB; ++kb) {
     const int bb = tid + kb * T;
@@ -217,79 +223,124 @@ __global__ void __launch_bounds__(FrColCfg<NY>::T, FrColCfg<NY>::MINB) fr_col(Fr
       for (int f = 0; f < RL; ++f) x[f] = buf[(b * RL + f) * W + w];
       DFT<RL, -1, C>::run(x);
 #pragma unroll
-      for (int f = 0; f < RL; ++f) acc[kb][f] = cmul(x[f], __ldg(a.hys + FastSched<NY>::iperm(b * RL + f)));
+      for (int f = 0; f < RL; ++f) x[f] = cmul(x[f], __ldg(a.hys + FastSched<NY>::iperm(b * RL + f)));
+      DFT<RL, 1, C>::run(x);
+#pragma unroll
+      for (int f = 0; f < RL; ++f) buf[(b * RL + f) * W + w] = x[f];
     }
   }
   __syncthreads();
-#pragma unroll
-  for (int kb = 0; kb < KB; ++kb) {
-    const int bb = tid + kb * T;
-    if (bb < CF::NBL) {
-      const int b = bb / W, w = bb - b * W;
-#pragma unroll
-      for (int f = 0; f < RL; ++f) buf[FastSched<NY>::iperm(b * RL + f) * W + w] = acc[kb][f];
-    }
-  }
-  FastSched<NY>::template run_t<1>(buf, W, 1, W, tw, true);
+  fstage_adj<NY, R1, NY / R0>(buf, W, 1, W, tw, true);
   __syncthreads();
-  // crop: output row r is the inverse transform's sample QY + r
-  for (int idx = tid; idx < ny * W; idx += T) {
-    const int r = idx / W, w = idx - r * W;
-    strip[idx] = buf[FastSched<NY>::perm(QY + r) * W + w];
+  // last inverse stage: output row r is sample QY + r = j + t Q0, t in [R0/4, 3R0/4)
+  for (int idx = tid; idx < Q0 * W; idx += T) {
+    const int j = idx / W, w = idx - j * W;
+    C x[R0];
+#pragma unroll
+    for (int f = 0; f < R0; ++f) x[f] = buf[(j + f * Q0) * W + w];
+    if (j) {
+      C wp[R0];
+      twiddle_powers<R0, 1>(tw, j, wp);
+#pragma unroll
+      for (int f = 1; f < R0; ++f) x[f] = cmul(x[f], wp[f]);
+    }
+    DFT<R0, 1, C>::run(x);
+#pragma unroll
+    for (int t = R0 / 4; t < 3 * R0 / 4; ++t) strip[(j + (t - R0 / 4) * Q0) * W + w] = x[t];
   }
 }
 
+// Row stride of fr_rowconv's shared buffer: the padded length rounded up to
+// 8 mod 16 elements, so the two rows of a half-warp use disjoint bank halves
+template <int NX> constexpr int fr_row_stride() { return NX + ((8 - NX % 16) + 16) % 16; }
+
 // Separable form, first pass: two rows per block, each convolved with hx on
-// the padded length (x-FFT of the rotated row, times C (-1)^u Hx(u), back to
-// natural order through registers, inverse x-FFT), cropped to nx columns and
-// stored as strips [nx / kFrW][ny][kFrW] (four threads per 32-byte sector).
+// the padded length, cropped to nx columns and stored as strips
+// [nx / kFrW][ny][kFrW].  Forward x-FFT of the rotated row (stage 0 straight
+// from global memory, half its inputs zero), then in registers the last
+// forward stage, C (-1)^u Hx(u) and the first stage of the inverse; the
+// inverse is the adjoint of the forward network (storage order in, natural
+// order out), and its last stage computes only the cropped outputs and
+// stores them, thread pairs (one per row) filling 32-byte strip sectors.
 template <int NX>
 __global__ void __launch_bounds__(512) fr_rowconv(FrArgs a) {
   typedef float2 C;
+  typedef FastSched<NX> S;
   constexpr int ROWS = 2, NT = 512;
-  constexpr int PER = (ROWS * NX + NT - 1) / NT;
+  constexpr int R0 = S::r0, R1 = S::r1, RL = S::rlast, Q0 = NX / R0, Q = NX / 4;
+  constexpr int LS = fr_row_stride<NX>();
+  static_assert(S::nstages == 3, "three-stage schedule expected");
+  static_assert(R0 % 4 == 0, "stage-0 radix must split the line into quarters");
   extern __shared__ __align__(16) unsigned char smem[];
-  C* buf = reinterpret_cast<C*>(smem);
-  C* twlo = buf + ROWS * NX;
+  C* buf = reinterpret_cast<C*>(smem);               // [ROWS][LS]
+  C* twlo = buf + ROWS * LS;
   C* twhi = twlo + kTwLo;
-  constexpr int Q = NX / 4;                        // = nx / 2
-  const int r0 = ROWS * blockIdx.x, nx = a.nx;
+  const int r0 = ROWS * blockIdx.x, nx = a.nx, ny = a.ny;
   load_tw_split(twlo, twhi, a.twx, NX);
-  const C* src = a.field + (size_t)r0 * nx;
-  for (int idx = threadIdx.x; idx < ROWS * NX; idx += NT) {
-    const int l = idx / NX, p = idx - l * NX;
-    // rotated line: position p holds field column p - 3Q (p >= 3Q) or p + Q (p < Q)
-    int c = -1;
-    if (p >= 3 * Q) c = p - 3 * Q;
-    else if (p < Q) c = p + Q;
-    buf[idx] = c >= 0 ? src[(size_t)l * nx + c] : make_float2(0.f, 0.f);
-  }
+  __syncthreads();
   const TwSplit<C> tw{twlo, twhi};
-  FastSched<NX>::template run_t<-1>(buf, ROWS, NX, 1, tw, false);
-  __syncthreads();
-  C v[PER];
+  const C* src = a.field + (size_t)r0 * nx;
+  // stage 0: rotated line, position p < Q holds column p + Q, p >= 3Q column p - 3Q
+  for (int idx = threadIdx.x; idx < ROWS * Q0; idx += NT) {
+    const int j = idx >> 1, l = idx & 1;
+    C x[R0];
 #pragma unroll
-  for (int i = 0; i < PER; ++i) {
-    const int idx = threadIdx.x + i * NT;
-    if (idx < ROWS * NX) {
-      const int l = idx / NX, p = idx - l * NX;
-      v[i] = cmul(buf[idx], __ldg(a.hxs + p));
+    for (int t = 0; t < R0; ++t) {
+      const int p = j + t * Q0;
+      if (t < R0 / 4) x[t] = src[(size_t)l * nx + p + Q];
+      else if (t >= 3 * R0 / 4) x[t] = src[(size_t)l * nx + p - 3 * Q];
+      else x[t] = make_float2(0.f, 0.f);
     }
+    if constexpr (R0 == 16) dft16_halfzero<-1>(x);
+    else DFT<R0, -1, C>::run(x);
+    if (j) {
+      C wp[R0];
+      twiddle_powers<R0, -1>(tw, j, wp);
+#pragma unroll
+      for (int f = 1; f < R0; ++f) x[f] = cmul(x[f], wp[f]);
+    }
+#pragma unroll
+    for (int f = 0; f < R0; ++f) buf[l * LS + j + f * Q0] = x[f];
   }
   __syncthreads();
-#pragma unroll
-  for (int i = 0; i < PER; ++i) {
-    const int idx = threadIdx.x + i * NT;
-    if (idx < ROWS * NX) {
-      const int l = idx / NX, p = idx - l * NX;
-      buf[l * NX + FastSched<NX>::iperm(p)] = v[i];
-    }
-  }
-  FastSched<NX>::template run_t<1>(buf, ROWS, NX, 1, tw, false);
+  fstage_t<NX, R1, NX / R0, -1>(buf, ROWS, LS, 1, tw, false);
   __syncthreads();
-  for (int idx = threadIdx.x; idx < ROWS * nx; idx += NT) {
-    const int w = idx % kFrW, l = (idx / kFrW) % ROWS, s = idx / (ROWS * kFrW);
-    a.R[((size_t)s * a.ny + r0 + l) * kFrW + w] = buf[l * NX + FastSched<NX>::perm(Q + s * kFrW + w)];
+  // last forward stage (no twiddles), the transfer function, first inverse stage
+  constexpr int NBL = NX / RL;
+  for (int idx = threadIdx.x; idx < ROWS * NBL; idx += NT) {
+    const int l = idx / NBL, b = idx - l * NBL;
+    C* p = buf + l * LS + b * RL;
+    C x[RL];
+#pragma unroll
+    for (int f = 0; f < RL; ++f) x[f] = p[f];
+    DFT<RL, -1, C>::run(x);
+#pragma unroll
+    for (int f = 0; f < RL; ++f) x[f] = cmul(x[f], __ldg(a.hxs + b * RL + f));
+    DFT<RL, 1, C>::run(x);
+#pragma unroll
+    for (int f = 0; f < RL; ++f) p[f] = x[f];
+  }
+  __syncthreads();
+  fstage_adj<NX, R1, NX / R0>(buf, ROWS, LS, 1, tw, false);
+  __syncthreads();
+  // last inverse stage: column c = sample Q + c = j + t Q0, t in [R0/4, 3R0/4)
+  for (int idx = threadIdx.x; idx < ROWS * Q0; idx += NT) {
+    const int j = idx >> 1, l = idx & 1;
+    C x[R0];
+#pragma unroll
+    for (int f = 0; f < R0; ++f) x[f] = buf[l * LS + j + f * Q0];
+    if (j) {
+      C wp[R0];
+      twiddle_powers<R0, 1>(tw, j, wp);
+#pragma unroll
+      for (int f = 1; f < R0; ++f) x[f] = cmul(x[f], wp[f]);
+    }
+    DFT<R0, 1, C>::run(x);
+#pragma unroll
+    for (int t = R0 / 4; t < 3 * R0 / 4; ++t) {
+      const int c = j + (t - R0 / 4) * Q0;
+      a.R[((size_t)(c / kFrW) * ny + r0 + l) * kFrW + (c % kFrW)] = x[t];
+    }
   }
 }
 
@@ -413,7 +464,11 @@ static oh_status run_fresnel_separable(oh_ctx* ctx, int nx, int ny, double dp, d
   const int scol = (NY * kFrW + fr_tw_entries(NY)) * (int)sizeof(float2);
   // rows convolved with hx and cropped to nx, then the nx / 2 strips with
   // hy (cropped to ny in place), then strips to rows
-  const int srow = (2 * NX + fr_tw_entries(NX)) * (int)sizeof(float2);
+  int row_ls = NX;
+  with_fast_n(NX, [&](auto nc) {
+    if constexpr (decltype(nc)::value > 0) row_ls = fr_row_stride<decltype(nc)::value>();
+  });
+  const int srow = (2 * row_ls + fr_tw_entries(NX)) * (int)sizeof(float2);
   OH_CUDA_TRY(cudaFuncSetAttribute(k.rowconv, cudaFuncAttributeMaxDynamicSharedMemorySize, srow));
   OH_CUDA_TRY(cudaFuncSetAttribute(k.col, cudaFuncAttributeMaxDynamicSharedMemorySize, scol));
   {
@@ -441,7 +496,7 @@ static oh_status run_fresnel(oh_ctx* ctx, int nx, int ny, double dp, double lamb
     FrKernels k;
     const bool even = nx % 2 == 0 && ny % 2 == 0;
     if (even && !getenv("OH_FRESNEL_GRID") && fr_pick(2 * nx, 2 * ny, &k) &&
-        (size_t)(2 * (2 * nx) + fr_tw_entries(2 * nx)) * sizeof(float2) <= max_smem_per_block())
+        (size_t)(2 * (2 * nx + 15) + fr_tw_entries(2 * nx)) * sizeof(float2) <= max_smem_per_block())
       return run_fresnel_separable(ctx, nx, ny, dp, lambda, z, static_cast<float2*>(field), k, st);
   }
   return run_fresnel_grid<R>(ctx, nx, ny, dp, lambda, z, field, st);
