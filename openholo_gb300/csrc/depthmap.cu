@@ -587,6 +587,25 @@ __global__ void __launch_bounds__(256) dm_out_pass(DMArgs<R> a) {
   const int yl = blockIdx.x;
   const C* row = a.V + (size_t)yl * a.Px;
   if constexpr (NX > 0) load_tw_split(twlo, twhi, static_cast<const C*>(a.plx.tw), NX);
+  if constexpr (NX > 0) {
+    if (a.xs) {
+      // V column p holds spectrum column kx = (iperm[p] + hx) mod Px, whose
+      // place in the inverse line is (kx + hx) mod Px = iperm[p]: the row is
+      // in the x-FFT's storage order, the input order of the adjoint network
+      // (output in natural order)
+      for (int p = threadIdx.x; p < NX; p += blockDim.x) buf[p] = row[p];
+      FastSched<NX>::run_adj(buf, 1, NX, 1, TwSplit<C>{twlo, twhi}, false);
+      __syncthreads();
+      for (int c = threadIdx.x; c < a.pnx; c += blockDim.x) {
+        int m = a.ox + c - a.hx; if (m < 0) m += NX;
+        C h = buf[m];
+        if (a.sig_x != 0) h = cmul(h, a.shx[c]);
+        a.fringe[(size_t)yl * a.pnx + c] = h.x;
+        if (a.field) a.field[(size_t)yl * a.pnx + c] = h;
+      }
+      return;
+    }
+  }
   if (a.xs) {
     // V column p holds spectrum column kx = (iperm[p] + hx) mod Px; the
     // inverse line wants it at j = (kx + hx) mod Px

@@ -358,32 +358,41 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
     }
   }
 
-  // SSB crop and inverse y-FFT input order: spectrum row ky -> i = (ky + hy) mod NY
+  // SSB crop, then the inverse y-FFT.  Spectrum row ky sits in the inverse
+  // line at (ky + hy) mod NY = iperm(p) for storage position p: the
+  // accumulators are in the forward FFT's storage order, the input order of
+  // the adjoint network, whose first stage (the adjoint of the last forward
+  // stage) runs here in registers; the output comes out in natural order.
 #pragma unroll
   for (int kb = 0; kb < KB; ++kb) {
     const int bb = tid + kb * T;
     if (bb < CF::NBL) {
       const int b = bb / W, w = bb - b * W;
       const int kx = kxw[w];
+      C x[RL];
 #pragma unroll
       for (int f = 0; f < RL; ++f) {
         int ky = FastSched<NY>::iperm(b * RL + f) + a.hy;      // spectrum row at storage position
         if (ky >= NY) ky -= NY;
         if (a.spectrum) a.spectrum[(size_t)ky * a.Px + kx] = acc[kb][f];
         const bool keep = kx >= a.cx1 && kx <= a.cx2 && ky >= a.cy1 && ky <= a.cy2;
-        int i = ky + a.hy;
-        if (i >= NY) i -= NY;
-        buf[i * W + w] = keep ? acc[kb][f] : make_float2(0.f, 0.f);
+        x[f] = keep ? acc[kb][f] : make_float2(0.f, 0.f);
       }
+      DFT<RL, 1, C>::run(x);
+#pragma unroll
+      for (int f = 0; f < RL; ++f) buf[(b * RL + f) * W + w] = x[f];
     }
   }
-  FastSched<NY>::template run_t<1>(buf, W, 1, W, tw, true);
+  __syncthreads();
+  fstage_adj<NY, R1, NY / R0>(buf, W, 1, W, tw, true);
+  __syncthreads();
+  fstage_adj<NY, R0, NY>(buf, W, 1, W, tw, true);
   __syncthreads();
   for (int idx = tid; idx < pny * W; idx += T) {
     const int yl = idx / W, w = idx - yl * W;
     int m = a.oy + yl - a.hy;
     if (m < 0) m += NY;
-    a.V[(size_t)yl * a.Px + kx0 + w] = cmul(buf[FastSched<NY>::perm(m) * W + w], a.shy[yl]);
+    a.V[(size_t)yl * a.Px + kx0 + w] = cmul(buf[m * W + w], a.shy[yl]);
   }
 }
 

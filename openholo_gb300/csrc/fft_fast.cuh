@@ -317,6 +317,15 @@ __device__ __forceinline__ void fstage_adj(C* buf, int nl, int ls, int es, const
   }
 }
 
+// the adjoints of the stages (R, M), (Rest, M/R), ... in reverse order, each
+// after a block barrier
+template <int N, int M, typename C, class TW, int R, int... Rest>
+__device__ __forceinline__ void fstages_adj(C* buf, int nl, int ls, int es, const TW& tw, bool line_fastest) {
+  if constexpr (sizeof...(Rest) > 0) fstages_adj<N, M / R, C, TW, Rest...>(buf, nl, ls, es, tw, line_fastest);
+  __syncthreads();
+  fstage_adj<N, R, M>(buf, nl, ls, es, tw, line_fastest);
+}
+
 // Row stride of a per-stage twiddle table: R - 1 rounded up to odd, so that
 // consecutive butterflies j read from distinct shared-memory bank pairs.
 constexpr int stage_tab_stride(int R) { return (R - 1) | 1; }
@@ -455,6 +464,12 @@ struct SchedImpl {
   template <int SGN, typename C, class TW>
   __device__ __forceinline__ static void run_t(C* buf, int nl, int ls, int es, const TW& tw, bool lf) {
     fstages_t<N, N, SGN, C, TW, R0, Rest...>(buf, nl, ls, es, tw, lf);
+  }
+  // unnormalised inverse DFT of a line in this schedule's storage order,
+  // output in natural order (the adjoint network)
+  template <typename C, class TW>
+  __device__ __forceinline__ static void run_adj(C* buf, int nl, int ls, int es, const TW& tw, bool lf) {
+    fstages_adj<N, N, C, TW, R0, Rest...>(buf, nl, ls, es, tw, lf);
   }
   // every stage after the first (the caller ran stage 0 itself)
   template <int SGN, typename C, class TW>
