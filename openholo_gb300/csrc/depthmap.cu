@@ -981,16 +981,21 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
             note_launch();
             if ((e = cudaGetLastError()) != cudaSuccess) rs = cuda_fail(e, "dm_col_fast launch");
           };
+          // the layer-step form with the SSB crop of a 2x-padded frame: the
+          // output mask as a compile-time constant
+          const bool ssb = a.horner && a.fkeep == col_ssb_keep<NY>();
           bool done = false;
           if constexpr (col_narrow_ok<NY>()) {
             if (wcol == 1) {
-              if (a.horner) launch(dm_col_fast<NY, 1, true>, ColCfg<NY, 1, true>::T, a.Px);
+              if (ssb) launch(dm_col_fast<NY, 1, true, true>, ColCfg<NY, 1, true>::T, a.Px);
+              else if (a.horner) launch(dm_col_fast<NY, 1, true>, ColCfg<NY, 1, true>::T, a.Px);
               else launch(dm_col_fast<NY, 1, false>, ColCfg<NY, 1, false>::T, a.Px);
               done = true;
             }
           }
           if (!done) {
-            if (a.horner) launch(dm_col_fast<NY, 2, true>, ColCfg<NY, 2, true>::T, a.nstrips);
+            if (ssb) launch(dm_col_fast<NY, 2, true, true>, ColCfg<NY, 2, true>::T, a.nstrips);
+            else if (a.horner) launch(dm_col_fast<NY, 2, true>, ColCfg<NY, 2, true>::T, a.nstrips);
             else launch(dm_col_fast<NY, 2, false>, ColCfg<NY, 2, false>::T, a.nstrips);
           }
         }

@@ -99,8 +99,27 @@ template <int NY, int W, bool STEP> struct ColCfg {
 // read of each strip still hits L2 (measured: 3072 faster, 4096 slower)
 template <int NY> constexpr bool col_narrow_ok() { return NY >= 3072 && NY <= 3840; }
 
+// Last-stage outputs f (bit f) that can reach the SSB crop of a 2x-padded
+// grid with the signal shifted along y (crop rows (NY/2 - NY/4) .. +NY/2 - 1
+// on the 1-based padded grid, spectrum row at storage position b RL + f =
+// (k_low + (NY/RL) f + NY/2) mod NY, k_low < NY/RL): the mask the host
+// derives from the crop window for that case.
+template <int NY> constexpr uint32_t col_ssb_keep() {
+  constexpr int RL = FastSched<NY>::rlast, q = NY / RL;
+  const int cropy = NY / 2, cy1 = cropy - cropy / 2 - 1, cy2 = cy1 + cropy - 1;
+  uint32_t m = 0;
+  for (int f = 0; f < RL; ++f)
+    for (int kl = 0; kl < q; ++kl) {
+      const int ky = (kl + q * f + NY / 2) % NY;
+      if (ky >= cy1 && ky <= cy2) { m |= 1u << f; break; }
+    }
+  return m;
+}
+
 // STEP: evenly spaced layers, accumulated with the layer-step recurrence.
-template <int NY, int W, bool STEP>
+// SSB: the output mask is col_ssb_keep<NY>() at compile time, so the last
+// stage's small DFT computes only the outputs that reach the crop.
+template <int NY, int W, bool STEP, bool SSB = false>
 __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::MINB) dm_col_fast(DMArgs<float> a) {
   typedef float2 C;
   typedef ColCfg<NY, W, STEP> CF;
@@ -178,6 +197,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
     }
   }
   const int nact = s_nact;
+  const uint32_t fkeep = SSB ? col_ssb_keep<NY>() : a.fkeep;
   const TwSplit<C> tw{twlo, twhi};
   const uint32_t strip_bytes = (uint32_t)(pny * SW * 8);
 
@@ -305,7 +325,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
         if constexpr (horner) {
 #pragma unroll
           for (int f = 0; f < RL; ++f) {
-            if (!((a.fkeep >> f) & 1u)) continue;         // outside the SSB crop for every b
+            if (!((fkeep >> f) & 1u)) continue;         // outside the SSB crop for every b
             const C d = dsm[(b * RL + f) * W + w];
             const C t = acc[kb][f];
             acc[kb][f] = make_float2(fmaf(t.x, d.x, fmaf(-t.y, d.y, x[f].x)), fmaf(t.x, d.y, fmaf(t.y, d.x, x[f].y)));
@@ -315,7 +335,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
         const C ex = exw[w];
 #pragma unroll
         for (int f = 0; f < RL; ++f) {
-          if (!((a.fkeep >> f) & 1u)) continue;           // outside the SSB crop for every b
+          if (!((fkeep >> f) & 1u)) continue;           // outside the SSB crop for every b
           const int p = b * RL + f;
           // H = C Ex exp(i (pi lambda z' fy^2 + k z' g)), both phase parts reduced
           float ph = fmaf(kz, gsm[p * W + w], eth[p]);
