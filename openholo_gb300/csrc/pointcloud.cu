@@ -92,7 +92,34 @@ __device__ __forceinline__ float pc_sqrt_approx(float a) {
   return r;
 }
 
+__device__ __forceinline__ float pc_rcp_approx(float a) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+  return r;
+}
+
 inline dim3 pc_grid_f32(int nx, int ny) { return dim3((nx + kPcTX - 1) / kPcTX, (ny + kPcTR - 1) / kPcTR); }
+
+// sin and cos of two phases in [-pi, pi]: the cosine on the FMA pipe (packed
+// two-lane FP32), the sine on the MUFU unit, which also serves the square
+// root and the reciprocal; with both on the MUFU unit it bounds the kernel,
+// with both on the FMA pipe that pipe does.  cos x = Q(x^2), a degree-6
+// polynomial in x^2 fitted here as a near-minimax approximation on [-pi, pi]
+// (Lawson-reweighted least squares on Chebyshev nodes); measured with FP32
+// Horner evaluation: |error| <= 4.2e-7 over [-pi, pi].
+__device__ __forceinline__ void pc_sincos2(float2 x, float2* sn, float2* cs) {
+  *sn = make_float2(__sinf(x.x), __sinf(x.y));
+  const float2 t = __fmul2_rn(x, x);
+  float2 q = make_float2(1.7247606e-09f, 1.7247606e-09f);
+  q = __ffma2_rn(q, t, make_float2(-2.7079776e-07f, -2.7079776e-07f));
+  q = __ffma2_rn(q, t, make_float2(2.4769966e-05f, 2.4769966e-05f));
+  q = __ffma2_rn(q, t, make_float2(-1.3887808e-03f, -1.3887808e-03f));
+  q = __ffma2_rn(q, t, make_float2(4.1666489e-02f, 4.1666489e-02f));
+  q = __ffma2_rn(q, t, make_float2(-4.9999988e-01f, -4.9999988e-01f));
+  *cs = __ffma2_rn(q, t, make_float2(1.f, 1.f));
+}
+
+__device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
 
 __global__ void __launch_bounds__(kPcTX * kPcFTY) pc_direct_f32(PCGeom g, const float4* __restrict__ prm,
                                                               const float* __restrict__ A, const float* __restrict__ RX,
@@ -100,20 +127,21 @@ __global__ void __launch_bounds__(kPcTX * kPcFTY) pc_direct_f32(PCGeom g, const 
                                                               const float* __restrict__ E, int n,
                                                               float2* __restrict__ field, float* __restrict__ fringe,
                                                               int accumulate_field) {
+  // per point: column terms [point][column]; row terms [point][ty][i] for
+  // tile row ty + kPcFTY i, so a thread reads its four rows with one 16-byte load
   __shared__ float sA[kPcPts][kPcTX];
   __shared__ float sX[kPcPts][kPcTX];
-  __shared__ float sB[kPcPts][kPcTR];
-  __shared__ float sR[kPcPts][kPcTR];
-  __shared__ float sE[kPcPts][kPcTR];
+  __shared__ __align__(16) float sB[kPcPts][kPcTR];
+  __shared__ __align__(16) float sR[kPcPts][kPcTR];
+  __shared__ __align__(16) float sE[kPcPts][kPcTR];
   __shared__ float4 sP[kPcPts];
+  static_assert(kPcRows == 4, "four rows per thread: two packed pairs");
   const int tx = threadIdx.x % kPcTX, ty = threadIdx.x / kPcTX;
   const int col = blockIdx.x * kPcTX + tx, row0 = blockIdx.y * kPcTR + ty;
   const float X = (float)(((double)col + 0.5) * g.px - g.hlx);
   const float nk = (float)(-g.k);
   const float inv2pi = 0.15915494309189533577f, two_pi = 6.28318530717958647692f;
-  float re[kPcRows], im[kPcRows];
-#pragma unroll
-  for (int i = 0; i < kPcRows; ++i) re[i] = im[i] = 0.f;
+  float2 re01 = f2(0.f), im01 = f2(0.f), re23 = f2(0.f), im23 = f2(0.f);
   for (int j0 = 0; j0 < n; j0 += kPcPts) {
     const int cnt = min(kPcPts, n - j0);
     __syncthreads();
@@ -125,12 +153,13 @@ __global__ void __launch_bounds__(kPcTX * kPcFTY) pc_direct_f32(PCGeom g, const 
       sX[j][c] = cc < g.nx ? RX[o] : 1.f;
     }
     for (int i = threadIdx.x; i < cnt * kPcTR; i += blockDim.x) {
-      int j = i / kPcTR, r = i - j * kPcTR;
+      int j = i / kPcTR, r = i - j * kPcTR;          // tile row r = ty' + kPcFTY i'
       int rr = blockIdx.y * kPcTR + r;
+      const int slot = (r % kPcFTY) * kPcRows + r / kPcFTY;
       size_t o = (size_t)(j0 + j) * g.ny + rr;
-      sB[j][r] = rr < g.ny ? B[o] : 0.f;
-      sR[j][r] = rr < g.ny ? RY[o] : 1.f;
-      sE[j][r] = rr < g.ny ? E[o] : 0.f;
+      sB[j][slot] = rr < g.ny ? B[o] : 0.f;
+      sR[j][slot] = rr < g.ny ? RY[o] : 1.f;
+      sE[j][slot] = rr < g.ny ? E[o] : 0.f;
     }
     for (int i = threadIdx.x; i < cnt; i += blockDim.x) sP[i] = prm[j0 + i];
     __syncthreads();
@@ -142,24 +171,34 @@ __global__ void __launch_bounds__(kPcTX * kPcFTY) pc_direct_f32(PCGeom g, const 
       const float ndx2 = nk * dx2;
       const float rx = sX[j][tx], a = sA[j][tx];
       const float rxb = rx + p.y;
+      const float4 ry4 = *reinterpret_cast<const float4*>(&sR[j][ty * kPcRows]);
+      const float4 e4 = *reinterpret_cast<const float4*>(&sE[j][ty * kPcRows]);
+      const float4 b4 = *reinterpret_cast<const float4*>(&sB[j][ty * kPcRows]);
 #pragma unroll
-      for (int i = 0; i < kPcRows; ++i) {
-        const int r = ty + kPcFTY * i;
-        const float ry = sR[j][r];
-        const float rr = pc_sqrt_approx(fmaf(ry, ry, dx2));
-        const float num = (rx + rr) + (ry + p.y);
-        const float den = (rr + ry) * rxb * (rx + rr);
-        const float rem = ndx2 * sE[j][r] * __fdividef(num, den);
-        float ph = (a + sB[j][r]) + rem;
-        ph = fmaf(-two_pi, rintf(ph * inv2pi), ph);
-        float sn, cs;
-        __sincosf(ph, &sn, &cs);
-        re[i] = fmaf(p.z, cs, re[i]);
-        im[i] = fmaf(p.z, sn, im[i]);
+      for (int h = 0; h < 2; ++h) {
+        const float2 ry = h ? make_float2(ry4.z, ry4.w) : make_float2(ry4.x, ry4.y);
+        const float2 ee = h ? make_float2(e4.z, e4.w) : make_float2(e4.x, e4.y);
+        const float2 bb = h ? make_float2(b4.z, b4.w) : make_float2(b4.x, b4.y);
+        const float2 t = __ffma2_rn(ry, ry, f2(dx2));
+        const float2 rr = make_float2(pc_sqrt_approx(t.x), pc_sqrt_approx(t.y));
+        const float2 s1 = __fadd2_rn(f2(rx), rr);                           // r_x + r
+        const float2 num = __fadd2_rn(s1, __fadd2_rn(ry, f2(p.y)));          // (r_x + r) + (r_y + rb)
+        const float2 den = __fmul2_rn(__fmul2_rn(__fadd2_rn(rr, ry), f2(rxb)), s1);
+        const float2 q = __fmul2_rn(num, make_float2(pc_rcp_approx(den.x), pc_rcp_approx(den.y)));
+        const float2 rem = __fmul2_rn(__fmul2_rn(f2(ndx2), ee), q);
+        float2 ph = __fadd2_rn(__fadd2_rn(f2(a), bb), rem);
+        const float2 k = __fmul2_rn(ph, f2(inv2pi));
+        ph = __ffma2_rn(f2(-two_pi), make_float2(rintf(k.x), rintf(k.y)), ph);
+        float2 sn, cs;
+        pc_sincos2(ph, &sn, &cs);
+        if (h) { re23 = __ffma2_rn(f2(p.z), cs, re23); im23 = __ffma2_rn(f2(p.z), sn, im23); }
+        else { re01 = __ffma2_rn(f2(p.z), cs, re01); im01 = __ffma2_rn(f2(p.z), sn, im01); }
       }
     }
   }
   if (col >= g.nx) return;
+  const float re[kPcRows] = {re01.x, re01.y, re23.x, re23.y};
+  const float im[kPcRows] = {im01.x, im01.y, im23.x, im23.y};
 #pragma unroll
   for (int i = 0; i < kPcRows; ++i) {
     const int row = row0 + kPcFTY * i;
