@@ -544,6 +544,23 @@ struct Rec {
   int tx, ty, w;
   float sx, base_t, c1, c2, c3, a0c, alpha, beta, kappa;
 };
+// the point list entry of slot k (-1 past the region's end)
+__device__ __forceinline__ int list_at(const int* __restrict__ list, int k, int e) {
+  return k < e ? __ldg(list + k) : -1;
+}
+__device__ __forceinline__ Rec load_rec_at(const WrpPt* __restrict__ pts, int idx) {
+  Rec r;
+  if (idx >= 0) {
+    const WrpPt* q = pts + idx;
+    r.tx = q->tx; r.ty = q->ty; r.w = q->w;
+    r.sx = q->sx; r.base_t = q->base_t; r.c1 = q->c1; r.c2 = q->c2; r.c3 = q->c3;
+    r.a0c = q->a0c; r.alpha = q->alpha; r.beta = q->beta; r.kappa = q->kappa;
+  } else {
+    r.tx = r.ty = 0; r.w = 0;                       // empty slot: every item writes zeros
+    r.sx = r.base_t = r.c1 = r.c2 = r.c3 = r.a0c = r.alpha = r.beta = r.kappa = 0.f;
+  }
+  return r;
+}
 __device__ __forceinline__ Rec load_rec(const WrpPt* __restrict__ pts, const int* __restrict__ list, int k, int e) {
   Rec r;
   if (k < e) {
@@ -615,7 +632,11 @@ __global__ void __launch_bounds__(tcw::kThreads, 3) wrp_tc(WRPGeom g, const WrpP
       offB1[m] = sw_off(2 * (rb + 32 * m) + 1, j);
       XB[m] = X0 + rb + 32 * m;
     }
+    // two-level prefetch: the list entry two stages ahead, the record of the
+    // next stage (its address known a stage in advance), so the dependent
+    // list -> record loads are not on one stage's critical path
     Rec q = load_rec(pts, list, b + j, e);
+    int idx_next = list_at(list, b + kPts + j, e);
     for (int it = 0; it < nst; ++it) {
       const int s = it % kStages;
       const uint32_t ph = (uint32_t)((it / kStages) & 1);
@@ -630,7 +651,8 @@ __global__ void __launch_bounds__(tcw::kThreads, 3) wrp_tc(WRPGeom g, const WrpP
       unsigned char* sAl = sAh + kTile;
       unsigned char* sBh = sAh + 2 * kTile;
       unsigned char* sBl = sAh + 3 * kTile;
-      const Rec qn = load_rec(pts, list, b + (it + 1) * kPts + j, e);
+      const Rec qn = load_rec_at(pts, idx_next);
+      idx_next = list_at(list, b + (it + 2) * kPts + j, e);
       // A: branch-free, rows outside the window (or the plane) get amplitude 0
 #pragma unroll
       for (int m = 0; m < 4; ++m) {
