@@ -68,7 +68,10 @@ __global__ void reduce_final(R* part, int nb) {
 // Enqueue a min/max reduction; result (min,max) lands in red[0], red[1] on the device.
 template <typename R>
 static oh_status reduce(oh_ctx* ctx, const void* in, size_t n, int op, const R* refp, R** red, cudaStream_t st, const char* slot) {
-  const int nb = 512;
+  // 16 blocks of 256 threads per SM: one load in flight per thread, so the
+  // thread count sets how many bytes are in flight (512 blocks kept the read
+  // of a 66 MB field near a quarter of the HBM bandwidth)
+  const int nb = (int)std::max<size_t>(1, std::min<size_t>((n + 255) / 256, 152 * 16));
   void* ptr;
   OH_TRY(scratch(ctx, slot, sizeof(R) * 2 * nb, &ptr));
   *red = (R*)ptr;
