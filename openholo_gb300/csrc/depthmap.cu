@@ -1171,10 +1171,21 @@ oh_status oh_depthmap_generate_host(oh_ctx* ctx, oh_precision prec, const oh_dep
   const size_t n = (size_t)p->pnx * p->pny;
   const size_t fsz = n * (prec == OH_FP64 ? sizeof(double) : sizeof(float));
   void* dev;
+  // A page-locked (or registered) fringe buffer is written by the output
+  // kernel itself through its device mapping: the result reaches host memory
+  // while the pass runs, with no device-to-host copy after it.  Pageable
+  // buffers get the copy.
+  void* fringe_mapped = nullptr;
   {
     std::lock_guard<std::mutex> lk(ctx->mu);
     int prev = 0; cudaGetDevice(&prev); cudaSetDevice(ctx->device);
     oh_status s = scratch(ctx, "host.io", 2 * n + (phase_host ? 4 * n : 0) + fsz + 1024, &dev);
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, fringe_host) == cudaSuccess) {
+      if (at.type == cudaMemoryTypeHost && at.devicePointer) fringe_mapped = at.devicePointer;
+    } else {
+      cudaGetLastError();
+    }
     cudaSetDevice(prev);
     if (s != OH_OK) return s;
   }
@@ -1187,8 +1198,9 @@ oh_status oh_depthmap_generate_host(oh_ctx* ctx, oh_precision prec, const oh_dep
   OH_CUDA_TRY(cudaMemcpyAsync(d_img, img_host, n, cudaMemcpyHostToDevice, st));
   OH_CUDA_TRY(cudaMemcpyAsync(d_depth, depth_host, n, cudaMemcpyHostToDevice, st));
   if (phase_host) OH_CUDA_TRY(cudaMemcpyAsync(d_phase, phase_host, 4 * n, cudaMemcpyHostToDevice, st));
-  OH_TRY(oh_depthmap_generate(ctx, prec, p, d_img, d_depth, d_phase, d_fringe, nullptr, nullptr, stream));
-  OH_CUDA_TRY(cudaMemcpyAsync(fringe_host, d_fringe, fsz, cudaMemcpyDeviceToHost, st));
+  OH_TRY(oh_depthmap_generate(ctx, prec, p, d_img, d_depth, d_phase, fringe_mapped ? fringe_mapped : d_fringe,
+                              nullptr, nullptr, stream));
+  if (!fringe_mapped) OH_CUDA_TRY(cudaMemcpyAsync(fringe_host, d_fringe, fsz, cudaMemcpyDeviceToHost, st));
   OH_CUDA_TRY(cudaStreamSynchronize(st));
   return OH_OK;
 }

@@ -245,6 +245,11 @@ def test_host_entry_point_matches_device(ctx, dev):
     fr_dev = run(ctx, dev, img, depth, p, None, "fp32")
     fr_host = dm.generate_host(ctx, p, img, depth)
     assert np.array_equal(fr_dev, fr_host)
+    # page-locked output: written by the output kernel through its mapping
+    pinned = torch.empty((ny, nx), dtype=torch.float32, pin_memory=True)
+    pinned.fill_(float("nan"))
+    fr_pinned = dm.generate_host(ctx, p, img, depth, out=pinned.numpy())
+    assert np.array_equal(fr_dev, fr_pinned)
 
 
 def test_table_cache_across_parameter_changes(ctx, dev):
