@@ -21,6 +21,7 @@
 // bounded by about k |E| / 2: a few rad for paraxial scenes, ~1e3 rad for
 // the strongly off-axis KETI sample over its full 1 mm SLM.
 // FP64 path: the direct formula in double precision.
+#include <algorithm>
 #include <cmath>
 #include <mutex>
 #include <vector>
@@ -38,44 +39,87 @@ constexpr int kPcChunk = 32768;    // points per table chunk
 constexpr int kPcTX = 32, kPcTY = 8, kPcPts = 64;
 
 // Per point: x_j, rb, amplitude; per point and column: A, r_x; per point
-// and row: B, r_y, E = r_y - rb.
+// and row: B, r_y, E = r_y - rb.  One block per point (grid-stride), so the
+// point's FP64 terms are formed once per thread and the table rows are
+// written coalesced.
+//
+// FP64 is slow on this part (about 1/64 of the FP32 rate), so only the large
+// phase terms use it.  With d = dx (or dy) and R = rb (or |z|),
+//   k (sqrt(d^2 + R^2) - R) = k d^2 / (2R) - k d^4 / (2R (r + R)^2),
+// the paraxial part (up to ~1e3 rad; k R up to ~1e6 rad) in FP64, reduced
+// mod 2 pi, the remainder in FP32.  The remainder is at most k d^4 / (8 R^3)
+// over the point's rows or columns; where that bound reaches 4 rad the point
+// keeps the all-FP64 form (strongly off-axis or near scenes).
 __global__ void pc_tables(PCGeom g, const float4* __restrict__ pts, int n, float4* __restrict__ prm,
                           float* __restrict__ A, float* __restrict__ RX, float* __restrict__ B,
                           float* __restrict__ RY, float* __restrict__ E) {
   const double two_pi = 6.283185307179586476925286766559;
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nthr = gridDim.x * blockDim.x;
-  for (int j = tid; j < n; j += nthr) {
-    float4 p = pts[j];
-    double x = (double)p.x * g.sx, y = (double)p.y * g.sy, z = (double)p.z * g.sz + g.off;
-    prm[j] = make_float4((float)x, (float)sqrt(y * y + z * z), p.w, 0.f);
-  }
-  for (long long idx = tid; idx < (long long)n * g.nx; idx += nthr) {
-    int j = (int)(idx / g.nx), c = (int)(idx - (long long)j * g.nx);
-    float4 p = pts[j];
-    double x = (double)p.x * g.sx, y = (double)p.y * g.sy, z = (double)p.z * g.sz + g.off;
-    double rb = sqrt(y * y + z * z);
-    double X = ((double)c + 0.5) * g.px - g.hlx;
-    double dx = X - x;
-    double rx = sqrt(dx * dx + rb * rb);
-    double ph = g.k * (dx * dx / (rx + rb)) - g.k * X * g.stx;      // k (r_x - rb) - k X sin tx
-    ph -= two_pi * rint(ph / two_pi);
-    A[idx] = (float)ph;
-    RX[idx] = (float)rx;
-  }
-  for (long long idx = tid; idx < (long long)n * g.ny; idx += nthr) {
-    int j = (int)(idx / g.ny), r = (int)(idx - (long long)j * g.ny);
-    float4 p = pts[j];
-    double y = (double)p.y * g.sy, z = (double)p.z * g.sz + g.off;
-    double Y = g.hly - ((double)r + 0.5) * g.py;
-    double dy = Y - y;
-    double ry = sqrt(dy * dy + z * z), rb = sqrt(y * y + z * z);
-    double kr = g.k * ry;
-    double ph = (kr - two_pi * rint(kr / two_pi)) - g.k * Y * g.sty;
-    ph -= two_pi * rint(ph / two_pi);
-    B[idx] = (float)ph;
-    RY[idx] = (float)ry;
-    E[idx] = (float)((dy * dy - y * y) / (ry + rb));     // r_y - rb without cancellation
+  const double inv_two_pi = 0.15915494309189533576888376337251;
+  for (int j = blockIdx.x; j < n; j += gridDim.x) {
+    const float4 p = pts[j];
+    const double x = (double)p.x * g.sx, y = (double)p.y * g.sy, z = (double)p.z * g.sz + g.off;
+    const double rb = sqrt(y * y + z * z), az = fabs(z);
+    if (threadIdx.x == 0) prm[j] = make_float4((float)x, (float)rb, p.w, 0.f);
+    const float kf = (float)g.k;
+    // x table
+    {
+      const double X0 = 0.5 * g.px - g.hlx, X1 = ((double)g.nx - 0.5) * g.px - g.hlx;
+      const double dm = fmax(fabs(X0 - x), fabs(X1 - x));
+      const bool fast = rb > 0.0 && g.k * (dm * dm) * (dm * dm) < 32.0 * rb * rb * rb;
+      const double ca = g.k / (2.0 * rb);
+      const float rbf = (float)rb;
+      for (int c = threadIdx.x; c < g.nx; c += blockDim.x) {
+        const double X = ((double)c + 0.5) * g.px - g.hlx;
+        const double dx = X - x, dx2 = dx * dx;
+        const size_t idx = (size_t)j * g.nx + c;
+        if (fast) {
+          double ph = fma(ca, dx2, -g.k * X * g.stx);
+          ph -= two_pi * rint(ph * inv_two_pi);
+          const float rxf = sqrtf((float)(dx2 + rb * rb));
+          const float sx = rxf + rbf, d2 = (float)dx2;
+          A[idx] = (float)ph - kf * d2 * d2 / (2.f * rbf * sx * sx);
+          RX[idx] = rxf;
+        } else {
+          const double rx = sqrt(dx2 + rb * rb);
+          double ph = g.k * (dx2 / (rx + rb)) - g.k * X * g.stx;      // k (r_x - rb) - k X sin tx
+          ph -= two_pi * rint(ph / two_pi);
+          A[idx] = (float)ph;
+          RX[idx] = (float)rx;
+        }
+      }
+    }
+    // y table
+    {
+      const double Y0 = g.hly - 0.5 * g.py, Y1 = g.hly - ((double)g.ny - 0.5) * g.py;
+      const double dm = fmax(fabs(Y0 - y), fabs(Y1 - y));
+      const bool fast = az > 0.0 && g.k * (dm * dm) * (dm * dm) < 32.0 * az * az * az;
+      double kz = g.k * az;
+      kz -= two_pi * rint(kz * inv_two_pi);
+      const double cb = g.k / (2.0 * az);
+      const float azf = (float)az, rbf = (float)rb;
+      for (int r = threadIdx.x; r < g.ny; r += blockDim.x) {
+        const double Y = g.hly - ((double)r + 0.5) * g.py;
+        const double dy = Y - y, dy2 = dy * dy;
+        const size_t idx = (size_t)j * g.ny + r;
+        if (fast) {
+          double ph = kz + fma(cb, dy2, -g.k * Y * g.sty);
+          ph -= two_pi * rint(ph * inv_two_pi);
+          const float ryf = sqrtf((float)(dy2 + z * z));
+          const float sy = ryf + azf, d2 = (float)dy2;
+          B[idx] = (float)ph - kf * d2 * d2 / (2.f * azf * sy * sy);
+          RY[idx] = ryf;
+          E[idx] = (float)((dy - y) * (dy + y)) / (ryf + rbf);           // r_y - rb without cancellation
+        } else {
+          const double ry = sqrt(dy2 + z * z);
+          const double kr = g.k * ry;
+          double ph = (kr - two_pi * rint(kr / two_pi)) - g.k * Y * g.sty;
+          ph -= two_pi * rint(ph / two_pi);
+          B[idx] = (float)ph;
+          RY[idx] = (float)ry;
+          E[idx] = (float)((dy2 - y * y) / (ry + rb));
+        }
+      }
+    }
   }
 }
 
@@ -295,7 +339,7 @@ oh_status pointcloud_enqueue(oh_ctx* ctx, int prec, const oh_pc_params* p, const
     const int cnt = std::min(chunk, n - j0);
     {
       KernelTimer kt(ctx, "pc_tables", st);
-      pc_tables<<<1024, 256, 0, st>>>(g, pts + j0, cnt, prm, A, RX, B, RY, E);
+      pc_tables<<<std::max(1, std::min(cnt, 152 * 8)), 256, 0, st>>>(g, pts + j0, cnt, prm, A, RX, B, RY, E);
       OH_LAUNCH_CHECK();
     }
     KernelTimer kt(ctx, "pc_direct_f32", st);
@@ -373,7 +417,7 @@ oh_status oh_pointcloud_noalloc(const oh_pc_params* p, const float* xyza, int n_
   float* E = RY + (size_t)chunk * p->ny;
   for (int j0 = 0; j0 < n_points; j0 += chunk) {
     const int cnt = std::min(chunk, n_points - j0);
-    pc_tables<<<1024, 256, 0, st>>>(g, pts + j0, cnt, prm, A, RX, B, RY, E);
+    pc_tables<<<std::max(1, std::min(cnt, 152 * 8)), 256, 0, st>>>(g, pts + j0, cnt, prm, A, RX, B, RY, E);
     OH_LAUNCH_CHECK();
     pc_direct_f32<<<pc_grid_f32(p->nx, p->ny), kPcTX * kPcFTY, 0, st>>>(g, prm, A, RX, B, RY, E, cnt, (float2*)field_out, (float*)fringe_out,
                                                   j0 > 0);
