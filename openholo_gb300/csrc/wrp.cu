@@ -193,23 +193,37 @@ __device__ __forceinline__ void wrp_for_bins(const WRPGeom& g, const WrpBins& b,
     for (int tx = x0; tx <= x1; ++tx) f(tc ? b.nd + ty * b.regions_x + tx : ty * b.tiles_x + tx);
 }
 
+// Bin counters and cursors are replicated kWrpRep times (replicas of one bin
+// a whole counter array apart): about 600 points share a plane-region
+// counter, and the replicas split that contention.  The replica of point k
+// is (k / 256) mod kWrpRep, so runs of consecutive points stay together in a
+// bin's list (the window kernels read the point records in list order, and
+// records of nearby points share cache lines).
+constexpr int kWrpRep = 8;
+__device__ __forceinline__ int wrp_replica(int k) { return (k >> 8) & (kWrpRep - 1); }
+
 __global__ void wrp_prep(WRPGeom g, const double* __restrict__ xyz, int n, WrpPt* __restrict__ pts,
-                         int* __restrict__ count, WrpBins bins) {
+                         int* __restrict__ count, int nbins, WrpBins bins) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     WrpPt q;
     wrp_point(g, xyz, k, &q);
     pts[k] = q;
-    wrp_for_bins(g, bins, q, [&](int t) { atomicAdd(&count[t], 1); });
+    int* c = count + (size_t)wrp_replica(k) * nbins;
+    wrp_for_bins(g, bins, q, [&](int t) { atomicAdd(&c[t], 1); });
   }
 }
 
-// exclusive scan of count[0..n) into start[0..n], single block
+// Exclusive scan of the replicated counts in (bin, replica) order, single
+// block: cursor[r * n + t] = first list slot of replica r of bin t,
+// start[t] = first slot of bin t, start[n] = total.
 __global__ void wrp_scan(const int* __restrict__ count, int* __restrict__ start, int* __restrict__ cursor, int n) {
   __shared__ int part[1024];
-  const int per = (n + blockDim.x - 1) / blockDim.x;
-  const int b = threadIdx.x * per, e = min(b + per, n);
+  const int m = n * kWrpRep;
+  const int per = (m + blockDim.x - 1) / blockDim.x;
+  const int b = threadIdx.x * per, e = min(b + per, m);
+  auto at = [&](int i) { return (size_t)(i % kWrpRep) * n + i / kWrpRep; };   // i = t kWrpRep + r
   int sum = 0;
-  for (int i = b; i < e; ++i) sum += count[i];
+  for (int i = b; i < e; ++i) sum += count[at(i)];
   part[threadIdx.x] = sum;
   __syncthreads();
   for (int off = 1; off < blockDim.x; off <<= 1) {
@@ -219,15 +233,20 @@ __global__ void wrp_scan(const int* __restrict__ count, int* __restrict__ start,
     __syncthreads();
   }
   int run = part[threadIdx.x] - sum;
-  for (int i = b; i < e; ++i) { start[i] = run; cursor[i] = run; run += count[i]; }
+  for (int i = b; i < e; ++i) {
+    if (i % kWrpRep == 0) start[i / kWrpRep] = run;
+    cursor[at(i)] = run;
+    run += count[at(i)];
+  }
   if (threadIdx.x == blockDim.x - 1) start[n] = part[threadIdx.x];
 }
 
-__global__ void wrp_fill(WRPGeom g, const WrpPt* __restrict__ pts, int n, int* __restrict__ cursor,
+__global__ void wrp_fill(WRPGeom g, const WrpPt* __restrict__ pts, int n, int* __restrict__ cursor, int nbins,
                          int* __restrict__ list, WrpBins bins) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const WrpPt q = pts[k];
-    wrp_for_bins(g, bins, q, [&](int t) { list[atomicAdd(&cursor[t], 1)] = k; });
+    int* c = cursor + (size_t)wrp_replica(k) * nbins;
+    wrp_for_bins(g, bins, q, [&](int t) { list[atomicAdd(&c[t], 1)] = k; });
   }
 }
 
@@ -868,9 +887,9 @@ oh_status oh_wrp_accumulate(oh_ctx* ctx, oh_precision prec, const oh_wrp_params*
     const int nbins = ntiles + (use_tc ? nregions : 0);
     void* ptr;
     const size_t off_cnt = ((size_t)n_points * sizeof(WrpPt) + 255) & ~(size_t)255;
-    const size_t off_start = off_cnt + (((size_t)nbins * 4 + 255) & ~(size_t)255);
+    const size_t off_start = off_cnt + (((size_t)nbins * kWrpRep * 4 + 255) & ~(size_t)255);
     const size_t off_cur = off_start + (((size_t)(nbins + 1) * 4 + 255) & ~(size_t)255);
-    const size_t off_list = off_cur + (((size_t)nbins * 4 + 255) & ~(size_t)255);
+    const size_t off_list = off_cur + (((size_t)nbins * kWrpRep * 4 + 255) & ~(size_t)255);
     OH_TRY(scratch(ctx, "wrp.bins", off_list + cap * sizeof(int), &ptr));
     char* base = (char*)ptr;
     WrpPt* pts = (WrpPt*)base;
@@ -882,13 +901,13 @@ oh_status oh_wrp_accumulate(oh_ctx* ctx, oh_precision prec, const oh_wrp_params*
     if (use_tc)
       OH_CUDA_TRY(cudaFuncSetAttribute(wrp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tcw::kSmemBytes));
     KernelTimer kt(ctx, "wrp_accumulate", st);
-    OH_CUDA_TRY(cudaMemsetAsync(cnt, 0, (size_t)nbins * 4, st));
+    OH_CUDA_TRY(cudaMemsetAsync(cnt, 0, (size_t)nbins * kWrpRep * 4, st));
     const int g1 = std::min((n_points + 255) / 256, 152 * 8);
-    wrp_prep<<<g1, 256, 0, st>>>(g, xyz, n_points, pts, cnt, bins);
+    wrp_prep<<<g1, 256, 0, st>>>(g, xyz, n_points, pts, cnt, nbins, bins);
     OH_LAUNCH_CHECK();
     wrp_scan<<<1, 1024, 0, st>>>(cnt, start, cur, nbins);
     OH_LAUNCH_CHECK();
-    wrp_fill<<<g1, 256, 0, st>>>(g, pts, n_points, cur, list, bins);
+    wrp_fill<<<g1, 256, 0, st>>>(g, pts, n_points, cur, nbins, list, bins);
     OH_LAUNCH_CHECK();
     if (use_tc) {
       KernelTimer kt2(ctx, "wrp_tc", st);
