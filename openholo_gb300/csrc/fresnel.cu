@@ -351,7 +351,8 @@ __global__ void __launch_bounds__(256) fr_strips_to_rows(FrArgs a) {
   const int x0 = blockIdx.x * 64, y0 = blockIdx.y * 32, nx = a.nx, ny = a.ny;
   const int ns = nx / kFrW;
   for (int i = threadIdx.x; i < 32 * 32; i += 256) {
-    const int s = i & 31, r = i >> 5;                 // 32 strips x 32 rows, 16 bytes each
+    const int r = i & 31, s = i >> 5;                 // 32 strips x 32 rows, 16 bytes each; a warp
+                                                      // reads 32 consecutive rows of one strip
     const int sg = x0 / kFrW + s, y = y0 + r;
     if (sg < ns && y < ny) {
       const float4 v = *reinterpret_cast<const float4*>(a.R + ((size_t)sg * ny + y) * kFrW);
