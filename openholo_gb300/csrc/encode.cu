@@ -23,18 +23,34 @@ __global__ void __launch_bounds__(256) reduce_partial(const void* __restrict__ i
   __shared__ R smin[256], smax[256];
   R mn = (R)INFINITY, mx = -(R)INFINITY;
   const R ref = refp ? refp[1] : (R)0;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+  auto take = [&](C c) {
     R v;
-    if (op == RED_MINMAX_REAL) v = static_cast<const R*>(in)[i];
-    else {
-      C c = static_cast<const C*>(in)[i];
-      if (op == RED_MAX_ABS) v = hypot(c.x, c.y);
-      else if (op == RED_MAX_NI) { R re = c.x + ref; v = re * re + c.y * c.y; }
-      else if (op == RED_MAX_PHASE) v = ratan2<R>(c.y, c.x) + (R)3.14159265358979323846;
-      else v = c.x;   // RED_MINMAX_SSB: real part
-    }
+    if (op == RED_MAX_ABS) v = hypot(c.x, c.y);
+    else if (op == RED_MAX_NI) { R re = c.x + ref; v = re * re + c.y * c.y; }
+    else if (op == RED_MAX_PHASE) v = ratan2<R>(c.y, c.x) + (R)3.14159265358979323846;
+    else v = c.x;   // RED_MINMAX_SSB: real part
     mn = v < mn ? v : mn;
     mx = v > mx ? v : mx;
+  };
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (op == RED_MINMAX_REAL) {
+    for (; i < n; i += stride) {
+      const R v = static_cast<const R*>(in)[i];
+      mn = v < mn ? v : mn;
+      mx = v > mx ? v : mx;
+    }
+  } else {
+    // four independent loads in flight per thread before the math
+    const C* src = static_cast<const C*>(in);
+    for (; i + 3 * stride < n; i += 4 * stride) {
+      C c[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) c[q] = src[i + q * stride];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) take(c[q]);
+    }
+    for (; i < n; i += stride) take(src[i]);
   }
   smin[threadIdx.x] = mn; smax[threadIdx.x] = mx;
   __syncthreads();
@@ -90,8 +106,7 @@ __global__ void __launch_bounds__(256) encode_map(int kind, int nx, int ny, cons
   typedef typename cplx_of<R>::type C;
   const R pi = (R)3.14159265358979323846;
   const size_t n = (size_t)nx * ny;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    C u = U[i];
+  auto emit = [&](size_t i, C u) {
     R* o = static_cast<R*>(out);
     switch (kind) {
       case OH_ENC_REAL: o[i] = u.x; break;
@@ -143,7 +158,18 @@ __global__ void __launch_bounds__(256) encode_map(int kind, int nx, int ny, cons
       } break;
       default: break;
     }
+  };
+  // four independent loads in flight per thread before the math
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < n; i += 4 * stride) {
+    C u[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) u[q] = U[i + q * stride];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) emit(i + q * stride, u[q]);
   }
+  for (; i < n; i += stride) emit(i, U[i]);
 }
 
 // SSB: zero half of the centred spectrum (fn_encoding.m:33-41).
