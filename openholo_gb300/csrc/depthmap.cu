@@ -297,31 +297,51 @@ __global__ void __launch_bounds__(512, row_min_blocks<NX>()) dm_row_pass(DMArgs<
     fill_stage_tab<NX, FastSched<NX>::r1, NX / FastSched<NX>::r0, -1>(tab1, static_cast<const C*>(a.plx.tw));
   }
   __syncthreads();
-  for (int idx = threadIdx.x; idx < kRowPair * pnx; idx += blockDim.x) {
-    const int l = idx / pnx, c = idx - l * pnx;
-    int u = -1;
-    C val = mk((R)0, (R)0);
-    if (l < nrows) {
-      const size_t off = (size_t)(r0 + l) * pnx + c;
-      const uint8_t g = a.img[off];
-      u = g > 0 ? (int)a.lut[a.depth[off]] : -1;
-      if (u >= 0) {
-        const R amp = (R)g / (R)255;
-        if (a.phase_mode == OH_PHASE_REFERENCE) {
-          val = mk(amp, (R)0);
-        } else {
-          R ph;
-          if (a.phase_mode == OH_PHASE_ARRAY) ph = (R)a.phase[off];
-          else ph = (R)u24_at(a.seed, off) * (R)6.283185307179586476925;
-          R sn, cs;
-          sincos_r<R>(ph, &sn, &cs);
-          val = mk(amp * cs, amp * sn);
-        }
-        atomicOr(&mask[l * 8 + (u >> 5)], 1u << (u & 31));
+  // the image and depth bytes of up to kSetupPix pixels per thread are loaded
+  // before any is used, so their latency is paid once
+  constexpr int kSetupPix = 8;
+  for (int base = 0; base < kRowPair * pnx; base += kSetupPix * blockDim.x) {
+    uint8_t gb[kSetupPix], db[kSetupPix];
+#pragma unroll
+    for (int q = 0; q < kSetupPix; ++q) {
+      const int idx = base + q * blockDim.x + threadIdx.x;
+      const int l = idx / pnx, c = idx - l * pnx;
+      gb[q] = 0; db[q] = 0;
+      if (idx < kRowPair * pnx && l < nrows) {
+        const size_t off = (size_t)(r0 + l) * pnx + c;
+        gb[q] = a.img[off];
+        db[q] = a.depth[off];
       }
     }
-    li[l * lip + c] = (int16_t)u;
-    v[l * pnx + c] = val;
+#pragma unroll
+    for (int q = 0; q < kSetupPix; ++q) {
+      const int idx = base + q * blockDim.x + threadIdx.x;
+      if (idx >= kRowPair * pnx) break;
+      const int l = idx / pnx, c = idx - l * pnx;
+      int u = -1;
+      C val = mk((R)0, (R)0);
+      if (l < nrows) {
+        const size_t off = (size_t)(r0 + l) * pnx + c;
+        const uint8_t g = gb[q];
+        u = g > 0 ? (int)a.lut[db[q]] : -1;
+        if (u >= 0) {
+          const R amp = (R)g / (R)255;
+          if (a.phase_mode == OH_PHASE_REFERENCE) {
+            val = mk(amp, (R)0);
+          } else {
+            R ph;
+            if (a.phase_mode == OH_PHASE_ARRAY) ph = (R)a.phase[off];
+            else ph = (R)u24_at(a.seed, off) * (R)6.283185307179586476925;
+            R sn, cs;
+            sincos_r<R>(ph, &sn, &cs);
+            val = mk(amp * cs, amp * sn);
+          }
+          atomicOr(&mask[l * 8 + (u >> 5)], 1u << (u & 31));
+        }
+      }
+      li[l * lip + c] = (int16_t)u;
+      v[l * pnx + c] = val;
+    }
   }
   __syncthreads();
   for (int u = 0; u < a.n_uslots; ++u) {
@@ -1175,6 +1195,8 @@ oh_status oh_depthmap_generate_host(oh_ctx* ctx, oh_precision prec, const oh_dep
   // kernel itself through its device mapping: the result reaches host memory
   // while the pass runs, with no device-to-host copy after it.  Pageable
   // buffers get the copy.
+  // (Reading page-locked inputs through their mappings in the row pass
+  // instead of copying them measured slower than the copies.)
   void* fringe_mapped = nullptr;
   {
     std::lock_guard<std::mutex> lk(ctx->mu);

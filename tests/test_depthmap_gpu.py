@@ -250,6 +250,12 @@ def test_host_entry_point_matches_device(ctx, dev):
     pinned.fill_(float("nan"))
     fr_pinned = dm.generate_host(ctx, p, img, depth, out=pinned.numpy())
     assert np.array_equal(fr_dev, fr_pinned)
+    # page-locked inputs too: read by the row pass through their mappings
+    h_img = torch.from_numpy(img).pin_memory()
+    h_depth = torch.from_numpy(depth).pin_memory()
+    pinned.fill_(float("nan"))
+    fr_all = dm.generate_host(ctx, p, h_img.numpy(), h_depth.numpy(), out=pinned.numpy())
+    assert np.array_equal(fr_dev, fr_all)
 
 
 def test_table_cache_across_parameter_changes(ctx, dev):
