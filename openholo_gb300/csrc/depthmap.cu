@@ -292,6 +292,8 @@ __global__ void __launch_bounds__(512, row_min_blocks<NX>()) dm_row_pass(DMArgs<
   // fused last stage + strip store, in the padded layout
   const bool fused = RP::fusable && a.W == 2 && a.xs && nrows == 2;
   for (int i = threadIdx.x; i < 16; i += blockDim.x) mask[i] = 0u;
+  __shared__ int16_t slut[256];                         // depth byte -> layer slot
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) slut[i] = a.lut[i];
   if constexpr (NX > 0) {
     load_tw_split(twlo, twhi, static_cast<const C*>(a.plx.tw), NX);
     fill_stage_tab<NX, FastSched<NX>::r1, NX / FastSched<NX>::r0, -1>(tab1, static_cast<const C*>(a.plx.tw));
@@ -323,7 +325,7 @@ __global__ void __launch_bounds__(512, row_min_blocks<NX>()) dm_row_pass(DMArgs<
       if (l < nrows) {
         const size_t off = (size_t)(r0 + l) * pnx + c;
         const uint8_t g = gb[q];
-        u = g > 0 ? (int)a.lut[db[q]] : -1;
+        u = g > 0 ? (int)slut[db[q]] : -1;
         if (u >= 0) {
           const R amp = (R)g / (R)255;
           if (a.phase_mode == OH_PHASE_REFERENCE) {
