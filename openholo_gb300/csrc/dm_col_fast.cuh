@@ -147,6 +147,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
   C* exw = reinterpret_cast<C*>(smem + Lo.exw);
   float* lfxw = reinterpret_cast<float*>(smem + Lo.lfxw);
   __shared__ int kxw[8];          // spectrum column of each strip column
+  __shared__ C dxw[8];            // its Dx factor (layer-step form)
   int16_t* list = reinterpret_cast<int16_t*>(smem + Lo.list);
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + Lo.mbar);  // [0] strip+flags, [1],[2] Ey
   __shared__ int s_nact;
@@ -175,27 +176,10 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
     if (a.xs) { kx = a.plx.iperm[kx0 + tid] + a.hx; if (kx >= a.Px) kx -= a.Px; }
     kxw[tid] = kx;
     lfxw[tid] = a.lfx[kx];
+    if (STEP) dxw[tid] = a.dxh[kx];
   }
   __syncthreads();
-  // layer-independent part of the angular-spectrum residual phase:
-  // psi = k z' g,  g = s^2 / (2 (1 + sqrt(1 - s))^2),  s = (lambda fx)^2 + (lambda fy)^2.
-  // With the layer-step recurrence the region holds instead the step factor
-  // D = H(z' - dz) / H(z') = Dx(fx) Dy(fy) exp(-i k dz g).
   constexpr bool horner = STEP;
-  C* const dsm = reinterpret_cast<C*>(smem + Lo.g);
-  for (int idx = tid; idx < NY * W; idx += T) {
-    const int p = idx / W, w = idx - p * W;
-    const float sv = lfxw[w] + a.lfyp[p];
-    const float den = 1.f + sqrtf(1.f - sv);
-    const float g = sv * sv * __fdividef(0.5f, den * den);
-    if constexpr (horner) {
-      float sn, cs;
-      sincospif(-a.kdz_pi * g, &sn, &cs);
-      dsm[idx] = cmul(cmul(a.dxh[kxw[w]], a.dyh[p]), make_float2(cs, sn));
-    } else {
-      gsm[idx] = g;
-    }
-  }
   const int nact = s_nact;
   const uint32_t fkeep = SSB ? col_ssb_keep<NY>() : a.fkeep;
   const TwSplit<C> tw{twlo, twhi};
@@ -213,9 +197,45 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
     mbar_expect_tx(bar, (uint32_t)(NY * 4));
     bulk_g2s((k & 1) ? ey1 : ey0, a.eth + (size_t)e * NY, (uint32_t)(NY * 4), bar);
   };
+  // the first layer's copies fly while the tables below are built
   if (tid == 0 && nact > 0) {
     issue_strip(0);
     if (!horner) issue_ey(0);
+  }
+
+  // layer-independent part of the angular-spectrum residual phase:
+  // psi = k z' g,  g = s^2 / (2 (1 + sqrt(1 - s))^2),  s = (lambda fx)^2 + (lambda fy)^2.
+  // With the layer-step recurrence the region holds instead the step factor
+  // D = H(z' - dz) / H(z') = Dx(fx) Dy(fy) exp(-i k dz g).  Each thread loads
+  // the fy terms of kDB elements before using them.
+  C* const dsm = reinterpret_cast<C*>(smem + Lo.g);
+  constexpr int kDB = 4;
+  for (int i0 = tid; i0 < NY * W; i0 += kDB * T) {
+    float lfy[kDB];
+    C dyv[kDB];
+#pragma unroll
+    for (int q = 0; q < kDB; ++q) {
+      const int idx = i0 + q * T;
+      const int p = idx < NY * W ? idx / W : 0;
+      lfy[q] = a.lfyp[p];
+      if constexpr (horner) dyv[q] = a.dyh[p];
+    }
+#pragma unroll
+    for (int q = 0; q < kDB; ++q) {
+      const int idx = i0 + q * T;
+      if (idx >= NY * W) break;
+      const int p = idx / W, w = idx - p * W;
+      const float sv = lfxw[w] + lfy[q];
+      const float den = 1.f + sqrtf(1.f - sv);
+      const float g = sv * sv * __fdividef(0.5f, den * den);
+      if constexpr (horner) {
+        float sn, cs;
+        sincospif(-a.kdz_pi * g, &sn, &cs);
+        dsm[idx] = cmul(cmul(dxw[w], dyv[q]), make_float2(cs, sn));
+      } else {
+        gsm[idx] = g;
+      }
+    }
   }
 
   // accumulators: last-stage butterfly bb = tid + kb*T of the strip (bb = b*W + w),
