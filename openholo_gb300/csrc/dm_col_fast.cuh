@@ -81,17 +81,32 @@ __host__ __device__ constexpr ColLayout col_layout(int Py, int pny, int W, int s
 // butterfly (NY/RL per column), two when that would exceed 768 threads.
 constexpr int kColStripW = 2;     // columns per strip of the row pass output
 
+// Last-stage butterflies per thread: the block has as many threads as the
+// smaller of the first two stages has butterflies (each stage then keeps all
+// its threads busy in one round), within 768 threads; e.g. 2048 = 16 16 8
+// takes 256 threads with two last-stage butterflies each instead of 512
+// threads of which the first two stages use half.
+template <int NY, int W> constexpr int col_kb() {
+  constexpr int nbl = (NY / FastSched<NY>::rlast) * W;
+  constexpr int i0 = NY / FastSched<NY>::r0, i1 = NY / FastSched<NY>::r1;
+  constexpr int mi = W * (i0 < i1 ? i0 : i1);
+  int kb = nbl > 768 ? 2 : 1;
+  while (kb < 4 && nbl % (2 * kb) == 0 && nbl / (2 * kb) >= mi) kb *= 2;
+  return kb;
+}
+
 template <int NY, int W, bool STEP> struct ColCfg {
   static constexpr int RL = FastSched<NY>::rlast;
   static constexpr int NBL = (NY / RL) * W;          // last-stage butterflies of the block's columns
-  static constexpr int KB = NBL > 768 ? 2 : 1;        // butterflies per thread
+  static constexpr int KB = col_kb<NY, W>();          // butterflies per thread
   static constexpr int T = ((NBL + KB - 1) / KB + 31) / 32 * 32;
   // two blocks per SM when two fit in shared memory (2x padding, pny =
   // NY / 2); otherwise one, and the register cap that two would impose
   // (spills at the longer lengths) is lifted
   static constexpr int SMEM =
       col_layout(NY, NY / 2, W, kColStripW, STEP, ((NY / 2) + 15) & ~15, kMaxEntries, col_tab_entries<NY>()).total;
-  static constexpr int MINB = 2 * (SMEM + 1024) <= 228 * 1024 ? 2 : 1;
+  static constexpr int FIT = (228 * 1024) / (SMEM + 1024);                // blocks per SM by shared memory
+  static constexpr int MINB = FIT >= 3 && T <= 256 ? 3 : (FIT >= 2 ? 2 : 1);
 };
 
 // One-column blocks (W = 1) over two-column strips, for the lengths where a
