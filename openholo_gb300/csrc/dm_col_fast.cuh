@@ -111,8 +111,9 @@ template <int NY, int W, bool STEP> struct ColCfg {
 
 // One-column blocks (W = 1) over two-column strips, for the lengths where a
 // two-column block's shared memory leaves one block per SM and the second
-// read of each strip still hits L2 (measured: 3072 faster, 4096 slower)
-template <int NY> constexpr bool col_narrow_ok() { return NY >= 3072 && NY <= 3840; }
+// read of each strip still hits L2 (measured faster at 3072 to 4096; at 4096
+// 5.02 -> 4.66 ms for a 64-layer frame)
+template <int NY> constexpr bool col_narrow_ok() { return NY >= 3072 && NY <= 4096; }
 
 // Last-stage outputs f (bit f) that can reach the SSB crop of a 2x-padded
 // grid with the signal shifted along y (crop rows (NY/2 - NY/4) .. +NY/2 - 1
