@@ -817,16 +817,19 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   a.err = ctx->dev_err;
   // FP32 with a compile-time FFT length: bulk-copy pipelined column pass
   // (dm_col_fast) with the widest strip whose shared-memory layout fits
-  int Wfast = 0, col_tab = 0;
+  int Wfast = 0, col_tab = 0, col_py = a.Py;      // col_py: stored column length of the fast pass
   bool fastlen = false;
   with_fast_n(a.Py, [&](auto nc) { fastlen = decltype(nc)::value > 0; });
   if (prec == 0 && fastlen) {
     // strips of two spectrum columns (two blocks per SM)
     with_fast_n(a.Py, [&](auto nc) {
-      if constexpr (decltype(nc)::value > 0) col_tab = col_tab_entries<decltype(nc)::value>();
+      if constexpr (decltype(nc)::value > 0) {
+        col_tab = col_tab_entries<decltype(nc)::value>();
+        col_py = col_len<decltype(nc)::value>();
+      }
     });
     if (a.Px % 2 == 0 &&
-        (size_t)col_layout(a.Py, a.pny, 2, kColStripW, false, occ_stride, su.n_entries, col_tab).total <= smax)
+        (size_t)col_layout(col_py, a.pny, 2, kColStripW, false, occ_stride, su.n_entries, col_tab).total <= smax)
       Wfast = 2;
   }
   int W = Wfast;
@@ -895,14 +898,14 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
     });
     const bool step = a.horner != 0;
     auto two_fit = [&](int w) {
-      return 2 * ((size_t)col_layout(a.Py, a.pny, w, kColStripW, step, occ_stride, su.n_entries, col_tab).total +
+      return 2 * ((size_t)col_layout(col_py, a.pny, w, kColStripW, step, occ_stride, su.n_entries, col_tab).total +
                   1024) <= (size_t)228 * 1024;
     };
     const char* ev = std::getenv("OH_DM_COL_NARROW");
     if (narrow && !(ev && std::atoi(ev) == 0) && !two_fit(2) && two_fit(1)) wcol = 1;
   }
   const size_t smem_col =
-      Wfast ? (size_t)col_layout(a.Py, a.pny, wcol, kColStripW, a.horner != 0, occ_stride, su.n_entries, col_tab).total
+      Wfast ? (size_t)col_layout(col_py, a.pny, wcol, kColStripW, a.horner != 0, occ_stride, su.n_entries, col_tab).total
             : (size_t)W * a.Py * sizeof(C) + W * (sizeof(C) + sizeof(R)) + (size_t)a.Py * sizeof(int);
   int row_tab = 0, row_ls = a.Px;
   with_fast_n_if<sizeof(R) == 4>(a.Px, [&](auto nc) {

@@ -77,6 +77,15 @@ __host__ __device__ constexpr ColLayout col_layout(int Py, int pny, int W, int s
 }
 
 
+// Column buffer layout: with an even last radix RL the last stage's 16
+// threads of a half-warp (butterflies b, inputs b RL + f) would all hit one
+// bank pair, so one element of padding follows every RL elements (element p
+// sits at p + p / RL; RL + 1 is odd).  Q0 = NY / r0 and the middle stage's
+// block size NY / r0 are multiples of RL, so every stage still addresses its
+// inputs with fixed strides (col_pad: the padded length, 0 pad for odd RL).
+template <int NY> constexpr bool col_padded() { return FastSched<NY>::rlast % 2 == 0; }
+template <int NY> constexpr int col_len() { return col_padded<NY>() ? NY + NY / FastSched<NY>::rlast : NY; }
+
 // Threads per block for a strip of W columns: one thread per last-stage
 // butterfly (NY/RL per column), two when that would exceed 768 threads.
 constexpr int kColStripW = 2;     // columns per strip of the row pass output
@@ -104,7 +113,8 @@ template <int NY, int W, bool STEP> struct ColCfg {
   // NY / 2); otherwise one, and the register cap that two would impose
   // (spills at the longer lengths) is lifted
   static constexpr int SMEM =
-      col_layout(NY, NY / 2, W, kColStripW, STEP, ((NY / 2) + 15) & ~15, kMaxEntries, col_tab_entries<NY>()).total;
+      col_layout(col_len<NY>(), NY / 2, W, kColStripW, STEP, ((NY / 2) + 15) & ~15, kMaxEntries,
+                 col_tab_entries<NY>()).total;
   static constexpr int FIT = (228 * 1024) / (SMEM + 1024);                // blocks per SM by shared memory
   static constexpr int MINB = FIT >= 3 && T <= 256 ? 3 : (FIT >= 2 ? 2 : 1);
 };
@@ -150,7 +160,13 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int kTab = col_tab_entries<NY>();
   constexpr int R1 = FastSched<NY>::r1;
-  const ColLayout Lo = col_layout(NY, a.pny, W, SW, STEP, a.occ_stride, a.n_entries, kTab);
+  const ColLayout Lo = col_layout(col_len<NY>(), a.pny, W, SW, STEP, a.occ_stride, a.n_entries, kTab);
+  // padded layout (see col_padded): element p at p + p / RL
+  constexpr bool PADL = col_padded<NY>();
+  constexpr int RLP = PADL ? RL + 1 : RL;                     // stored length of RL elements
+  constexpr int Q0P = PADL ? Q0 + Q0 / RL : Q0;               // stored stride of stage-0 outputs
+  constexpr int M1 = NY / R0, M1P = PADL ? M1 + M1 / RL : M1; // middle-stage block, stored
+  auto pidx = [](int p) { return PADL ? p + p / RL : p; };
   C* buf = reinterpret_cast<C*>(smem + Lo.buf);
   C* const stg = reinterpret_cast<C*>(smem + Lo.stg);            // row-pass strip of the layer (single buffer)
   uint8_t* const occ = smem + Lo.occ;                             // its row flags
@@ -247,9 +263,9 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
       if constexpr (horner) {
         float sn, cs;
         sincospif(-a.kdz_pi * g, &sn, &cs);
-        dsm[idx] = cmul(cmul(dxw[w], dyv[q]), make_float2(cs, sn));
+        dsm[pidx(p) * W + w] = cmul(cmul(dxw[w], dyv[q]), make_float2(cs, sn));
       } else {
-        gsm[idx] = g;
+        gsm[pidx(p) * W + w] = g;
       }
     }
   }
@@ -292,7 +308,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
           if (bb < CF::NBL) {
             const int b = bb / W, w = bb - b * W;
 #pragma unroll
-            for (int f = 0; f < RL; ++f) acc[kb][f] = cmul(acc[kb][f], dsm[(b * RL + f) * W + w]);
+            for (int f = 0; f < RL; ++f) acc[kb][f] = cmul(acc[kb][f], dsm[(b * RLP + f) * W + w]);
           }
         }
       }
@@ -331,7 +347,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
         for (int f = 1; f < R0; ++f) x[f] = cmul(x[f], wp[f]);
       }
 #pragma unroll
-      for (int f = 0; f < R0; ++f) buf[(j + f * Q0) * W + w] = x[f];
+      for (int f = 0; f < R0; ++f) buf[(pidx(j) + f * Q0P) * W + w] = x[f];
     }
     // middle stage(s); the leading barrier also frees the strip buffer
     __syncthreads();
@@ -339,7 +355,8 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
       fence_proxy_async_smem();
       issue_strip(k + 1);
     }
-    if constexpr (kTab > 0) fstage_tab<NY, R1, NY / R0, -1>(buf, W, 1, W, tab1, true);
+    static_assert(kTab > 0 || !PADL, "the padded layout needs the middle stage's table");
+    if constexpr (kTab > 0) fstage_tab<NY, R1, M1, -1, C, M1P, RLP>(buf, W, 1, W, tab1, true);
     else fstage_t<NY, R1, NY / R0, -1>(buf, W, 1, W, tw, true);
     __syncthreads();
     // last stage (stride 1, no twiddles) fused with the transfer-function
@@ -356,13 +373,13 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
         const int b = bb / W, w = bb - b * W;
         C x[RL];
 #pragma unroll
-        for (int f = 0; f < RL; ++f) x[f] = buf[(b * RL + f) * W + w];
+        for (int f = 0; f < RL; ++f) x[f] = buf[(b * RLP + f) * W + w];
         DFT<RL, -1, C>::run(x);
         if constexpr (horner) {
 #pragma unroll
           for (int f = 0; f < RL; ++f) {
             if (!((fkeep >> f) & 1u)) continue;         // outside the SSB crop for every b
-            const C d = dsm[(b * RL + f) * W + w];
+            const C d = dsm[(b * RLP + f) * W + w];
             const C t = acc[kb][f];
             acc[kb][f] = make_float2(fmaf(t.x, d.x, fmaf(-t.y, d.y, x[f].x)), fmaf(t.x, d.y, fmaf(t.y, d.x, x[f].y)));
           }
@@ -374,7 +391,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
           if (!((fkeep >> f) & 1u)) continue;           // outside the SSB crop for every b
           const int p = b * RL + f;
           // H = C Ex exp(i (pi lambda z' fy^2 + k z' g)), both phase parts reduced
-          float ph = fmaf(kz, gsm[p * W + w], eth[p]);
+          float ph = fmaf(kz, gsm[(b * RLP + f) * W + w], eth[p]);
           ph = fmaf(-two_pi, rintf(ph * inv2pi), ph);
           float sn, cs;
           __sincosf(ph, &sn, &cs);
@@ -436,19 +453,19 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
       }
       DFT<RL, 1, C>::run(x);
 #pragma unroll
-      for (int f = 0; f < RL; ++f) buf[(b * RL + f) * W + w] = x[f];
+      for (int f = 0; f < RL; ++f) buf[(b * RLP + f) * W + w] = x[f];
     }
   }
   __syncthreads();
-  fstage_adj<NY, R1, NY / R0>(buf, W, 1, W, tw, true);
+  fstage_adj<NY, R1, M1, C, TwSplit<C>, M1P, RLP>(buf, W, 1, W, tw, true);
   __syncthreads();
-  fstage_adj<NY, R0, NY>(buf, W, 1, W, tw, true);
+  fstage_adj<NY, R0, NY, C, TwSplit<C>, col_len<NY>(), Q0P, PADL ? RL : 0>(buf, W, 1, W, tw, true);
   __syncthreads();
   for (int idx = tid; idx < pny * W; idx += T) {
     const int yl = idx / W, w = idx - yl * W;
     int m = a.oy + yl - a.hy;
     if (m < 0) m += NY;
-    a.V[(size_t)yl * a.Px + kx0 + w] = cmul(buf[m * W + w], a.shy[yl]);
+    a.V[(size_t)yl * a.Px + kx0 + w] = cmul(buf[pidx(m) * W + w], a.shy[yl]);
   }
 }
 

@@ -289,7 +289,11 @@ __device__ __forceinline__ void fstage_t(C* buf, int nl, int ls, int es, const T
 // a line in the forward transform's storage order, compute its unnormalised
 // inverse DFT with the output in natural order (the forward network maps x to
 // P F x, its adjoint maps P y to F^H y = N F^-1 y).
-template <int N, int R, int M, typename C, class TW>
+//
+// BS, TS and JG describe a padded layout: block blk starts at element blk BS,
+// input t of a butterfly sits TS elements after input t - 1, and offset j is
+// stored at j + j / JG (JG > 0) or j.
+template <int N, int R, int M, typename C, class TW, int BS = M, int TS = M / R, int JG = 0>
 __device__ __forceinline__ void fstage_adj(C* buf, int nl, int ls, int es, const TW& tw, bool line_fastest) {
   constexpr int Q = M / R;
   constexpr int TWS = N / M;
@@ -300,8 +304,8 @@ __device__ __forceinline__ void fstage_adj(C* buf, int nl, int ls, int es, const
     if (line_fastest) { b = idx / nl; line = idx - b * nl; }
     else { line = idx / NB; b = idx - line * NB; }
     const int blk = b / Q, j = b - blk * Q;
-    const int base = line * ls + (blk * M + j) * es;
-    const int st = Q * es;
+    const int base = line * ls + (blk * BS + (JG > 0 ? j + j / (JG > 0 ? JG : 1) : j)) * es;
+    const int st = TS * es;
     C x[R];
 #pragma unroll
     for (int t = 0; t < R; ++t) x[t] = buf[base + t * st];
@@ -330,12 +334,12 @@ __device__ __forceinline__ void fstages_adj(C* buf, int nl, int ls, int es, cons
 // consecutive butterflies j read from distinct shared-memory bank pairs.
 constexpr int stage_tab_stride(int R) { return (R - 1) | 1; }
 
-// One stage with its twiddles from a per-stage table: tab[j TS + f - 1] =
-// W^(SGN j f N/M) for butterfly offset j < M/R, output f = 1..R-1, TS =
-// stage_tab_stride(R).  BS is the
-// storage distance between consecutive blocks of M elements (M, or more for a
-// padded layout).
-template <int N, int R, int M, int SGN, typename C, int BS = M>
+// One stage with its twiddles from a per-stage table: tab[j S + f - 1] =
+// W^(SGN j f N/M) for butterfly offset j < M/R, output f = 1..R-1, S =
+// stage_tab_stride(R).  BS is the storage distance between consecutive
+// blocks of M elements and TS that between a butterfly's inputs (M and M/R,
+// or more for a padded layout).
+template <int N, int R, int M, int SGN, typename C, int BS = M, int TS = M / R>
 __device__ __forceinline__ void fstage_tab(C* buf, int nl, int ls, int es, const C* __restrict__ tab,
                                            bool line_fastest) {
   constexpr int Q = M / R;
@@ -347,7 +351,7 @@ __device__ __forceinline__ void fstage_tab(C* buf, int nl, int ls, int es, const
     else { line = idx / NB; b = idx - line * NB; }
     const int blk = b / Q, j = b - blk * Q;
     const int base = line * ls + (blk * BS + j) * es;
-    const int st = Q * es;
+    const int st = TS * es;
     C x[R];
 #pragma unroll
     for (int t = 0; t < R; ++t) x[t] = buf[base + t * st];
