@@ -231,20 +231,34 @@ template <int NX> constexpr int row_min_blocks() { return NX > 0 && NX <= 4320 ?
 // conflict free the plain layout (LS = NX, BS = M1) is kept.
 template <int NX, bool FAST = (NX > 0)> struct RowPad {
   static constexpr bool fusable = false;
-  static constexpr int LS = NX, BS = 0, LSMAX = NX;
+  static constexpr int LS = NX, BS = 0, LSMAX = NX, RLP = 0, JG = 0, BPB = 1;
 };
 template <int NX> struct RowPad<NX, true> {
   typedef FastSched<NX> S;
   static constexpr bool fusable = S::nstages == 3 && NX / S::rlast == 256;
   static constexpr int M1 = NX / S::r0, Q1 = M1 / S::r1, RL = S::rlast, NB1 = NX / S::r1;
   static constexpr int BPB = M1 % RL == 0 ? M1 / RL : 0;    // last-stage butterflies per block
-  static constexpr bool conflict_free(int bs, int ls) {
-    if (BPB == 0) return false;
+  // element p of a row at (p / M1) bs + (p % M1) + rp ((p % M1) / RL): rp = 1
+  // pads every RL elements (an even RL puts a half-warp of the last stage
+  // on one bank pair otherwise), bs - M1 (1 + rp / RL) pads every block
+  static constexpr int at(int p, int bs, int rp) { return (p / M1) * bs + p % M1 + rp * ((p % M1) / RL); }
+  static constexpr bool conflict_free(int bs, int ls, int rp) {
+    if (BPB == 0 || Q1 != RL) return false;
+    for (int h = 0; h < 2 * M1 / 16; ++h) {           // stage 0 stores, line-major: at most 2-way
+      int seen = 0, twice = 0;                        // (the per-RL pad skips a pair every RL stores)
+      for (int i = 0; i < 16; ++i) {
+        const int idx = h * 16 + i, line = idx / M1, j = idx % M1;
+        const int e = line * ls + at(j, bs, rp);
+        if (twice & (1 << (e % 16))) return false;
+        if (seen & (1 << (e % 16))) twice |= 1 << (e % 16);
+        seen |= 1 << (e % 16);
+      }
+    }
     for (int h = 0; h < 2 * NB1 / 16; ++h) {          // middle stage, line-major
       int seen = 0;
       for (int i = 0; i < 16; ++i) {
         const int idx = h * 16 + i, line = idx / NB1, b = idx % NB1;
-        const int e = line * ls + (b / Q1) * bs + b % Q1;
+        const int e = line * ls + at((b / Q1) * M1 + b % Q1, bs, rp);
         if (seen & (1 << (e % 16))) return false;
         seen |= 1 << (e % 16);
       }
@@ -253,22 +267,32 @@ template <int NX> struct RowPad<NX, true> {
       int seen = 0;
       for (int i = 0; i < 16; ++i) {
         const int idx = h * 16 + i, b = idx >> 1, l = idx & 1;
-        const int e = l * ls + (b / BPB) * bs + (b % BPB) * RL;
+        const int e = l * ls + at(b * RL, bs, rp);
         if (seen & (1 << (e % 16))) return false;
         seen |= 1 << (e % 16);
       }
     }
     return true;
   }
-  static constexpr int PADB = ((Q1 - M1) % 16 + 16) % 16;
-  static constexpr int pick_ls() {
-    for (int ls = S::r0 * (M1 + PADB); ls < S::r0 * (M1 + PADB) + 16; ++ls)
-      if (conflict_free(M1 + PADB, ls)) return ls;
-    return 0;
+  // first (rp, block pad, row stride) free of conflicts in the middle and
+  // last stages (stage-0 stores at most 2-way), plain layout preferred;
+  // packed as rp << 24 | pad << 16 | (ls - base), or -1
+  static constexpr int search() {
+    for (int rp = 0; rp <= (RL % 2 == 0 ? 1 : 0); ++rp)
+      for (int pad = 0; pad < 16; ++pad) {
+        const int bs = M1 + rp * (M1 / RL) + pad, base = S::r0 * bs;
+        for (int d = 0; d < 16; ++d)
+          if (conflict_free(bs, base + d, rp)) return rp << 24 | pad << 16 | d;
+      }
+    return -1;
   }
-  static constexpr bool padded = fusable && pick_ls() > 0;
-  static constexpr int LS = padded ? pick_ls() : NX;
-  static constexpr int BS = padded ? M1 + PADB : M1;
+  static constexpr int found = fusable ? search() : -1;
+  static constexpr bool padded = found >= 0;
+  static constexpr int RP = padded ? found >> 24 : 0;
+  static constexpr int BS = padded ? M1 + RP * (M1 / RL) + ((found >> 16) & 0xff) : M1;
+  static constexpr int LS = padded ? S::r0 * BS + (found & 0xffff) : NX;
+  static constexpr int RLP = RL + RP;                        // stored length of RL elements
+  static constexpr int JG = RP ? RL : 0;                    // stage-0 offset j stored at j + j / JG
   static constexpr int LSMAX = LS > NX ? LS : NX;
 };
 
@@ -396,7 +420,7 @@ __global__ void __launch_bounds__(512, row_min_blocks<NX>()) dm_row_pass(DMArgs<
 #pragma unroll
           for (int f = 1; f < R0; ++f) x[f] = cmul(x[f], wp[f]);
         }
-        C* bl = buf + l * ls;
+        C* bl = buf + l * ls + (fused && RP::JG > 0 ? j / (RP::JG > 0 ? RP::JG : 1) : 0);
 #pragma unroll
         for (int f = 0; f < R0; ++f) bl[j + f * bs] = x[f];
       }
@@ -408,13 +432,13 @@ __global__ void __launch_bounds__(512, row_min_blocks<NX>()) dm_row_pass(DMArgs<
           // its row) of the same 32-byte strip sector
           constexpr int RL = FastSched<NX>::rlast;
           __syncthreads();
-          fstage_tab<NX, FastSched<NX>::r1, NX / FastSched<NX>::r0, -1, C, RP::BS>(buf, kRowPair, RP::LS, 1, tab1,
-                                                                                  false);
+          fstage_tab<NX, FastSched<NX>::r1, NX / FastSched<NX>::r0, -1, C, RP::BS, RP::RLP>(buf, kRowPair, RP::LS, 1,
+                                                                                           tab1, false);
           __syncthreads();
           {
             const int b = threadIdx.x >> 1, l = threadIdx.x & 1;
             C x[RL];
-            const C* src = buf + l * RP::LS + (b / RP::BPB) * RP::BS + (b % RP::BPB) * RL;
+            const C* src = buf + l * RP::LS + (b / RP::BPB) * RP::BS + (b % RP::BPB) * RP::RLP;
 #pragma unroll
             for (int t = 0; t < RL; ++t) x[t] = src[t];
             DFT<RL, -1, C>::run(x);
