@@ -144,7 +144,10 @@ oh_status oh_depthmap_generate(oh_ctx* ctx, oh_precision prec,
                                const float* phase, void* fringe_out,
                                void* field_out, void* spectrum_out,
                                void* stream);
-/* Same with host buffers; copies in and out on the given stream and waits. */
+/* Same with host buffers; copies in and out on the given stream and waits.
+ * A page-locked fringe_host (cudaHostAlloc / cudaHostRegister) is written by
+ * the output kernel through its device mapping, with no copy after the frame;
+ * a pageable one is filled by a device-to-host copy. */
 oh_status oh_depthmap_generate_host(oh_ctx* ctx, oh_precision prec,
                                     const oh_depthmap_params* p,
                                     const uint8_t* img_host,
