@@ -255,7 +255,8 @@ __device__ __forceinline__ void dft16_halfzero(C* x) {
 
 // ---- one stage --------------------------------------------------------------
 
-template <int N, int R, int M, int SGN, typename C, class TW>
+// BS / TS: stored block and input strides of a padded layout (M and M/R plain)
+template <int N, int R, int M, int SGN, typename C, class TW, int BS = M, int TS = M / R>
 __device__ __forceinline__ void fstage_t(C* buf, int nl, int ls, int es, const TW& tw, bool line_fastest) {
   constexpr int Q = M / R;
   constexpr int TWS = N / M;
@@ -266,8 +267,8 @@ __device__ __forceinline__ void fstage_t(C* buf, int nl, int ls, int es, const T
     if (line_fastest) { b = idx / nl; line = idx - b * nl; }
     else { line = idx / NB; b = idx - line * NB; }
     const int blk = b / Q, j = b - blk * Q;
-    const int base = line * ls + (blk * M + j) * es;
-    const int st = Q * es;
+    const int base = line * ls + (blk * BS + j) * es;
+    const int st = TS * es;
     C x[R];
 #pragma unroll
     for (int t = 0; t < R; ++t) x[t] = buf[base + t * st];

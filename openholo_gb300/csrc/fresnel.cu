@@ -250,9 +250,31 @@ __global__ void __launch_bounds__(FrColCfg<NY>::T, FrColCfg<NY>::MINB) fr_col(Fr
   }
 }
 
-// Row stride of fr_rowconv's shared buffer: the padded length rounded up to
-// 8 mod 16 elements, so the two rows of a half-warp use disjoint bank halves
-template <int NX> constexpr int fr_row_stride() { return NX + ((8 - NX % 16) + 16) % 16; }
+// Shared-memory layout of fr_rowconv's two rows: element p of row l at
+// l LS + (p / M1) BS + p % M1 + RP ((p % M1) / RL), M1 = NX / r0 (a stage-0
+// block).  RP pads one element after every RL (an even last radix otherwise
+// puts a half-warp of the last stage on few bank pairs), BS - M1 (1 + RP/RL)
+// pads each block (middle-stage half-warps that cross a block), and LS makes
+// the two rows of a stage-0 half-warp use other bank pairs.  The layouts
+// were found by an exhaustive search over (RP, block pad, LS) minimising
+// the shared-memory wavefronts of the three access patterns; other lengths
+// keep LS = the padded length rounded to 8 mod 16 and no element pads.
+template <int NX> struct FrRowPad {
+  typedef FastSched<NX> S;
+  static constexpr int M1 = NX / S::r0, RL = S::rlast;
+  static constexpr int RP = NX == 7680 || NX == 4096 || NX == 2048 ? 1 : 0;
+  static constexpr int PADB = NX == 7680 ? 14 : NX == 2048 ? 8 : NX == 3840 ? 15 : NX == 4320 ? 1 : 0;
+  static constexpr int BS = M1 + RP * (M1 / RL) + PADB;
+  static constexpr int LS = NX == 7680 ? 8168 : NX == 4096 ? 4360 : NX == 2048 ? 2440 : NX == 3840 ? 4088
+                          : NX == 4320 ? 4344 : NX + ((8 - NX % 16) + 16) % 16;
+  static constexpr int RLP = RL + RP;
+  static constexpr int BPB = M1 / RL;                        // last-stage butterflies per block
+  static_assert(RP == 0 || M1 % RL == 0, "the element pad needs whole last-stage groups per block");
+  static_assert(LS >= S::r0 * BS, "rows must not overlap");
+  // stored offset of j < M1 within its block
+  __device__ __forceinline__ static int in_blk(int j) { return RP ? j + j / RL : j; }
+};
+template <int NX> constexpr int fr_row_stride() { return FrRowPad<NX>::LS; }
 
 // Separable form, first pass: two rows per block, each convolved with hx on
 // the padded length, cropped to nx columns and stored as strips
@@ -268,7 +290,8 @@ __global__ void __launch_bounds__(512) fr_rowconv(FrArgs a) {
   typedef FastSched<NX> S;
   constexpr int ROWS = 2, NT = 512;
   constexpr int R0 = S::r0, R1 = S::r1, RL = S::rlast, Q0 = NX / R0, Q = NX / 4;
-  constexpr int LS = fr_row_stride<NX>();
+  typedef FrRowPad<NX> FP;
+  constexpr int LS = FP::LS;
   static_assert(S::nstages == 3, "three-stage schedule expected");
   static_assert(R0 % 4 == 0, "stage-0 radix must split the line into quarters");
   extern __shared__ __align__(16) unsigned char smem[];
@@ -299,17 +322,18 @@ __global__ void __launch_bounds__(512) fr_rowconv(FrArgs a) {
 #pragma unroll
       for (int f = 1; f < R0; ++f) x[f] = cmul(x[f], wp[f]);
     }
+    C* bl = buf + l * LS + FP::in_blk(j);
 #pragma unroll
-    for (int f = 0; f < R0; ++f) buf[l * LS + j + f * Q0] = x[f];
+    for (int f = 0; f < R0; ++f) bl[f * FP::BS] = x[f];
   }
   __syncthreads();
-  fstage_t<NX, R1, NX / R0, -1>(buf, ROWS, LS, 1, tw, false);
+  fstage_t<NX, R1, NX / R0, -1, C, TwSplit<C>, FP::BS, FP::RLP>(buf, ROWS, LS, 1, tw, false);
   __syncthreads();
   // last forward stage (no twiddles), the transfer function, first inverse stage
   constexpr int NBL = NX / RL;
   for (int idx = threadIdx.x; idx < ROWS * NBL; idx += NT) {
     const int l = idx / NBL, b = idx - l * NBL;
-    C* p = buf + l * LS + b * RL;
+    C* p = buf + l * LS + (b / FP::BPB) * FP::BS + (b % FP::BPB) * FP::RLP;
     C x[RL];
 #pragma unroll
     for (int f = 0; f < RL; ++f) x[f] = p[f];
@@ -321,14 +345,15 @@ __global__ void __launch_bounds__(512) fr_rowconv(FrArgs a) {
     for (int f = 0; f < RL; ++f) p[f] = x[f];
   }
   __syncthreads();
-  fstage_adj<NX, R1, NX / R0>(buf, ROWS, LS, 1, tw, false);
+  fstage_adj<NX, R1, NX / R0, C, TwSplit<C>, FP::BS, FP::RLP>(buf, ROWS, LS, 1, tw, false);
   __syncthreads();
   // last inverse stage: column c = sample Q + c = j + t Q0, t in [R0/4, 3R0/4)
   for (int idx = threadIdx.x; idx < ROWS * Q0; idx += NT) {
     const int j = idx >> 1, l = idx & 1;
     C x[R0];
+    const C* bl = buf + l * LS + FP::in_blk(j);
 #pragma unroll
-    for (int f = 0; f < R0; ++f) x[f] = buf[l * LS + j + f * Q0];
+    for (int f = 0; f < R0; ++f) x[f] = bl[f * FP::BS];
     if (j) {
       C wp[R0];
       twiddle_powers<R0, 1>(tw, j, wp);
@@ -496,8 +521,12 @@ static oh_status run_fresnel(oh_ctx* ctx, int nx, int ny, double dp, double lamb
   if constexpr (sizeof(R) == 4) {
     FrKernels k;
     const bool even = nx % 2 == 0 && ny % 2 == 0;
+    int row_ls = 0;
+    with_fast_n(2 * nx, [&](auto nc) {
+      if constexpr (decltype(nc)::value > 0) row_ls = fr_row_stride<decltype(nc)::value>();
+    });
     if (even && !getenv("OH_FRESNEL_GRID") && fr_pick(2 * nx, 2 * ny, &k) &&
-        (size_t)(2 * (2 * nx + 15) + fr_tw_entries(2 * nx)) * sizeof(float2) <= max_smem_per_block())
+        (size_t)(2 * row_ls + fr_tw_entries(2 * nx)) * sizeof(float2) <= max_smem_per_block())
       return run_fresnel_separable(ctx, nx, ny, dp, lambda, z, static_cast<float2*>(field), k, st);
   }
   return run_fresnel_grid<R>(ctx, nx, ny, dp, lambda, z, field, st);

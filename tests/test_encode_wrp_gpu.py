@@ -182,7 +182,8 @@ def test_fresnel_propagate(ctx, shape):
         assert np.linalg.norm(t.cpu().numpy() - ref) <= tol * np.linalg.norm(ref), precision
 
 
-@pytest.mark.parametrize("shape", [(540, 960), (512, 512), (1080, 960)])
+@pytest.mark.parametrize("shape", [(540, 960), (512, 512), (1080, 960), (540, 1920), (512, 1024), (512, 2048),
+                                   (1080, 2160)])
 def test_fresnel_propagate_separable(ctx, shape):
     """FP32 sizes whose padded lengths have compile-time FFT schedules run the
     three-pass separable path; it must equal the padded-grid oracle, and
