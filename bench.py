@@ -258,7 +258,8 @@ def plain_gpu_path(img_t, depth_t, zt, lut, torch):
     return frame
 
 
-SECONDARY_OPS = ("pointcloud", "pls", "wrp", "batch")
+SECONDARY_OPS = ("pointcloud", "pls", "wrp", "batch", "square")
+SQUARE_SIDE, SQUARE_LAYERS = 2048, 16     # --op square: the batch's largest frame shape
 
 
 def secondary_measurements(ctx, dev, torch, reps=5, ops=SECONDARY_OPS, warmup=1):
@@ -293,7 +294,23 @@ def secondary_measurements(ctx, dev, torch, reps=5, ops=SECONDARY_OPS, warmup=1)
         _sec_wrp(ctx, dev, torch, st, timed, out, reps + warmup)
     if "batch" in ops:
         _sec_batch(ctx, dev, torch, out, reps, warmup)
+    if "square" in ops:
+        _sec_square(ctx, dev, torch, timed, out)
     return out
+
+
+def _sec_square(ctx, dev, torch, timed, out):
+    """One square depth-map frame of the batch workload's largest shape
+    (2048 x 2048, 16 layers, 2x pad: a 4096 x 4096 FFT grid), seeded scene."""
+    from openholo_gb300 import depthmap as dm, scenes
+    side, L = SQUARE_SIDE, SQUARE_LAYERS
+    img, depth = scenes.depthmap_scene(5, side, side)
+    p = dm.make_params(pnx=side, pny=side, num_of_depth=L, pad=2, phase_mode=dm.OH_PHASE_SEEDED, seed=3)
+    ti, td = torch.from_numpy(img).to(dev), torch.from_numpy(depth).to(dev)
+    fr = torch.empty((side, side), dtype=torch.float32, device=dev)
+    ms = timed(lambda: dm.generate(ctx, p, ti, td, fringe=fr))
+    out[f"depthmap_{side}x{side}_L{L}"] = {"ms_per_frame": ms, "frames_per_s": 1000.0 / ms,
+                                           "what": "one frame of the batch workload's largest shape, 2x pad"}
 
 
 BATCH_FRAMES, BATCH_SEED = 64, 4
