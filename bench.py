@@ -49,6 +49,41 @@ WORKLOAD = ("depth-map layered angular-spectrum CGH 1920x1080, 32 layers z 0.30-
             "3840x2160 FFT grid, per-pixel seeded random phase, symmetrization encoding, fp32")
 
 
+def profile_figure(fname, kernel):
+    """A per-launch figure of `kernel` from a JSON summary under profiles/
+    (ncu captures), or None."""
+    path = ROOT / "profiles" / fname
+    if not path.exists():
+        return None
+    return json.loads(path.read_text()).get(kernel)
+
+
+def compute_roofline(kernel, ms_per_launch, peaks):
+    """Issue-side roofline of one kernel: warp instructions per launch (ncu,
+    profiles/instructions.json) over its measured launch time, against the
+    peak issue rate and the FMA and MUFU pipe rates measured by
+    oh_measure_issue_peaks on this GPU."""
+    inst = profile_figure("instructions.json", kernel)
+    if not inst or not peaks or ms_per_launch <= 0:
+        return {"kernel": kernel, "ms_per_launch": ms_per_launch, "instructions": None}
+    s = ms_per_launch * 1e-3
+    r = {"kernel": kernel, "ms_per_launch": ms_per_launch, "bound": "issue", "unit": "warp inst/s",
+         "achieved": inst["warp_inst"] / s, "peak": peaks["ffma_warp_inst_per_s"], "peak_source": "measured"}
+    r["frac"] = r["achieved"] / r["peak"]
+    if inst.get("fma"):
+        r["fma_pipe_frac"] = inst["fma"] / s / peaks["ffma_warp_inst_per_s"]
+    if inst.get("xu"):
+        r["mufu_frac"] = inst["xu"] * 32 / s / peaks["mufu_per_s"]
+    return r
+
+
+def load_bf16_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return float(json.loads(p.read_text()).get("bf16_tflops", 1900.0)), "measured"
+    return 1900.0, "fallback"
+
+
 def load_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -169,49 +204,90 @@ def dist_setup():
     return world, rank, local
 
 
-def cpu_frame_sample(img, depth, phase, layers_sampled=2, workers=None):
-    """Oracle port on the host: `layers_sampled` full-size layers plus the
-    encode, extrapolated to the 32-layer frame.  Returns (frames/s, sample text)."""
+def cpu_frame(img, depth, phase, workers=None, layers=None):
+    """The oracle port on the host cores: the whole 32-layer frame (or the
+    render entries in `layers`) plus the encode, float64 numpy/scipy
+    pocketfft with `workers` threads.  Returns (seconds, fringe, field)."""
     from oracle import depthmap as odm
     workers = workers or os.cpu_count()
     p = odm.DMParams(pnx=NX, pny=NY, num_of_depth=LAYERS, pad=PAD)
-    idx = list(range(0, LAYERS, max(1, LAYERS // layers_sampled)))[:layers_sampled]
     t0 = time.perf_counter()
-    U = odm.calc_holo(img, depth, p, phase=phase, workers=workers, layers=idx)
-    t1 = time.perf_counter()
-    odm.encode_symmetrization(U, p, workers=workers)
-    t2 = time.perf_counter()
-    frame_s = (t1 - t0) * LAYERS / len(idx) + (t2 - t1)
-    return 1.0 / frame_s, (f"{len(idx)} of {LAYERS} layers of the 1920x1080 frame + full encode, float64 numpy/"
-                           f"scipy pocketfft with {workers} threads, layer time x{LAYERS / len(idx):.0f}")
+    U = odm.calc_holo(img, depth, p, phase=phase, workers=workers, layers=layers)
+    fringe, field = odm.encode_symmetrization(U, p, workers=workers, return_field=True)
+    return time.perf_counter() - t0, fringe, field
+
+
+CPU_SAMPLE = ("one whole 1920x1080 32-layer frame per step (all layers, 2x pad, encode), float64 numpy/scipy "
+              "pocketfft with {w} threads; the reference's depth-map CPU code needs Qt and FFTW, so its "
+              "line-by-line restatement (oracle/depthmap.py) runs")
 
 
 def run_reference(args, world, rank):
-    """--impl reference: the CPU restatement of the reference's depth-map path."""
+    """--impl reference: the CPU restatement of the reference's depth-map path,
+    whole frames.  Warm-up steps run one layer plus the encode (they only
+    warm the FFT plans and caches); every timed step is a full frame."""
     if rank != 0:
         return
     from openholo_gb300 import scenes
     img, depth = scenes.depthmap_scene(SCENE_SEED, NY, NX)
     phase = scenes.seeded_phase(PHASE_SEED, NY, NX)
-    for _ in range(args.warmup):
-        cpu_frame_sample(img, depth, phase, layers_sampled=1)
-    vals = []
-    sample = ""
-    for _ in range(args.steps):
-        v, sample = cpu_frame_sample(img, depth, phase, layers_sampled=1)
-        vals.append(v)
-    fps = 1.0 / statistics.mean(1.0 / v for v in vals)
     cores = os.cpu_count()
+    for _ in range(args.warmup):
+        cpu_frame(img, depth, phase, workers=cores, layers=[LAYERS // 2])
+    secs = []
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        secs.append(cpu_frame(img, depth, phase, workers=cores)[0])
+    wall = time.perf_counter() - t_all
+    fps = len(secs) / sum(secs)
     line = {"metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 / fps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": {"workload": WORKLOAD.replace("fp32", "float64 CPU"), "pnx": NX, "pny": NY, "layers": LAYERS,
                        "pad": PAD},
             "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
-                             "sample": "per step: " + sample + "; the reference's depth-map CPU code needs Qt "
-                                       "and FFTW, so its line-by-line restatement (oracle/depthmap.py) runs"},
-            "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                             "sample": CPU_SAMPLE.format(w=cores) + "; warm-up steps: one layer + encode"},
+            "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "timed_region_s": wall, "frame_s": {"min": min(secs), "max": max(secs)}}
     print(json.dumps(line), flush=True)
+
+
+def reconstruct_intensity(fringe, z, lam=532e-9, pitch=8e-6):
+    """Numerical reconstruction used for PSNR: the real fringe propagated by
+    the angular spectrum over +z (back to a layer plane; the frame was formed
+    with d = -z), intensity |U|^2, float64 numpy on the host."""
+    ny, nx = fringe.shape
+    fx = np.fft.fftfreq(nx, pitch)
+    fy = np.fft.fftfreq(ny, pitch)
+    s = 1.0 - (lam * fx[None, :]) ** 2 - (lam * fy[:, None]) ** 2
+    H = np.exp(1j * (2 * math.pi / lam) * z * np.sqrt(np.maximum(s, 0.0)))
+    u = np.fft.ifft2(np.fft.fft2(fringe.astype(np.float64)) * H)
+    return np.abs(u) ** 2
+
+
+def error_report(got_fringe, got_field, ref_fringe, ref_field, focus_z=(0.30, 0.325, 0.35)):
+    """Max and RMS complex error of the field, relative L2 of field and fringe
+    against the FP64 oracle, and the reconstruction PSNR (intensities
+    normalised by the oracle reconstruction's maximum) at the nearest, middle
+    and farthest layer depths."""
+    d = got_field.astype(np.complex128) - ref_field
+    scale = np.abs(ref_field).max()
+    rep = {"field_rel_l2": float(np.linalg.norm(d) / np.linalg.norm(ref_field)),
+           "field_max_abs": float(np.abs(d).max()), "field_max_abs_rel": float(np.abs(d).max() / scale),
+           "field_rms": float(np.sqrt(np.mean(np.abs(d) ** 2))),
+           "field_rms_rel": float(np.sqrt(np.mean(np.abs(d) ** 2)) / np.sqrt(np.mean(np.abs(ref_field) ** 2))),
+           "fringe_rel_l2": float(np.linalg.norm(got_fringe.astype(np.float64) - ref_fringe) /
+                                  np.linalg.norm(ref_fringe))}
+    ps = {}
+    for z in focus_z:
+        a = reconstruct_intensity(got_fringe, z)
+        b = reconstruct_intensity(ref_fringe, z)
+        m = b.max()
+        mse = float(np.mean((a / m - b / m) ** 2))
+        ps[f"{z:.3f}"] = 10 * math.log10(1.0 / mse) if mse > 0 else float("inf")
+    rep["psnr_db"] = ps
+    rep["psnr_db_min"] = min(ps.values())
+    return rep
 
 
 def plain_gpu_path(img_t, depth_t, zt, lut, torch):
@@ -262,7 +338,7 @@ SECONDARY_OPS = ("pointcloud", "pls", "wrp", "batch", "square")
 SQUARE_SIDE, SQUARE_LAYERS = 2048, 16     # --op square: the batch's largest frame shape
 
 
-def secondary_measurements(ctx, dev, torch, reps=5, ops=SECONDARY_OPS, warmup=1):
+def secondary_measurements(ctx, dev, torch, reps=5, ops=SECONDARY_OPS, warmup=1, peaks=None):
     """The other operators at their own workloads (seeded synthetic inputs):
     pointcloud: KETI exact-r sum 1024x1024 x 5000 points + phase-only encoding;
     pls: the same shape through the paraxial cwoPLS::Fresnel sum (tensor-core
@@ -287,11 +363,11 @@ def secondary_measurements(ctx, dev, torch, reps=5, ops=SECONDARY_OPS, warmup=1)
 
     n, nx, ny = 5000, 1024, 1024
     if "pointcloud" in ops:
-        _sec_pointcloud(ctx, dev, torch, st, timed, out, n, nx, ny)
+        _sec_pointcloud(ctx, dev, torch, st, timed, out, n, nx, ny, peaks)
     if "pls" in ops:
-        _sec_pls(ctx, dev, torch, st, timed, out, n, nx, ny, reps + warmup)
+        _sec_pls(ctx, dev, torch, st, timed, out, n, nx, ny, reps + warmup, peaks)
     if "wrp" in ops:
-        _sec_wrp(ctx, dev, torch, st, timed, out, reps + warmup)
+        _sec_wrp(ctx, dev, torch, st, timed, out, reps + warmup, peaks)
     if "batch" in ops:
         _sec_batch(ctx, dev, torch, out, reps, warmup)
     if "square" in ops:
@@ -313,18 +389,9 @@ def _sec_square(ctx, dev, torch, timed, out):
                                            "what": "one frame of the batch workload's largest shape, 2x pad"}
 
 
-BATCH_FRAMES, BATCH_SEED = 64, 4
-
-
 def batch_workload():
-    """64 frames: side s from {512, 768, 1024, 1536, 2048}, layers 8..64 and
-    wavelength from {450, 532, 633} nm, drawn from SplitMix64 stream 9 of
-    seed 4; square frames, 2x pad, seeded per-pixel phase, FP32."""
     from openholo_gb300 import scenes
-    u = scenes.uniform(BATCH_SEED, 9, 3 * BATCH_FRAMES).reshape(BATCH_FRAMES, 3)
-    sides = [512, 768, 1024, 1536, 2048]
-    lams = [450e-9, 532e-9, 633e-9]
-    return [(sides[int(a * 5)], 8 + int(b * 57), lams[int(c * 3)]) for a, b, c in u]
+    return scenes.batch_workload()
 
 
 def _sec_batch(ctx, dev, torch, out, reps, warmup):
@@ -334,10 +401,10 @@ def _sec_batch(ctx, dev, torch, out, reps, warmup):
     frames = []
     for i, (side, L, lam) in enumerate(work):
         if side not in scene:
-            img, depth = scenes.depthmap_scene(SCENE_SEED + side, side, side)
+            img, depth = scenes.depthmap_scene(scenes.BATCH_SCENE_SEED + side, side, side)
             scene[side] = (torch.from_numpy(img).to(dev), torch.from_numpy(depth).to(dev))
         p = dm.make_params(pnx=side, pny=side, num_of_depth=L, lam=lam, pad=2, phase_mode=dm.OH_PHASE_SEEDED,
-                           seed=PHASE_SEED + i)
+                           seed=scenes.BATCH_PHASE_SEED + i)
         frames.append((p, scene[side][0], scene[side][1],
                        torch.empty((side, side), dtype=torch.float32, device=dev)))
     model = sum(L * 32 * (2 * side) ** 2 + 32 * (2 * side) ** 2 + 2 * side * side for side, L, _ in work)
@@ -355,17 +422,49 @@ def _sec_batch(ctx, dev, torch, out, reps, warmup):
         stream.synchronize()
     ms = a.elapsed_time(b) / reps
     out["batch_64_frames_mixed"] = {
-        "ms_per_batch": ms, "frames_per_s": BATCH_FRAMES * 1000.0 / ms,
+        "ms_per_batch": ms, "frames_per_s": len(work) * 1000.0 / ms,
         "model_bytes_per_batch": model, "model_gbs": model / (ms * 1e-3) / 1e9,
         "kernels_per_batch": (launch_count() - n0) / reps,
+        "roofline": {"bound": "hbm", "unit": "GB/s", "achieved": model / (ms * 1e-3) / 1e9,
+                     "peak": load_peaks()[0], "frac": model / (ms * 1e-3) / 1e9 / load_peaks()[0],
+                     "peak_source": load_peaks()[1],
+                     "what": "model bytes (the reference pipeline's FFT passes over the padded grid) per batch "
+                             "time; the kernels skip the zero padding and empty rows, so the model can exceed "
+                             "the bytes they move"},
         "what": "64 depth-map frames in one CUDA-graph launch: side 512-2048 px, 8-64 layers, 450/532/633 nm, "
                 "2x pad, FP32; model bytes = sum over frames of L*32*Np + 32*Np + 2N"}
 
 
-def _sec_pointcloud(ctx, dev, torch, st, timed, out, n, nx, ny):
+def gpu_error_report(got, ref, torch, pitch, lam, z):
+    """Field errors of `got` against the FP64 `ref` (device tensors): relative
+    L2, max and RMS complex error (relative to max |ref| and RMS |ref|), and
+    the PSNR of the angular-spectrum reconstruction at distance z
+    (intensities normalised by the reference reconstruction's maximum),
+    computed in float64 with torch.fft."""
+    g = got.to(torch.complex128)
+    d = g - ref
+    rep = {"rel_l2": float(torch.linalg.norm(d) / torch.linalg.norm(ref)),
+           "max_abs_rel": float(d.abs().max() / ref.abs().max()),
+           "rms_rel": float(torch.sqrt((d.abs() ** 2).mean()) / torch.sqrt((ref.abs() ** 2).mean()))}
+    ny, nx = ref.shape
+    fx = torch.fft.fftfreq(nx, pitch, dtype=torch.float64, device=ref.device)
+    fy = torch.fft.fftfreq(ny, pitch, dtype=torch.float64, device=ref.device)
+    sq = torch.sqrt(torch.clamp(1.0 - (lam * fx[None, :]) ** 2 - (lam * fy[:, None]) ** 2, min=0.0))
+    H = torch.polar(torch.ones_like(sq), (2 * math.pi / lam) * z * sq)
+    ia = torch.fft.ifft2(torch.fft.fft2(g) * H).abs() ** 2
+    ib = torch.fft.ifft2(torch.fft.fft2(ref) * H).abs() ** 2
+    m = ib.max()
+    mse = float(((ia - ib) / m).pow(2).mean())
+    rep["psnr_db"] = 10 * math.log10(1.0 / mse) if mse > 0 else float("inf")
+    rep["psnr_plane_z"] = z
+    return rep
+
+
+def _sec_pointcloud(ctx, dev, torch, st, timed, out, n, nx, ny, peaks=None):
     import ctypes as C
     from openholo_gb300 import _lib, scenes
-    pts = torch.from_numpy(scenes.pointcloud_scene(11, n).astype(np.float32)).to(dev)
+    pts_np = scenes.pointcloud_scene(11, n).astype(np.float32)
+    pts = torch.from_numpy(pts_np).to(dev)
     p = _lib.PcParams(1.0, 1.0, 1.0, 0.0, 8e-6, 8e-6, nx, ny, 532e-9, 0.0, 0.0)
     f32 = torch.empty((ny, nx), dtype=torch.complex64, device=dev)
     u8 = torch.empty((ny, nx), dtype=torch.uint8, device=dev)
@@ -375,14 +474,25 @@ def _sec_pointcloud(ctx, dev, torch, st, timed, out, n, nx, ny):
                   C.c_void_p(f32.data_ptr()), None, st)
         _lib.call("oh_encode", ctx.handle, 0, 9, nx, ny, C.c_void_p(f32.data_ptr()), C.c_void_p(u8.data_ptr()), st)
     ms = timed(pc)
+    kms = kernel_breakdown(ctx, torch, pc)
     f64 = torch.empty((ny, nx), dtype=torch.complex128, device=dev)
     _lib.call("oh_pointcloud", ctx.handle, 1, C.byref(p), C.c_void_p(pts.data_ptr()), n,
               C.c_void_p(f64.data_ptr()), None, st)
     torch.cuda.synchronize()
-    err = float(torch.linalg.norm(f32.to(torch.complex128) - f64) / torch.linalg.norm(f64))
-    out["pointcloud_1024x1024_5000pts"] = {"ms_per_hologram": ms, "holograms_per_s": 1000.0 / ms,
-                                           "point_pixel_terms_per_s": n * nx * ny / (ms / 1000.0),
-                                           "rel_err_vs_fp64": err, "dtype": "f32 (FP64-reduced phase tables)"}
+    acc = gpu_error_report(f32, f64, torch, 8e-6, 532e-9, -float(np.mean(pts_np[:, 2])))
+    acc["reference"] = "the FP64 path (equal to the CPU oracle to 1e-9 in the tests)"
+    res = {"ms_per_hologram": ms, "holograms_per_s": 1000.0 / ms,
+           "point_pixel_terms_per_s": n * nx * ny / (ms / 1000.0), "kernels_ms": kms,
+           "rel_err_vs_fp64": acc["rel_l2"], "accuracy": acc, "dtype": "f32 (FP64-reduced phase tables)"}
+    t_direct = kms.get("pc_direct_f32")
+    if peaks and t_direct:
+        mufu = 3.0 * n * nx * ny          # per term: sqrt.approx, rcp.approx, sin.approx
+        res["roofline"] = {"bound": "mufu", "kernel": "pc_direct_f32", "unit": "MUFU results/s",
+                           "achieved": mufu / (t_direct * 1e-3), "peak": peaks["mufu_per_s"],
+                           "frac": mufu / (t_direct * 1e-3) / peaks["mufu_per_s"], "peak_source": "measured",
+                           "algorithmic_per_launch": mufu,
+                           "issue": compute_roofline("pc_direct_f32", t_direct, peaks)}
+    out["pointcloud_1024x1024_5000pts"] = res
     del f64
 
 
@@ -400,7 +510,7 @@ def kernel_breakdown(ctx, torch, fn, calls=5):
     return {k: v[0] / calls for k, v in kt.items()}
 
 
-def _sec_pls(ctx, dev, torch, st, timed, out, n, nx, ny, calls):
+def _sec_pls(ctx, dev, torch, st, timed, out, n, nx, ny, calls, peaks=None):
     import ctypes as C
     from openholo_gb300 import _lib, scenes
     pls_pts = torch.from_numpy(scenes.pls_scene(11, n)).to(dev)
@@ -419,11 +529,16 @@ def _sec_pls(ctx, dev, torch, st, timed, out, n, nx, ny, calls):
         useful = 8.0 * nx * ny * n          # complex multiply-adds as real flops, counted once
         pls_res["tensor"]["gemm_useful_tflops"] = useful / (tc_ms * 1e-3) / 1e12
         pls_res["tensor"]["gemm_issued_tflops"] = 3 * 2.0 * ny * (2 * nx) * (2 * n) / (tc_ms * 1e-3) / 1e12
+        bf16, kind = load_bf16_peak()
+        pls_res["roofline"] = {"bound": "tensor", "kernel": "pls_tc_gemm", "unit": "TFLOP/s",
+                               "achieved": pls_res["tensor"]["gemm_issued_tflops"], "peak": bf16,
+                               "frac": pls_res["tensor"]["gemm_issued_tflops"] / bf16, "peak_source": kind,
+                               "what": "issued BF16 flops (three split products of the real embedding)"}
     out["pls_fresnel_1024x1024_5000pts"] = pls_res
     del pls_out
 
 
-def _sec_wrp(ctx, dev, torch, st, timed, out, calls):
+def _sec_wrp(ctx, dev, torch, st, timed, out, calls, peaks=None):
     import ctypes as C
     from openholo_gb300 import _lib, scenes
     npts, hx, hy, dp, lam = 200_000, 3840, 2160, 3.74e-6, 532e-9
@@ -441,9 +556,44 @@ def _sec_wrp(ctx, dev, torch, st, timed, out, calls):
         _lib.call("oh_fresnel_propagate", ctx.handle, 0, hx, hy, dp, lam, z_wrp, C.c_void_p(wrp.data_ptr()), st)
         _lib.call("oh_encode", ctx.handle, 0, 9, hx, hy, C.c_void_p(wrp.data_ptr()), C.c_void_p(hol.data_ptr()), st)
     ms3 = timed(wrp_frame)
-    out["wrp_200k_64x64_fresnel_3840x2160"] = {"ms_per_hologram": ms3, "holograms_per_s": 1000.0 / ms3,
-                                               "kernels_ms": kernel_breakdown(ctx, torch, wrp_frame),
-                                               "dtype": "f32"}
+    kms = kernel_breakdown(ctx, torch, wrp_frame)
+    res = {"ms_per_hologram": ms3, "holograms_per_s": 1000.0 / ms3, "kernels_ms": kms, "dtype": "f32"}
+    # accuracy of the propagated hologram field against the FP64 path (WRP and
+    # padded-grid Fresnel in double; both equal the CPU oracle in the tests)
+    w64 = torch.zeros((hy, hx), dtype=torch.complex128, device=dev)
+    _lib.call("oh_wrp_accumulate", ctx.handle, 1, C.byref(wp), C.c_void_p(t_xyz.data_ptr()), npts,
+              C.c_void_p(w64.data_ptr()), st)
+    _lib.call("oh_fresnel_propagate", ctx.handle, 1, hx, hy, dp, lam, z_wrp, C.c_void_p(w64.data_ptr()), st)
+    wrp.zero_()
+    _lib.call("oh_wrp_accumulate", ctx.handle, 0, C.byref(wp), C.c_void_p(t_xyz.data_ptr()), npts,
+              C.c_void_p(wrp.data_ptr()), st)
+    _lib.call("oh_fresnel_propagate", ctx.handle, 0, hx, hy, dp, lam, z_wrp, C.c_void_p(wrp.data_ptr()), st)
+    torch.cuda.synchronize()
+    acc = gpu_error_report(wrp, w64, torch, dp, lam, -z_wrp - 5e-3)
+    acc["reference"] = "the FP64 path (WRP and padded-grid Fresnel in double)"
+    res["accuracy"] = acc
+    del w64
+    torch.cuda.empty_cache()
+    if peaks:
+        bf16 = load_bf16_peak()
+        t_tc = kms.get("wrp_tc")
+        if t_tc:
+            flops = 3 * 8.0 * npts * 64 * 64          # complex window MACs as real flops, x3 split products
+            res["roofline"] = {"bound": "tensor", "kernel": "wrp_tc", "unit": "TFLOP/s",
+                               "achieved": flops / (t_tc * 1e-3) / 1e12, "peak": bf16[0],
+                               "frac": flops / (t_tc * 1e-3) / 1e12 / bf16[0], "peak_source": bf16[1],
+                               "algorithmic_flops_per_launch": flops,
+                               "issue": compute_roofline("wrp_tc", t_tc, peaks)}
+        fr_ms = sum(v for k, v in kms.items() if k.startswith("fresnel_"))
+        if fr_ms:
+            hbm, kind = load_peaks()
+            fb = 2 * 32 * (2 * hx) * (2 * hy)          # two padded 2-pass FFTs, 8 B read + 8 B written per pass
+            res["roofline_fresnel"] = {"bound": "hbm", "unit": "GB/s", "achieved": fb / (fr_ms * 1e-3) / 1e9,
+                                       "peak": hbm, "frac": fb / (fr_ms * 1e-3) / 1e9 / hbm,
+                                       "peak_source": kind, "algorithmic_bytes": fb,
+                                       "issue_rowconv": compute_roofline("fresnel_rowconv",
+                                                                         kms.get("fresnel_rowconv", 0), peaks)}
+    out["wrp_200k_64x64_fresnel_3840x2160"] = res
 
 
 def main():
@@ -454,6 +604,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-baselines", action="store_true", help="skip the CPU and plain-GPU comparison legs")
     ap.add_argument("--no-secondary", action="store_true", help="skip the point-cloud and WRP workloads")
+    ap.add_argument("--record", default=None,
+                    help="append one JSON-lines accuracy record (max/RMS error, PSNR, fallbacks) to this file")
     ap.add_argument("--op", choices=SECONDARY_OPS, default=None,
                     help="time one secondary workload alone (steps calls after warmup) and print its line")
     args = ap.parse_args()
@@ -550,11 +702,15 @@ def main():
              "dm_col_pass": LAYERS * 16 * Np + 16 * Np,
              "dm_out_pass": 16 * Np}
     alg_bytes = model.get(dom_name, 0)
-    achieved = alg_bytes / (dom_ms / dom_n / 1000.0) / 1e9 if dom_ms > 0 else 0.0
-    traffic_path = ROOT / "profiles" / "traffic.json"
-    traffic = None
-    if traffic_path.exists():
-        traffic = json.loads(traffic_path.read_text()).get(dom_name)
+    launch_s = dom_ms / dom_n / 1000.0 if dom_ms > 0 else float("inf")
+    achieved = alg_bytes / launch_s / 1e9
+    traffic = profile_figure("traffic.json", dom_name)
+    roof = {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+            "algorithmic_bytes_per_launch": alg_bytes}
+    if traffic:
+        roof["traffic_gbs"] = traffic / launch_s / 1e9
+        roof["traffic_frac"] = roof["traffic_gbs"] / peak
 
     out = {"metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -568,23 +724,37 @@ def main():
                                "max": 1000.0 * max(wall)}},
            "gpu_launches": launches,
            "kernels_ms_per_frame": {k: v[0] / args.steps for k, v in ktimes.items()},
-           "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                        "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
-                        "algorithmic_bytes_per_launch": alg_bytes},
+           "roofline": roof,
            "clocks": clocks}
+
+    peaks = None
+    if rank == 0 and world == 1:
+        from openholo_gb300 import _lib
+        try:
+            peaks = _lib.measure_issue_peaks(local)
+            out["compute_peaks"] = peaks
+            out["roofline_compute"] = {k: compute_roofline(k, v[0] / v[1], peaks) for k, v in ktimes.items()}
+        except Exception as e:  # pragma: no cover
+            out["compute_peaks"] = {"error": str(e)[:200]}
 
     if rank == 0 and world == 1 and not args.no_secondary:
         try:
-            out["other_operators"] = secondary_measurements(ctx, dev, torch)
+            out["other_operators"] = secondary_measurements(ctx, dev, torch, peaks=peaks)
         except Exception as e:  # pragma: no cover
             out["other_operators"] = {"error": str(e)[:300]}
         torch.cuda.empty_cache()
     if rank == 0 and world == 1 and not args.no_baselines:
-        # accuracy of this frame against the FP64 path (pinned to the oracle in tests)
+        # FP64 mode of the same frame (the reference computes in double)
         f64 = dm.generate(ctx, p, d_img, d_depth, precision="fp64")
         torch.cuda.synchronize()
-        f32 = fringe.double()
-        out["accuracy"] = {"rel_err_vs_fp64": float(torch.linalg.norm(f32 - f64) / torch.linalg.norm(f64))}
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(3):
+            dm.generate(ctx, p, d_img, d_depth, precision="fp64", fringe=f64)
+        b.record()
+        torch.cuda.synchronize()
+        ms64 = a.elapsed_time(b) / 3
+        out["fp64_mode"] = {"value": 1000.0 / ms64, "unit": "frames/s", "ms_per_frame": ms64}
         # plain FP32 GPU path (reference structure on cuFFT)
         try:
             lut, zt = dm.levels(p)
@@ -608,13 +778,39 @@ def main():
             del frame
         except Exception as e:  # pragma: no cover
             out["plain_gpu_path"] = {"error": str(e)[:200]}
+        # the FP32 frame's field, for the error report
+        field32 = torch.empty((NY, NX), dtype=torch.complex64, device=dev)
+        field64 = torch.empty((NY, NX), dtype=torch.complex128, device=dev)
+        dm.generate(ctx, p, d_img, d_depth, fringe=fringe, field=field32)
+        dm.generate(ctx, p, d_img, d_depth, precision="fp64", fringe=f64, field=field64)
+        torch.cuda.synchronize()
+        got_fr, got_field = fringe.cpu().numpy(), field32.cpu().numpy()
+        got64_fr, got64_field = f64.cpu().numpy(), field64.cpu().numpy()
+        del f64, field32, field64
         torch.cuda.empty_cache()
-        phase = scenes.seeded_phase(PHASE_SEED, NY, NX)
-        v, sample = cpu_frame_sample(img, depth, phase, layers_sampled=2)
-        out["cpu_baseline"] = {"value": v, "unit": "frames/s", "cores": os.cpu_count(), "kind": "port",
-                               "sample": sample}
+        # CPU baseline: one whole frame of the oracle port, whose output is also
+        # the FP64 reference of the error report
+        phase = scenes.seeded_phase(rank_seed(PHASE_SEED, rank), NY, NX)
+        cores = os.cpu_count()
+        secs, ref_fr, ref_field = cpu_frame(img, depth, phase, workers=cores)
+        out["cpu_baseline"] = {"value": 1.0 / secs, "unit": "frames/s", "cores": cores, "kind": "port",
+                               "sample": CPU_SAMPLE.format(w=cores)}
+        out["accuracy"] = {"fp32_vs_fp64_oracle": error_report(got_fr, got_field, ref_fr, ref_field),
+                           "fp64_vs_fp64_oracle": error_report(got64_fr, got64_field, ref_fr, ref_field,
+                                                               focus_z=(0.325,)),
+                           "what": "whole 1920x1080 frame against the CPU oracle (float64); PSNR of "
+                                   "angular-spectrum reconstructions of the fringe at the given depths"}
+        out["accuracy"]["rel_err_vs_fp64"] = out["accuracy"]["fp32_vs_fp64_oracle"]["fringe_rel_l2"]
     if rank == 0:
         print(json.dumps(out), flush=True)
+        if args.record:
+            with open(args.record, "a") as fh:
+                rec = {"when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime()), "workload": WORKLOAD,
+                       "value": out["value"], "accuracy": out.get("accuracy"),
+                       "other_operators_accuracy": {k: v.get("accuracy") for k, v in
+                                                    (out.get("other_operators") or {}).items()
+                                                    if isinstance(v, dict) and "accuracy" in v}}
+                fh.write(json.dumps(rec) + "\n")
     if pg:
         pg.destroy_process_group()
 

@@ -70,6 +70,16 @@ oh_status   oh_ctx_set_timing(oh_ctx* ctx, int on);
 int         oh_ctx_read_timing(oh_ctx* ctx, int reset, const char** names,
                                double* ms, long* launches, int cap);
 const char* oh_version(void);
+/* Issue-rate microbenchmarks on `device` (no reference counterpart): the
+ * compute-side roofline denominators.  Times eight independent dependency
+ * chains per thread over whole waves with CUDA events (best of two after a
+ * warm-up) and returns scalar FP32 FMA warp instructions per second (also the
+ * peak warp-instruction issue rate), packed two-lane FP32 FMA warp
+ * instructions per second, and sin.approx.f32 results per second (the
+ * multi-function unit).  sm_mhz_hint (nullable) receives the SM clock implied
+ * by the FMA rate at four warp instructions per SM per clock.  Synchronous. */
+oh_status   oh_measure_issue_peaks(int device, double* ffma_per_s, double* ffma2_per_s,
+                                   double* mufu_per_s, double* sm_mhz_hint);
 /* Synchronises `stream` and reports OH_ERR_TIMEOUT if a kernel of this
  * context gave up a bounded wait since the last check (the flag is then
  * cleared); OH_OK otherwise. */
@@ -274,7 +284,9 @@ oh_status oh_pointcloud_host(oh_ctx* ctx, oh_precision prec,
  *     number of points is accepted (processed in chunks).
  *   - The first call on a device looks up the array's device address
  *     (cudaGetSymbolAddress) with that device current; make that first call
- *     before any stream capture.
+ *     before any stream capture.  The address is cached per CUDA context,
+ *     so after a device reset the next call looks it up again (again
+ *     outside any capture).
  *   - Every call shares the one array and leaves the last call's tables in
  *     it; calls that overlap on the GPU (different streams or host threads)
  *     race on it.  Outputs are written in full (field) or accumulated

@@ -118,6 +118,7 @@ SIGNATURES = {
     "oh_version": (C.c_char_p, []),
     "oh_ctx_set_timing": (_i, [_vp, _i]),
     "oh_ctx_device_status": (_i, [_vp, _vp]),
+    "oh_measure_issue_peaks": (_i, [_i, C.POINTER(_d), C.POINTER(_d), C.POINTER(_d), C.POINTER(_d)]),
     "oh_ctx_read_timing": (_i, [_vp, _i, C.POINTER(C.c_char_p), C.POINTER(_d), C.POINTER(C.c_long), _i]),
     "oh_fft_supported": (_i, [_i, _i]),
     "oh_fft2d": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _i, _i, _vp]),
@@ -211,3 +212,13 @@ class Context:
 
 def launch_count() -> int:
     return int(lib().oh_kernel_launch_count())
+
+
+def measure_issue_peaks(device: int = 0) -> dict:
+    """Issue-rate microbenchmarks (oh_measure_issue_peaks): scalar and packed
+    FP32 FMA warp instructions per second and sin.approx results per second
+    on `device`."""
+    a, b, c, m = _d(), _d(), _d(), _d()
+    call("oh_measure_issue_peaks", device, C.byref(a), C.byref(b), C.byref(c), C.byref(m))
+    return {"ffma_warp_inst_per_s": a.value, "ffma2_warp_inst_per_s": b.value, "mufu_per_s": c.value,
+            "fp32_fma_flops_per_s": max(2 * 32 * a.value, 2 * 64 * b.value), "sm_mhz_implied": m.value}

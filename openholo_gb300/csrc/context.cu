@@ -15,6 +15,23 @@ static thread_local std::string t_last_error;
 void note_launch(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
 uint64_t launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
 void set_error(const std::string& msg) { t_last_error = msg; }
+
+int sm_count() {
+  static std::atomic<int> cached[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return 152;
+  if (dev < 64) {
+    const int c = cached[dev].load(std::memory_order_relaxed);
+    if (c > 0) return c;
+  }
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+    cudaGetLastError();
+    n = 152;
+  }
+  if (dev < 64) cached[dev].store(n, std::memory_order_relaxed);
+  return n;
+}
 oh_status fail(oh_status s, const std::string& msg) { t_last_error = msg; return s; }
 oh_status cuda_fail(cudaError_t e, const char* what) {
   t_last_error = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";

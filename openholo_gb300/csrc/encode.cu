@@ -87,7 +87,7 @@ static oh_status reduce(oh_ctx* ctx, const void* in, size_t n, int op, const R* 
   // 16 blocks of 256 threads per SM: one load in flight per thread, so the
   // thread count sets how many bytes are in flight (512 blocks kept the read
   // of a 66 MB field near a quarter of the HBM bandwidth)
-  const int nb = (int)std::max<size_t>(1, std::min<size_t>((n + 255) / 256, 152 * 16));
+  const int nb = (int)std::max<size_t>(1, std::min<size_t>((n + 255) / 256, oh::sm_count() * 16));
   void* ptr;
   OH_TRY(scratch(ctx, slot, sizeof(R) * 2 * nb, &ptr));
   *red = (R*)ptr;
@@ -217,7 +217,7 @@ template <typename R>
 static oh_status run_encode(oh_ctx* ctx, int kind, int nx, int ny, const void* field, void* out, cudaStream_t st) {
   typedef typename cplx_of<R>::type C;
   const size_t n = (size_t)nx * ny;
-  const int grid = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+  const int grid = (int)std::min<size_t>((n + 255) / 256, oh::sm_count() * 16);
   R* red1 = nullptr;
   R* red2 = nullptr;
   if (kind >= OH_ENC_SSB_LEFT && kind <= OH_ENC_SSB_BOTTOM) {
@@ -270,7 +270,7 @@ oh_status oh_normalize_u8(oh_ctx* ctx, oh_precision prec, int nx, int ny, const 
   OH_TRY(cs.status());
   if (nx < 1 || ny < 1 || !in || !out) return fail(OH_ERR_INVALID_ARG, "oh_normalize_u8: bad size or null buffer");
   const size_t n = (size_t)nx * ny;
-  const int grid = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+  const int grid = (int)std::min<size_t>((n + 255) / 256, oh::sm_count() * 16);
   if (prec == OH_FP64) {
     double* red;
     OH_TRY(reduce<double>(ctx, in, n, RED_MINMAX_REAL, (const double*)nullptr, &red, st, "norm.red"));

@@ -108,7 +108,7 @@ static oh_status run_fresnel_grid(oh_ctx* ctx, int nx, int ny, double dp, double
   OH_TRY(scratch(ctx, "fr.B", n2 * sizeof(C), &pb));
   const bool have = prev_b == pb && ctx->fresnel_key == key;
   ctx->fresnel_key = key;
-  const int grid = 152 * 8;
+  const int grid = oh::sm_count() * 8;
   if (!have) {
     fresnel_kernel_sample<R><<<grid, 256, 0, st>>>(NX, NY, dp, lambda, z, (C*)pb);
     OH_LAUNCH_CHECK();

@@ -66,7 +66,7 @@ oh_status run_lightfield(oh_ctx* ctx, const LFGeom& g, const float* lf, const fl
   const int B = g.ns * g.nt;
   void* xp;
   OH_TRY(scratch(ctx, "lf.views", (size_t)B * g.nu * g.nv * sizeof(C), &xp));
-  const int grid = 152 * 8;
+  const int grid = oh::sm_count() * 8;
   KernelTimer kt(ctx, "lightfield", st);
   lf_pack<R><<<grid, 256, 0, st>>>(g, lf, phase, static_cast<C*>(xp));
   OH_LAUNCH_CHECK();

@@ -57,6 +57,10 @@ void note_launch(int n = 1);
 // Kernels launched by this library so far (all threads).
 uint64_t launches_so_far();
 
+// Streaming multiprocessors of the current device (queried once per device
+// and cached); grid sizes that aim at whole waves are multiples of it.
+int sm_count();
+
 // Per-thread last-error message.
 void set_error(const std::string& msg);
 oh_status fail(oh_status s, const std::string& msg);

@@ -330,7 +330,7 @@ static oh_status run_pls(oh_ctx* ctx, int prec, const oh_pls_params* p, const oh
   PlsPt* q = static_cast<PlsPt*>(pp);
   {
     KernelTimer kt(ctx, "pls_prep", st);
-    pls_prep<<<std::min((n + 63) / 64, 152 * 32), 64, 0, st>>>(g, pts, n, q);
+    pls_prep<<<std::min((n + 63) / 64, oh::sm_count() * 32), 64, 0, st>>>(g, pts, n, q);
     OH_LAUNCH_CHECK();
   }
   int engine = p->engine;
@@ -364,7 +364,7 @@ static oh_status run_pls(oh_ctx* ctx, int prec, const oh_pls_params* p, const oh
     const int cnt = std::min(chunk, n - k0);
     {
       KernelTimer kt(ctx, "pls_tables", st);
-      pls_tables<<<152 * 8, 256, 0, st>>>(g, q + k0, cnt, ex, ey);
+      pls_tables<<<oh::sm_count() * 8, 256, 0, st>>>(g, q + k0, cnt, ex, ey);
       OH_LAUNCH_CHECK();
     }
     with_pls_mode(p->mode, [&](auto mc) {

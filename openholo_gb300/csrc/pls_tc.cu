@@ -403,8 +403,7 @@ oh_status pls_tensor_enqueue(oh_ctx* ctx, const PlsGeom& g, const PlsPt* pts, in
     // at least 8 K blocks), else the best filling
     int splits = 1;
     {
-      int sms = 152;
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      const int sms = oh::sm_count();
       const int smax = std::max(1, kb_total / 8);
       double best = -1.0;
       for (int sp = 1; sp <= std::min(smax, 32); ++sp) {

@@ -339,7 +339,7 @@ oh_status pointcloud_enqueue(oh_ctx* ctx, int prec, const oh_pc_params* p, const
     const int cnt = std::min(chunk, n - j0);
     {
       KernelTimer kt(ctx, "pc_tables", st);
-      pc_tables<<<std::max(1, std::min(cnt, 152 * 8)), 256, 0, st>>>(g, pts + j0, cnt, prm, A, RX, B, RY, E);
+      pc_tables<<<std::max(1, std::min(cnt, oh::sm_count() * 8)), 256, 0, st>>>(g, pts + j0, cnt, prm, A, RX, B, RY, E);
       OH_LAUNCH_CHECK();
     }
     KernelTimer kt(ctx, "pc_direct_f32", st);
@@ -361,20 +361,54 @@ static __device__ __align__(256) unsigned char g_pc_noalloc_scratch[kNoAllocScra
 constexpr int kMaxDevices = 64;
 static std::mutex g_noalloc_mu;
 static void* g_noalloc_ptr[kMaxDevices] = {nullptr};
+static unsigned long long g_noalloc_ctx_id[kMaxDevices] = {0};
 
-// Device address of the scratch array on the current device (first call on
-// a device does the lookup).
+// Unique id of the CUDA context current on this thread (0 if unknown).  A
+// device reset destroys the primary context and the module with it, so the
+// scratch array's address is cached per context id, not per device index.
+static unsigned long long current_ctx_id() {
+  typedef int (*get_current_t)(void**);
+  typedef int (*get_id_t)(void*, unsigned long long*);
+  static get_current_t get_current = nullptr;
+  static get_id_t get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    looked_up = true;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (get_current_t)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (get_id_t)f;
+    cudaGetLastError();
+  }
+  void* c = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&c) != 0 || !c || get_id(c, &id) != 0) return 0;
+  return id;
+}
+
+// Device address of the scratch array in the current device's context.  The
+// first call in a context (the first call on a device, and the first after
+// a device reset) looks the address up with cudaGetSymbolAddress.
 static oh_status noalloc_scratch(void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
   if (dev < 0 || dev >= kMaxDevices) return fail(OH_ERR_INVALID_ARG, "device index above the supported maximum");
+  e = cudaSetDevice(dev);   // makes the device's primary context current
+  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  const unsigned long long id = current_ctx_id();
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
+  if (!g_noalloc_ptr[dev] || id == 0 || g_noalloc_ctx_id[dev] != id) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_pc_noalloc_scratch);
     if (e != cudaSuccess || !p) return cuda_fail(e == cudaSuccess ? cudaErrorInvalidSymbol : e, "cudaGetSymbolAddress(point-cloud scratch)");
     g_noalloc_ptr[dev] = p;
+    g_noalloc_ctx_id[dev] = id;
   }
   *out = g_noalloc_ptr[dev];
   return OH_OK;
@@ -402,7 +436,6 @@ oh_status oh_pointcloud_noalloc(const oh_pc_params* p, const float* xyza, int n_
   void* base = nullptr;
   OH_TRY(noalloc_scratch(&base));
   PCGeom g = make_geom(p);
-  dim3 grid((p->nx + kPcTX - 1) / kPcTX, (p->ny + kPcTY - 1) / kPcTY);
   const float4* pts = reinterpret_cast<const float4*>(xyza);
   if (n_points == 0) {
     if (field_out) OH_CUDA_TRY(cudaMemsetAsync(field_out, 0, (size_t)p->nx * p->ny * sizeof(float2), st));
@@ -417,7 +450,7 @@ oh_status oh_pointcloud_noalloc(const oh_pc_params* p, const float* xyza, int n_
   float* E = RY + (size_t)chunk * p->ny;
   for (int j0 = 0; j0 < n_points; j0 += chunk) {
     const int cnt = std::min(chunk, n_points - j0);
-    pc_tables<<<std::max(1, std::min(cnt, 152 * 8)), 256, 0, st>>>(g, pts + j0, cnt, prm, A, RX, B, RY, E);
+    pc_tables<<<std::max(1, std::min(cnt, oh::sm_count() * 8)), 256, 0, st>>>(g, pts + j0, cnt, prm, A, RX, B, RY, E);
     OH_LAUNCH_CHECK();
     pc_direct_f32<<<pc_grid_f32(p->nx, p->ny), kPcTX * kPcFTY, 0, st>>>(g, prm, A, RX, B, RY, E, cnt, (float2*)field_out, (float*)fringe_out,
                                                   j0 > 0);

@@ -176,7 +176,7 @@ oh_status run_propagate(oh_ctx* ctx, int method, int nx, int ny, double dx, doub
   double* fxv = reinterpret_cast<double*>(ty + NY);
   double* fyv = fxv + NX;
   const PropAxis X{NX, 1.0 / (NX * dx)}, Y{NY, 1.0 / (NY * dy)};
-  const int grid = 152 * 8;
+  const int grid = oh::sm_count() * 8;
   const double zt = z / lambda;                 // exp(i k z) = exp(2 pi i z / lambda)
   const double carrier = zt - std::rint(zt);
   {

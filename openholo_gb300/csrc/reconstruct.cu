@@ -146,7 +146,7 @@ oh_status run_eye(oh_ctx* ctx, const oh_eye_params* p, const void* fringe, void*
   void* b;
   OH_TRY(scratch(ctx, "eye.a", npx * sizeof(C), &a));
   OH_TRY(scratch(ctx, "eye.b", npx * sizeof(C), &b));
-  const int grid = 152 * 8;
+  const int grid = oh::sm_count() * 8;
   KernelTimer kt(ctx, "eye_reconstruct", st);
   eye_tables<<<(nx + ny + 255) / 256, 256, 0, st>>>(g, lam, f, feff, t1x, t1y, t2x, t2y);
   OH_LAUNCH_CHECK();

@@ -28,7 +28,7 @@ static oh_ctx* shim_ctx() {
   return g_shim_ctx[dev];
 }
 
-static inline int nblocks(long long n) { return (int)std::min<long long>((n + 511) / 512, 152LL * 64); }
+static inline int nblocks(long long n) { return (int)std::min<long long>((n + 511) / 512, (long long)oh::sm_count() * 64); }
 
 __global__ void shim_depth_sources(double2* u, const unsigned char* img, const unsigned char* dimg, const double* didx,
                                    int dtr, double2 rp, double2 cp, long long n, int flag, unsigned int defq) {

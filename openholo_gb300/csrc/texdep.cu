@@ -161,7 +161,7 @@ oh_status run_texdep(oh_ctx* ctx, int mode, const oh_texdep_params* p, const uin
   const double k_turn = 1.0 / lam;                              // k / (2 pi)
   const double tn = std::tan(std::asin(lam / (2.0 * px)));     // half-width = int(|dz| tn / px)
   TexGeom g{p->nx, p->ny, 0, p->range_lo, p->range_hi, 0, p->dep_from_texture ? 1 : 0};
-  const int grid = 152 * 8;
+  const int grid = oh::sm_count() * 8;
   if (mode == OH_TEXDEP_SINGLE) {
     if (p->z == 0.0) return fail(OH_ERR_INVALID_ARG, "z must be non-zero");
     const double wd = std::fabs(p->z) * tn / px;

@@ -902,7 +902,7 @@ oh_status oh_wrp_accumulate(oh_ctx* ctx, oh_precision prec, const oh_wrp_params*
       OH_CUDA_TRY(cudaFuncSetAttribute(wrp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tcw::kSmemBytes));
     KernelTimer kt(ctx, "wrp_accumulate", st);
     OH_CUDA_TRY(cudaMemsetAsync(cnt, 0, (size_t)nbins * kWrpRep * 4, st));
-    const int g1 = std::min((n_points + 255) / 256, 152 * 8);
+    const int g1 = std::min((n_points + 255) / 256, oh::sm_count() * 8);
     wrp_prep<<<g1, 256, 0, st>>>(g, xyz, n_points, pts, cnt, nbins, bins);
     OH_LAUNCH_CHECK();
     wrp_scan<<<1, 1024, 0, st>>>(cnt, start, cur, nbins);
@@ -923,7 +923,7 @@ oh_status oh_wrp_accumulate(oh_ctx* ctx, oh_precision prec, const oh_wrp_params*
     }
     return OH_OK;
   }
-  const int grid = std::min(n_points, 152 * 32);
+  const int grid = std::min(n_points, oh::sm_count() * 32);
   KernelTimer kt(ctx, "wrp_accumulate", st);
   if (prec == OH_FP64) wrp_accumulate_kernel<double><<<grid, 256, 0, st>>>(g, xyz, n_points, (double2*)wrp);
   else wrp_accumulate_kernel<float><<<grid, 256, 0, st>>>(g, xyz, n_points, (float2*)wrp);
@@ -941,7 +941,7 @@ oh_status oh_wrp_matlab(oh_ctx* ctx, oh_precision prec, int res, double pitch, d
   if (n_points == 0) return OH_OK;
   WrpMGeom g{res, pitch, lambda, z_wrp};
   KernelTimer kt(ctx, "wrp_matlab", st);
-  const int grid = std::min(n_points, 152 * 16);
+  const int grid = std::min(n_points, oh::sm_count() * 16);
   if (prec == OH_FP64) wrp_matlab_kernel<double><<<grid, 256, 0, st>>>(g, xyz, phase, n_points, (double2*)holo);
   else wrp_matlab_kernel<float><<<grid, 256, 0, st>>>(g, xyz, phase, n_points, (float2*)holo);
   OH_LAUNCH_CHECK();

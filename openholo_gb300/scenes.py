@@ -147,3 +147,19 @@ def mesh_scene(seed: int, cells: int = 5, size: float = 170e-6, z0: float = 0.1,
         flat = flat[[0, 2, 1]]
     tris.append(flat.reshape(-1))
     return np.array(tris, dtype=np.float64)
+
+
+BATCH_FRAMES, BATCH_SEED = 64, 4
+BATCH_SCENE_SEED, BATCH_PHASE_SEED = 2024, 77
+
+
+def batch_workload(n: int = BATCH_FRAMES, seed: int = BATCH_SEED):
+    """The mixed depth-map batch: n square frames, side from {512, 768, 1024,
+    1536, 2048}, layers 8..64 and wavelength from {450, 532, 633} nm, drawn
+    from SplitMix64 stream 9 of `seed`.  Frame i uses the Gaussian scene of
+    seed BATCH_SCENE_SEED + side and the seeded per-pixel phase
+    BATCH_PHASE_SEED + i; 2x pad, FP32.  Returns [(side, layers, lambda)]."""
+    u = uniform(seed, 9, 3 * n).reshape(n, 3)
+    sides = [512, 768, 1024, 1536, 2048]
+    lams = [450e-9, 532e-9, 633e-9]
+    return [(sides[int(a * 5)], 8 + int(b * 57), lams[int(c * 3)]) for a, b, c in u]

@@ -10,9 +10,11 @@ from openholo_gb300._lib import OhError
 
 pytestmark = pytest.mark.gpu
 
-# (pny, pnx, layers, wavelength): scheduled FFT lengths (1024, 1536, 1080x1920)
-# and a generic one (192 x 240)
-FRAMES = [(512, 512, 6, 633e-9), (96, 120, 5, 450e-9), (768, 768, 9, 532e-9), (540, 960, 4, 450e-9)]
+# (pny, pnx, layers, wavelength): scheduled FFT lengths (1024, 1536, 1080x1920,
+# and padded length 4096 along x and along y, whose shared-memory lines carry
+# the per-radix pads) and a generic one (192 x 240)
+FRAMES = [(512, 512, 6, 633e-9), (96, 120, 5, 450e-9), (768, 768, 9, 532e-9), (540, 960, 4, 450e-9),
+          (384, 2048, 3, 532e-9), (2048, 384, 3, 633e-9)]
 
 
 def _frames(seed):

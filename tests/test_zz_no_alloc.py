@@ -65,6 +65,31 @@ def test_noalloc_matches_regular_entry_point(ctx, shape, n):
         assert _rel(fringe, ref_fringe) < TOL
 
 
+def test_noalloc_leaves_device_memory_unchanged(ctx):
+    """After a first call (which looks up the array's address), a call takes
+    no device memory: the device's free bytes and torch's allocations are
+    the same before and after it, and its result still equals the regular
+    entry point's."""
+    p = _params(512, 384)
+    pts = torch.from_numpy(scenes.pointcloud_scene(8, 2000).astype(np.float32)).cuda()
+    ref_field, _ = _regular(ctx, p, pts)
+    field = torch.empty((p.ny, p.nx), dtype=torch.complex64, device="cuda")
+    call = lambda: _lib.call("oh_pointcloud_noalloc", C.byref(p), C.c_void_p(pts.data_ptr()), pts.shape[0],
+                             C.c_void_p(field.data_ptr()), None, _stream())
+    call()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    torch_bytes0 = torch.cuda.memory_allocated()
+    field.zero_()
+    torch.cuda.synchronize()
+    call()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert torch.cuda.memory_allocated() == torch_bytes0
+    assert _rel(field, ref_field) < TOL
+
+
 def test_noalloc_rejects_fields_beyond_its_scratch(lib_built):
     p = _params(16384, 16384)
     pts = torch.zeros((4, 4), dtype=torch.float32, device="cuda")
