@@ -296,6 +296,27 @@ oh_status oh_pointcloud_host(oh_ctx* ctx, oh_precision prec,
 oh_status oh_pointcloud_noalloc(const oh_pc_params* p, const float* xyza, int n_points,
                                 void* field_out, void* fringe_out, void* stream);
 
+/* ---- tensor-core convolutions (the learned surrogate's building blocks) ----
+ * No reference counterpart.  NHWC BF16 tensors on the device with channel
+ * strides x_cs / mask_cs / out_cs (elements, multiples of 8; tensors 16-byte
+ * aligned), n images of h x w pixels; widths below 128 must divide 128.
+ * oh_conv2d_bf16: out[p][co] = act(bias[co] + sum_{t, ci} x[p + sign*off_t][ci] W[co][t*cin + ci])
+ *   taps 9 (3x3, zero padding 1; off_t = (t%3 - 1, t/3 - 1)) or 1; cin and
+ *   cout multiples of 32 (cout <= 1024); W BF16 [cout][taps*cin]; bias FP32
+ *   or NULL; relu != 0 applies max(., 0); mask (nullable) zeroes outputs
+ *   where mask[p][co] <= 0.  sign = -1 with W[ci][t*cout + co] (the layer's
+ *   weights transposed) gives the gradient with respect to the layer input.
+ *   FP32 accumulation on the tcgen05 tensor cores, BF16 output.
+ * oh_conv2d_wgrad_bf16: dwt[t*cin + ci][co] += sum_p x[p + off_t][ci] dz[p][co]
+ *   (FP32, accumulated: zero it first); cout 32, 64, 128 or 256; widths
+ *   below 64 must divide 64. */
+oh_status oh_conv2d_bf16(oh_ctx* ctx, int taps, int sign, int n, int h, int w, int cin, int cout,
+                         const void* x, int x_cs, const void* wmat, const float* bias, int relu,
+                         const void* mask, int mask_cs, void* out, int out_cs, void* stream);
+oh_status oh_conv2d_wgrad_bf16(oh_ctx* ctx, int taps, int n, int h, int w, int cin, int cout,
+                               const void* x, int x_cs, const void* dz, int dz_cs, float* dwt,
+                               void* stream);
+
 /* ---- propagation in the MATLAB tools' forms --------------------------------
  * OH_PROP_FRESNEL_TF (FresnelPropagation.m:1-16): ifft2(fft2(U) .* H) with
  *   H = exp(i k z) exp(-i pi lambda z (fx^2 + fy^2)) on the FFT-ordered grid; no padding.

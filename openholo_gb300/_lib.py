@@ -119,6 +119,8 @@ SIGNATURES = {
     "oh_ctx_set_timing": (_i, [_vp, _i]),
     "oh_ctx_device_status": (_i, [_vp, _vp]),
     "oh_measure_issue_peaks": (_i, [_i, C.POINTER(_d), C.POINTER(_d), C.POINTER(_d), C.POINTER(_d)]),
+    "oh_conv2d_bf16": (_i, [_vp, _i, _i, _i, _i, _i, _i, _i, _vp, _i, _vp, _vp, _i, _vp, _i, _vp, _i, _vp]),
+    "oh_conv2d_wgrad_bf16": (_i, [_vp, _i, _i, _i, _i, _i, _i, _vp, _i, _vp, _i, _vp, _vp]),
     "oh_ctx_read_timing": (_i, [_vp, _i, C.POINTER(C.c_char_p), C.POINTER(_d), C.POINTER(C.c_long), _i]),
     "oh_fft_supported": (_i, [_i, _i]),
     "oh_fft2d": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _i, _i, _vp]),

@@ -1,0 +1,475 @@
+// Implicit-GEMM convolutions on the tcgen05 tensor cores (BF16 operands,
+// FP32 accumulation in TMEM), the compute core of the learned surrogate.
+//
+// Activations are NHWC BF16 with a channel stride that is a multiple of 32
+// (64 bytes), so 32 channels of one pixel are one 64-byte line of a
+// 64-byte-swizzled shared-memory tile.
+//
+// conv_fwd_tc: Y[p][co] = sum_{tap, ci} X[p + s*off(tap)][ci] W[co][tap*cin + ci]
+//   GEMM with M = 128 pixels (a bx x by patch), N = BN output channels,
+//   K = taps x cin in 32-channel steps.  The A tile of a K step is one TMA
+//   load of the 4-D activation map at the tap's offset: out-of-range pixels
+//   read as zero, which is the convolution's zero padding.  s = +1 is the
+//   forward convolution; s = -1 with the transposed weight matrix
+//   Wt[ci][tap*cout + co] is the gradient with respect to the input (dgrad).
+//   Epilogue: + bias, ReLU, multiplication by (mask > 0) (the ReLU derivative
+//   of the layer below, for dgrad), BF16 store with an output channel stride
+//   (so a layer can write straight into one half of a concatenation buffer).
+// conv_wgrad_tc: dW^T[tap*cin + ci][co] += sum_p X[p + off(tap)][ci] dZ[p][co]
+//   GEMM with M = 128 rows of the (tap, ci) space (four 32-channel groups,
+//   each its own TMA load at its tap's offset), N = cout, K = pixels in
+//   64-pixel steps; both operands are MN-major (channels contiguous), K split
+//   across CTAs, partial sums added with vector reductions.
+//
+// Roles (128 threads): thread 0 issues TMA loads into a ring of stages,
+// thread 32 issues tcgen05.mma and releases stages with tcgen05.commit, all
+// four warps read the accumulator (warp w owns TMEM lanes 32w..32w+31).  Every
+// mbarrier wait gives up after `wait_limit` SM clocks: the CTA then sets the
+// device error word, lets its copies and MMAs land, frees TMEM and returns.
+#include <cuda_bf16.h>
+#include <algorithm>
+#include "context.h"
+#include "tc_common.cuh"
+#include "unet.cuh"
+
+namespace oh {
+
+namespace {
+
+constexpr int kConvThreads = 128;
+
+template <int BN> struct FwdCfg {
+  static constexpr int kA = 128 * 64;                 // 128 pixels x 32 channels
+  static constexpr int kB = BN * 64;                  // BN rows x 32 K
+  static constexpr int kStage = kA + kB;
+  static constexpr int kStages = BN >= 256 ? 4 : BN >= 128 ? 6 : 8;
+  static constexpr int kTmem = BN < 32 ? 32 : BN;
+  static constexpr int kSmem = kStages * kStage + 1024 + 256;
+};
+
+template <int BN>
+__global__ void __launch_bounds__(kConvThreads) conv_fwd_tc(const __grid_constant__ CUtensorMap mX,
+                                                            const __grid_constant__ CUtensorMap mW, ConvArgs a) {
+  typedef FwdCfg<BN> Cfg;
+  extern __shared__ unsigned char smem_raw[];
+  const uint32_t raw = tc::su32(smem_raw);
+  unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+  uint64_t* full = reinterpret_cast<uint64_t*>(base + Cfg::kStages * Cfg::kStage);
+  uint64_t* empty = full + Cfg::kStages;
+  uint64_t* done = empty + Cfg::kStages;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+  int* issued = abort_flag + 1;
+  int* consumed = abort_flag + 2;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  int t = blockIdx.x;
+  const int tx = t % a.tiles_x; t /= a.tiles_x;
+  const int ty = t % a.tiles_y;
+  const int img = t / a.tiles_y;
+  const int x0 = tx * a.bx, y0 = ty * a.by;
+  const int co0 = blockIdx.y * BN;
+  const int cchunks = a.cin >> 5;
+  const int nk = a.taps * cchunks;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < Cfg::kStages; ++s) { tc::mb_init(&full[s], 1); tc::mb_init(&empty[s], 1); }
+    tc::mb_init(done, 1);
+    *abort_flag = 0; *issued = 0; *consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) tc::tmem_alloc(tmem_slot, Cfg::kTmem);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (threadIdx.x == 0) {
+    int it = 0;
+    for (; it < nk; ++it) {
+      const int s = it % Cfg::kStages;
+      const uint32_t ph = (uint32_t)((it / Cfg::kStages) & 1);
+      if (!tc::mb_wait(&empty[s], ph ^ 1u, a.wait_limit) || *((volatile int*)abort_flag)) {
+        atomicExch(abort_flag, 1);
+        break;
+      }
+      const int tap = it / cchunks, cc = it - tap * cchunks;
+      int dx = 0, dy = 0;
+      if (a.taps == 9) { dx = (tap % 3 - 1) * a.sign; dy = (tap / 3 - 1) * a.sign; }
+      unsigned char* st = base + s * Cfg::kStage;
+      tc::mb_expect_tx(&full[s], (uint32_t)Cfg::kStage);
+      tc::tma_load_4d(st, &mX, cc * 32, x0 + dx, y0 + dy, img, &full[s]);
+      tc::tma_load_2d(st + Cfg::kA, &mW, tap * a.cin + cc * 32, co0, &full[s]);
+    }
+    *issued = it;
+  } else if (threadIdx.x == 32) {
+    constexpr uint32_t idesc = tc::idesc_bf16(128, BN, 0, 0);
+    int it = 0;
+    for (; it < nk; ++it) {
+      const int s = it % Cfg::kStages;
+      const uint32_t ph = (uint32_t)((it / Cfg::kStages) & 1);
+      if (!tc::mb_wait(&full[s], ph, a.wait_limit) || *((volatile int*)abort_flag)) {
+        atomicExch(abort_flag, 1);
+        break;
+      }
+      tc::fence_after();
+      const uint32_t sa = tc::su32(base + s * Cfg::kStage);
+      const uint64_t da = tc::desc_sw64(sa, 16, 512), db = tc::desc_sw64(sa + Cfg::kA, 16, 512);
+#pragma unroll
+      for (int kk = 0; kk < 2; ++kk) {
+        const uint64_t adv = (uint64_t)((kk * 32) >> 4);      // 16 BF16 = 32 bytes along K
+        tc::umma_bf16(tmem, da + adv, db + adv, idesc, (it | kk) ? 1u : 0u);
+      }
+      tc::umma_commit(&empty[s]);
+    }
+    *consumed = it;
+    tc::umma_commit(done);
+  }
+  __syncwarp();
+  const bool ok_done = tc::mb_wait(done, 0, a.wait_limit);
+  tc::fence_after();
+  const bool good = __syncthreads_and(ok_done && !*((volatile int*)abort_flag));
+  if (good) {
+    const int m = warp * 32 + lane;
+    const int px = x0 + (m % a.bx), py = y0 + (m / a.bx);
+    const bool inside = px < a.w && py < a.h;
+    const size_t pix = ((size_t)img * a.h + py) * a.w + px;
+#pragma unroll 1
+    for (int c = 0; c < BN / 32; ++c) {
+      uint32_t r[32];
+      tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), r);
+      const int cb = co0 + c * 32;
+      if (!inside || cb >= a.cout) continue;
+      float v[32];
+#pragma unroll
+      for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
+      if (a.bias) {
+#pragma unroll
+        for (int q = 0; q < 32; ++q) v[q] += __ldg(a.bias + cb + q);
+      }
+      if (a.relu) {
+#pragma unroll
+        for (int q = 0; q < 32; ++q) v[q] = fmaxf(v[q], 0.f);
+      }
+      if (a.mask) {
+        const uint4* mp = reinterpret_cast<const uint4*>(a.mask + pix * a.mask_cs + cb);
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+          const uint4 mv = __ldg(mp + g);
+          const __nv_bfloat162* mb = reinterpret_cast<const __nv_bfloat162*>(&mv);
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const float2 f = __bfloat1622float2(mb[e]);
+            if (!(f.x > 0.f)) v[g * 8 + 2 * e] = 0.f;
+            if (!(f.y > 0.f)) v[g * 8 + 2 * e + 1] = 0.f;
+          }
+        }
+      }
+      uint4* op = reinterpret_cast<uint4*>(a.out + pix * a.out_cs + cb);
+#pragma unroll
+      for (int g = 0; g < 4; ++g) {
+        uint4 o;
+        __nv_bfloat162* ob = reinterpret_cast<__nv_bfloat162*>(&o);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) ob[e] = __floats2bfloat162_rn(v[g * 8 + 2 * e], v[g * 8 + 2 * e + 1]);
+        op[g] = o;
+      }
+    }
+  } else if (threadIdx.x == 0) {
+    atomicOr(a.err, 2);
+  }
+  if (threadIdx.x == 0) {
+    for (int it = *consumed; it < *issued; ++it)
+      tc::mb_wait(&full[it % Cfg::kStages], (uint32_t)((it / Cfg::kStages) & 1), a.wait_limit);
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc::fence_after();
+    tc::tmem_dealloc(tmem, Cfg::kTmem);
+  }
+}
+
+template <int BN> struct WgCfg {
+  static constexpr int kKp = 64;                       // pixels per K step
+  static constexpr int kBox = kKp * 64;                // one 32-channel group of kKp pixels
+  static constexpr int kA = 4 * kBox;                  // four (tap, 32-channel) groups
+  static constexpr int kB = (BN / 32) * kBox;
+  static constexpr int kStage = kA + kB;
+  static constexpr int kStages = BN >= 256 ? 4 : 5;
+  static constexpr int kTmem = BN < 32 ? 32 : BN;
+  static constexpr int kSmem = kStages * kStage + 1024 + 256;
+};
+
+template <int BN>
+__global__ void __launch_bounds__(kConvThreads) conv_wgrad_tc(const __grid_constant__ CUtensorMap mX,
+                                                              const __grid_constant__ CUtensorMap mD, WgArgs a) {
+  typedef WgCfg<BN> Cfg;
+  extern __shared__ unsigned char smem_raw[];
+  const uint32_t raw = tc::su32(smem_raw);
+  unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+  uint64_t* full = reinterpret_cast<uint64_t*>(base + Cfg::kStages * Cfg::kStage);
+  uint64_t* empty = full + Cfg::kStages;
+  uint64_t* done = empty + Cfg::kStages;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+  int* issued = abort_flag + 1;
+  int* consumed = abort_flag + 2;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  const int cchunks = a.cin >> 5;
+  const int groups = a.taps * cchunks;
+  const int g0 = blockIdx.x * 4;
+  const long long kb_total = (long long)a.n * a.tiles_y * a.tiles_x;
+  const int kb0 = (int)(kb_total * blockIdx.y / gridDim.y);
+  const int kb1 = (int)(kb_total * (blockIdx.y + 1) / gridDim.y);
+  const int nk = kb1 - kb0;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < Cfg::kStages; ++s) { tc::mb_init(&full[s], 1); tc::mb_init(&empty[s], 1); }
+    tc::mb_init(done, 1);
+    *abort_flag = 0; *issued = 0; *consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) tc::tmem_alloc(tmem_slot, Cfg::kTmem);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (threadIdx.x == 0) {
+    int it = 0;
+    for (; it < nk; ++it) {
+      const int s = it % Cfg::kStages;
+      const uint32_t ph = (uint32_t)((it / Cfg::kStages) & 1);
+      if (!tc::mb_wait(&empty[s], ph ^ 1u, a.wait_limit) || *((volatile int*)abort_flag)) {
+        atomicExch(abort_flag, 1);
+        break;
+      }
+      int kb = kb0 + it;
+      const int tx = kb % a.tiles_x; kb /= a.tiles_x;
+      const int ty = kb % a.tiles_y;
+      const int img = kb / a.tiles_y;
+      const int x0 = tx * a.bx, y0 = ty * a.by;
+      unsigned char* st = base + s * Cfg::kStage;
+      tc::mb_expect_tx(&full[s], (uint32_t)Cfg::kStage);
+#pragma unroll
+      for (int g = 0; g < 4; ++g) {
+        const int gg = min(g0 + g, groups - 1);     // rows past the last group: loaded, never stored
+        const int tap = gg / cchunks, cc = gg - tap * cchunks;
+        int dx = 0, dy = 0;
+        if (a.taps == 9) { dx = tap % 3 - 1; dy = tap / 3 - 1; }
+        tc::tma_load_4d(st + g * Cfg::kBox, &mX, cc * 32, x0 + dx, y0 + dy, img, &full[s]);
+      }
+#pragma unroll
+      for (int j = 0; j < BN / 32; ++j)
+        tc::tma_load_4d(st + Cfg::kA + j * Cfg::kBox, &mD, j * 32, x0, y0, img, &full[s]);
+    }
+    *issued = it;
+  } else if (threadIdx.x == 32) {
+    constexpr uint32_t idesc = tc::idesc_bf16(128, BN, 1, 1);
+    int it = 0;
+    for (; it < nk; ++it) {
+      const int s = it % Cfg::kStages;
+      const uint32_t ph = (uint32_t)((it / Cfg::kStages) & 1);
+      if (!tc::mb_wait(&full[s], ph, a.wait_limit) || *((volatile int*)abort_flag)) {
+        atomicExch(abort_flag, 1);
+        break;
+      }
+      tc::fence_after();
+      const uint32_t sa = tc::su32(base + s * Cfg::kStage);
+#pragma unroll
+      for (int kk = 0; kk < Cfg::kKp / 16; ++kk) {
+        // 16 pixels = two 8-line K groups, 1024 bytes
+        const uint64_t da = tc::desc_sw64(sa + kk * 1024, Cfg::kBox, 512);
+        const uint64_t db = tc::desc_sw64(sa + Cfg::kA + kk * 1024, Cfg::kBox, 512);
+        tc::umma_bf16(tmem, da, db, idesc, (it | kk) ? 1u : 0u);
+      }
+      tc::umma_commit(&empty[s]);
+    }
+    *consumed = it;
+    tc::umma_commit(done);
+  }
+  __syncwarp();
+  const bool ok_done = tc::mb_wait(done, 0, a.wait_limit);
+  tc::fence_after();
+  const bool good = __syncthreads_and(ok_done && !*((volatile int*)abort_flag));
+  if (good && nk > 0) {
+    const int m = warp * 32 + lane;
+    const int row = g0 * 32 + m;                      // (tap, ci) row of dW^T
+    const bool live = row < groups * 32;
+#pragma unroll 1
+    for (int c = 0; c < BN / 32; ++c) {
+      uint32_t r[32];
+      tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), r);
+      if (!live) continue;
+      float* dst = a.dwt + (size_t)row * a.cout + c * 32;
+#pragma unroll
+      for (int q = 0; q < 32; q += 4)
+        asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst + q), "f"(__uint_as_float(r[q])),
+                     "f"(__uint_as_float(r[q + 1])), "f"(__uint_as_float(r[q + 2])), "f"(__uint_as_float(r[q + 3]))
+                     : "memory");
+    }
+  } else if (!good && threadIdx.x == 0) {
+    atomicOr(a.err, 2);
+  }
+  if (threadIdx.x == 0) {
+    for (int it = *consumed; it < *issued; ++it)
+      tc::mb_wait(&full[it % Cfg::kStages], (uint32_t)((it / Cfg::kStages) & 1), a.wait_limit);
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc::fence_after();
+    tc::tmem_dealloc(tmem, Cfg::kTmem);
+  }
+}
+
+// Patch of `pixels` pixels for an image row of width w: bx = min(w, pixels),
+// by = pixels / bx; widths below `pixels` must divide it.
+bool patch_shape(int w, int pixels, int* bx, int* by) {
+  if (w >= pixels) { *bx = pixels; *by = 1; return true; }
+  if (pixels % w) return false;
+  *bx = w; *by = pixels / w;
+  return true;
+}
+
+template <int BN>
+oh_status launch_fwd(const CUtensorMap& mX, const CUtensorMap& mW, const ConvArgs& a, int tiles, cudaStream_t st) {
+  typedef FwdCfg<BN> Cfg;
+  OH_CUDA_TRY(cudaFuncSetAttribute(conv_fwd_tc<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmem));
+  conv_fwd_tc<BN><<<dim3(tiles, (a.cout + BN - 1) / BN), kConvThreads, Cfg::kSmem, st>>>(mX, mW, a);
+  OH_LAUNCH_CHECK();
+  return OH_OK;
+}
+
+template <int BN>
+oh_status launch_wgrad(const CUtensorMap& mX, const CUtensorMap& mD, const WgArgs& a, int mtiles, int splits,
+                       cudaStream_t st) {
+  typedef WgCfg<BN> Cfg;
+  OH_CUDA_TRY(cudaFuncSetAttribute(conv_wgrad_tc<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmem));
+  conv_wgrad_tc<BN><<<dim3(mtiles, splits), kConvThreads, Cfg::kSmem, st>>>(mX, mD, a);
+  OH_LAUNCH_CHECK();
+  return OH_OK;
+}
+
+}  // namespace
+
+oh_status tc_arch_check() {
+  int dev = 0, major = 0, minor = 0;
+  OH_CUDA_TRY(cudaGetDevice(&dev));
+  OH_CUDA_TRY(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+  OH_CUDA_TRY(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
+  if (major != 10 || minor != 3) return fail(OH_ERR_UNSUPPORTED_SIZE, "the tensor-core convolutions are built for sm_103a");
+  return OH_OK;
+}
+
+oh_status conv_enqueue(oh_ctx* ctx, const ConvDesc& d, cudaStream_t st, const char* timer_name) {
+  if (d.cin % 32 || d.cin <= 0 || d.cout <= 0 || d.cout % 32 || d.cout > 1024 || (d.taps != 9 && d.taps != 1))
+    return fail(OH_ERR_INVALID_ARG, "convolution: cin and cout must be positive multiples of 32 (cout <= 1024), taps 1 or 9");
+  if (d.x_cs % 8 || d.out_cs % 8 || (d.mask && (d.mask_cs % 8 || d.mask_cs < d.cout)) || d.x_cs < d.cin ||
+      d.out_cs < d.cout)
+    return fail(OH_ERR_INVALID_ARG, "convolution: channel strides must be multiples of 8 and cover the channels");
+  if (!d.x || !d.w_mat || !d.out) return fail(OH_ERR_INVALID_ARG, "convolution: null tensor");
+  if ((reinterpret_cast<uintptr_t>(d.x) | reinterpret_cast<uintptr_t>(d.w_mat) | reinterpret_cast<uintptr_t>(d.out) |
+       reinterpret_cast<uintptr_t>(d.mask)) & 15)
+    return fail(OH_ERR_INVALID_ARG, "convolution: tensors must be 16-byte aligned");
+  OH_TRY(tc_arch_check());
+  ConvArgs a{};
+  if (!patch_shape(d.w, 128, &a.bx, &a.by)) return fail(OH_ERR_UNSUPPORTED_SIZE, "convolution: widths below 128 must divide 128");
+  a.taps = d.taps; a.cin = d.cin; a.cout = d.cout; a.w = d.w; a.h = d.h; a.n = d.n;
+  a.tiles_x = (d.w + a.bx - 1) / a.bx; a.tiles_y = (d.h + a.by - 1) / a.by;
+  a.sign = d.sign;
+  a.bias = d.bias; a.relu = d.relu;
+  a.mask = reinterpret_cast<const __nv_bfloat16*>(d.mask); a.mask_cs = d.mask_cs;
+  a.out = reinterpret_cast<__nv_bfloat16*>(d.out); a.out_cs = d.out_cs;
+  a.err = ctx->dev_err;
+  a.wait_limit = d.wait_limit > 0 ? d.wait_limit : 2000000000LL;
+  const long long tiles = (long long)a.tiles_x * a.tiles_y * d.n;
+  if (tiles > 0x7fffffffLL) return fail(OH_ERR_UNSUPPORTED_SIZE, "convolution: too many pixel tiles");
+  // output-channel tile: the largest power of two up to 256 that divides
+  // cout, halved while the grid is under two waves
+  int bn = 256;
+  while (d.cout % bn) bn /= 2;
+  while (bn > 32 && tiles * ((d.cout + bn - 1) / bn) < 2LL * sm_count()) bn /= 2;
+  CUtensorMap mX, mW;
+  OH_TRY(tc::map_act4d(&mX, d.x, d.cin, d.x_cs, d.w, d.h, d.n, a.bx, a.by));
+  OH_TRY(tc::map_mat2d(&mW, d.w_mat, d.taps * d.cin, d.cout, bn));
+  KernelTimer kt(ctx, timer_name, st);
+  switch (bn) {
+    case 32: return launch_fwd<32>(mX, mW, a, (int)tiles, st);
+    case 64: return launch_fwd<64>(mX, mW, a, (int)tiles, st);
+    case 128: return launch_fwd<128>(mX, mW, a, (int)tiles, st);
+    default: return launch_fwd<256>(mX, mW, a, (int)tiles, st);
+  }
+}
+
+oh_status wgrad_enqueue(oh_ctx* ctx, const WgradDesc& d, cudaStream_t st, const char* timer_name) {
+  if (d.cin % 32 || d.cin <= 0 || (d.cout != 32 && d.cout != 64 && d.cout != 128 && d.cout != 256) ||
+      (d.taps != 9 && d.taps != 1))
+    return fail(OH_ERR_INVALID_ARG, "weight gradient: cin a positive multiple of 32, cout 32, 64, 128 or 256, taps 1 or 9");
+  if (d.x_cs % 8 || d.dz_cs % 8 || d.x_cs < d.cin || d.dz_cs < d.cout)
+    return fail(OH_ERR_INVALID_ARG, "weight gradient: channel strides must be multiples of 8 and cover the channels");
+  if (!d.x || !d.dz || !d.dwt) return fail(OH_ERR_INVALID_ARG, "weight gradient: null tensor");
+  if ((reinterpret_cast<uintptr_t>(d.x) | reinterpret_cast<uintptr_t>(d.dz) | reinterpret_cast<uintptr_t>(d.dwt)) & 15)
+    return fail(OH_ERR_INVALID_ARG, "weight gradient: tensors must be 16-byte aligned");
+  OH_TRY(tc_arch_check());
+  WgArgs a{};
+  if (!patch_shape(d.w, 64, &a.bx, &a.by)) return fail(OH_ERR_UNSUPPORTED_SIZE, "weight gradient: widths below 64 must divide 64");
+  a.taps = d.taps; a.cin = d.cin; a.cout = d.cout; a.w = d.w; a.h = d.h; a.n = d.n;
+  a.tiles_x = (d.w + a.bx - 1) / a.bx; a.tiles_y = (d.h + a.by - 1) / a.by;
+  a.dwt = d.dwt;
+  a.err = ctx->dev_err;
+  a.wait_limit = d.wait_limit > 0 ? d.wait_limit : 2000000000LL;
+  const int groups = d.taps * (d.cin / 32);
+  const int mtiles = (groups + 3) / 4;
+  const long long kb_total = (long long)a.tiles_x * a.tiles_y * d.n;
+  // K splits: about four CTAs per SM over all M tiles, each with at least 16 K steps
+  long long splits = std::max(1LL, (4LL * sm_count() + mtiles - 1) / mtiles);
+  splits = std::min(splits, std::max(1LL, kb_total / 16));
+  splits = std::min(splits, 65535LL);
+  CUtensorMap mX, mD;
+  OH_TRY(tc::map_act4d(&mX, d.x, d.cin, d.x_cs, d.w, d.h, d.n, a.bx, a.by));
+  OH_TRY(tc::map_act4d(&mD, d.dz, d.cout, d.dz_cs, d.w, d.h, d.n, a.bx, a.by));
+  KernelTimer kt(ctx, timer_name, st);
+  switch (d.cout) {
+    case 32: return launch_wgrad<32>(mX, mD, a, mtiles, (int)splits, st);
+    case 64: return launch_wgrad<64>(mX, mD, a, mtiles, (int)splits, st);
+    case 128: return launch_wgrad<128>(mX, mD, a, mtiles, (int)splits, st);
+    default: return launch_wgrad<256>(mX, mD, a, mtiles, (int)splits, st);
+  }
+}
+
+}  // namespace oh
+
+using namespace oh;
+
+extern "C" {
+
+oh_status oh_conv2d_bf16(oh_ctx* ctx, int taps, int sign, int n, int h, int w, int cin, int cout, const void* x,
+                         int x_cs, const void* wmat, const float* bias, int relu, const void* mask, int mask_cs,
+                         void* out, int out_cs, void* stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  CallScope cs(ctx, st);
+  OH_TRY(cs.status());
+  if (n < 1 || h < 1 || w < 1 || (sign != 1 && sign != -1)) return fail(OH_ERR_INVALID_ARG, "convolution: bad sizes or sign");
+  ConvDesc d{};
+  d.taps = taps; d.sign = sign; d.n = n; d.h = h; d.w = w; d.cin = cin; d.cout = cout;
+  d.x = x; d.x_cs = x_cs; d.w_mat = wmat; d.bias = bias; d.relu = relu; d.mask = mask; d.mask_cs = mask_cs;
+  d.out = out; d.out_cs = out_cs;
+  return conv_enqueue(ctx, d, st, "conv_fwd_tc");
+}
+
+oh_status oh_conv2d_wgrad_bf16(oh_ctx* ctx, int taps, int n, int h, int w, int cin, int cout, const void* x, int x_cs,
+                               const void* dz, int dz_cs, float* dwt, void* stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  CallScope cs(ctx, st);
+  OH_TRY(cs.status());
+  if (n < 1 || h < 1 || w < 1) return fail(OH_ERR_INVALID_ARG, "weight gradient: bad sizes");
+  WgradDesc d{};
+  d.taps = taps; d.n = n; d.h = h; d.w = w; d.cin = cin; d.cout = cout;
+  d.x = x; d.x_cs = x_cs; d.dz = dz; d.dz_cs = dz_cs; d.dwt = dwt;
+  return wgrad_enqueue(ctx, d, st, "conv_wgrad_tc");
+}
+
+}  // extern "C"
