@@ -154,6 +154,16 @@ oh_status oh_depthmap_generate(oh_ctx* ctx, oh_precision prec,
                                const float* phase, void* fringe_out,
                                void* field_out, void* spectrum_out,
                                void* stream);
+/* One complex source field instead of the image/depth layers (no reference
+ * counterpart; the learned surrogate's second step): field_in [pny][pnx]
+ * (oh_c64 for OH_FP32, oh_c128 for OH_FP64, device) taken as a single layer
+ * at distance z (the layer's z'), then the same padded angular-spectrum
+ * propagation, crop and encoding as oh_depthmap_generate with parameters p
+ * (pad, pitch, wavelength, sig_location; the level and phase fields are
+ * unused).  The carrier exp(i k z) multiplies the source as it does a layer. */
+oh_status oh_depthmap_propagate_field(oh_ctx* ctx, oh_precision prec, const oh_depthmap_params* p,
+                                      const void* field_in, double z, void* fringe_out, void* field_out,
+                                      void* spectrum_out, void* stream);
 /* Same with host buffers; copies in and out on the given stream and waits.
  * A page-locked fringe_host (cudaHostAlloc / cudaHostRegister) is written by
  * the output kernel through its device mapping, with no copy after the frame;
@@ -316,6 +326,98 @@ oh_status oh_conv2d_bf16(oh_ctx* ctx, int taps, int sign, int n, int h, int w, i
 oh_status oh_conv2d_wgrad_bf16(oh_ctx* ctx, int taps, int n, int h, int w, int cin, int cout,
                                const void* x, int x_cs, const void* dz, int dz_cs, float* dwt,
                                void* stream);
+
+/* ---- learned surrogate: U-Net (no reference counterpart) ---------------------
+ * A 4-level U-Net mapping an RGB-D frame to the complex mid-plane field of the
+ * plain layered angular-spectrum method: encoder levels of 32, 64, 128 and
+ * 256 channels (3x3 convolution + ReLU, twice; 2x2 average pooling between
+ * levels), decoder levels that upsample (nearest, 2x), concatenate the
+ * encoder output of the same level and apply two 3x3 convolutions + ReLU, and
+ * a 1x1 head to 2 channels (re, im).  BF16 weights and activations, FP32
+ * accumulation on the tcgen05 tensor cores, FP32 master weights, Adam.
+ * Input: rgbd uint8 [n][h][w][4] on the device (R, G, B and a depth byte; the
+ * depth channel is depth_lut[byte]); output: field float2 [n][h][w] =
+ * out_scale * (head output).  h and w multiples of 8; level widths w >> l
+ * below 128 must divide 128.  The network owns its device memory (weights,
+ * optimizer state and the activations of max_batch frames of
+ * max_height x max_width), allocated by oh_unet_create.
+ * Parameters are exchanged as one flat FP32 array, layer by layer (enc0a,
+ * enc0b, ..., enc3b, dec2a, dec2b, dec1a, dec1b, dec0a, dec0b, head), each
+ * W[cout][taps][cin] then b[cout]; enc0a has cin = 4, dec{l}a has
+ * cin = c_l + c_{l+1} (encoder channels first). */
+typedef struct oh_unet oh_unet;
+typedef struct oh_unet_config {
+  int max_batch, max_height, max_width;
+  uint64_t seed;                 /* He-normal initial weights from a SplitMix64 stream */
+  float out_scale;               /* field units per head output unit */
+  float depth_lut[256];          /* depth byte -> input channel 3 */
+} oh_unet_config;
+void      oh_unet_config_default(oh_unet_config* cfg);
+oh_status oh_unet_create(oh_ctx* ctx, const oh_unet_config* cfg, oh_unet** net);
+oh_status oh_unet_destroy(oh_unet* net);
+size_t    oh_unet_param_count(const oh_unet* net);
+/* Synchronous copies of the flat parameter array (set also resets Adam). */
+oh_status oh_unet_get_params(oh_unet* net, float* host);
+oh_status oh_unet_set_params(oh_unet* net, const float* host);
+/* Inference: field_out float2 [n][h][w] (device). */
+oh_status oh_unet_forward(oh_unet* net, const uint8_t* rgbd, int n, int h, int w, void* field_out,
+                          void* stream);
+/* Forward and backward pass of a batch against target float2 [n][h][w]
+ * (device): loss = mean over pixels and both components of
+ * (head output - target / out_scale)^2, written to loss_out (device float,
+ * nullable); the gradients stay in the network (oh_unet_get_grads copies
+ * them out in the flat parameter layout, synchronously). */
+oh_status oh_unet_compute_grads(oh_unet* net, const uint8_t* rgbd, const void* target, int n, int h,
+                                int w, float* loss_out, void* stream);
+oh_status oh_unet_get_grads(oh_unet* net, float* host);
+/* Adam update from the last computed gradients (bias-corrected). */
+oh_status oh_unet_adam_step(oh_unet* net, float lr, float beta1, float beta2, float eps, void* stream);
+/* compute_grads + adam_step (beta1 0.9, beta2 0.999, eps 1e-8). */
+oh_status oh_unet_train_step(oh_unet* net, const uint8_t* rgbd, const void* target, int n, int h, int w,
+                             float lr, float* loss_out, void* stream);
+
+/* Seeded synthetic RGB-D frames (training and test inputs; no reference
+ * counterpart): rgbd uint8 [n][h][w][4], frame f from seed + f.  R, G and B
+ * are sums of 20 Gaussians (SplitMix64 streams 3, 1 and 5; centres uniform
+ * over the frame, sigma 20-200 px times min(h, w)/1080, amplitude 0.2-1),
+ * each scaled by its maximum to 0-255; the depth byte is a sum of 8 broad
+ * Gaussians (stream 2, sigma 200-600 px scaled) rescaled min..max to 0-255.
+ * FP32 evaluation (the FP64 twin may differ by one level at rounding ties). */
+oh_status oh_scene_rgbd(oh_ctx* ctx, uint64_t seed, int n, int h, int w, uint8_t* rgbd, void* stream);
+
+/* The learned surrogate around the plain layered angular-spectrum method.
+ * dm: the plain frame's parameters (pnx x pny is the network's frame; the G
+ * byte of rgbd is the intensity image and the depth byte the depth map;
+ * the source phase is the reference constant 1).  z_mid: the mid plane.
+ * oh_surrogate_mid_field: the plain method's field on the mid plane (its
+ *   layers propagated over z' - z_mid, full spectrum) -> oh_c64 [pny][pnx];
+ *   the network's training target.
+ * oh_surrogate_generate: the network's mid-plane field, carried over z_mid
+ *   to the hologram plane with the plain frame's padding, crop and encoding
+ *   (fringe_out float [pny][pnx]; field_mid_out, nullable, receives the
+ *   mid-plane field used).  check != 0 also computes the plain mid-plane
+ *   field, reports the PSNR of the mid-plane intensity |F|^2 (peak: the plain
+ *   field's maximum intensity) and the complex errors relative to it, and
+ *   when the PSNR is below psnr_threshold_db uses the plain field for this
+ *   frame (fell_back = 1); with check the call synchronises `stream` to read
+ *   the comparison. */
+typedef struct oh_surrogate_params {
+  oh_depthmap_params dm;
+  double z_mid;
+  float  psnr_threshold_db;
+  int    check;
+} oh_surrogate_params;
+typedef struct oh_surrogate_report {
+  int   checked, fell_back;
+  float psnr_db;          /* mid-plane intensity PSNR against the plain method */
+  float rel_err;          /* ||F_net - F|| / ||F|| */
+  float max_abs_err;      /* max |F_net - F| / max |F| */
+  float rms_err;          /* rms |F_net - F| / max |F| */
+} oh_surrogate_report;
+oh_status oh_surrogate_mid_field(oh_ctx* ctx, const oh_depthmap_params* p, double z_mid, const uint8_t* rgbd,
+                                 void* field_mid, void* stream);
+oh_status oh_surrogate_generate(oh_ctx* ctx, oh_unet* net, const oh_surrogate_params* sp, const uint8_t* rgbd,
+                                void* fringe_out, void* field_mid_out, oh_surrogate_report* rep, void* stream);
 
 /* ---- propagation in the MATLAB tools' forms --------------------------------
  * OH_PROP_FRESNEL_TF (FresnelPropagation.m:1-16): ifft2(fft2(U) .* H) with

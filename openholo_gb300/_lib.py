@@ -83,6 +83,23 @@ PLS_HUYGENS, PLS_FRESNEL, PLS_CGH_FRESNEL = 0, 1, 2
 PLS_ENGINE_AUTO, PLS_ENGINE_DIRECT, PLS_ENGINE_GEMM, PLS_ENGINE_TENSOR = 0, 1, 2, 3
 
 
+class UnetConfig(C.Structure):
+    """oh_unet_config (include/oh.h)."""
+    _fields_ = [("max_batch", C.c_int), ("max_height", C.c_int), ("max_width", C.c_int), ("seed", C.c_uint64),
+                ("out_scale", C.c_float), ("depth_lut", C.c_float * 256)]
+
+
+class SurrogateParams(C.Structure):
+    """oh_surrogate_params (include/oh.h)."""
+    _fields_ = [("dm", DepthmapParams), ("z_mid", C.c_double), ("psnr_threshold_db", C.c_float), ("check", C.c_int)]
+
+
+class SurrogateReport(C.Structure):
+    """oh_surrogate_report (include/oh.h)."""
+    _fields_ = [("checked", C.c_int), ("fell_back", C.c_int), ("psnr_db", C.c_float), ("rel_err", C.c_float),
+                ("max_abs_err", C.c_float), ("rms_err", C.c_float)]
+
+
 class TexdepParams(C.Structure):
     """oh_texdep_params (include/oh.h)."""
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("px", C.c_double), ("py", C.c_double), ("lambda_", C.c_double),
@@ -121,6 +138,21 @@ SIGNATURES = {
     "oh_measure_issue_peaks": (_i, [_i, C.POINTER(_d), C.POINTER(_d), C.POINTER(_d), C.POINTER(_d)]),
     "oh_conv2d_bf16": (_i, [_vp, _i, _i, _i, _i, _i, _i, _i, _vp, _i, _vp, _vp, _i, _vp, _i, _vp, _i, _vp]),
     "oh_conv2d_wgrad_bf16": (_i, [_vp, _i, _i, _i, _i, _i, _i, _vp, _i, _vp, _i, _vp, _vp]),
+    "oh_unet_config_default": (None, [_vp]),
+    "oh_depthmap_propagate_field": (_i, [_vp, _i, _vp, _vp, _d, _vp, _vp, _vp, _vp]),
+    "oh_scene_rgbd": (_i, [_vp, C.c_uint64, _i, _i, _i, _vp, _vp]),
+    "oh_surrogate_mid_field": (_i, [_vp, _vp, _d, _vp, _vp, _vp]),
+    "oh_surrogate_generate": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "oh_unet_create": (_i, [_vp, _vp, C.POINTER(_vp)]),
+    "oh_unet_destroy": (_i, [_vp]),
+    "oh_unet_param_count": (C.c_size_t, [_vp]),
+    "oh_unet_get_params": (_i, [_vp, _vp]),
+    "oh_unet_set_params": (_i, [_vp, _vp]),
+    "oh_unet_get_grads": (_i, [_vp, _vp]),
+    "oh_unet_forward": (_i, [_vp, _vp, _i, _i, _i, _vp, _vp]),
+    "oh_unet_compute_grads": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp, _vp]),
+    "oh_unet_adam_step": (_i, [_vp, C.c_float, C.c_float, C.c_float, C.c_float, _vp]),
+    "oh_unet_train_step": (_i, [_vp, _vp, _vp, _i, _i, _i, C.c_float, _vp, _vp]),
     "oh_ctx_read_timing": (_i, [_vp, _i, C.POINTER(C.c_char_p), C.POINTER(_d), C.POINTER(C.c_long), _i]),
     "oh_fft_supported": (_i, [_i, _i]),
     "oh_fft2d": (_i, [_vp, _i, _i, _i, _vp, _vp, _i, _i, _i, _vp]),

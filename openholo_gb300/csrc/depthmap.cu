@@ -58,6 +58,7 @@ struct DMArgs {
   const float* phase;
   int phase_mode;
   uint64_t seed;
+  const C* src;          // complex source field [pny][pnx] (one layer, img/depth unused) or null
   // device tables (written by dm_setup)
   int16_t* lut;          // 256
   int16_t* uslot_of_entry;
@@ -333,7 +334,7 @@ __global__ void __launch_bounds__(512, row_min_blocks<NX>()) dm_row_pass(DMArgs<
       const int idx = base + q * blockDim.x + threadIdx.x;
       const int l = idx / pnx, c = idx - l * pnx;
       gb[q] = 0; db[q] = 0;
-      if (idx < kRowPair * pnx && l < nrows) {
+      if (idx < kRowPair * pnx && l < nrows && !a.src) {
         const size_t off = (size_t)(r0 + l) * pnx + c;
         gb[q] = a.img[off];
         db[q] = a.depth[off];
@@ -346,7 +347,12 @@ __global__ void __launch_bounds__(512, row_min_blocks<NX>()) dm_row_pass(DMArgs<
       const int l = idx / pnx, c = idx - l * pnx;
       int u = -1;
       C val = mk((R)0, (R)0);
-      if (l < nrows) {
+      if (l < nrows && a.src) {
+        // a complex source field: every pixel in the one layer slot
+        u = 0;
+        val = a.src[(size_t)(r0 + l) * pnx + c];
+        if (c == 0) atomicOr(&mask[l * 8], 1u);
+      } else if (l < nrows) {
         const size_t off = (size_t)(r0 + l) * pnx + c;
         const uint8_t g = gb[q];
         u = g > 0 ? (int)slut[db[q]] : -1;
@@ -763,17 +769,25 @@ struct DMScratch { size_t R, V, occ, tables; };
 
 // Enqueues one frame.  With sizes_only set, computes the frame's scratch
 // needs into it and returns without allocating or launching anything.
+// src (nullable): a complex source field [pny][pnx] (oh_c64 / oh_c128) taken
+// as the one layer, at z' = src_z, instead of the image/depth layers.
 template <typename R, int KMAX>
 static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const uint8_t* img,
                               const uint8_t* depth, const float* phase, void* fringe, void* field,
-                              void* spectrum, cudaStream_t st, DMScratch* sizes_only = nullptr) {
+                              void* spectrum, cudaStream_t st, DMScratch* sizes_only = nullptr,
+                              const void* src = nullptr, double src_z = 0.0) {
   typedef typename cplx_of<R>::type C;
   const int prec = sizeof(R) == 8 ? 1 : 0;
   Levels L;
   OH_TRY(compute_levels(p, &L));
-  const int nd = p->num_of_depth;
+  int nd = p->num_of_depth;
   std::vector<int> render;
-  if (p->render_depth) render.assign(p->render_depth, p->render_depth + p->n_render_depth);
+  if (src) {
+    nd = 1;
+    L.ztrans.assign(1, src_z);
+    for (int b = 0; b < 256; ++b) L.lut[b] = 0;
+    render.push_back(1);
+  } else if (p->render_depth) render.assign(p->render_depth, p->render_depth + p->n_render_depth);
   else for (int i = 1; i <= nd; ++i) render.push_back(i);
   if ((int)render.size() > kMaxEntries) return fail(OH_ERR_INVALID_ARG, "more than 256 render_depth entries");
   for (int d : render) if (d < 1 || d > nd) return fail(OH_ERR_INVALID_ARG, "render_depth entry outside 1..num_of_depth");
@@ -791,7 +805,7 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
     const double k = 2.0 * M_PI / p->lambda;
     // rand_phase * carrier exp(i k z') (HologramGenerator_GPU.cpp:267-273)
     double rre = 1.0, rim = 0.0;
-    if (p->phase_mode == OH_PHASE_REFERENCE) { rre = p->rand_phase_re; rim = p->rand_phase_im; }
+    if (p->phase_mode == OH_PHASE_REFERENCE && !src) { rre = p->rand_phase_re; rim = p->rand_phase_im; }
     double cre = std::cos(k * z), cim = std::sin(k * z);
     double are = rre * cre - rim * cim, aim = rre * cim + rim * cre;
     if (prec == 0) {
@@ -820,6 +834,7 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   a.ssx = p->ppx * a.Px; a.ssy = p->ppy * a.Py;
   a.lambda = p->lambda; a.k = 2.0 * M_PI / p->lambda;
   a.img = img; a.depth = depth; a.phase = phase;
+  a.src = static_cast<const C*>(src);
   a.phase_mode = p->phase_mode; a.seed = p->seed;
   a.sig_x = p->sig_location_x; a.sig_y = p->sig_location_y;
   // Encoding_Symmetrization crop window (HologramGenerator.cpp:486-514), on the padded grid
@@ -982,7 +997,7 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
     // layer flags
     struct Key {
       DMSetup su;
-      int prec, pnx, pny, Px, Py, sig_x, sig_y, ey_perm, horner;
+      int prec, pnx, pny, Px, Py, sig_x, sig_y, ey_perm, horner, src_mode;
       double ppx, ppy, lambda;
       const void* tables;
       const void* iperm;
@@ -991,6 +1006,7 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
     key.su = su;
     key.prec = prec; key.pnx = a.pnx; key.pny = a.pny; key.Px = a.Px; key.Py = a.Py;
     key.sig_x = a.sig_x; key.sig_y = a.sig_y; key.ey_perm = a.ey_perm; key.horner = a.horner;
+    key.src_mode = src ? 1 : 0;
     key.ppx = a.ppx; key.ppy = a.ppy; key.lambda = a.lambda;
     key.tables = base; key.iperm = a.ply.iperm;
     std::string ks(reinterpret_cast<const char*>(&key), sizeof(key));
@@ -1073,6 +1089,15 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   return OH_OK;
 }
 
+// One FP32 frame with the caller holding the context (the surrogate's two
+// uses: image/depth layers, or one complex source field at src_z).
+oh_status depthmap_enqueue_f32(oh_ctx* ctx, const oh_depthmap_params* p, const uint8_t* img, const uint8_t* depth,
+                               void* fringe, void* field, const void* src, double src_z, cudaStream_t st) {
+  OH_TRY(validate(p));
+  if (!fringe || (!src && (!img || !depth))) return fail(OH_ERR_INVALID_ARG, "depth-map frame: missing buffers");
+  return run_depthmap<float, 36>(ctx, p, img, depth, nullptr, fringe, field, nullptr, st, nullptr, src, src_z);
+}
+
 }  // namespace oh
 
 using namespace oh;
@@ -1119,6 +1144,22 @@ oh_status oh_depthmap_generate(oh_ctx* ctx, oh_precision prec, const oh_depthmap
   if (p->phase_mode == OH_PHASE_ARRAY && !phase) return fail(OH_ERR_INVALID_ARG, "OH_PHASE_ARRAY needs a phase array");
   if (prec == OH_FP64) return run_depthmap<double, 18>(ctx, p, img, depth, phase, fringe_out, field_out, spectrum_out, st);
   return run_depthmap<float, 36>(ctx, p, img, depth, phase, fringe_out, field_out, spectrum_out, st);
+}
+
+oh_status oh_depthmap_propagate_field(oh_ctx* ctx, oh_precision prec, const oh_depthmap_params* p,
+                                      const void* field_in, double z, void* fringe_out, void* field_out,
+                                      void* spectrum_out, void* stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  CallScope cs(ctx, st);
+  OH_TRY(cs.status());
+  OH_TRY(validate(p));
+  if (!field_in || !fringe_out) return fail(OH_ERR_INVALID_ARG, "field_in and fringe_out are required");
+  if (!std::isfinite(z)) return fail(OH_ERR_INVALID_ARG, "propagation distance must be finite");
+  if (prec == OH_FP64)
+    return run_depthmap<double, 18>(ctx, p, nullptr, nullptr, nullptr, fringe_out, field_out, spectrum_out, st, nullptr,
+                                    field_in, z);
+  return run_depthmap<float, 36>(ctx, p, nullptr, nullptr, nullptr, fringe_out, field_out, spectrum_out, st, nullptr,
+                                 field_in, z);
 }
 
 oh_status oh_depthmap_generate_batch(oh_ctx* ctx, oh_precision prec, const oh_depthmap_frame* frames, int n,

@@ -74,6 +74,22 @@ def generate(ctx: _lib.Context, p: DepthmapParams, img, depth, phase=None, preci
     return fringe
 
 
+def propagate_field(ctx: _lib.Context, p: DepthmapParams, field, z: float, precision="fp32", fringe=None,
+                    out_field=None, stream=None):
+    """One complex source field (device tensor [pny][pnx]) as a single layer at
+    distance z through the frame pipeline (oh_depthmap_propagate_field);
+    returns the fringe."""
+    import torch
+    prec = OH_FP64 if precision == "fp64" else OH_FP32
+    if fringe is None:
+        fringe = torch.empty((p.pny, p.pnx), dtype=torch.float64 if prec == OH_FP64 else torch.float32,
+                             device=field.device)
+    ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None
+    _lib.call("oh_depthmap_propagate_field", ctx.handle, prec, C.byref(p), ptr(field), z, ptr(fringe), ptr(out_field),
+              None, _stream_ptr(stream))
+    return fringe
+
+
 def generate_batch(ctx: _lib.Context, frames, precision="fp32", graph=False, stream=None):
     """Run a list of frames in one call (oh_depthmap_generate_batch).  Each
     entry is (params, img, depth, fringe) or (params, img, depth, fringe,

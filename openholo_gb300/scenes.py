@@ -163,3 +163,20 @@ def batch_workload(n: int = BATCH_FRAMES, seed: int = BATCH_SEED):
     sides = [512, 768, 1024, 1536, 2048]
     lams = [450e-9, 532e-9, 633e-9]
     return [(sides[int(a * 5)], 8 + int(b * 57), lams[int(c * 3)]) for a, b, c in u]
+
+
+def rgbd_scene(seed: int, h: int, w: int) -> np.ndarray:
+    """uint8 [h][w][4] RGB-D frame, the float64 twin of oh_scene_rgbd: R, G,
+    B = Gaussian sums of streams 3, 1, 5 (20 Gaussians, sigma 20-200 px
+    scaled by min(h, w)/1080) each rescaled by its maximum, depth = stream 2
+    (8 Gaussians, sigma 200-600 px scaled) rescaled min..max.  G and depth
+    equal depthmap_scene(seed, h, w)."""
+    scale = min(h, w) / 1080.0
+    out = np.empty((h, w, 4), dtype=np.uint8)
+    for c, stream in enumerate((3, 1, 5)):
+        v = gaussian_sum(seed, stream, h, w, 20, (20 * scale, 200 * scale))
+        out[..., c] = np.clip(np.rint(255.0 * v / v.max()), 0, 255).astype(np.uint8)
+    d = gaussian_sum(seed, 2, h, w, 8, (200 * scale, 600 * scale))
+    d = (d - d.min()) / max(d.max() - d.min(), 1e-300)
+    out[..., 3] = np.clip(np.rint(255.0 * d), 0, 255).astype(np.uint8)
+    return out

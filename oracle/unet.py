@@ -102,67 +102,73 @@ def layer_shapes(in_ch=4, chans=(32, 64, 128, 256), out_ch=2):
     return L
 
 
-def forward(params, x, chans=(32, 64, 128, 256)):
-    """params: dict name -> (W [cout,taps,cin], b [cout]).  Returns (pred, cache)."""
+def _same(a):
+    return a
+
+
+def forward(params, x, chans=(32, 64, 128, 256), rnd=_same):
+    """params: dict name -> (W [cout,taps,cin], b [cout]).  Returns (pred, cache).
+    rnd is applied to every stored activation (identity: exact float64;
+    a BF16 rounding function: the storage precision of the CUDA kernels)."""
     cache = {}
     h = x
     enc = []
     for l in range(len(chans)):
-        a = conv(h, *params[f"enc{l}a"], relu=True)
-        e = conv(a, *params[f"enc{l}b"], relu=True)
+        a = rnd(conv(h, *params[f"enc{l}a"], relu=True))
+        e = rnd(conv(a, *params[f"enc{l}b"], relu=True))
         cache[f"enc{l}a_in"], cache[f"enc{l}a_out"], cache[f"enc{l}b_out"] = h, a, e
         enc.append(e)
         if l + 1 < len(chans):
-            h = pool(e)
+            h = rnd(pool(e))
     d = enc[-1]
     for l in range(len(chans) - 2, -1, -1):
         cat = np.concatenate([enc[l], up(d)], axis=3)
-        a = conv(cat, *params[f"dec{l}a"], relu=True)
-        d = conv(a, *params[f"dec{l}b"], relu=True)
+        a = rnd(conv(cat, *params[f"dec{l}a"], relu=True))
+        d = rnd(conv(a, *params[f"dec{l}b"], relu=True))
         cache[f"dec{l}a_in"], cache[f"dec{l}a_out"], cache[f"dec{l}b_out"] = cat, a, d
     pred = conv(d, *params["head"])
     cache["head_in"] = d
     return pred, cache
 
 
-def loss_and_grads(params, x, target, chans=(32, 64, 128, 256)):
+def loss_and_grads(params, x, target, chans=(32, 64, 128, 256), rnd=_same):
     """Mean squared error over all pixels and output channels, the gradient
-    of every weight and bias (dict name -> (dW, db)) and the prediction."""
-    pred, c = forward(params, x, chans)
+    of every weight and bias (dict name -> (dW, db)) and the prediction.
+    rnd: as in forward, applied to the stored activations and activation
+    gradients (weight and bias gradients stay unrounded)."""
+    pred, c = forward(params, x, chans, rnd)
     diff = pred - target
     loss = float(np.mean(diff ** 2))
     dpred = 2.0 * diff / diff.size
-    return loss, backward(params, c, dpred, chans), pred
+    return loss, backward(params, c, dpred, chans, rnd), pred
 
 
-def backward(params, c, dpred, chans=(32, 64, 128, 256)):
+def backward(params, c, dpred, chans=(32, 64, 128, 256), rnd=_same):
     """Gradients of every layer given d(loss)/d(pred) and the forward cache."""
     nlev = len(chans)
     g = {}
     Wh, _ = params["head"]
     g["head"] = (conv_wgrad(c["head_in"], dpred, 1), dpred.sum(axis=(0, 1, 2)))
     dd = conv_dgrad(dpred, Wh)          # d(output of dec0b)
+    dz_b = rnd(dd * (c["dec0b_out"] > 0))
     denc = [None] * nlev
-    # decoder levels from 0 (top, last computed) to nlev-2
+    # decoder levels from 0 (top, last computed) to nlev-2; dz_b is the
+    # gradient of dec{l}b's pre-activation
     for l in range(0, nlev - 1):
-        dz_b = dd * (c[f"dec{l}b_out"] > 0)
         g[f"dec{l}b"] = (conv_wgrad(c[f"dec{l}a_out"], dz_b), dz_b.sum(axis=(0, 1, 2)))
-        da = conv_dgrad(dz_b, params[f"dec{l}b"][0])
-        dz_a = da * (c[f"dec{l}a_out"] > 0)
+        dz_a = rnd(conv_dgrad(dz_b, params[f"dec{l}b"][0]) * (c[f"dec{l}a_out"] > 0))
         g[f"dec{l}a"] = (conv_wgrad(c[f"dec{l}a_in"], dz_a), dz_a.sum(axis=(0, 1, 2)))
-        dcat = conv_dgrad(dz_a, params[f"dec{l}a"][0])
+        dcat = rnd(conv_dgrad(dz_a, params[f"dec{l}a"][0]))
         denc[l] = dcat[..., :chans[l]]
-        dd = up_back(dcat[..., chans[l]:])           # d(output of dec{l+1}b), or of enc{nlev-1}b
-    # encoder from the bottleneck up
-    de = dd                                          # d(enc{nlev-1}b output) from the decoder
+        below = c[f"dec{l + 1}b_out"] if l + 1 < nlev - 1 else c[f"enc{nlev - 1}b_out"]
+        dz_b = rnd(up_back(dcat[..., chans[l]:]) * (below > 0))
+    # encoder from the bottleneck up; dz_b is the gradient of enc{l}b's pre-activation
     for l in range(nlev - 1, -1, -1):
         if l < nlev - 1:
-            de = denc[l] + pool_back(dpool)
-        dz_b = de * (c[f"enc{l}b_out"] > 0)
+            dz_b = rnd((denc[l] + pool_back(dpool)) * (c[f"enc{l}b_out"] > 0))
         g[f"enc{l}b"] = (conv_wgrad(c[f"enc{l}a_out"], dz_b), dz_b.sum(axis=(0, 1, 2)))
-        da = conv_dgrad(dz_b, params[f"enc{l}b"][0])
-        dz_a = da * (c[f"enc{l}a_out"] > 0)
+        dz_a = rnd(conv_dgrad(dz_b, params[f"enc{l}b"][0]) * (c[f"enc{l}a_out"] > 0))
         g[f"enc{l}a"] = (conv_wgrad(c[f"enc{l}a_in"], dz_a), dz_a.sum(axis=(0, 1, 2)))
         if l > 0:
-            dpool = conv_dgrad(dz_a, params[f"enc{l}a"][0])   # d(pooled input of level l)
+            dpool = rnd(conv_dgrad(dz_a, params[f"enc{l}a"][0]))   # d(pooled input of level l)
     return g
