@@ -334,11 +334,13 @@ def plain_gpu_path(img_t, depth_t, zt, lut, torch):
     return frame
 
 
-SECONDARY_OPS = ("pointcloud", "pls", "wrp", "batch", "square")
+SECONDARY_OPS = ("pointcloud", "pls", "wrp", "batch", "square", "unet")
+UNET_SIDE, UNET_SAMPLES, UNET_BATCH, UNET_LR, UNET_ZMID = 1024, 20000, 4, 1e-3, 0.325
 SQUARE_SIDE, SQUARE_LAYERS = 2048, 16     # --op square: the batch's largest frame shape
 
 
-def secondary_measurements(ctx, dev, torch, reps=5, ops=SECONDARY_OPS, warmup=1, peaks=None):
+def secondary_measurements(ctx, dev, torch, reps=5, ops=SECONDARY_OPS, warmup=1, peaks=None,
+                           samples=UNET_SAMPLES):
     """The other operators at their own workloads (seeded synthetic inputs):
     pointcloud: KETI exact-r sum 1024x1024 x 5000 points + phase-only encoding;
     pls: the same shape through the paraxial cwoPLS::Fresnel sum (tensor-core
@@ -372,7 +374,86 @@ def secondary_measurements(ctx, dev, torch, reps=5, ops=SECONDARY_OPS, warmup=1,
         _sec_batch(ctx, dev, torch, out, reps, warmup)
     if "square" in ops:
         _sec_square(ctx, dev, torch, timed, out)
+    if "unet" in ops:
+        _sec_unet(ctx, dev, torch, timed, out, samples)
     return out
+
+
+def unet_fwd_flops(side):
+    """Forward FLOPs of one side x side frame through the U-Net (multiply-adds
+    x 2, the first layer's 4 input channels padded to 32 as computed)."""
+    from openholo_gb300 import surrogate
+    f = 0
+    for name, cin, cout, taps in surrogate.layer_shapes():
+        lvl = int(name[3]) if name[:3] in ("enc", "dec") else 0
+        f += 2 * (side >> lvl) ** 2 * taps * (32 if cin == 4 else cin) * cout
+    return f
+
+
+def _sec_unet(ctx, dev, torch, timed, out, samples):
+    """The learned form: a U-Net (32/64/128/256 channels, 3x3 convolutions,
+    BF16, FP32 accumulation, all convolutions on the tensor cores) trained on
+    the GPU on `samples` seeded 1024x1024 RGB-D frames against the plain
+    method's mid-plane field (32 layers over 0.30-0.35 m, mid plane 0.325 m,
+    2x pad), then evaluated on 32 held-out frames with the 40 dB PSNR gate."""
+    from openholo_gb300 import depthmap as dm, surrogate
+    side, B = UNET_SIDE, UNET_BATCH
+    p = dm.make_params(pnx=side, pny=side, num_of_depth=32, pad=2)
+    lut, _ = dm.levels(p)
+    dl = np.where(lut > 0, (lut - 1) / 31.0, 0.0).astype(np.float32)
+    probe = surrogate.scenes_rgbd(ctx, 10 ** 6, 1, side, side)[0]
+    rms = float(torch.sqrt((surrogate.mid_field(ctx, p, UNET_ZMID, probe).abs() ** 2).mean()))
+    net = surrogate.UNet(ctx, max_batch=B, max_height=side, max_width=side, seed=1, out_scale=rms, depth_lut=dl)
+    try:
+        # training throughput of the step alone (fixed batch)
+        x = surrogate.scenes_rgbd(ctx, 5, B, side, side)
+        tg = torch.zeros((B, side, side, 2), dtype=torch.float32, device=dev)
+        step_ms = timed(lambda: net.train_step(x, tg, 0.0))
+        f1 = unet_fwd_flops(side)
+        res = {"train_step_ms_batch4": step_ms, "train_samples_per_s": B * 1000.0 / step_ms,
+               "fwd_gflop_per_frame": f1 / 1e9, "train_tflops": 3 * f1 * B / (step_ms * 1e-3) / 1e12,
+               "train_kernels_ms": kernel_breakdown(ctx, torch, lambda: net.train_step(x, tg, 0.0), calls=2)}
+        bf16, kind = load_bf16_peak()
+        res["roofline"] = {"bound": "tensor", "unit": "TFLOP/s", "achieved": res["train_tflops"], "peak": bf16,
+                           "frac": res["train_tflops"] / bf16, "peak_source": kind,
+                           "what": "forward + input-gradient + weight-gradient convolutions (3 x forward FLOPs) per "
+                                   "training step time"}
+        net.set_params(net.get_params())     # fresh Adam state for the real run
+        t0 = time.perf_counter()
+        losses = surrogate.train(ctx, net, p, UNET_ZMID, samples, B, UNET_LR, seed=1000)
+        torch.cuda.synchronize()
+        res["training"] = {"samples": samples, "batch": B, "lr": UNET_LR, "seconds": time.perf_counter() - t0,
+                           "loss_first": float(np.mean(losses[:10])), "loss_last": float(np.mean(losses[-10:])),
+                           "what": "each sample a fresh seeded scene, target generated on the GPU by the plain "
+                                   "method inside the timed loop"}
+        # held-out evaluation with the 40 dB gate
+        reps = []
+        for s in range(32):
+            r = surrogate.scenes_rgbd(ctx, 9 * 10 ** 6 + s, 1, side, side)[0]
+            reps.append(surrogate.generate(ctx, net, p, UNET_ZMID, r, check=True, psnr_threshold_db=40.0)[1])
+        ps = [r["psnr_db"] for r in reps]
+        res["accuracy"] = {"psnr_db_mean": float(np.mean(ps)), "psnr_db_min": float(np.min(ps)),
+                           "psnr_db_max": float(np.max(ps)), "rel_err_mean": float(np.mean([r["rel_err"] for r in reps])),
+                           "max_abs_err_mean": float(np.mean([r["max_abs_err"] for r in reps])),
+                           "rms_err_mean": float(np.mean([r["rms_err"] for r in reps])),
+                           "fallbacks": int(sum(r["fell_back"] for r in reps)), "frames": len(reps),
+                           "threshold_db": 40.0,
+                           "what": "mid-plane intensity PSNR of the prediction against the plain method (peak = "
+                                   "max plain intensity); complex errors relative to the plain field"}
+        # throughput: surrogate alone, surrogate judged on every frame, plain frame
+        r = surrogate.scenes_rgbd(ctx, 9 * 10 ** 6, 1, side, side)[0]
+        fr = torch.empty((side, side), dtype=torch.float32, device=dev)
+        ms_sg = timed(lambda: surrogate.generate(ctx, net, p, UNET_ZMID, r, check=False, fringe=fr))
+        ms_chk = timed(lambda: surrogate.generate(ctx, net, p, UNET_ZMID, r, check=True, fringe=fr))
+        g, d = r[..., 1].contiguous(), r[..., 3].contiguous()
+        ms_plain = timed(lambda: dm.generate(ctx, p, g, d, fringe=fr))
+        res["frames_per_s"] = {"surrogate": 1000.0 / ms_sg, "surrogate_checked_every_frame": 1000.0 / ms_chk,
+                               "plain_method": 1000.0 / ms_plain}
+        res["what"] = ("1024x1024 RGB-D -> U-Net mid-plane field -> angular-spectrum propagation over 0.325 m, "
+                       "2x pad, symmetrization encoding; plain method: the same frame's 32 layers")
+        out["unet_surrogate_1024"] = res
+    finally:
+        net.close()
 
 
 def _sec_square(ctx, dev, torch, timed, out):
@@ -604,6 +685,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-baselines", action="store_true", help="skip the CPU and plain-GPU comparison legs")
     ap.add_argument("--no-secondary", action="store_true", help="skip the point-cloud and WRP workloads")
+    ap.add_argument("--unet-samples", type=int, default=UNET_SAMPLES,
+                    help="training samples of the learned form (other_operators.unet_surrogate_1024)")
     ap.add_argument("--record", default=None,
                     help="append one JSON-lines accuracy record (max/RMS error, PSNR, fallbacks) to this file")
     ap.add_argument("--op", choices=SECONDARY_OPS, default=None,
@@ -619,7 +702,7 @@ def main():
         from openholo_gb300 import Context
         torch.cuda.set_device(local)
         res = secondary_measurements(Context(local), torch.device("cuda", local), torch, reps=args.steps,
-                                     ops=(args.op,), warmup=args.warmup)
+                                     ops=(args.op,), warmup=args.warmup, samples=args.unet_samples)
         if rank == 0:
             print(json.dumps({"op": args.op, "steps": args.steps, "warmup": args.warmup, **res}), flush=True)
         return
@@ -739,7 +822,8 @@ def main():
 
     if rank == 0 and world == 1 and not args.no_secondary:
         try:
-            out["other_operators"] = secondary_measurements(ctx, dev, torch, peaks=peaks)
+            out["other_operators"] = secondary_measurements(ctx, dev, torch, peaks=peaks,
+                                                            samples=args.unet_samples)
         except Exception as e:  # pragma: no cover
             out["other_operators"] = {"error": str(e)[:300]}
         torch.cuda.empty_cache()
