@@ -80,6 +80,15 @@ const char* oh_version(void);
  * by the FMA rate at four warp instructions per SM per clock.  Synchronous. */
 oh_status   oh_measure_issue_peaks(int device, double* ffma_per_s, double* ffma2_per_s,
                                    double* mufu_per_s, double* sm_mhz_hint);
+/* Error-path test hook (no reference counterpart).  While set, the kernels
+ * selected by kernel_mask (1: depth-map column pass, 2: point-sum tensor-core
+ * GEMM, 4: tensor-core convolutions) first wait on a device flag that nothing
+ * sets, for at most `cycles` SM clocks, and then take their bounded-wait error
+ * path: they let their copies and tensor-core operations land, free their
+ * tensor memory, set the context's error word and return without writing
+ * results, so oh_ctx_device_status reports OH_ERR_TIMEOUT.  cycles = 0 turns
+ * the hook off.  For testing the error path; never set in production. */
+oh_status   oh_ctx_set_test_stall(oh_ctx* ctx, int kernel_mask, long long cycles);
 /* Synchronises `stream` and reports OH_ERR_TIMEOUT if a kernel of this
  * context gave up a bounded wait since the last check (the flag is then
  * cleared); OH_OK otherwise. */

@@ -247,8 +247,8 @@ oh_status oh_ctx_create(oh_ctx** ctx, int device) {
   oh_ctx* c = new oh_ctx();
   c->device = device;
   e = cudaEventCreateWithFlags(&c->last_done, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaMalloc(&c->dev_err, sizeof(int));
-  if (e == cudaSuccess) e = cudaMemset(c->dev_err, 0, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&c->dev_err, 2 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(c->dev_err, 0, 2 * sizeof(int));
   cudaSetDevice(prev);
   if (e != cudaSuccess) { delete c; return cuda_fail(e, "context set-up"); }
   *ctx = c;
@@ -322,6 +322,16 @@ oh_status oh_ctx_device_status(oh_ctx* ctx, void* stream) {
     OH_CUDA_TRY(cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), st));
     return fail(OH_ERR_TIMEOUT, "a bounded device-side wait ran out (copy into shared memory did not complete)");
   }
+  return OH_OK;
+}
+
+oh_status oh_ctx_set_test_stall(oh_ctx* ctx, int kernel_mask, long long cycles) {
+  if (!ctx) return fail(OH_ERR_INVALID_ARG, "null context");
+  if (kernel_mask < 0 || cycles < 0 || cycles > 4000000000LL)
+    return fail(OH_ERR_INVALID_ARG, "test stall: mask >= 0 and 0 <= cycles <= 4e9");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->stall_mask = cycles > 0 ? kernel_mask : 0;
+  ctx->stall_cycles = cycles;
   return OH_OK;
 }
 

@@ -15,7 +15,11 @@ struct oh_ctx {
   int device = 0;
   std::mutex mu;
   cudaEvent_t last_done = nullptr;   // recorded at the end of every call
-  int* dev_err = nullptr;             // set by kernels whose bounded waits ran out
+  int* dev_err = nullptr;             // [0]: set by kernels whose bounded waits ran out; [1]: a flag nothing sets
+  // error-path test hook (oh_ctx_set_test_stall): kernels in stall_mask wait
+  // on dev_err[1] for at most stall_cycles SM clocks before their first stage
+  int stall_mask = 0;
+  long long stall_cycles = 0;
   std::string dm_setup_key;           // parameters of the depth-map tables now in scratch
   std::string fresnel_key;            // parameters of the Fresnel spectrum in scratch "fr.B"
   bool force_dm_setup = false;        // rebuild the depth-map tables even when cached (graph capture)

@@ -85,6 +85,8 @@ struct DMArgs {
   int xs;                // 1: R and V columns are in the row FFT's storage order (fast passes), 0: kx order
   int hzx, hzy;          // 1: 2x padding with a radix-16 first stage (stage-0 inputs 4..11 are zero)
   int* err;              // device error word (bounded waits that ran out)
+  const int* stall_flag; // error-path test hook: wait on this never-set flag before the first layer
+  long long stall_cycles;
   // evenly spaced layers (fast column pass): step dz = z'_e - z'_(e-1) of the
   // render entries; D = Dx(fx) Dy(fy) exp(-i k dz g) per spectrum element
   int horner;
@@ -854,6 +856,7 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   const int occ_stride = (a.pny + 15) & ~15;
   a.occ_stride = occ_stride;
   a.err = ctx->dev_err;
+  if (ctx->stall_mask & kStallDepthmapColumn) { a.stall_flag = ctx->dev_err + 1; a.stall_cycles = ctx->stall_cycles; }
   // FP32 with a compile-time FFT length: bulk-copy pipelined column pass
   // (dm_col_fast) with the widest strip whose shared-memory layout fits
   int Wfast = 0, col_tab = 0, col_py = a.Py;      // col_py: stored column length of the fast pass

@@ -284,6 +284,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
     uint64_t* const bar_e = (k & 1) ? &mbar[2] : &mbar[1];
     bool ok = mbar_wait_bounded(&mbar[0], (uint32_t)(k & 1));
     ok = ok && (horner || mbar_wait_bounded(bar_e, (uint32_t)((k >> 1) & 1)));
+    if (k == 0 && a.stall_flag && tid == 0) ok = ok && stall_on_unset_flag(a.stall_flag, a.stall_cycles);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) atomicOr(a.err, 1);
       // let this block's copies still in flight land before leaving

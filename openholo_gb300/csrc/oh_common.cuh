@@ -52,6 +52,19 @@ template <int SGN, typename C, typename R> __host__ __device__ __forceinline__ C
   return r;
 }
 
+// Error-path test hook: spin on a device flag that nothing sets, for at most
+// `cycles` SM clocks.  Returns false when the bound ran out (always, unless
+// the flag were set), so the caller takes its bounded-wait error path.
+__device__ __forceinline__ bool stall_on_unset_flag(const int* flag, long long cycles) {
+  const long long t0 = clock64();
+  while (*((volatile const int*)flag) == 0) {
+    if (clock64() - t0 > cycles) return false;
+  }
+  return true;
+}
+// kernel_mask bits of oh_ctx_set_test_stall
+constexpr int kStallDepthmapColumn = 1, kStallPointSumGemm = 2, kStallConvolution = 4;
+
 // Launch accounting (read through oh_kernel_launch_count()).
 void note_launch(int n = 1);
 // Kernels launched by this library so far (all threads).

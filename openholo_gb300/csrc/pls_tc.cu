@@ -62,6 +62,15 @@ __device__ __forceinline__ bool mb_wait(uint64_t* b, uint32_t parity) {
   return true;
 }
 
+// as mb_wait, also giving up as soon as another role has set *abort
+__device__ __forceinline__ bool mb_wait_live(uint64_t* b, uint32_t parity, const int* abort) {
+  const long long t0 = clock64();
+  while (!mb_try(b, parity)) {
+    if (*((volatile const int*)abort) || clock64() - t0 > kWaitCycles) return false;
+  }
+  return true;
+}
+
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int c0, int c1, uint64_t* bar) {
   asm volatile(
       "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
@@ -119,6 +128,8 @@ struct TcArgs {
   int vec4;         // out rows start on 16-byte boundaries (base aligned, cols % 4 == 0)
   float* out;
   int* err;
+  const int* stall_flag;   // error-path test hook (oh_ctx_set_test_stall), null otherwise
+  long long stall_cycles;
 };
 
 __global__ void __launch_bounds__(128, 1) pls_tc_gemm(const __grid_constant__ CUtensorMap mAhi,
@@ -171,7 +182,7 @@ __global__ void __launch_bounds__(128, 1) pls_tc_gemm(const __grid_constant__ CU
     for (; it < nkb; ++it) {
       const int s = it % kStages;
       const uint32_t ph = (uint32_t)((it / kStages) & 1);
-      if (!mb_wait(&empty[s], ph ^ 1u) || *((volatile int*)abort_flag)) {
+      if (!mb_wait_live(&empty[s], ph ^ 1u, abort_flag) || *((volatile int*)abort_flag)) {
         atomicExch(abort_flag, 1);
         break;
       }
@@ -186,7 +197,12 @@ __global__ void __launch_bounds__(128, 1) pls_tc_gemm(const __grid_constant__ CU
   } else if (threadIdx.x == 32) {
     // MMA issuer
     int it = 0;
-    for (; it < nkb; ++it) {
+    bool stalled = false;
+    if (a.stall_flag && !stall_on_unset_flag(a.stall_flag, a.stall_cycles)) {
+      atomicExch(abort_flag, 1);         // nothing consumed; the drain lets issued copies land
+      stalled = true;
+    }
+    for (; it < nkb && !stalled; ++it) {
       const int s = it % kStages;
       const uint32_t ph = (uint32_t)((it / kStages) & 1);
       if (!mb_wait(&full[s], ph)) {
@@ -429,7 +445,8 @@ oh_status pls_tensor_enqueue(oh_ctx* ctx, const PlsGeom& g, const PlsPt* pts, in
     OH_TRY(make_map(&mBhi, bhi, kpad, npad, kBN));
     OH_TRY(make_map(&mBlo, blo, kpad, npad, kBN));
     const int vec4 = ((reinterpret_cast<uintptr_t>(out) & 15) == 0 && ((2 * g.nx) & 3) == 0) ? 1 : 0;
-    TcArgs a{kb_total, splits, g.mode, g.ny, 2 * g.nx, atomic ? 1 : 0, vec4, static_cast<float*>(out), err};
+    TcArgs a{kb_total, splits, g.mode, g.ny, 2 * g.nx, atomic ? 1 : 0, vec4, static_cast<float*>(out), err,
+             (ctx->stall_mask & kStallPointSumGemm) ? ctx->dev_err + 1 : nullptr, ctx->stall_cycles};
     KernelTimer kt(ctx, "pls_tc_gemm", st);
     pls_tc_gemm<<<dim3(npad / kBN, mpad / kBM, splits), 128, kSmemBytes, st>>>(mAhi, mAlo, mBhi, mBlo, a);
     OH_LAUNCH_CHECK();

@@ -19,7 +19,8 @@ struct ConvArgs {
   __nv_bfloat16* out;
   int out_cs;
   int* err;
-  long long wait_limit;
+  const int* stall_flag;           // error-path test hook (oh_ctx_set_test_stall), null otherwise
+  long long stall_cycles;
 };
 
 // Device-side arguments of conv_wgrad_tc.
@@ -28,7 +29,8 @@ struct WgArgs {
   int bx, by, tiles_x, tiles_y;
   float* dwt;                      // [taps*cin][cout], accumulated
   int* err;
-  long long wait_limit;
+  const int* stall_flag;           // error-path test hook, null otherwise
+  long long stall_cycles;
 };
 
 // One convolution (forward, or input gradient with sign = -1 and the
@@ -43,7 +45,6 @@ struct ConvDesc {
   int relu;
   const void* mask; int mask_cs;
   void* out; int out_cs;
-  long long wait_limit;            // 0: about one second
 };
 
 // Weight gradient dW^T[taps*cin][cout] += X (tap-shifted) ^T dZ over all pixels.
@@ -52,7 +53,6 @@ struct WgradDesc {
   const void* x; int x_cs;
   const void* dz; int dz_cs;
   float* dwt;
-  long long wait_limit;
 };
 
 oh_status tc_arch_check();

@@ -24,8 +24,11 @@
 // Roles (128 threads): thread 0 issues TMA loads into a ring of stages,
 // thread 32 issues tcgen05.mma and releases stages with tcgen05.commit, all
 // four warps read the accumulator (warp w owns TMEM lanes 32w..32w+31).  Every
-// mbarrier wait gives up after `wait_limit` SM clocks: the CTA then sets the
-// device error word, lets its copies and MMAs land, frees TMEM and returns.
+// mbarrier wait gives up after about one second of SM clock: the CTA then
+// sets the device error word, lets its copies and MMAs land, frees TMEM and
+// returns.  Pipeline waits (a stage's copies, a stage's release) also give
+// up as soon as the other role has aborted; the final waits for the MMAs and
+// for copies still in flight keep the full bound.
 #include <cuda_bf16.h>
 #include <algorithm>
 #include "context.h"
@@ -37,6 +40,15 @@ namespace oh {
 namespace {
 
 constexpr int kConvThreads = 128;
+constexpr long long kWaitCycles = 2000000000LL;      // ~1 s at 2 GHz
+
+__device__ __forceinline__ bool wait_live(uint64_t* b, uint32_t parity, const int* abort) {
+  const long long t0 = clock64();
+  while (!tc::mb_try(b, parity)) {
+    if (*((volatile const int*)abort) || clock64() - t0 > kWaitCycles) return false;
+  }
+  return true;
+}
 
 template <int BN> struct FwdCfg {
   static constexpr int kA = 128 * 64;                 // 128 pixels x 32 channels
@@ -89,7 +101,7 @@ __global__ void __launch_bounds__(kConvThreads) conv_fwd_tc(const __grid_constan
     for (; it < nk; ++it) {
       const int s = it % Cfg::kStages;
       const uint32_t ph = (uint32_t)((it / Cfg::kStages) & 1);
-      if (!tc::mb_wait(&empty[s], ph ^ 1u, a.wait_limit) || *((volatile int*)abort_flag)) {
+      if (!wait_live(&empty[s], ph ^ 1u, abort_flag) || *((volatile int*)abort_flag)) {
         atomicExch(abort_flag, 1);
         break;
       }
@@ -105,10 +117,15 @@ __global__ void __launch_bounds__(kConvThreads) conv_fwd_tc(const __grid_constan
   } else if (threadIdx.x == 32) {
     constexpr uint32_t idesc = tc::idesc_bf16(128, BN, 0, 0);
     int it = 0;
-    for (; it < nk; ++it) {
+    bool stalled = false;
+    if (a.stall_flag && !stall_on_unset_flag(a.stall_flag, a.stall_cycles)) {
+      atomicExch(abort_flag, 1);
+      stalled = true;
+    }
+    for (; it < nk && !stalled; ++it) {
       const int s = it % Cfg::kStages;
       const uint32_t ph = (uint32_t)((it / Cfg::kStages) & 1);
-      if (!tc::mb_wait(&full[s], ph, a.wait_limit) || *((volatile int*)abort_flag)) {
+      if (!wait_live(&full[s], ph, abort_flag) || *((volatile int*)abort_flag)) {
         atomicExch(abort_flag, 1);
         break;
       }
@@ -126,7 +143,7 @@ __global__ void __launch_bounds__(kConvThreads) conv_fwd_tc(const __grid_constan
     tc::umma_commit(done);
   }
   __syncwarp();
-  const bool ok_done = tc::mb_wait(done, 0, a.wait_limit);
+  const bool ok_done = tc::mb_wait(done, 0, kWaitCycles);
   tc::fence_after();
   const bool good = __syncthreads_and(ok_done && !*((volatile int*)abort_flag));
   if (good) {
@@ -180,7 +197,7 @@ __global__ void __launch_bounds__(kConvThreads) conv_fwd_tc(const __grid_constan
   }
   if (threadIdx.x == 0) {
     for (int it = *consumed; it < *issued; ++it)
-      tc::mb_wait(&full[it % Cfg::kStages], (uint32_t)((it / Cfg::kStages) & 1), a.wait_limit);
+      tc::mb_wait(&full[it % Cfg::kStages], (uint32_t)((it / Cfg::kStages) & 1), kWaitCycles);
   }
   tc::fence_before();
   __syncthreads();
@@ -242,7 +259,7 @@ __global__ void __launch_bounds__(kConvThreads) conv_wgrad_tc(const __grid_const
     for (; it < nk; ++it) {
       const int s = it % Cfg::kStages;
       const uint32_t ph = (uint32_t)((it / Cfg::kStages) & 1);
-      if (!tc::mb_wait(&empty[s], ph ^ 1u, a.wait_limit) || *((volatile int*)abort_flag)) {
+      if (!wait_live(&empty[s], ph ^ 1u, abort_flag) || *((volatile int*)abort_flag)) {
         atomicExch(abort_flag, 1);
         break;
       }
@@ -269,10 +286,15 @@ __global__ void __launch_bounds__(kConvThreads) conv_wgrad_tc(const __grid_const
   } else if (threadIdx.x == 32) {
     constexpr uint32_t idesc = tc::idesc_bf16(128, BN, 1, 1);
     int it = 0;
-    for (; it < nk; ++it) {
+    bool stalled = false;
+    if (a.stall_flag && !stall_on_unset_flag(a.stall_flag, a.stall_cycles)) {
+      atomicExch(abort_flag, 1);
+      stalled = true;
+    }
+    for (; it < nk && !stalled; ++it) {
       const int s = it % Cfg::kStages;
       const uint32_t ph = (uint32_t)((it / Cfg::kStages) & 1);
-      if (!tc::mb_wait(&full[s], ph, a.wait_limit) || *((volatile int*)abort_flag)) {
+      if (!wait_live(&full[s], ph, abort_flag) || *((volatile int*)abort_flag)) {
         atomicExch(abort_flag, 1);
         break;
       }
@@ -291,7 +313,7 @@ __global__ void __launch_bounds__(kConvThreads) conv_wgrad_tc(const __grid_const
     tc::umma_commit(done);
   }
   __syncwarp();
-  const bool ok_done = tc::mb_wait(done, 0, a.wait_limit);
+  const bool ok_done = tc::mb_wait(done, 0, kWaitCycles);
   tc::fence_after();
   const bool good = __syncthreads_and(ok_done && !*((volatile int*)abort_flag));
   if (good && nk > 0) {
@@ -315,7 +337,7 @@ __global__ void __launch_bounds__(kConvThreads) conv_wgrad_tc(const __grid_const
   }
   if (threadIdx.x == 0) {
     for (int it = *consumed; it < *issued; ++it)
-      tc::mb_wait(&full[it % Cfg::kStages], (uint32_t)((it / Cfg::kStages) & 1), a.wait_limit);
+      tc::mb_wait(&full[it % Cfg::kStages], (uint32_t)((it / Cfg::kStages) & 1), kWaitCycles);
   }
   tc::fence_before();
   __syncthreads();
@@ -384,7 +406,7 @@ oh_status conv_enqueue(oh_ctx* ctx, const ConvDesc& d, cudaStream_t st, const ch
   a.mask = reinterpret_cast<const __nv_bfloat16*>(d.mask); a.mask_cs = d.mask_cs;
   a.out = reinterpret_cast<__nv_bfloat16*>(d.out); a.out_cs = d.out_cs;
   a.err = ctx->dev_err;
-  a.wait_limit = d.wait_limit > 0 ? d.wait_limit : 2000000000LL;
+  if (ctx->stall_mask & kStallConvolution) { a.stall_flag = ctx->dev_err + 1; a.stall_cycles = ctx->stall_cycles; }
   const long long tiles = (long long)a.tiles_x * a.tiles_y * d.n;
   if (tiles > 0x7fffffffLL) return fail(OH_ERR_UNSUPPORTED_SIZE, "convolution: too many pixel tiles");
   // output-channel tile: the largest power of two up to 256 that divides
@@ -420,7 +442,7 @@ oh_status wgrad_enqueue(oh_ctx* ctx, const WgradDesc& d, cudaStream_t st, const 
   a.tiles_x = (d.w + a.bx - 1) / a.bx; a.tiles_y = (d.h + a.by - 1) / a.by;
   a.dwt = d.dwt;
   a.err = ctx->dev_err;
-  a.wait_limit = d.wait_limit > 0 ? d.wait_limit : 2000000000LL;
+  if (ctx->stall_mask & kStallConvolution) { a.stall_flag = ctx->dev_err + 1; a.stall_cycles = ctx->stall_cycles; }
   const int groups = d.taps * (d.cin / 32);
   const int mtiles = (groups + 3) / 4;
   const long long kb_total = (long long)a.tiles_x * a.tiles_y * d.n;
