@@ -22,6 +22,7 @@
 #include <cuda_bf16.h>
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -35,8 +36,20 @@ namespace {
 constexpr int kLevels = 4;
 constexpr int kInCh = 4, kOutCh = 2, kInPad = 32;
 
+// per-layer kernel-timer names (OH_UNET_LAYER_TIMING=1 at creation)
+constexpr const char* kLayerTimerNames[3][15] = {
+    {"fwd_enc0a", "fwd_enc0b", "fwd_enc1a", "fwd_enc1b", "fwd_enc2a", "fwd_enc2b", "fwd_enc3a", "fwd_enc3b",
+     "fwd_dec2a", "fwd_dec2b", "fwd_dec1a", "fwd_dec1b", "fwd_dec0a", "fwd_dec0b", "fwd_head"},
+    {"dgrad_enc0a", "dgrad_enc0b", "dgrad_enc1a", "dgrad_enc1b", "dgrad_enc2a", "dgrad_enc2b", "dgrad_enc3a",
+     "dgrad_enc3b", "dgrad_dec2a", "dgrad_dec2b", "dgrad_dec1a", "dgrad_dec1b", "dgrad_dec0a", "dgrad_dec0b",
+     "dgrad_head"},
+    {"wgrad_enc0a", "wgrad_enc0b", "wgrad_enc1a", "wgrad_enc1b", "wgrad_enc2a", "wgrad_enc2b", "wgrad_enc3a",
+     "wgrad_enc3b", "wgrad_dec2a", "wgrad_dec2b", "wgrad_dec1a", "wgrad_dec1b", "wgrad_dec0a", "wgrad_dec0b",
+     "wgrad_head"}};
+
 struct Layer {
   int cin, cin_pad, cout, taps;
+  const char* tn[3] = {"unet_conv_fwd", "unet_conv_dgrad", "unet_conv_wgrad"};   // timer names
   size_t off_w, off_b;            // offsets in the flat FP32 parameter array
   float* dwt;                     // [taps*cin_pad][cout]
   float* db;                      // [cout]
@@ -435,7 +448,7 @@ oh_status unet_forward(oh_unet* u, const uint8_t* rgbd, int n, int h, int w, flo
     d.taps = L.taps; d.sign = 1; d.n = n; d.h = hl; d.w = wl; d.cin = L.cin_pad; d.cout = L.cout;
     d.x = x; d.x_cs = x_cs; d.w_mat = L.wf; d.bias = u->P + L.off_b; d.relu = 1;
     d.out = y; d.out_cs = y_cs;
-    return conv_enqueue(ctx, d, st, "unet_conv_fwd");
+    return conv_enqueue(ctx, d, st, L.tn[0]);
   };
   // encoder
   const void* xin = u->in0;
@@ -499,7 +512,7 @@ oh_status unet_backward(oh_unet* u, const float2* target, int n, int h, int w, c
     WgradDesc d{};
     d.taps = L.taps; d.n = n; d.h = hl; d.w = wl; d.cin = L.cin_pad; d.cout = L.cout;
     d.x = x; d.x_cs = x_cs; d.dz = dz; d.dz_cs = L.cout; d.dwt = L.dwt;
-    OH_TRY(wgrad_enqueue(ctx, d, st, "unet_conv_wgrad"));
+    OH_TRY(wgrad_enqueue(ctx, d, st, L.tn[2]));
     KernelTimer kt(ctx, "unet_bias_grad", st);
     const long long np = (long long)n * hl * wl;
     unet_bias_grad<<<grid_for(np * L.cout), 256, 0, st>>>(
@@ -513,7 +526,7 @@ oh_status unet_backward(oh_unet* u, const float2* target, int n, int h, int w, c
     d.taps = L.taps; d.sign = -1; d.n = n; d.h = hl; d.w = wl; d.cin = L.cout; d.cout = L.cin_pad;
     d.x = dz; d.x_cs = L.cout; d.w_mat = L.wd; d.bias = nullptr; d.relu = 0; d.mask = mask; d.mask_cs = mask_cs;
     d.out = out; d.out_cs = out_cs;
-    return conv_enqueue(ctx, d, st, "unet_conv_dgrad");
+    return conv_enqueue(ctx, d, st, L.tn[1]);
   };
   // decoder, top level first: dZ1 holds the gradient of dec{l}b's pre-activation
   for (int l = 0; l < kLevels - 1; ++l) {
@@ -624,6 +637,12 @@ oh_status oh_unet_create(oh_ctx* ctx, const oh_unet_config* cfg, oh_unet** out) 
   for (int l = 0; l < kLevels; ++l) { add(cprev, u->chans[l], 9); add(u->chans[l], u->chans[l], 9); cprev = u->chans[l]; }
   for (int l = kLevels - 2; l >= 0; --l) { add(u->chans[l] + u->chans[l + 1], u->chans[l], 9); add(u->chans[l], u->chans[l], 9); }
   add(u->chans[0], kOutCh, 1);
+  {
+    const char* ev = std::getenv("OH_UNET_LAYER_TIMING");
+    if (ev && std::atoi(ev) != 0)
+      for (size_t i = 0; i < u->layers.size(); ++i)
+        for (int k = 0; k < 3; ++k) u->layers[i].tn[k] = kLayerTimerNames[k][i];
+  }
   oh_status rc = OH_OK;
   auto cleanup = [&]() {
     for (void* p : u->allocs) cudaFree(p);

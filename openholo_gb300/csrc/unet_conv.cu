@@ -50,42 +50,54 @@ __device__ __forceinline__ bool wait_live(uint64_t* b, uint32_t parity, const in
   return true;
 }
 
+constexpr int pow2_at_least(int n) { return n <= 32 ? 32 : n <= 64 ? 64 : n <= 128 ? 128 : n <= 256 ? 256 : 512; }
+
 template <int BN> struct FwdCfg {
   static constexpr int kA = 128 * 64;                 // 128 pixels x 32 channels
   static constexpr int kB = BN * 64;                  // BN rows x 32 K
   static constexpr int kStage = kA + kB;
-  static constexpr int kStages = BN >= 256 ? 4 : BN >= 128 ? 6 : 8;
-  static constexpr int kTmem = BN < 32 ? 32 : BN;
+  static constexpr int kStages = BN >= 192 ? 5 : 6;
+  static constexpr int kTmemBuf = pow2_at_least(BN);  // columns of one accumulator
+  static constexpr int kTmem = 2 * kTmemBuf;          // two accumulators: MMA and epilogue overlap
+  static constexpr int kThreads = 192;                // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
   static constexpr int kSmem = kStages * kStage + 1024 + 256;
 };
 
+// Persistent CTAs: CTA i takes pixel tiles i, i + gridDim.x, ... of output
+// channel tile blockIdx.y.  The TMA producer streams the K steps of all its
+// tiles through one ring of stages; the MMA issuer accumulates tile j into
+// TMEM buffer j & 1 and commits it to the epilogue warps, which drain it
+// (bias, ReLU, mask, BF16 store) while the next tile accumulates in the
+// other buffer.
 template <int BN>
-__global__ void __launch_bounds__(kConvThreads) conv_fwd_tc(const __grid_constant__ CUtensorMap mX,
-                                                            const __grid_constant__ CUtensorMap mW, ConvArgs a) {
+__global__ void __launch_bounds__(FwdCfg<BN>::kThreads) conv_fwd_tc(const __grid_constant__ CUtensorMap mX,
+                                                                    const __grid_constant__ CUtensorMap mW,
+                                                                    ConvArgs a) {
   typedef FwdCfg<BN> Cfg;
   extern __shared__ unsigned char smem_raw[];
   const uint32_t raw = tc::su32(smem_raw);
   unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
   uint64_t* full = reinterpret_cast<uint64_t*>(base + Cfg::kStages * Cfg::kStage);
   uint64_t* empty = full + Cfg::kStages;
-  uint64_t* done = empty + Cfg::kStages;
+  uint64_t* tfull = empty + Cfg::kStages;              // [2] accumulator ready (MMA commit)
+  uint64_t* tempty = tfull + 2;                        // [2] accumulator drained (4 epilogue warps)
+  uint64_t* done = tempty + 2;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
   int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
   int* issued = abort_flag + 1;
   int* consumed = abort_flag + 2;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-  int t = blockIdx.x;
-  const int tx = t % a.tiles_x; t /= a.tiles_x;
-  const int ty = t % a.tiles_y;
-  const int img = t / a.tiles_y;
-  const int x0 = tx * a.bx, y0 = ty * a.by;
+  const long long tiles = (long long)a.n * a.tiles_y * a.tiles_x;
+  const int ntl = blockIdx.x < tiles ? (int)((tiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
   const int co0 = blockIdx.y * BN;
   const int cchunks = a.cin >> 5;
   const int nk = a.taps * cchunks;
+  const long long nsteps = (long long)ntl * nk;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < Cfg::kStages; ++s) { tc::mb_init(&full[s], 1); tc::mb_init(&empty[s], 1); }
+    for (int b = 0; b < 2; ++b) { tc::mb_init(&tfull[b], 1); tc::mb_init(&tempty[b], 4); }
     tc::mb_init(done, 1);
     *abort_flag = 0; *issued = 0; *consumed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -96,108 +108,151 @@ __global__ void __launch_bounds__(kConvThreads) conv_fwd_tc(const __grid_constan
   tc::fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (threadIdx.x == 0) {
-    int it = 0;
-    for (; it < nk; ++it) {
-      const int s = it % Cfg::kStages;
-      const uint32_t ph = (uint32_t)((it / Cfg::kStages) & 1);
-      if (!wait_live(&empty[s], ph ^ 1u, abort_flag) || *((volatile int*)abort_flag)) {
-        atomicExch(abort_flag, 1);
-        break;
-      }
-      const int tap = it / cchunks, cc = it - tap * cchunks;
-      int dx = 0, dy = 0;
-      if (a.taps == 9) { dx = (tap % 3 - 1) * a.sign; dy = (tap / 3 - 1) * a.sign; }
-      unsigned char* st = base + s * Cfg::kStage;
-      tc::mb_expect_tx(&full[s], (uint32_t)Cfg::kStage);
-      tc::tma_load_4d(st, &mX, cc * 32, x0 + dx, y0 + dy, img, &full[s]);
-      tc::tma_load_2d(st + Cfg::kA, &mW, tap * a.cin + cc * 32, co0, &full[s]);
-    }
-    *issued = it;
-  } else if (threadIdx.x == 32) {
-    constexpr uint32_t idesc = tc::idesc_bf16(128, BN, 0, 0);
-    int it = 0;
-    bool stalled = false;
-    if (a.stall_flag && !stall_on_unset_flag(a.stall_flag, a.stall_cycles)) {
-      atomicExch(abort_flag, 1);
-      stalled = true;
-    }
-    for (; it < nk && !stalled; ++it) {
-      const int s = it % Cfg::kStages;
-      const uint32_t ph = (uint32_t)((it / Cfg::kStages) & 1);
-      if (!wait_live(&full[s], ph, abort_flag) || *((volatile int*)abort_flag)) {
-        atomicExch(abort_flag, 1);
-        break;
-      }
-      tc::fence_after();
-      const uint32_t sa = tc::su32(base + s * Cfg::kStage);
-      const uint64_t da = tc::desc_sw64(sa, 16, 512), db = tc::desc_sw64(sa + Cfg::kA, 16, 512);
-#pragma unroll
-      for (int kk = 0; kk < 2; ++kk) {
-        const uint64_t adv = (uint64_t)((kk * 32) >> 4);      // 16 BF16 = 32 bytes along K
-        tc::umma_bf16(tmem, da + adv, db + adv, idesc, (it | kk) ? 1u : 0u);
-      }
-      tc::umma_commit(&empty[s]);
-    }
-    *consumed = it;
-    tc::umma_commit(done);
-  }
-  __syncwarp();
-  const bool ok_done = tc::mb_wait(done, 0, kWaitCycles);
-  tc::fence_after();
-  const bool good = __syncthreads_and(ok_done && !*((volatile int*)abort_flag));
-  if (good) {
-    const int m = warp * 32 + lane;
-    const int px = x0 + (m % a.bx), py = y0 + (m / a.bx);
-    const bool inside = px < a.w && py < a.h;
-    const size_t pix = ((size_t)img * a.h + py) * a.w + px;
-#pragma unroll 1
-    for (int c = 0; c < BN / 32; ++c) {
-      uint32_t r[32];
-      tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), r);
-      const int cb = co0 + c * 32;
-      if (!inside || cb >= a.cout) continue;
-      float v[32];
-#pragma unroll
-      for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
-      if (a.bias) {
-#pragma unroll
-        for (int q = 0; q < 32; ++q) v[q] += __ldg(a.bias + cb + q);
-      }
-      if (a.relu) {
-#pragma unroll
-        for (int q = 0; q < 32; ++q) v[q] = fmaxf(v[q], 0.f);
-      }
-      if (a.mask) {
-        const uint4* mp = reinterpret_cast<const uint4*>(a.mask + pix * a.mask_cs + cb);
-#pragma unroll
-        for (int g = 0; g < 4; ++g) {
-          const uint4 mv = __ldg(mp + g);
-          const __nv_bfloat162* mb = reinterpret_cast<const __nv_bfloat162*>(&mv);
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const float2 f = __bfloat1622float2(mb[e]);
-            if (!(f.x > 0.f)) v[g * 8 + 2 * e] = 0.f;
-            if (!(f.y > 0.f)) v[g * 8 + 2 * e + 1] = 0.f;
+  auto tile_origin = [&](int j, int* img, int* x0, int* y0) {
+    long long t = blockIdx.x + (long long)j * gridDim.x;
+    const int tx = (int)(t % a.tiles_x); t /= a.tiles_x;
+    const int ty = (int)(t % a.tiles_y);
+    *img = (int)(t / a.tiles_y);
+    *x0 = tx * a.bx; *y0 = ty * a.by;
+  };
+
+  if (warp == 0) {
+    if (lane == 0) {
+      long long g = 0;
+      for (int j = 0; j < ntl && g >= 0; ++j) {
+        int img, x0, y0;
+        tile_origin(j, &img, &x0, &y0);
+        for (int it = 0; it < nk; ++it, ++g) {
+          const int s = (int)(g % Cfg::kStages);
+          const uint32_t ph = (uint32_t)((g / Cfg::kStages) & 1);
+          if (!wait_live(&empty[s], ph ^ 1u, abort_flag) || *((volatile int*)abort_flag)) {
+            atomicExch(abort_flag, 1);
+            *issued = (int)g;
+            g = -1;
+            break;
           }
+          const int tap = it / cchunks, cc = it - tap * cchunks;
+          int dx = 0, dy = 0;
+          if (a.taps == 9) { dx = (tap % 3 - 1) * a.sign; dy = (tap / 3 - 1) * a.sign; }
+          unsigned char* st = base + s * Cfg::kStage;
+          tc::mb_expect_tx(&full[s], (uint32_t)Cfg::kStage);
+          tc::tma_load_4d(st, &mX, cc * 32, x0 + dx, y0 + dy, img, &full[s]);
+          tc::tma_load_2d(st + Cfg::kA, &mW, tap * a.cin + cc * 32, co0, &full[s]);
         }
       }
-      uint4* op = reinterpret_cast<uint4*>(a.out + pix * a.out_cs + cb);
-#pragma unroll
-      for (int g = 0; g < 4; ++g) {
-        uint4 o;
-        __nv_bfloat162* ob = reinterpret_cast<__nv_bfloat162*>(&o);
-#pragma unroll
-        for (int e = 0; e < 4; ++e) ob[e] = __floats2bfloat162_rn(v[g * 8 + 2 * e], v[g * 8 + 2 * e + 1]);
-        op[g] = o;
-      }
+      if (g >= 0) *issued = (int)nsteps;
     }
-  } else if (threadIdx.x == 0) {
-    atomicOr(a.err, 2);
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = tc::idesc_bf16(128, BN, 0, 0);
+      long long g = 0;
+      bool stop = false;
+      if (a.stall_flag && !stall_on_unset_flag(a.stall_flag, a.stall_cycles)) {
+        atomicExch(abort_flag, 1);
+        stop = true;
+      }
+      for (int j = 0; j < ntl && !stop; ++j) {
+        const int b = j & 1;
+        if (!wait_live(&tempty[b], (uint32_t)(((j >> 1) & 1) ^ 1), abort_flag)) {
+          atomicExch(abort_flag, 1);
+          break;
+        }
+        tc::fence_after();
+        const uint32_t acc = tmem + (uint32_t)(b * Cfg::kTmemBuf);
+        for (int it = 0; it < nk; ++it, ++g) {
+          const int s = (int)(g % Cfg::kStages);
+          const uint32_t ph = (uint32_t)((g / Cfg::kStages) & 1);
+          if (!wait_live(&full[s], ph, abort_flag) || *((volatile int*)abort_flag)) {
+            atomicExch(abort_flag, 1);
+            stop = true;
+            break;
+          }
+          tc::fence_after();
+          const uint32_t sa = tc::su32(base + s * Cfg::kStage);
+          const uint64_t da = tc::desc_sw64(sa, 16, 512), db = tc::desc_sw64(sa + Cfg::kA, 16, 512);
+#pragma unroll
+          for (int kk = 0; kk < 2; ++kk) {
+            const uint64_t adv = (uint64_t)((kk * 32) >> 4);      // 16 BF16 = 32 bytes along K
+            tc::umma_bf16(acc, da + adv, db + adv, idesc, (it | kk) ? 1u : 0u);
+          }
+          tc::umma_commit(&empty[s]);
+        }
+        if (!stop) tc::umma_commit(&tfull[b]);
+      }
+      *consumed = (int)g;
+      tc::umma_commit(done);                             // arrives when every MMA issued above has completed
+    }
+  } else {
+    // epilogue warps 2-5: TMEM lane quarter (warp % 4) = pixels 32 (warp % 4) .. + 31 of the tile
+    const int q = warp & 3;
+    const int m = q * 32 + lane;
+    for (int j = 0; j < ntl; ++j) {
+      const int b = j & 1;
+      bool ok = true;
+      if (lane == 0) ok = wait_live(&tfull[b], (uint32_t)((j >> 1) & 1), abort_flag);
+      ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+      if (!ok) break;
+      tc::fence_after();
+      int img, x0, y0;
+      tile_origin(j, &img, &x0, &y0);
+      const int px = x0 + (m % a.bx), py = y0 + (m / a.bx);
+      const bool inside = px < a.w && py < a.h;
+      const size_t pix = ((size_t)img * a.h + py) * a.w + px;
+#pragma unroll 1
+      for (int c = 0; c < BN / 32; ++c) {
+        uint32_t r[32];
+        tc::tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * Cfg::kTmemBuf + c * 32), r);
+        const int cb = co0 + c * 32;
+        if (!inside || cb >= a.cout) continue;
+        float v[32];
+#pragma unroll
+        for (int e = 0; e < 32; ++e) v[e] = __uint_as_float(r[e]);
+        if (a.bias) {
+#pragma unroll
+          for (int e = 0; e < 32; ++e) v[e] += __ldg(a.bias + cb + e);
+        }
+        if (a.relu) {
+#pragma unroll
+          for (int e = 0; e < 32; ++e) v[e] = fmaxf(v[e], 0.f);
+        }
+        if (a.mask) {
+          const uint4* mp = reinterpret_cast<const uint4*>(a.mask + pix * a.mask_cs + cb);
+#pragma unroll
+          for (int g4 = 0; g4 < 4; ++g4) {
+            const uint4 mv = __ldg(mp + g4);
+            const __nv_bfloat162* mb = reinterpret_cast<const __nv_bfloat162*>(&mv);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const float2 f = __bfloat1622float2(mb[e]);
+              if (!(f.x > 0.f)) v[g4 * 8 + 2 * e] = 0.f;
+              if (!(f.y > 0.f)) v[g4 * 8 + 2 * e + 1] = 0.f;
+            }
+          }
+        }
+        uint4* op = reinterpret_cast<uint4*>(a.out + pix * a.out_cs + cb);
+#pragma unroll
+        for (int g4 = 0; g4 < 4; ++g4) {
+          uint4 o;
+          __nv_bfloat162* ob = reinterpret_cast<__nv_bfloat162*>(&o);
+#pragma unroll
+          for (int e = 0; e < 4; ++e) ob[e] = __floats2bfloat162_rn(v[g4 * 8 + 2 * e], v[g4 * 8 + 2 * e + 1]);
+          op[g4] = o;
+        }
+      }
+      tc::fence_before();
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::su32(&tempty[b])) : "memory");
+    }
   }
+  __syncwarp();
+  // every MMA issued has completed before TMEM is freed; copies issued but
+  // not consumed land before the CTA exits
+  if (threadIdx.x == 0) tc::mb_wait(done, 0, kWaitCycles);
+  __syncthreads();
   if (threadIdx.x == 0) {
-    for (int it = *consumed; it < *issued; ++it)
-      tc::mb_wait(&full[it % Cfg::kStages], (uint32_t)((it / Cfg::kStages) & 1), kWaitCycles);
+    if (*((volatile int*)abort_flag)) atomicOr(a.err, 2);
+    for (int g = *consumed; g < *issued; ++g)
+      tc::mb_wait(&full[g % Cfg::kStages], (uint32_t)((g / Cfg::kStages) & 1), kWaitCycles);
   }
   tc::fence_before();
   __syncthreads();
@@ -357,10 +412,18 @@ bool patch_shape(int w, int pixels, int* bx, int* by) {
 }
 
 template <int BN>
-oh_status launch_fwd(const CUtensorMap& mX, const CUtensorMap& mW, const ConvArgs& a, int tiles, cudaStream_t st) {
+oh_status launch_fwd(const CUtensorMap& mX, const CUtensorMap& mW, const ConvArgs& a, long long tiles, cudaStream_t st) {
   typedef FwdCfg<BN> Cfg;
   OH_CUDA_TRY(cudaFuncSetAttribute(conv_fwd_tc<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmem));
-  conv_fwd_tc<BN><<<dim3(tiles, (a.cout + BN - 1) / BN), kConvThreads, Cfg::kSmem, st>>>(mX, mW, a);
+  // persistent grid: the CTAs that fit on an SM by shared memory and tensor
+  // memory (512 columns), at most four, times the SMs, spread over the
+  // output-channel tiles
+  const int by_smem = (int)((228 * 1024) / (Cfg::kSmem + 1024));
+  const int per_sm = std::max(1, std::min(4, std::min(by_smem, 512 / Cfg::kTmem)));
+  const int ctiles = (a.cout + BN - 1) / BN;
+  const long long want = std::max(1LL, (long long)sm_count() * per_sm / ctiles);
+  const int gx = (int)std::min(tiles, want);
+  conv_fwd_tc<BN><<<dim3(gx, ctiles), Cfg::kThreads, Cfg::kSmem, st>>>(mX, mW, a);
   OH_LAUNCH_CHECK();
   return OH_OK;
 }
@@ -409,20 +472,25 @@ oh_status conv_enqueue(oh_ctx* ctx, const ConvDesc& d, cudaStream_t st, const ch
   if (ctx->stall_mask & kStallConvolution) { a.stall_flag = ctx->dev_err + 1; a.stall_cycles = ctx->stall_cycles; }
   const long long tiles = (long long)a.tiles_x * a.tiles_y * d.n;
   if (tiles > 0x7fffffffLL) return fail(OH_ERR_UNSUPPORTED_SIZE, "convolution: too many pixel tiles");
-  // output-channel tile: the largest power of two up to 256 that divides
-  // cout, halved while the grid is under two waves
-  int bn = 256;
-  while (d.cout % bn) bn /= 2;
-  while (bn > 32 && tiles * ((d.cout + bn - 1) / bn) < 2LL * sm_count()) bn /= 2;
+  // output-channel tile: all of cout up to 256 (384 as two halves), else the
+  // largest of 256, 192, 128, 96, 64, 32 that divides it; halved while the
+  // pixel tiles alone cannot fill two CTAs per SM
+  int bn = 32;
+  for (int c : {256, 192, 128, 96, 64})
+    if (d.cout % c == 0) { bn = c; break; }
+  while ((bn == 256 || bn == 128 || bn == 64 || bn == 192) && tiles * ((d.cout + bn - 1) / bn) < 2LL * sm_count())
+    bn /= 2;
   CUtensorMap mX, mW;
   OH_TRY(tc::map_act4d(&mX, d.x, d.cin, d.x_cs, d.w, d.h, d.n, a.bx, a.by));
   OH_TRY(tc::map_mat2d(&mW, d.w_mat, d.taps * d.cin, d.cout, bn));
   KernelTimer kt(ctx, timer_name, st);
   switch (bn) {
-    case 32: return launch_fwd<32>(mX, mW, a, (int)tiles, st);
-    case 64: return launch_fwd<64>(mX, mW, a, (int)tiles, st);
-    case 128: return launch_fwd<128>(mX, mW, a, (int)tiles, st);
-    default: return launch_fwd<256>(mX, mW, a, (int)tiles, st);
+    case 32: return launch_fwd<32>(mX, mW, a, tiles, st);
+    case 64: return launch_fwd<64>(mX, mW, a, tiles, st);
+    case 96: return launch_fwd<96>(mX, mW, a, tiles, st);
+    case 128: return launch_fwd<128>(mX, mW, a, tiles, st);
+    case 192: return launch_fwd<192>(mX, mW, a, tiles, st);
+    default: return launch_fwd<256>(mX, mW, a, tiles, st);
   }
 }
 
