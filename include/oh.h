@@ -80,6 +80,14 @@ const char* oh_version(void);
  * by the FMA rate at four warp instructions per SM per clock.  Synchronous. */
 oh_status   oh_measure_issue_peaks(int device, double* ffma_per_s, double* ffma2_per_s,
                                    double* mufu_per_s, double* sm_mhz_hint);
+/* Upper bound on the depth-map layer buffer (the row pass's strips of every
+ * depth layer, pny * 2 pnx * 8 bytes per layer at pad 2 in FP32): frames whose
+ * layers would exceed it run the row and column passes in chunks of layers,
+ * handing the spectrum accumulators on between chunks (FP32 frames with
+ * compile-time column lengths and the default render list; others keep one
+ * buffer for all layers).  Results are the same either way.  0 restores
+ * the default of 2 GiB. */
+oh_status   oh_ctx_set_depthmap_layer_limit(oh_ctx* ctx, size_t bytes);
 /* Error-path test hook (no reference counterpart).  While set, the kernels
  * selected by kernel_mask (1: depth-map column pass, 2: point-sum tensor-core
  * GEMM, 4: tensor-core convolutions) first wait on a device flag that nothing

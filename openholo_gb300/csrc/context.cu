@@ -325,6 +325,13 @@ oh_status oh_ctx_device_status(oh_ctx* ctx, void* stream) {
   return OH_OK;
 }
 
+oh_status oh_ctx_set_depthmap_layer_limit(oh_ctx* ctx, size_t bytes) {
+  if (!ctx) return fail(OH_ERR_INVALID_ARG, "null context");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->dm_layer_limit = bytes ? bytes : (size_t)2 << 30;
+  return OH_OK;
+}
+
 oh_status oh_ctx_set_test_stall(oh_ctx* ctx, int kernel_mask, long long cycles) {
   if (!ctx) return fail(OH_ERR_INVALID_ARG, "null context");
   if (kernel_mask < 0 || cycles < 0 || cycles > 4000000000LL)

@@ -18,6 +18,9 @@ struct oh_ctx {
   int* dev_err = nullptr;             // [0]: set by kernels whose bounded waits ran out; [1]: a flag nothing sets
   // error-path test hook (oh_ctx_set_test_stall): kernels in stall_mask wait
   // on dev_err[1] for at most stall_cycles SM clocks before their first stage
+  // depth-map layer buffer (row-pass strips of every layer slot): frames
+  // whose strips would exceed this run in layer chunks (fast FP32 path)
+  size_t dm_layer_limit = (size_t)2 << 30;
   int stall_mask = 0;
   long long stall_cycles = 0;
   std::string dm_setup_key;           // parameters of the depth-map tables now in scratch

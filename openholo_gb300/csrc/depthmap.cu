@@ -87,6 +87,13 @@ struct DMArgs {
   int* err;              // device error word (bounded waits that ran out)
   const int* stall_flag; // error-path test hook: wait on this never-set flag before the first layer
   long long stall_cycles;
+  // layer chunks (fast FP32 path): this launch pair covers layer slots (and
+  // render entries) [slot0, slot1); R and occ hold only those slots; the
+  // column pass's accumulators pass between chunks through accbuf
+  int slot0, slot1;
+  int e0, e1;            // render entries of this chunk (all entries when unchunked)
+  int chunk_first, chunk_last;
+  C* accbuf;
   // evenly spaced layers (fast column pass): step dz = z'_e - z'_(e-1) of the
   // render entries; D = Dx(fx) Dy(fy) exp(-i k dz g) per spectrum element
   int horner;
@@ -378,12 +385,13 @@ __global__ void __launch_bounds__(512, row_min_blocks<NX>()) dm_row_pass(DMArgs<
     }
   }
   __syncthreads();
-  for (int u = 0; u < a.n_uslots; ++u) {
+  for (int u = a.slot0; u < a.slot1; ++u) {
     const bool p0 = (mask[u >> 5] >> (u & 31)) & 1u;
     const bool p1 = (mask[8 + (u >> 5)] >> (u & 31)) & 1u;
+    const int ur = u - a.slot0;                       // slot within this chunk's buffers
     if (threadIdx.x < nrows) {
       const bool pr = threadIdx.x == 0 ? p0 : p1;
-      a.occ[(size_t)u * a.occ_stride + r0 + threadIdx.x] = pr ? 1 : 0;
+      a.occ[(size_t)ur * a.occ_stride + r0 + threadIdx.x] = pr ? 1 : 0;
     }
     if (!(p0 || p1)) continue;
     if (threadIdx.x == 0) a.slot_any[u] = 1;
@@ -450,7 +458,7 @@ __global__ void __launch_bounds__(512, row_min_blocks<NX>()) dm_row_pass(DMArgs<
 #pragma unroll
             for (int t = 0; t < RL; ++t) x[t] = src[t];
             DFT<RL, -1, C>::run(x);
-            float4* d4 = reinterpret_cast<float4*>(a.Rbuf + (size_t)u * a.nstrips * a.pny * 2);
+            float4* d4 = reinterpret_cast<float4*>(a.Rbuf + (size_t)ur * a.nstrips * a.pny * 2);
             const size_t rowoff = (size_t)r0 + l;
             if constexpr (RL % 2 == 0) {
 #pragma unroll
@@ -496,7 +504,7 @@ __global__ void __launch_bounds__(512, row_min_blocks<NX>()) dm_row_pass(DMArgs<
     }
     // store: strip s holds rows r0, r0+1 contiguously -> 2*W values per strip
     // (W is a power of two: index split with shifts)
-    C* dst = a.Rbuf + (size_t)u * a.nstrips * a.pny * a.W;
+    C* dst = a.Rbuf + (size_t)ur * a.nstrips * a.pny * a.W;
     const int W = a.W, lw = a.lw;
     if (sizeof(R) == 4 && W == 2 && nrows == 2 && a.xs) {
       // FP32, strips of two columns, FFT storage order: a thread pair moves
@@ -767,7 +775,7 @@ static oh_status validate(const oh_depthmap_params* p) {
 }
 
 // Scratch bytes one frame needs: R strips, V rows, occupancy flags, tables.
-struct DMScratch { size_t R, V, occ, tables; };
+struct DMScratch { size_t R, V, occ, tables, acc; };
 
 // Enqueues one frame.  With sizes_only set, computes the frame's scratch
 // needs into it and returns without allocating or launching anything.
@@ -832,6 +840,8 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   a.ox = (a.Px - a.pnx) / 2; a.oy = (a.Py - a.pny) / 2;
   a.hx = a.Px / 2; a.hy = a.Py / 2;
   a.n_entries = su.n_entries; a.n_uslots = su.n_uslots;
+  a.slot0 = 0; a.slot1 = su.n_uslots; a.e0 = 0; a.e1 = su.n_entries;
+  a.chunk_first = 1; a.chunk_last = 1; a.accbuf = nullptr;
   a.ppx = p->ppx; a.ppy = p->ppy;
   a.ssx = p->ppx * a.Px; a.ssy = p->ppy * a.Py;
   a.lambda = p->lambda; a.k = 2.0 * M_PI / p->lambda;
@@ -932,6 +942,19 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   a.hzy = (p->pad == 2 && r0y == 16 && (a.Py % 16) == 0 && a.oy * 4 == a.Py && a.hy * 2 == a.Py) ? 1 : 0;
   // fast column pass: one-column blocks over the two-column strips where
   // that turns one block per SM into two
+  // layer chunks: when the strips of every layer slot would exceed the
+  // context's layer-buffer limit, the fast FP32 path runs the row and column
+  // passes per chunk of slots, the column pass handing its accumulators on
+  // through a buffer of one spectrum (slots must map one to one onto render
+  // entries, as with the default render list)
+  const size_t per_slot = (size_t)a.pny * a.Px * sizeof(C);
+  const size_t nU_ = su.n_uslots, nE_ = su.n_entries;
+  size_t lc = nU_;
+  bool identity = nU_ == nE_;
+  for (size_t e = 0; e < nE_ && identity; ++e) identity = su.uslot_of_entry[e] == (int16_t)e;
+  if (Wfast && identity && nU_ > 1 && nU_ * per_slot > ctx->dm_layer_limit)
+    lc = std::max<size_t>(1, ctx->dm_layer_limit / per_slot);
+  const int nchunks = (int)((nU_ + lc - 1) / lc);
   int wcol = Wfast;
   if (Wfast) {
     bool narrow = false;
@@ -944,7 +967,9 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
                   1024) <= (size_t)228 * 1024;
     };
     const char* ev = std::getenv("OH_DM_COL_NARROW");
-    if (narrow && !(ev && std::atoi(ev) == 0) && !two_fit(2) && two_fit(1)) wcol = 1;
+    // the extended kernel (layer chunks, test hook) takes whole strips
+    const bool ext_mode = (ctx->stall_mask & kStallDepthmapColumn) != 0 || nchunks > 1;
+    if (narrow && !(ev && std::atoi(ev) == 0) && !ext_mode && !two_fit(2) && two_fit(1)) wcol = 1;
   }
   const size_t smem_col =
       Wfast ? (size_t)col_layout(col_py, a.pny, wcol, kColStripW, a.horner != 0, occ_stride, su.n_entries, col_tab).total
@@ -965,8 +990,24 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   // scratch
   void* ptr;
   const size_t nE = su.n_entries, nU = su.n_uslots;
-  const size_t bytes_R = nU * a.pny * (size_t)a.Px * sizeof(C), bytes_V = (size_t)a.pny * a.Px * sizeof(C),
-               bytes_occ = nU * (size_t)occ_stride + 16;
+  size_t bytes_acc = 0;
+  if (nchunks > 1) {
+    with_fast_n(a.Py, [&](auto nc) {
+      constexpr int NY = decltype(nc)::value;
+      if constexpr (NY > 0) {
+        const bool step = a.horner != 0;
+        const size_t blocks = wcol == 1 ? (size_t)a.Px : (size_t)a.nstrips;
+        size_t per_block;
+        if (wcol == 1) per_block = step ? (size_t)ColCfg<NY, 1, true>::T * ColCfg<NY, 1, true>::KB * ColCfg<NY, 1, true>::RL
+                                        : (size_t)ColCfg<NY, 1, false>::T * ColCfg<NY, 1, false>::KB * ColCfg<NY, 1, false>::RL;
+        else per_block = step ? (size_t)ColCfg<NY, 2, true>::T * ColCfg<NY, 2, true>::KB * ColCfg<NY, 2, true>::RL
+                              : (size_t)ColCfg<NY, 2, false>::T * ColCfg<NY, 2, false>::KB * ColCfg<NY, 2, false>::RL;
+        bytes_acc = blocks * per_block * sizeof(C);
+      }
+    });
+  }
+  const size_t bytes_R = std::min(nU, lc) * per_slot, bytes_V = (size_t)a.pny * a.Px * sizeof(C),
+               bytes_occ = std::min(nU, lc) * (size_t)occ_stride + 16;
   // small tables share one buffer
   size_t off = 0;
   auto carve = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; };
@@ -977,12 +1018,13 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
          o_shy = carve(a.pny * sizeof(C)), o_shx = carve(a.pnx * sizeof(C)), o_any = carve(nU * sizeof(int)),
          o_dxh = carve(a.horner ? a.Px * sizeof(C) : 0), o_dyh = carve(a.horner ? a.Py * sizeof(C) : 0);
   if (sizes_only) {
-    *sizes_only = DMScratch{bytes_R, bytes_V, bytes_occ, off};
+    *sizes_only = DMScratch{bytes_R, bytes_V, bytes_occ, off, bytes_acc};
     return OH_OK;
   }
   OH_TRY(scratch(ctx, "dm.R", bytes_R, &ptr)); a.Rbuf = (C*)ptr;
   OH_TRY(scratch(ctx, "dm.V", bytes_V, &ptr)); a.V = (C*)ptr;
   OH_TRY(scratch(ctx, "dm.occ", bytes_occ, &ptr)); a.occ = (uint8_t*)ptr;
+  if (bytes_acc) { OH_TRY(scratch(ctx, "dm.acc", bytes_acc, &ptr)); a.accbuf = (C*)ptr; }
   OH_TRY(scratch(ctx, "dm.tables", off, &ptr));
   char* base = (char*)ptr;
   a.lut = (int16_t*)(base + o_lut); a.uslot_of_entry = (int16_t*)(base + o_use); a.kzp = (R*)(base + o_kz);
@@ -1024,6 +1066,13 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
   }
   // the FP32 path uses the compile-time FFT schedules; FP64 the generic engine
   oh_status rs = OH_OK;
+  for (int chunk = 0; chunk < nchunks; ++chunk) {
+  a.slot0 = (int)(chunk * lc);
+  a.slot1 = (int)std::min(nU, (chunk + 1) * lc);
+  a.e0 = nchunks > 1 ? a.slot0 : 0;
+  a.e1 = nchunks > 1 ? a.slot1 : (int)nE;
+  a.chunk_first = chunk == 0;
+  a.chunk_last = chunk == nchunks - 1;
   with_fast_n_if<sizeof(R) == 4>(a.Px, [&](auto nc) {
     constexpr int NX = decltype(nc)::value;
     cudaError_t e = cudaFuncSetAttribute(dm_row_pass<R, NX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_row);
@@ -1052,6 +1101,8 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
           // the layer-step form with the SSB crop of a 2x-padded frame: the
           // output mask as a compile-time constant
           const bool ssb = a.horner && a.fkeep == col_ssb_keep<NY>();
+          // layer chunks or the test hook: the extended kernel (runtime SSB mask)
+          const bool ext = nchunks > 1 || a.stall_flag;
           bool done = false;
           if constexpr (col_narrow_ok<NY>()) {
             if (wcol == 1) {
@@ -1062,7 +1113,9 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
             }
           }
           if (!done) {
-            if (ssb) launch(dm_col_fast<NY, 2, true, true>, ColCfg<NY, 2, true>::T, a.nstrips);
+            if (ext && a.horner) launch(dm_col_fast<NY, 2, true, false, true>, ColCfg<NY, 2, true>::T, a.nstrips);
+            else if (ext) launch(dm_col_fast<NY, 2, false, false, true>, ColCfg<NY, 2, false>::T, a.nstrips);
+            else if (ssb) launch(dm_col_fast<NY, 2, true, true>, ColCfg<NY, 2, true>::T, a.nstrips);
             else if (a.horner) launch(dm_col_fast<NY, 2, true>, ColCfg<NY, 2, true>::T, a.nstrips);
             else launch(dm_col_fast<NY, 2, false>, ColCfg<NY, 2, false>::T, a.nstrips);
           }
@@ -1071,6 +1124,7 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
       OH_TRY(rs);
     }
   }
+  }   // layer chunks
   if (!Wfast) {
     cudaError_t e = cudaFuncSetAttribute(dm_col_pass<R, KMAX, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(dm_col_pass)");
@@ -1194,15 +1248,17 @@ oh_status oh_depthmap_generate_batch(oh_ctx* ctx, oh_precision prec, const oh_de
   // size the scratch once for the largest frame
   std::vector<DMScratch> sz(n);
   OH_TRY(run_all(sz.data()));
-  DMScratch mx{0, 0, 0, 0};
+  DMScratch mx{0, 0, 0, 0, 0};
   for (const DMScratch& z : sz) {
     mx.R = std::max(mx.R, z.R); mx.V = std::max(mx.V, z.V);
     mx.occ = std::max(mx.occ, z.occ); mx.tables = std::max(mx.tables, z.tables);
+    mx.acc = std::max(mx.acc, z.acc);
   }
   void* ptr;
   OH_TRY(scratch(ctx, "dm.R", mx.R, &ptr));
   OH_TRY(scratch(ctx, "dm.V", mx.V, &ptr));
   OH_TRY(scratch(ctx, "dm.occ", mx.occ, &ptr));
+  if (mx.acc) OH_TRY(scratch(ctx, "dm.acc", mx.acc, &ptr));
   OH_TRY(scratch(ctx, "dm.tables", mx.tables, &ptr));
   bool graph = (flags & OH_BATCH_GRAPH) && st != nullptr;
   if (graph) {

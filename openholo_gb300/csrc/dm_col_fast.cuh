@@ -145,7 +145,9 @@ template <int NY> constexpr uint32_t col_ssb_keep() {
 // STEP: evenly spaced layers, accumulated with the layer-step recurrence.
 // SSB: the output mask is col_ssb_keep<NY>() at compile time, so the last
 // stage's small DFT computes only the outputs that reach the crop.
-template <int NY, int W, bool STEP, bool SSB = false>
+// EXT: the layer-chunk hand-over of the accumulators and the error-path
+// test hook; the frames that need neither run the kernel without them.
+template <int NY, int W, bool STEP, bool SSB = false, bool EXT = false>
 __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::MINB) dm_col_fast(DMArgs<float> a) {
   typedef float2 C;
   typedef ColCfg<NY, W, STEP> CF;
@@ -180,9 +182,12 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
   float* lfxw = reinterpret_cast<float*>(smem + Lo.lfxw);
   __shared__ int kxw[8];          // spectrum column of each strip column
   __shared__ C dxw[8];            // its Dx factor (layer-step form)
-  int16_t* list = reinterpret_cast<int16_t*>(smem + Lo.list);
+  // active render entries of this chunk, list[0..nact); list[-1] holds the
+  // entry before the first (the previous chunk's last active one, or one less
+  // than the first), so the layer-step gap is e - list[k - 1] for every k
+  int16_t* list = reinterpret_cast<int16_t*>(smem + Lo.list) + 1;
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + Lo.mbar);  // [0] strip+flags, [1],[2] Ey
-  __shared__ int s_nact;
+  __shared__ int s_nact, s_last;
 
   const int tid = threadIdx.x;
   const int s = blockIdx.x / (SW / W);                // row-pass strip
@@ -194,10 +199,19 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
     mbar_init(&mbar[1], 1);
     mbar_init(&mbar[2], 1);
     fence_mbar_init();
-    int n = 0;
-    for (int e = 0; e < a.n_entries; ++e)
-      if (a.slot_any[a.uslot_of_entry[e]]) list[n++] = (int16_t)e;
+    // this chunk's active entries, the last active entry before it (the
+    // layer-step gap) and the last active entry of the frame (its transfer
+    // function finishes the recurrence)
+    int n = 0, prev = -1, last = -1;
+    for (int e = 0; e < a.n_entries; ++e) {
+      if (!a.slot_any[a.uslot_of_entry[e]]) continue;
+      if (e < a.e0) prev = e;
+      else if (e < a.e1) list[n++] = (int16_t)e;
+      last = e;
+    }
     s_nact = n;
+    s_last = last;
+    list[-1] = (int16_t)(prev >= 0 ? prev : (n > 0 ? list[0] - 1 : 0));
   }
   load_tw_split(twlo, twhi, static_cast<const C*>(a.ply.tw), NY);
   if constexpr (kTab > 0) fill_stage_tab<NY, R1, NY / R0, -1>(tab1, static_cast<const C*>(a.ply.tw));
@@ -218,7 +232,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
   const uint32_t strip_bytes = (uint32_t)(pny * SW * 8);
 
   auto issue_strip = [&](int k) {
-    const int u = a.uslot_of_entry[list[k]];
+    const int u = a.uslot_of_entry[list[k]] - (EXT ? a.slot0 : 0);      // slot within this chunk's buffers
     mbar_expect_tx(&mbar[0], strip_bytes + (uint32_t)a.occ_stride);
     bulk_g2s(stg, a.Rbuf + ((size_t)u * a.nstrips + s) * pny * SW, strip_bytes, &mbar[0]);
     bulk_g2s(occ, a.occ + (size_t)u * a.occ_stride, (uint32_t)a.occ_stride, &mbar[0]);
@@ -277,6 +291,27 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
   for (int kb = 0; kb < KB; ++kb)
 #pragma unroll
     for (int f = 0; f < RL; ++f) acc[kb][f] = make_float2(0.f, 0.f);
+  if (EXT && !a.chunk_first) {
+    // the accumulators of the earlier layer chunks
+    const C* accb = a.accbuf + (size_t)blockIdx.x * KB * RL * T + tid;
+#pragma unroll
+    for (int kb = 0; kb < KB; ++kb)
+#pragma unroll
+      for (int f = 0; f < RL; ++f) acc[kb][f] = accb[(kb * RL + f) * T];
+  }
+  if (EXT && a.stall_flag) {
+    // error-path test hook: wait on a flag that nothing sets, then leave as a
+    // timed-out copy wait does (the first layer's copies land first)
+    const bool stalled = tid == 0 && !stall_on_unset_flag(a.stall_flag, a.stall_cycles);
+    if (__syncthreads_or(stalled)) {
+      if (tid == 0) atomicOr(a.err, 1);
+      if (nact > 0) {
+        mbar_wait_bounded(&mbar[0], 0u);
+        if (!horner) mbar_wait_bounded(&mbar[1], 0u);
+      }
+      return;
+    }
+  }
 
   for (int k = 0; k < nact; ++k) {
     // one barrier: layer k's strip and Ey have landed, and the previous
@@ -284,7 +319,6 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
     uint64_t* const bar_e = (k & 1) ? &mbar[2] : &mbar[1];
     bool ok = mbar_wait_bounded(&mbar[0], (uint32_t)(k & 1));
     ok = ok && (horner || mbar_wait_bounded(bar_e, (uint32_t)((k >> 1) & 1)));
-    if (k == 0 && a.stall_flag && tid == 0) ok = ok && stall_on_unset_flag(a.stall_flag, a.stall_cycles);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) atomicOr(a.err, 1);
       // let this block's copies still in flight land before leaving
@@ -299,7 +333,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
     }
     const int e = list[k];
     if (tid < W && !horner) exw[tid] = a.exc[(size_t)e * a.Px + kxw[tid]];
-    const int gap = k ? e - list[k - 1] : 1;
+    const int gap = e - list[k - 1];
     if constexpr (horner) {
       // layers without pixels since the previous one: acc D^(gap - 1)
       for (int r = 1; r < gap; ++r) {
@@ -402,12 +436,22 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
       }
     }
   }
+  if (EXT && !a.chunk_last) {
+    // more layer chunks follow: hand the accumulators on (this chunk's
+    // copies have all landed: the last layer's strip was waited for above)
+    C* accb = a.accbuf + (size_t)blockIdx.x * KB * RL * T + tid;
+#pragma unroll
+    for (int kb = 0; kb < KB; ++kb)
+#pragma unroll
+      for (int f = 0; f < RL; ++f) accb[(kb * RL + f) * T] = acc[kb][f];
+    return;
+  }
   __syncthreads();
 
   // recurrence: apply the last layer's transfer function
   //   H = C Ex exp(i (pi lambda z' fy^2 + k z' g)), as in the per-layer form
-  if (horner && nact > 0) {
-    const int e = list[nact - 1];
+  if (horner && s_last >= 0) {
+    const int e = s_last;
     const float kz = a.kzp[e];
     const float inv2pi = 0.15915494309189533577f, two_pi = 6.28318530717958647692f;
 #pragma unroll
