@@ -86,7 +86,7 @@ oh_status   oh_measure_issue_peaks(int device, double* ffma_per_s, double* ffma2
  * handing the spectrum accumulators on between chunks (FP32 frames with
  * compile-time column lengths and the default render list; others keep one
  * buffer for all layers).  Results are the same either way.  0 restores
- * the default of 2 GiB. */
+ * the default of 8 GiB. */
 oh_status   oh_ctx_set_depthmap_layer_limit(oh_ctx* ctx, size_t bytes);
 /* Error-path test hook (no reference counterpart).  While set, the kernels
  * selected by kernel_mask (1: depth-map column pass, 2: point-sum tensor-core

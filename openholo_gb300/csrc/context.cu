@@ -328,7 +328,7 @@ oh_status oh_ctx_device_status(oh_ctx* ctx, void* stream) {
 oh_status oh_ctx_set_depthmap_layer_limit(oh_ctx* ctx, size_t bytes) {
   if (!ctx) return fail(OH_ERR_INVALID_ARG, "null context");
   std::lock_guard<std::mutex> lk(ctx->mu);
-  ctx->dm_layer_limit = bytes ? bytes : (size_t)2 << 30;
+  ctx->dm_layer_limit = bytes ? bytes : (size_t)8 << 30;
   return OH_OK;
 }
 

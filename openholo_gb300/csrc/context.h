@@ -20,7 +20,7 @@ struct oh_ctx {
   // on dev_err[1] for at most stall_cycles SM clocks before their first stage
   // depth-map layer buffer (row-pass strips of every layer slot): frames
   // whose strips would exceed this run in layer chunks (fast FP32 path)
-  size_t dm_layer_limit = (size_t)2 << 30;
+  size_t dm_layer_limit = (size_t)8 << 30;
   int stall_mask = 0;
   long long stall_cycles = 0;
   std::string dm_setup_key;           // parameters of the depth-map tables now in scratch

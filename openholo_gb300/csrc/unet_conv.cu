@@ -102,6 +102,9 @@ __global__ void __launch_bounds__(FwdCfg<BN>::kThreads) conv_fwd_tc(const __grid
     *abort_flag = 0; *issued = 0; *consumed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  __shared__ float sbias[BN];               // this CTA's output-channel biases (0 without bias)
+  for (int c = threadIdx.x; c < BN; c += blockDim.x)
+    sbias[c] = (a.bias && co0 + c < a.cout) ? a.bias[co0 + c] : 0.f;
   if (warp == 1) tc::tmem_alloc(tmem_slot, Cfg::kTmem);
   tc::fence_before();
   __syncthreads();
@@ -207,10 +210,8 @@ __global__ void __launch_bounds__(FwdCfg<BN>::kThreads) conv_fwd_tc(const __grid
         float v[32];
 #pragma unroll
         for (int e = 0; e < 32; ++e) v[e] = __uint_as_float(r[e]);
-        if (a.bias) {
 #pragma unroll
-          for (int e = 0; e < 32; ++e) v[e] += __ldg(a.bias + cb + e);
-        }
+        for (int e = 0; e < 32; ++e) v[e] += sbias[c * 32 + e];
         if (a.relu) {
 #pragma unroll
           for (int e = 0; e < 32; ++e) v[e] = fmaxf(v[e], 0.f);
