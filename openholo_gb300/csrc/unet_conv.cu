@@ -9,7 +9,10 @@
 //   GEMM with M = 128 pixels (a bx x by patch), N = BN output channels,
 //   K = taps x cin in 32-channel steps.  The A tile of a K step is one TMA
 //   load of the 4-D activation map at the tap's offset: out-of-range pixels
-//   read as zero, which is the convolution's zero padding.  s = +1 is the
+//   read as zero, which is the convolution's zero padding.  When a tile is
+//   128 pixels of one image row, one 136-pixel load of the row at dy (from
+//   x - 1) serves all three dx taps: their A operands start 0, 1 and 2 pixel
+//   rows into it, so each K step of 32 channels loads a third of the input.  s = +1 is the
 //   forward convolution; s = -1 with the transposed weight matrix
 //   Wt[ci][tap*cout + co] is the gradient with respect to the input (dgrad).
 //   Epilogue: + bias, ReLU, multiplication by (mask > 0) (the ReLU derivative
@@ -31,6 +34,7 @@
 // for copies still in flight keep the full bound.
 #include <cuda_bf16.h>
 #include <algorithm>
+#include <cstdlib>
 #include "context.h"
 #include "tc_common.cuh"
 #include "unet.cuh"
@@ -52,11 +56,18 @@ __device__ __forceinline__ bool wait_live(uint64_t* b, uint32_t parity, const in
 
 constexpr int pow2_at_least(int n) { return n <= 32 ? 32 : n <= 64 ? 64 : n <= 128 ? 128 : n <= 256 ? 256 : 512; }
 
-template <int BN> struct FwdCfg {
-  static constexpr int kA = 128 * 64;                 // 128 pixels x 32 channels
-  static constexpr int kB = BN * 64;                  // BN rows x 32 K
+template <int BN, bool HALO = false> struct FwdCfg {
+  // HALO: one 136-pixel row box per (dy, 32 channels) serves the three dx
+  // taps, whose A operands start 0, 1 and 2 pixel rows into it
+  static constexpr int kABox = HALO ? 136 * 64 : 128 * 64;
+  static constexpr int kA = (kABox + 1023) / 1024 * 1024;
+  static constexpr int kBBox = BN * 64;                // BN rows x 32 K
+  static constexpr int kBStride = (kBBox + 1023) / 1024 * 1024;
+  static constexpr int kTapsPerStage = HALO ? 3 : 1;
+  static constexpr int kB = kTapsPerStage * kBStride;
   static constexpr int kStage = kA + kB;
-  static constexpr int kStages = BN >= 192 ? 5 : 6;
+  static constexpr int kStagesRaw = (BN <= 64 ? 80 : 200) * 1024 / kStage;
+  static constexpr int kStages = HALO ? (kStagesRaw < 2 ? 2 : kStagesRaw > 6 ? 6 : kStagesRaw) : (BN >= 192 ? 5 : 6);
   static constexpr int kTmemBuf = pow2_at_least(BN);  // columns of one accumulator
   static constexpr int kTmem = 2 * kTmemBuf;          // two accumulators: MMA and epilogue overlap
   static constexpr int kThreads = 192;                // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
@@ -69,11 +80,11 @@ template <int BN> struct FwdCfg {
 // TMEM buffer j & 1 and commits it to the epilogue warps, which drain it
 // (bias, ReLU, mask, BF16 store) while the next tile accumulates in the
 // other buffer.
-template <int BN>
-__global__ void __launch_bounds__(FwdCfg<BN>::kThreads) conv_fwd_tc(const __grid_constant__ CUtensorMap mX,
-                                                                    const __grid_constant__ CUtensorMap mW,
-                                                                    ConvArgs a) {
-  typedef FwdCfg<BN> Cfg;
+template <int BN, bool HALO>
+__global__ void __launch_bounds__(FwdCfg<BN, HALO>::kThreads) conv_fwd_tc(const __grid_constant__ CUtensorMap mX,
+                                                                          const __grid_constant__ CUtensorMap mW,
+                                                                          ConvArgs a) {
+  typedef FwdCfg<BN, HALO> Cfg;
   extern __shared__ unsigned char smem_raw[];
   const uint32_t raw = tc::su32(smem_raw);
   unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
@@ -92,7 +103,7 @@ __global__ void __launch_bounds__(FwdCfg<BN>::kThreads) conv_fwd_tc(const __grid
   const int ntl = blockIdx.x < tiles ? (int)((tiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
   const int co0 = blockIdx.y * BN;
   const int cchunks = a.cin >> 5;
-  const int nk = a.taps * cchunks;
+  const int nk = (HALO ? 3 : a.taps) * cchunks;
   const long long nsteps = (long long)ntl * nk;
 
   if (threadIdx.x == 0) {
@@ -134,13 +145,26 @@ __global__ void __launch_bounds__(FwdCfg<BN>::kThreads) conv_fwd_tc(const __grid
             g = -1;
             break;
           }
-          const int tap = it / cchunks, cc = it - tap * cchunks;
-          int dx = 0, dy = 0;
-          if (a.taps == 9) { dx = (tap % 3 - 1) * a.sign; dy = (tap / 3 - 1) * a.sign; }
           unsigned char* st = base + s * Cfg::kStage;
-          tc::mb_expect_tx(&full[s], (uint32_t)Cfg::kStage);
-          tc::tma_load_4d(st, &mX, cc * 32, x0 + dx, y0 + dy, img, &full[s]);
-          tc::tma_load_2d(st + Cfg::kA, &mW, tap * a.cin + cc * 32, co0, &full[s]);
+          if constexpr (HALO) {
+            // row y0 + dy' from x0 - 1: the dx' = -1, 0, +1 taps start 0, 1, 2 rows in
+            const int dyi = it / cchunks, cc = it - dyi * cchunks;
+            const int dyp = dyi - 1;
+            tc::mb_expect_tx(&full[s], (uint32_t)(Cfg::kABox + 3 * Cfg::kBBox));
+            tc::tma_load_4d(st, &mX, cc * 32, x0 - 1, y0 + dyp, img, &full[s]);
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+              const int tap = 3 * (1 + a.sign * dyp) + (1 + a.sign * (j - 1));
+              tc::tma_load_2d(st + Cfg::kA + j * Cfg::kBStride, &mW, tap * a.cin + cc * 32, co0, &full[s]);
+            }
+          } else {
+            const int tap = it / cchunks, cc = it - tap * cchunks;
+            int dx = 0, dy = 0;
+            if (a.taps == 9) { dx = (tap % 3 - 1) * a.sign; dy = (tap / 3 - 1) * a.sign; }
+            tc::mb_expect_tx(&full[s], (uint32_t)Cfg::kStage);
+            tc::tma_load_4d(st, &mX, cc * 32, x0 + dx, y0 + dy, img, &full[s]);
+            tc::tma_load_2d(st + Cfg::kA, &mW, tap * a.cin + cc * 32, co0, &full[s]);
+          }
         }
       }
       if (g >= 0) *issued = (int)nsteps;
@@ -172,11 +196,19 @@ __global__ void __launch_bounds__(FwdCfg<BN>::kThreads) conv_fwd_tc(const __grid
           }
           tc::fence_after();
           const uint32_t sa = tc::su32(base + s * Cfg::kStage);
-          const uint64_t da = tc::desc_sw64(sa, 16, 512), db = tc::desc_sw64(sa + Cfg::kA, 16, 512);
 #pragma unroll
-          for (int kk = 0; kk < 2; ++kk) {
-            const uint64_t adv = (uint64_t)((kk * 32) >> 4);      // 16 BF16 = 32 bytes along K
-            tc::umma_bf16(acc, da + adv, db + adv, idesc, (it | kk) ? 1u : 0u);
+          for (int j = 0; j < Cfg::kTapsPerStage; ++j) {
+            // HALO: tap dx' = j - 1 starts j pixel rows (64 bytes each) into the
+            // row box; the swizzle follows the absolute shared-memory address,
+            // which the TMA write and the MMA read share, so the start address
+            // simply moves (matrix base offset 0)
+            const uint64_t da = tc::desc_sw64(sa + (HALO ? j * 64 : 0), 16, 512);
+            const uint64_t db = tc::desc_sw64(sa + Cfg::kA + j * Cfg::kBStride, 16, 512);
+#pragma unroll
+            for (int kk = 0; kk < 2; ++kk) {
+              const uint64_t adv = (uint64_t)((kk * 32) >> 4);      // 16 BF16 = 32 bytes along K
+              tc::umma_bf16(acc, da + adv, db + adv, idesc, (it | j | kk) ? 1u : 0u);
+            }
           }
           tc::umma_commit(&empty[s]);
         }
@@ -412,10 +444,10 @@ bool patch_shape(int w, int pixels, int* bx, int* by) {
   return true;
 }
 
-template <int BN>
+template <int BN, bool HALO>
 oh_status launch_fwd(const CUtensorMap& mX, const CUtensorMap& mW, const ConvArgs& a, long long tiles, cudaStream_t st) {
-  typedef FwdCfg<BN> Cfg;
-  OH_CUDA_TRY(cudaFuncSetAttribute(conv_fwd_tc<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmem));
+  typedef FwdCfg<BN, HALO> Cfg;
+  OH_CUDA_TRY(cudaFuncSetAttribute(conv_fwd_tc<BN, HALO>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmem));
   // persistent grid: the CTAs that fit on an SM by shared memory and tensor
   // memory (512 columns), at most four, times the SMs, spread over the
   // output-channel tiles
@@ -424,7 +456,7 @@ oh_status launch_fwd(const CUtensorMap& mX, const CUtensorMap& mW, const ConvArg
   const int ctiles = (a.cout + BN - 1) / BN;
   const long long want = std::max(1LL, (long long)sm_count() * per_sm / ctiles);
   const int gx = (int)std::min(tiles, want);
-  conv_fwd_tc<BN><<<dim3(gx, ctiles), Cfg::kThreads, Cfg::kSmem, st>>>(mX, mW, a);
+  conv_fwd_tc<BN, HALO><<<dim3(gx, ctiles), Cfg::kThreads, Cfg::kSmem, st>>>(mX, mW, a);
   OH_LAUNCH_CHECK();
   return OH_OK;
 }
@@ -481,17 +513,20 @@ oh_status conv_enqueue(oh_ctx* ctx, const ConvDesc& d, cudaStream_t st, const ch
     if (d.cout % c == 0) { bn = c; break; }
   while ((bn == 256 || bn == 128 || bn == 64 || bn == 192) && tiles * ((d.cout + bn - 1) / bn) < 2LL * sm_count())
     bn /= 2;
+  // 3x3 over whole 128-pixel rows: one halo row box per (dy, 32 channels)
+  const char* hv = std::getenv("OH_CONV_HALO");
+  const bool halo = d.taps == 9 && a.by == 1 && a.bx == 128 && !(hv && std::atoi(hv) == 0);
   CUtensorMap mX, mW;
-  OH_TRY(tc::map_act4d(&mX, d.x, d.cin, d.x_cs, d.w, d.h, d.n, a.bx, a.by));
+  OH_TRY(tc::map_act4d(&mX, d.x, d.cin, d.x_cs, d.w, d.h, d.n, halo ? 136 : a.bx, a.by));
   OH_TRY(tc::map_mat2d(&mW, d.w_mat, d.taps * d.cin, d.cout, bn));
   KernelTimer kt(ctx, timer_name, st);
   switch (bn) {
-    case 32: return launch_fwd<32>(mX, mW, a, tiles, st);
-    case 64: return launch_fwd<64>(mX, mW, a, tiles, st);
-    case 96: return launch_fwd<96>(mX, mW, a, tiles, st);
-    case 128: return launch_fwd<128>(mX, mW, a, tiles, st);
-    case 192: return launch_fwd<192>(mX, mW, a, tiles, st);
-    default: return launch_fwd<256>(mX, mW, a, tiles, st);
+    case 32: return halo ? launch_fwd<32, true>(mX, mW, a, tiles, st) : launch_fwd<32, false>(mX, mW, a, tiles, st);
+    case 64: return halo ? launch_fwd<64, true>(mX, mW, a, tiles, st) : launch_fwd<64, false>(mX, mW, a, tiles, st);
+    case 96: return halo ? launch_fwd<96, true>(mX, mW, a, tiles, st) : launch_fwd<96, false>(mX, mW, a, tiles, st);
+    case 128: return halo ? launch_fwd<128, true>(mX, mW, a, tiles, st) : launch_fwd<128, false>(mX, mW, a, tiles, st);
+    case 192: return halo ? launch_fwd<192, true>(mX, mW, a, tiles, st) : launch_fwd<192, false>(mX, mW, a, tiles, st);
+    default: return halo ? launch_fwd<256, true>(mX, mW, a, tiles, st) : launch_fwd<256, false>(mX, mW, a, tiles, st);
   }
 }
 
