@@ -435,6 +435,170 @@ __global__ void __launch_bounds__(kConvThreads) conv_wgrad_tc(const __grid_const
   }
 }
 
+// Weight gradient over whole 64-pixel rows (3x3, w >= 64): one CTA per
+// (32-channel input chunk cc, group of dy rows) and K range.  Per K step
+// (64 pixels of one row) it loads, for each of its dy, one 72-pixel row box
+// of X starting at x - 1, and the dZ tile once.  The A operand of dy reads
+// that box with a leading-dimension offset of one pixel row (64 bytes):
+// M group g (rows 32 g .. 32 g + 31) is the box shifted by g pixels, i.e.
+// the taps dx = g - 1 for g < 3 (group 3 is computed and dropped).  One
+// accumulator per dy shares the dZ tile.
+template <int BN> struct WgHCfg {
+  static constexpr int kABox = 72 * 64;
+  static constexpr int kAStride = (kABox + 1023) / 1024 * 1024;
+  static constexpr int kTmemBuf = pow2_at_least(BN);
+  static constexpr int kNdy = (512 / kTmemBuf) >= 3 ? 3 : 2;   // dy rows per CTA (accumulators)
+  static constexpr int kTmem = pow2_at_least(kNdy * kTmemBuf) > 512 ? 512 : pow2_at_least(kNdy * kTmemBuf);
+  static constexpr int kBBox = 64 * 64;                // 64 pixels x 32 channels of dZ
+  static constexpr int kA = kNdy * kAStride;
+  static constexpr int kB = (BN / 32) * kBBox;
+  static constexpr int kStage = kA + kB;
+  static constexpr int kStagesRaw = 200 * 1024 / kStage;
+  static constexpr int kStages = kStagesRaw > 6 ? 6 : kStagesRaw;
+  static constexpr int kSmem = kStages * kStage + 1024 + 256;
+};
+
+template <int BN>
+__global__ void __launch_bounds__(kConvThreads) conv_wgrad_halo(const __grid_constant__ CUtensorMap mX,
+                                                                const __grid_constant__ CUtensorMap mD, WgArgs a) {
+  typedef WgHCfg<BN> Cfg;
+  extern __shared__ unsigned char smem_raw[];
+  const uint32_t raw = tc::su32(smem_raw);
+  unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+  uint64_t* full = reinterpret_cast<uint64_t*>(base + Cfg::kStages * Cfg::kStage);
+  uint64_t* empty = full + Cfg::kStages;
+  uint64_t* done = empty + Cfg::kStages;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+  int* issued = abort_flag + 1;
+  int* consumed = abort_flag + 2;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  const int cchunks = a.cin >> 5;
+  const int cc = blockIdx.x % cchunks;
+  const int dy0 = (blockIdx.x / cchunks) * Cfg::kNdy;           // first dy index (0..2) of this CTA
+  const int ndy = min(Cfg::kNdy, 3 - dy0);
+  const long long kb_total = (long long)a.n * a.tiles_y * a.tiles_x;
+  const int kb0 = (int)(kb_total * blockIdx.y / gridDim.y);
+  const int kb1 = (int)(kb_total * (blockIdx.y + 1) / gridDim.y);
+  const int nk = kb1 - kb0;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < Cfg::kStages; ++s) { tc::mb_init(&full[s], 1); tc::mb_init(&empty[s], 1); }
+    tc::mb_init(done, 1);
+    *abort_flag = 0; *issued = 0; *consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) tc::tmem_alloc(tmem_slot, Cfg::kTmem);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (threadIdx.x == 0) {
+    int it = 0;
+    for (; it < nk; ++it) {
+      const int s = it % Cfg::kStages;
+      const uint32_t ph = (uint32_t)((it / Cfg::kStages) & 1);
+      if (!wait_live(&empty[s], ph ^ 1u, abort_flag) || *((volatile int*)abort_flag)) {
+        atomicExch(abort_flag, 1);
+        break;
+      }
+      int kb = kb0 + it;
+      const int tx = kb % a.tiles_x; kb /= a.tiles_x;
+      const int ty = kb % a.tiles_y;
+      const int img = kb / a.tiles_y;
+      const int x0 = tx * a.bx, y0 = ty * a.by;
+      unsigned char* st = base + s * Cfg::kStage;
+      tc::mb_expect_tx(&full[s], (uint32_t)(ndy * Cfg::kABox + Cfg::kB));
+      for (int d = 0; d < ndy; ++d)
+        tc::tma_load_4d(st + d * Cfg::kAStride, &mX, cc * 32, x0 - 1, y0 + (dy0 + d - 1), img, &full[s]);
+#pragma unroll
+      for (int j = 0; j < BN / 32; ++j)
+        tc::tma_load_4d(st + Cfg::kA + j * Cfg::kBBox, &mD, j * 32, x0, y0, img, &full[s]);
+    }
+    *issued = it;
+  } else if (threadIdx.x == 32) {
+    constexpr uint32_t idesc = tc::idesc_bf16(128, BN, 1, 1);
+    int it = 0;
+    bool stalled = false;
+    if (a.stall_flag && !stall_on_unset_flag(a.stall_flag, a.stall_cycles)) {
+      atomicExch(abort_flag, 1);
+      stalled = true;
+    }
+    for (; it < nk && !stalled; ++it) {
+      const int s = it % Cfg::kStages;
+      const uint32_t ph = (uint32_t)((it / Cfg::kStages) & 1);
+      if (!wait_live(&full[s], ph, abort_flag) || *((volatile int*)abort_flag)) {
+        atomicExch(abort_flag, 1);
+        break;
+      }
+      tc::fence_after();
+      const uint32_t sa = tc::su32(base + s * Cfg::kStage);
+      for (int d = 0; d < ndy; ++d) {
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+          // 16 pixels = two 8-row K groups, 1024 bytes; M groups one pixel row apart
+          const uint64_t da = tc::desc_sw64(sa + d * Cfg::kAStride + kk * 1024, 64, 512);
+          const uint64_t db = tc::desc_sw64(sa + Cfg::kA + kk * 1024, Cfg::kBBox, 512);
+          tc::umma_bf16(tmem + (uint32_t)(d * Cfg::kTmemBuf), da, db, idesc, (it | kk) ? 1u : 0u);
+        }
+      }
+      tc::umma_commit(&empty[s]);
+    }
+    *consumed = it;
+    tc::umma_commit(done);
+  }
+  __syncwarp();
+  const bool ok_done = tc::mb_wait(done, 0, kWaitCycles);
+  tc::fence_after();
+  const bool good = __syncthreads_and(ok_done && !*((volatile int*)abort_flag));
+  if (good && nk > 0 && warp < 3) {
+    // warp g = tap dx = g - 1 of each dy: dW^T row (3 dy + g) cin + cc 32 + lane
+    for (int d = 0; d < ndy; ++d) {
+      const int tap = 3 * (dy0 + d) + warp;
+      const int row = tap * a.cin + cc * 32 + lane;
+#pragma unroll 1
+      for (int c = 0; c < BN / 32; ++c) {
+        uint32_t r[32];
+        tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(d * Cfg::kTmemBuf + c * 32), r);
+        float* dst = a.dwt + (size_t)row * a.cout + c * 32;
+#pragma unroll
+        for (int q = 0; q < 32; q += 4)
+          asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst + q), "f"(__uint_as_float(r[q])),
+                       "f"(__uint_as_float(r[q + 1])), "f"(__uint_as_float(r[q + 2])), "f"(__uint_as_float(r[q + 3]))
+                       : "memory");
+      }
+    }
+  } else if (!good && threadIdx.x == 0) {
+    atomicOr(a.err, 2);
+  }
+  if (threadIdx.x == 0) {
+    for (int it = *consumed; it < *issued; ++it)
+      tc::mb_wait(&full[it % Cfg::kStages], (uint32_t)((it / Cfg::kStages) & 1), kWaitCycles);
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc::fence_after();
+    tc::tmem_dealloc(tmem, Cfg::kTmem);
+  }
+}
+
+template <int BN>
+oh_status launch_wgrad_halo(const CUtensorMap& mX, const CUtensorMap& mD, const WgArgs& a, long long kb_total,
+                            cudaStream_t st) {
+  typedef WgHCfg<BN> Cfg;
+  OH_CUDA_TRY(cudaFuncSetAttribute(conv_wgrad_halo<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmem));
+  const int gx = (a.cin / 32) * ((3 + Cfg::kNdy - 1) / Cfg::kNdy);
+  long long splits = std::max(1LL, (4LL * sm_count() + gx - 1) / gx);
+  splits = std::min(splits, std::max(1LL, kb_total / 16));
+  splits = std::min(splits, 65535LL);
+  conv_wgrad_halo<BN><<<dim3(gx, (int)splits), kConvThreads, Cfg::kSmem, st>>>(mX, mD, a);
+  OH_LAUNCH_CHECK();
+  return OH_OK;
+}
+
 // Patch of `pixels` pixels for an image row of width w: bx = min(w, pixels),
 // by = pixels / bx; widths below `pixels` must divide it.
 bool patch_shape(int w, int pixels, int* bx, int* by) {
@@ -550,6 +714,19 @@ oh_status wgrad_enqueue(oh_ctx* ctx, const WgradDesc& d, cudaStream_t st, const 
   const int groups = d.taps * (d.cin / 32);
   const int mtiles = (groups + 3) / 4;
   const long long kb_total = (long long)a.tiles_x * a.tiles_y * d.n;
+  // 3x3 over whole 64-pixel rows: one row box per (dy, 32 channels) feeds the three dx taps
+  const char* hv = std::getenv("OH_CONV_HALO");
+  if (d.taps == 9 && a.by == 1 && a.bx == 64 && d.cout <= 128 && !(hv && std::atoi(hv) == 0)) {
+    CUtensorMap mX, mD;
+    OH_TRY(tc::map_act4d(&mX, d.x, d.cin, d.x_cs, d.w, d.h, d.n, 72, 1));
+    OH_TRY(tc::map_act4d(&mD, d.dz, d.cout, d.dz_cs, d.w, d.h, d.n, 64, 1));
+    KernelTimer kt(ctx, timer_name, st);
+    switch (d.cout) {
+      case 32: return launch_wgrad_halo<32>(mX, mD, a, kb_total, st);
+      case 64: return launch_wgrad_halo<64>(mX, mD, a, kb_total, st);
+      default: return launch_wgrad_halo<128>(mX, mD, a, kb_total, st);
+    }
+  }
   // K splits: about four CTAs per SM over all M tiles, each with at least 16 K steps
   long long splits = std::max(1LL, (4LL * sm_count() + mtiles - 1) / mtiles);
   splits = std::min(splits, std::max(1LL, kb_total / 16));

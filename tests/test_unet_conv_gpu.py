@@ -74,8 +74,12 @@ def test_conv_input_gradient_with_mask(ctx, n, h, w, cin, cout):
 
 @pytest.mark.parametrize("n,h,w,cin,cout,taps", [(1, 16, 128, 32, 32, 9), (2, 12, 64, 96, 64, 9),
                                                  (1, 8, 16, 64, 128, 9), (1, 32, 96, 128, 256, 9),
-                                                 (1, 8, 128, 32, 64, 1)])
+                                                 (1, 8, 128, 32, 64, 1), (1, 8, 128, 64, 128, 9),
+                                                 (2, 6, 100, 32, 32, 9), (1, 4, 192, 192, 64, 9)])
 def test_conv_weight_gradient(ctx, n, h, w, cin, cout, taps):
+    """Widths of at least 64 with 3x3 taps and up to 128 output channels run
+    the row-box kernel (three dx taps from one load); the others the
+    four-group kernel."""
     rng = np.random.default_rng(cin + cout + h)
     x = bf16(rng, (n, h, w, cin))
     dz = bf16(rng, (n, h, w, cout))
