@@ -202,20 +202,37 @@ __global__ void unet_skip_pool_back_mask(const __nv_bfloat16* __restrict__ skip,
   }
 }
 
-// bias gradient: db[c] += sum over pixels of dz[p][c] (C <= 256 divides 256)
+// bias gradient: db[c] += sum over pixels of dz[p][c] (C a multiple of 8,
+// at most 256).  Thread t takes channels 8 (t % (C/8)) .. + 7 of pixel lane
+// t / (C/8) with one 16-byte load per pixel; the lanes are summed in shared
+// memory and added with one atomic per channel and block.
 __global__ void __launch_bounds__(256) unet_bias_grad(const __nv_bfloat16* __restrict__ dz, int cs, int C, long long npix,
                                                       float* __restrict__ db) {
-  __shared__ float red[256];
-  const int lanes = 256 / C;
-  const int c = threadIdx.x % C, r = threadIdx.x / C;
-  float acc = 0.f;
-  for (long long p = blockIdx.x * (long long)lanes + r; p < npix; p += (long long)gridDim.x * lanes)
-    acc += bf(dz[p * cs + c]);
-  red[threadIdx.x] = acc;
+  __shared__ float red[256][9];
+  const int c8n = C / 8;
+  const int lanes = 256 / c8n;
+  const int c8 = threadIdx.x % c8n, r = threadIdx.x / c8n;
+  float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (r < lanes) {
+    for (long long p = blockIdx.x * (long long)lanes + r; p < npix; p += (long long)gridDim.x * lanes) {
+      const uint4 v = *reinterpret_cast<const uint4*>(dz + p * cs + 8 * c8);
+      const __nv_bfloat162* vb = reinterpret_cast<const __nv_bfloat162*>(&v);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float2 f = __bfloat1622float2(vb[e]);
+        acc[2 * e] += f.x;
+        acc[2 * e + 1] += f.y;
+      }
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < 8; ++e) red[threadIdx.x][e] = acc[e];
   __syncthreads();
-  if (r == 0) {
-    for (int k = 1; k < lanes; ++k) acc += red[k * C + c];
-    atomicAdd(db + c, acc);
+  if (threadIdx.x < C) {
+    const int cc8 = threadIdx.x / 8, e = threadIdx.x % 8;
+    float sum = 0.f;
+    for (int k = 0; k < lanes; ++k) sum += red[k * c8n + cc8][e];
+    atomicAdd(db + threadIdx.x, sum);
   }
 }
 
@@ -515,7 +532,7 @@ oh_status unet_backward(oh_unet* u, const float2* target, int n, int h, int w, c
     OH_TRY(wgrad_enqueue(ctx, d, st, L.tn[2]));
     KernelTimer kt(ctx, "unet_bias_grad", st);
     const long long np = (long long)n * hl * wl;
-    unet_bias_grad<<<grid_for(np * L.cout), 256, 0, st>>>(
+    unet_bias_grad<<<grid_for(np * L.cout / 8), 256, 0, st>>>(
         static_cast<const __nv_bfloat16*>(dz), L.cout, L.cout, np, L.db);
     OH_LAUNCH_CHECK();
     return OH_OK;
