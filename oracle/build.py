@@ -10,9 +10,17 @@ build_reference(): when the reference tree is present, compiles the
                    oracle/_ref/libketi_ref.so (sequential; the reference's
                    OpenMP loop races on its output) and
                    oracle/_ref/libketi_ref_omp.so (-fopenmp, timing only).
-                   Nothing is copied out of the reference tree.  The depth-map
-                   and WRP sources need Qt, FFTW or the closed CWO DLL and are
-                   not built.
+                   Nothing is copied out of the reference tree.
+build_reference_depthmap():
+                   when the reference tree is present, compiles the device
+                   code of the reference's depth-map kernels
+                   (OpenHolo_DepthMap/Hologram/src/HologramKernel.cu), where
+                   it lies, into oracle/_ref/dm_ref.cubin for sm_103a, and
+                   records the entry names ptxas reports in
+                   oracle/_ref/dm_ref_entries.txt.  oracle/dm_reference.py runs
+                   these kernels on a GPU in the reference's call sequence.
+                   The depth-map host code (Qt, FFTW) and the WRP sources (the
+                   closed CWO DLL) are not built.
 """
 from __future__ import annotations
 
@@ -62,6 +70,32 @@ def build_reference() -> Path | None:
     return REF_OUT / "libketi_ref.so"
 
 
+DM_KERNEL_SRC = REFERENCE_ROOT / "OpenHolo_DepthMap/Hologram/src/HologramKernel.cu"
+
+
+def build_reference_depthmap() -> Path | None:
+    src = DM_KERNEL_SRC
+    if not src.exists():
+        return None
+    REF_OUT.mkdir(exist_ok=True)
+    out = REF_OUT / "dm_ref.cubin"
+    names = REF_OUT / "dm_ref_entries.txt"
+    if _fresh(out, [src]) and names.exists():
+        return out
+    nvcc = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
+    r = subprocess.run([nvcc, "-cubin", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-Xptxas", "-v", "-w",
+                        "-o", str(out), str(src)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+    entries = []
+    for line in (r.stdout + r.stderr).splitlines():
+        if "Compiling entry function '" in line:
+            entries.append(line.split("'")[1])
+    names.write_text("\n".join(sorted(set(entries))) + "\n")
+    return out
+
+
 if __name__ == "__main__":
     print(build_oracle())
     print(build_reference())
+    print(build_reference_depthmap())

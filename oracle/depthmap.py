@@ -19,8 +19,11 @@ A float64 numpy restatement of the reference's depth-map path
 
 Layers are accumulated sequentially (the reference's OpenMP layer loop races
 on U_complex_, HologramGenerator_CPU.cpp:129/215).  FFTW is replaced by
-numpy/scipy pocketfft (FFTW and Qt are not available), so the oracle pins
-the reference's algorithm, not FFTW's rounding.
+numpy/scipy pocketfft (FFTW and Qt are not available).  At pad 1 the oracle
+reproduces the reference's own GPU kernels (HologramKernel.cu, compiled from
+its source and run in the order of Calc_Holo_GPU / encoding_GPU with cuFFT)
+to FP64 rounding: tests/test_dm_reference_golden.py against the fixtures in
+tests/golden/dm_reference_gpu.npz.
 
 Extensions beyond the reference, used by the 1920x1080 / 32-layer workload:
   pad = 2   the layer field is embedded, centred (offset n/2), in a 2x grid;
