@@ -88,9 +88,16 @@ oh_status   oh_measure_issue_peaks(int device, double* ffma_per_s, double* ffma2
  * buffer for all layers).  Results are the same either way.  0 restores
  * the default of 8 GiB. */
 oh_status   oh_ctx_set_depthmap_layer_limit(oh_ctx* ctx, size_t bytes);
+/* Depth-map batches (no reference counterpart): 1 (default) runs a batch
+ * whose frames the persistent batch kernel carries (FP32, padded lengths
+ * 1024, 1536, 2048, 3072 and 4096 along both axes, evenly spaced layers, the
+ * SSB crop of a 2x pad, one layer buffer) as one launch of that kernel; 0
+ * runs every batch as per-frame launches.  Results are the same either way. */
+oh_status   oh_ctx_set_depthmap_batch_mode(oh_ctx* ctx, int persistent);
 /* Error-path test hook (no reference counterpart).  While set, the kernels
  * selected by kernel_mask (1: depth-map column pass, 2: point-sum tensor-core
- * GEMM, 4: tensor-core convolutions) first wait on a device flag that nothing
+ * GEMM, 4: tensor-core convolutions, 8: the persistent depth-map batch
+ * kernel, outside graph replay) first wait on a device flag that nothing
  * sets, for at most `cycles` SM clocks, and then take their bounded-wait error
  * path: they let their copies and tensor-core operations land, free their
  * tensor memory, set the context's error word and return without writing

@@ -58,6 +58,7 @@ void drop_graphs(oh_ctx* ctx) {
   for (auto& kv : ctx->graphs)
     if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
   ctx->graphs.clear();
+  ctx->batch_plans.clear();
 }
 
 oh_status scratch(oh_ctx* ctx, const char* name, size_t bytes, void** out) {
@@ -329,6 +330,14 @@ oh_status oh_ctx_set_depthmap_layer_limit(oh_ctx* ctx, size_t bytes) {
   if (!ctx) return fail(OH_ERR_INVALID_ARG, "null context");
   std::lock_guard<std::mutex> lk(ctx->mu);
   ctx->dm_layer_limit = bytes ? bytes : (size_t)8 << 30;
+  return OH_OK;
+}
+
+oh_status oh_ctx_set_depthmap_batch_mode(oh_ctx* ctx, int persistent) {
+  if (!ctx) return fail(OH_ERR_INVALID_ARG, "null context");
+  if (persistent != 0 && persistent != 1) return fail(OH_ERR_INVALID_ARG, "batch mode must be 0 or 1");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->dm_batch_persistent = persistent;
   return OH_OK;
 }
 

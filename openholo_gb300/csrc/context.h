@@ -5,6 +5,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <utility>
@@ -29,6 +30,16 @@ struct oh_ctx {
   // captured depth-map batches: key -> executable graph and the table key it leaves behind
   struct Graph { cudaGraphExec_t exec = nullptr; std::string dm_key; int launches = 0; };
   std::map<std::string, Graph> graphs;
+  // persistent depth-map batches: key -> plan (descriptors, tables, graph)
+  struct BatchPlanBase { virtual ~BatchPlanBase() = default; };
+  std::map<std::string, std::unique_ptr<BatchPlanBase>> batch_plans;
+  // persistent batch kernel: 0 off (per-frame launches); tuned settings per
+  // (padded length, device) and the file they persist in (empty: none)
+  int dm_batch_persistent = 1;
+  struct BatchTune { int ctas_per_sm = 2, row_pairs = 1, col_blocks = 1, out_rows = 2, lag = 1; double ms = 0; };
+  std::map<std::string, BatchTune> batch_tune;
+  std::string tune_file;
+  bool tune_loaded = false;
   struct Buf { void* p = nullptr; size_t bytes = 0; };
   std::map<std::string, Buf> scratch;
   struct PlanBufs { oh::FFTPlan plan; void* tw = nullptr; int* perm = nullptr; int* iperm = nullptr; };

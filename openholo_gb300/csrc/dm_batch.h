@@ -1,0 +1,68 @@
+// Persistent batch kernel of the depth-map pipeline: shared declarations of
+// the host planner (depthmap.cu) and the kernel (dm_batch.cu).
+//
+// A batch of frames becomes one list of work items, each a range of blocks
+// of one pass of one frame (row pairs, column strips or output rows).  One
+// launch of dm_batch_kernel, one or two blocks per SM, takes items from the
+// list in order through a global ticket counter.  Before an item's body runs
+// its block waits, bounded, until the items it reads from have finished
+// (per-frame completion counters):
+//   column items of frame f: every row item of f, and every output item of
+//     the frame that last used f's V ring slot;
+//   output items of f: every column item of f;
+//   row items of f: every column item of the frame that last used f's R and
+//     occupancy ring slot.
+// An item's block only waits on items taken before its own, and a block
+// that has taken an item is resident, so the oldest unfinished item always
+// progresses.  A wait that runs out (about a second of SM clock, or the
+// error-path test hook) sets the launch's abort word and the context's
+// error word; every block then stops at its next item.
+#pragma once
+#include "dm_kernels.cuh"
+
+namespace oh {
+
+// Padded lengths (Px and Py) the batch kernel carries, as length classes.
+constexpr int kBatchLens[] = {1024, 1536, 2048, 3072, 4096};
+constexpr int kBatchNumLens = 5;
+constexpr int kBatchThreads = 256;
+// Columns per column block for each class: one-column blocks over the
+// two-column strips at 3072 and 4096 (as the per-frame pass picks there).
+__host__ __device__ constexpr int batch_col_w(int cls) { return cls >= 3 ? 1 : 2; }
+
+enum : int { kItemRow = 0, kItemCol = 1, kItemOut = 2 };
+
+// 16-byte aligned: the kernel copies `a` into shared memory as int4 words.
+struct alignas(16) BatchFrame {
+  DMArgs<float> a;
+  int xcls, ycls;          // classes of Px and Py
+  int n_items[3];          // row, column and output items
+  int dep_row;             // frame whose column items free this frame's R/occ slot (-1: none)
+  int dep_col;             // frame whose output items free this frame's V slot (-1: none)
+};
+static_assert(sizeof(DMArgs<float>) % 16 == 0, "frame arguments are copied as int4 words");
+static_assert(sizeof(BatchFrame) % 16 == 0, "frame records keep 16-byte alignment");
+
+// Item: x = frame, y = kind | class << 4, z = first block, w = blocks.
+struct BatchLaunch {
+  const BatchFrame* frames;
+  const int4* items;
+  int n_items;
+  unsigned* ctl;           // [0] ticket, [1] abort, [2..3] unused, then 3 counters per frame
+  int* err;                // context error word
+  const int* stall_flag;   // error-path test hook: a flag nothing sets (or null)
+  long long stall_cycles;
+  long long wait_cycles;   // bound of a dependency wait
+  int grid;
+  size_t smem;
+};
+
+constexpr int kBatchCtlHead = 4;
+
+oh_status dm_batch_launch(const BatchLaunch& L, cudaStream_t st);
+oh_status dm_batch_setup_launch(const BatchFrame* frames, const DMSetup* su, int n, cudaStream_t st);
+// Resident blocks per SM of the batch kernel with `smem` bytes of dynamic
+// shared memory (0 when it does not fit).
+int dm_batch_occupancy(size_t smem);
+
+}  // namespace oh

@@ -104,11 +104,13 @@ template <int NY, int W> constexpr int col_kb() {
   return kb;
 }
 
-template <int NY, int W, bool STEP> struct ColCfg {
+// TT > 0: a block of exactly TT threads (the persistent batch kernel's
+// block size), each taking ceil(NBL / TT) last-stage butterflies.
+template <int NY, int W, bool STEP, int TT = 0> struct ColCfg {
   static constexpr int RL = FastSched<NY>::rlast;
   static constexpr int NBL = (NY / RL) * W;          // last-stage butterflies of the block's columns
-  static constexpr int KB = col_kb<NY, W>();          // butterflies per thread
-  static constexpr int T = ((NBL + KB - 1) / KB + 31) / 32 * 32;
+  static constexpr int KB = TT > 0 ? (NBL + TT - 1) / TT : col_kb<NY, W>();   // butterflies per thread
+  static constexpr int T = TT > 0 ? TT : ((NBL + KB - 1) / KB + 31) / 32 * 32;
   // two blocks per SM when two fit in shared memory (2x padding, pny =
   // NY / 2); otherwise one, and the register cap that two would impose
   // (spills at the longer lengths) is lifted
@@ -147,10 +149,13 @@ template <int NY> constexpr uint32_t col_ssb_keep() {
 // stage's small DFT computes only the outputs that reach the crop.
 // EXT: the layer-chunk hand-over of the accumulators and the error-path
 // test hook; the frames that need neither run the kernel without them.
-template <int NY, int W, bool STEP, bool SSB = false, bool EXT = false>
-__global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::MINB) dm_col_fast(DMArgs<float> a) {
+// Block body for column block blk (a strip, or one column of a strip when
+// W = 1).  TT: see ColCfg.  PERSIST: the block goes on to other work after
+// this one, so its mbarriers are invalidated at the end.
+template <int NY, int W, bool STEP, bool SSB, bool EXT, int TT, bool PERSIST>
+__device__ __forceinline__ void dm_col_body(const DMArgs<float>& a, int blk) {
   typedef float2 C;
-  typedef ColCfg<NY, W, STEP> CF;
+  typedef ColCfg<NY, W, STEP, TT> CF;
   constexpr int SW = kColStripW;
   static_assert(W == 1 || W == SW, "a block takes one column or a whole strip");
   constexpr int T = CF::T;
@@ -180,19 +185,21 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
   C* const tab1 = reinterpret_cast<C*>(smem + Lo.tab);            // stage 1: [NY/R0/R1][R1-1]
   C* exw = reinterpret_cast<C*>(smem + Lo.exw);
   float* lfxw = reinterpret_cast<float*>(smem + Lo.lfxw);
-  __shared__ int kxw[8];          // spectrum column of each strip column
-  __shared__ C dxw[8];            // its Dx factor (layer-step form)
+  ColShared* const csh = dm_col_shared();
+  int* const kxw = csh->kxw;      // spectrum column of each strip column
+  C* const dxw = csh->dxw;        // its Dx factor (layer-step form)
   // active render entries of this chunk, list[0..nact); list[-1] holds the
   // entry before the first (the previous chunk's last active one, or one less
   // than the first), so the layer-step gap is e - list[k - 1] for every k
   int16_t* list = reinterpret_cast<int16_t*>(smem + Lo.list) + 1;
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + Lo.mbar);  // [0] strip+flags, [1],[2] Ey
-  __shared__ int s_nact, s_last;
+  int& s_nact = csh->nact;
+  int& s_last = csh->last;
 
   const int tid = threadIdx.x;
-  const int s = blockIdx.x / (SW / W);                // row-pass strip
-  const int csel = (blockIdx.x % (SW / W)) * W;       // first of its columns this block takes
-  const int kx0 = blockIdx.x * W;
+  const int s = blk / (SW / W);                      // row-pass strip
+  const int csel = (blk % (SW / W)) * W;              // first of its columns this block takes
+  const int kx0 = blk * W;
   const int pny = a.pny;
   if (tid == 0) {
     mbar_init(&mbar[0], 1);
@@ -293,7 +300,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
     for (int f = 0; f < RL; ++f) acc[kb][f] = make_float2(0.f, 0.f);
   if (EXT && !a.chunk_first) {
     // the accumulators of the earlier layer chunks
-    const C* accb = a.accbuf + (size_t)blockIdx.x * KB * RL * T + tid;
+    const C* accb = a.accbuf + (size_t)blk * KB * RL * T + tid;
 #pragma unroll
     for (int kb = 0; kb < KB; ++kb)
 #pragma unroll
@@ -439,7 +446,7 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
   if (EXT && !a.chunk_last) {
     // more layer chunks follow: hand the accumulators on (this chunk's
     // copies have all landed: the last layer's strip was waited for above)
-    C* accb = a.accbuf + (size_t)blockIdx.x * KB * RL * T + tid;
+    C* accb = a.accbuf + (size_t)blk * KB * RL * T + tid;
 #pragma unroll
     for (int kb = 0; kb < KB; ++kb)
 #pragma unroll
@@ -512,6 +519,19 @@ __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::M
     if (m < 0) m += NY;
     a.V[(size_t)yl * a.Px + kx0 + w] = cmul(buf[pidx(m) * W + w], a.shy[yl]);
   }
+  if constexpr (PERSIST) {
+    __syncthreads();
+    if (tid == 0) {
+      mbar_inval(&mbar[0]);
+      mbar_inval(&mbar[1]);
+      mbar_inval(&mbar[2]);
+    }
+  }
+}
+
+template <int NY, int W, bool STEP, bool SSB = false, bool EXT = false>
+__global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::MINB) dm_col_fast(DMArgs<float> a) {
+  dm_col_body<NY, W, STEP, SSB, EXT, 0, false>(a, blockIdx.x);
 }
 
 }  // namespace oh

@@ -63,7 +63,7 @@ __device__ __forceinline__ bool stall_on_unset_flag(const int* flag, long long c
   return true;
 }
 // kernel_mask bits of oh_ctx_set_test_stall
-constexpr int kStallDepthmapColumn = 1, kStallPointSumGemm = 2, kStallConvolution = 4;
+constexpr int kStallDepthmapColumn = 1, kStallPointSumGemm = 2, kStallConvolution = 4, kStallDepthmapBatch = 8;
 
 // Launch accounting (read through oh_kernel_launch_count()).
 void note_launch(int n = 1);
