@@ -509,6 +509,11 @@ def _sec_batch(ctx, dev, torch, out, reps, warmup):
         return a.elapsed_time(b) / reps, (launch_count() - n0) / reps
 
     ms_pf, k_pf = run(0)
+    with torch.cuda.stream(stream):
+        t0 = time.perf_counter()
+        dm.autotune_batch(ctx, frames, reps=2, stream=stream)
+        stream.synchronize()
+        tune_s = time.perf_counter() - t0
     ms, kernels = run(1)
     out["batch_64_frames_mixed_per_frame_launches"] = {
         "ms_per_batch": ms_pf, "frames_per_s": len(work) * 1000.0 / ms_pf, "kernels_per_batch": k_pf,
@@ -518,6 +523,7 @@ def _sec_batch(ctx, dev, torch, out, reps, warmup):
         "ms_per_batch": ms, "frames_per_s": len(work) * 1000.0 / ms,
         "model_bytes_per_batch": model, "model_gbs": model / (ms * 1e-3) / 1e9,
         "kernels_per_batch": kernels,
+        "autotune": {"seconds": tune_s, **{str(n): dm.batch_tuning(ctx, n) for n in (1024, 1536, 2048, 3072, 4096)}},
         "roofline": {"bound": "hbm", "unit": "GB/s", "achieved": model / (ms * 1e-3) / 1e9,
                      "peak": load_peaks()[0], "frac": model / (ms * 1e-3) / 1e9 / load_peaks()[0],
                      "peak_source": load_peaks()[1],

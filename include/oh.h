@@ -222,6 +222,33 @@ oh_status oh_depthmap_generate_batch(oh_ctx* ctx, oh_precision prec,
                                      const oh_depthmap_frame* frames, int n_frames,
                                      unsigned flags, void* stream);
 
+/* Autotuner of the persistent batch kernel (no reference counterpart).  For
+ * each padded length the kernel carries that has square frames in `frames`
+ * (same rules as oh_depthmap_generate_batch), times those frames as a batch
+ * `reps` times per candidate and keeps the fastest settings: blocks per SM
+ * (1, 2), pipeline lag between a frame's passes (0, 1), columns per column
+ * block (1, 2), row pairs per row item (1, 2, 4), column blocks per column
+ * item (1, 2) and output rows per output item (1, 2, 4, 8), by coordinate
+ * descent from the current entry (a change must gain 1 %).  Entries are kept
+ * per (padded length, compute capability, SM count) in the context, used by
+ * every later batch, and written to the tune file when one is set.  The
+ * frames' outputs hold the last trial's results (equal to a normal run's).
+ * The FFT radix order is not a tuning parameter: the fused passes fix it
+ * (radix-16 first stage over the zero half, a last stage of 256 butterflies
+ * per row). */
+oh_status oh_depthmap_autotune_batch(oh_ctx* ctx, const oh_depthmap_frame* frames, int n, int reps,
+                                     void* stream);
+/* The settings batches of padded length padded_len use on the context's
+ * device: {blocks per SM, lag, column width, row pairs per item, column
+ * blocks per item, output rows per item}; *ms (nullable) = the tuned batch
+ * time, 0 for the defaults. */
+oh_status oh_depthmap_batch_tuning(oh_ctx* ctx, int padded_len, int settings[6], double* ms);
+/* Tune file: loads its entries (if the file exists) and makes later
+ * autotune calls rewrite it; NULL or "" sets no file.  One line per entry:
+ * key ctas_per_sm lag col_w row_pairs col_blocks out_rows ms. */
+oh_status oh_ctx_set_autotune_file(oh_ctx* ctx, const char* path);
+
+
 /* Layer index per depth byte (256 entries, 0 = no layer), exactly the
  * reference's binning (change_depth_quan_*, HologramGenerator_CPU.cpp:74-103)
  * and the z' of each level (dlevel_transform_).  z_out holds num_of_depth

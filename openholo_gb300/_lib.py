@@ -138,6 +138,9 @@ SIGNATURES = {
     "oh_ctx_set_test_stall": (_i, [_vp, _i, C.c_longlong]),
     "oh_ctx_set_depthmap_layer_limit": (_i, [_vp, C.c_size_t]),
     "oh_ctx_set_depthmap_batch_mode": (_i, [_vp, _i]),
+    "oh_depthmap_autotune_batch": (_i, [_vp, _vp, _i, _i, _vp]),
+    "oh_depthmap_batch_tuning": (_i, [_vp, _i, C.POINTER(_i), C.POINTER(_d)]),
+    "oh_ctx_set_autotune_file": (_i, [_vp, C.c_char_p]),
     "oh_measure_issue_peaks": (_i, [_i, C.POINTER(_d), C.POINTER(_d), C.POINTER(_d), C.POINTER(_d)]),
     "oh_conv2d_bf16": (_i, [_vp, _i, _i, _i, _i, _i, _i, _i, _vp, _i, _vp, _vp, _i, _vp, _i, _vp, _i, _vp]),
     "oh_conv2d_wgrad_bf16": (_i, [_vp, _i, _i, _i, _i, _i, _i, _vp, _i, _vp, _i, _vp, _vp]),

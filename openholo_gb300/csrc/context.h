@@ -36,7 +36,8 @@ struct oh_ctx {
   // persistent batch kernel: 0 off (per-frame launches); tuned settings per
   // (padded length, device) and the file they persist in (empty: none)
   int dm_batch_persistent = 1;
-  struct BatchTune { int ctas_per_sm = 2, row_pairs = 1, col_blocks = 1, out_rows = 2, lag = 1; double ms = 0; };
+  // col_w 0: the class's default column-block width
+  struct BatchTune { int ctas_per_sm = 2, lag = 1, col_w = 0, row_pairs = 1, col_blocks = 1, out_rows = 2; double ms = 0; };
   std::map<std::string, BatchTune> batch_tune;
   std::string tune_file;
   bool tune_loaded = false;

@@ -25,6 +25,7 @@
 // The 2x zero-padding (pad = 2) never materialises: padded rows are skipped
 // and padded columns are zeros written straight into shared memory.
 #include <algorithm>
+#include <cstdio>
 #include <cstdlib>
 #include <cmath>
 #include <cstring>
@@ -679,6 +680,24 @@ struct BatchSettings {
   oh_ctx::BatchTune per[kBatchNumLens];
 };
 
+static int batch_width(const BatchSettings& bs, int cls) {
+  const int w = bs.per[cls].col_w;
+  return w && batch_col_w_ok(cls, w) ? w : batch_col_w(cls);
+}
+
+// Shared memory of a column block of width w for this frame (the layer-step
+// form the batch kernel carries).
+static size_t batch_col_smem(const DMArgs<float>& a, int w) {
+  size_t b = 0;
+  with_fast_n(a.Py, [&](auto nc) {
+    constexpr int NY = decltype(nc)::value;
+    if constexpr (NY > 0)
+      b = (size_t)col_layout(col_len<NY>(), a.pny, w, kColStripW, true, a.occ_stride, a.n_entries,
+                             col_tab_entries<NY>()).total;
+  });
+  return b;
+}
+
 // Tuned settings for padded length len on the current device, or the
 // defaults.
 static oh_ctx::BatchTune batch_tune_for(oh_ctx* ctx, int len) {
@@ -698,7 +717,8 @@ static oh_status batch_plan_build(oh_ctx* ctx, const oh_depthmap_frame* frames, 
     maxR = std::max(maxR, fi[i].sz.R);
     maxV = std::max(maxV, fi[i].sz.V);
     maxO = std::max(maxO, fi[i].sz.occ);
-    smem = std::max({smem, fi[i].smem_row, fi[i].smem_col, fi[i].smem_out});
+    const int yc = batch_class(fi[i].a.Py);
+    smem = std::max({smem, fi[i].smem_row, batch_col_smem(fi[i].a, batch_width(bs, yc)), fi[i].smem_out});
     tables += (fi[i].sz.tables + 255) & ~(size_t)255;
     slots += (size_t)fi[i].a.n_uslots;
   }
@@ -722,11 +742,12 @@ static oh_status batch_plan_build(oh_ctx* ctx, const oh_depthmap_frame* frames, 
     const oh_ctx::BatchTune& tx = bs.per[xc];
     const oh_ctx::BatchTune& ty = bs.per[yc];
     const int npairs = (a.pny + kRowPair - 1) / kRowPair;
-    const int ncolb = batch_col_w(yc) == 1 ? a.Px : a.nstrips;
+    const int wc = batch_width(bs, yc);
+    const int ncolb = wc == 1 ? a.Px : a.nstrips;
     for (int b = 0; b < npairs; b += tx.row_pairs)
       rows[i].push_back(make_int4(i, kItemRow | xc << 4, b, std::min(tx.row_pairs, npairs - b)));
     for (int b = 0; b < ncolb; b += ty.col_blocks)
-      cols[i].push_back(make_int4(i, kItemCol | yc << 4, b, std::min(ty.col_blocks, ncolb - b)));
+      cols[i].push_back(make_int4(i, kItemCol | yc << 4 | (wc == 2) << 8, b, std::min(ty.col_blocks, ncolb - b)));
     for (int b = 0; b < a.pny; b += tx.out_rows)
       outs[i].push_back(make_int4(i, kItemOut | xc << 4, b, std::min(tx.out_rows, a.pny - b)));
     BatchFrame& F = bf[i];
@@ -800,6 +821,37 @@ static oh_status batch_plan_build(oh_ctx* ctx, const oh_depthmap_frame* frames, 
 // some frame is outside what the batch kernel carries (FP32 fast lengths of
 // kBatchLens, layer-step column form with the SSB crop, one layer buffer),
 // and the caller runs the per-frame launches instead.
+// Plans every frame; *ok = false when some frame is outside the batch kernel.
+static oh_status batch_frame_infos(oh_ctx* ctx, const oh_depthmap_frame* frames, int n, cudaStream_t st,
+                                   std::vector<FrameInfo<float>>* fi, bool* ok) {
+  fi->assign(n, FrameInfo<float>());
+  *ok = true;
+  for (int i = 0; i < n; ++i) {
+    const oh_depthmap_frame& f = frames[i];
+    OH_TRY((run_depthmap<float, 36>(ctx, &f.params, f.img, f.depth, f.phase, f.fringe, f.field, nullptr, st,
+                                    &(*fi)[i])));
+    const FrameInfo<float>& x = (*fi)[i];
+    if (batch_class(x.a.Px) < 0 || batch_class(x.a.Py) < 0 || !x.Wfast || !x.a.xs || x.nchunks != 1 ||
+        !batch_col_ok(x))
+      *ok = false;
+  }
+  return OH_OK;
+}
+
+// Settings of a batch: each class's tuned entry; the launch-wide ones from
+// the class with the most work.
+static BatchSettings batch_settings(oh_ctx* ctx, const std::vector<FrameInfo<float>>& fi) {
+  BatchSettings bs;
+  double best = -1.0;
+  for (int c = 0; c < kBatchNumLens; ++c) bs.per[c] = batch_tune_for(ctx, kBatchLens[c]);
+  std::vector<double> work(kBatchNumLens, 0.0);
+  for (const FrameInfo<float>& x : fi)
+    work[batch_class(std::max(x.a.Px, x.a.Py))] += (double)x.a.Px * x.a.Py * (x.a.n_entries + 1);
+  for (int c = 0; c < kBatchNumLens; ++c)
+    if (work[c] > best) { best = work[c]; bs.ctas_per_sm = bs.per[c].ctas_per_sm; bs.lag = bs.per[c].lag; }
+  return bs;
+}
+
 static oh_status batch_persistent(oh_ctx* ctx, const oh_depthmap_frame* frames, int n, unsigned flags,
                                   const std::string& key, cudaStream_t st, bool* handled) {
   *handled = false;
@@ -808,31 +860,17 @@ static oh_status batch_persistent(oh_ctx* ctx, const oh_depthmap_frame* frames, 
   const bool stall = (ctx->stall_mask & kStallDepthmapBatch) != 0;
   if (P && !P->eligible) return OH_OK;
   if (!P) {
-    std::vector<FrameInfo<float>> fi(n);
-    for (int i = 0; i < n; ++i) {
-      const oh_depthmap_frame& f = frames[i];
-      OH_TRY((run_depthmap<float, 36>(ctx, &f.params, f.img, f.depth, f.phase, f.fringe, f.field, nullptr, st,
-                                      &fi[i])));
-      const DMArgs<float>& a = fi[i].a;
-      const int xc = batch_class(a.Px), yc = batch_class(a.Py);
-      if (xc < 0 || yc < 0 || !fi[i].Wfast || !a.xs || fi[i].nchunks != 1 || fi[i].wcol != batch_col_w(yc) ||
-          !batch_col_ok(fi[i])) {
-        if (ctx->batch_plans.size() >= 16) ctx->batch_plans.clear();
-        std::unique_ptr<BatchPlan> no(new BatchPlan());
-        no->eligible = false;
-        ctx->batch_plans[key] = std::move(no);
-        return OH_OK;
-      }
+    std::vector<FrameInfo<float>> fi;
+    bool ok = false;
+    OH_TRY(batch_frame_infos(ctx, frames, n, st, &fi, &ok));
+    if (!ok) {
+      if (ctx->batch_plans.size() >= 16) ctx->batch_plans.clear();
+      std::unique_ptr<BatchPlan> no(new BatchPlan());
+      no->eligible = false;
+      ctx->batch_plans[key] = std::move(no);
+      return OH_OK;
     }
-    // settings: the tuned entry of the class with the most work
-    BatchSettings bs;
-    double best = -1.0;
-    for (int c = 0; c < kBatchNumLens; ++c) bs.per[c] = batch_tune_for(ctx, kBatchLens[c]);
-    std::vector<double> work(kBatchNumLens, 0.0);
-    for (int i = 0; i < n; ++i)
-      work[batch_class(std::max(fi[i].a.Px, fi[i].a.Py))] += (double)fi[i].a.Px * fi[i].a.Py * (fi[i].a.n_entries + 1);
-    for (int c = 0; c < kBatchNumLens; ++c)
-      if (work[c] > best) { best = work[c]; bs.ctas_per_sm = bs.per[c].ctas_per_sm; bs.lag = bs.per[c].lag; }
+    const BatchSettings bs = batch_settings(ctx, fi);
     std::unique_ptr<BatchPlan> np;
     OH_TRY(batch_plan_build(ctx, frames, n, fi, bs, st, &np));
     if (ctx->batch_plans.size() >= 16) ctx->batch_plans.clear();
@@ -868,6 +906,105 @@ static oh_status batch_persistent(oh_ctx* ctx, const oh_depthmap_frame* frames, 
   if (stall) { L.stall_flag = ctx->dev_err + 1; L.stall_cycles = ctx->stall_cycles; }
   KernelTimer kt(ctx, "dm_batch", st);
   return dm_batch_launch(L, st);
+}
+
+// ---- autotuner: per padded length and device, the batch kernel's blocks
+// per SM, pipeline lag, column-block width and item sizes, chosen by timing
+// the frames of that length (coordinate descent from the current entry;
+// a change must gain 1 %).  Entries persist in the context's tune file.
+
+static oh_status batch_trial(oh_ctx* ctx, const oh_depthmap_frame* frames, const std::vector<FrameInfo<float>>& fi,
+                             const BatchSettings& bs, int reps, cudaStream_t st, double* ms) {
+  std::unique_ptr<BatchPlan> P;
+  OH_TRY(batch_plan_build(ctx, frames, (int)fi.size(), fi, bs, st, &P));
+  auto run = [&]() -> oh_status {
+    OH_CUDA_TRY(cudaMemsetAsync(P->ctl, 0, P->ctl_bytes, st));
+    return dm_batch_launch(P->L, st);
+  };
+  OH_TRY(run());
+  cudaEvent_t a = nullptr, b = nullptr;
+  OH_CUDA_TRY(cudaEventCreate(&a));
+  OH_CUDA_TRY(cudaEventCreate(&b));
+  oh_status rs = OH_OK;
+  cudaEventRecord(a, st);
+  for (int r = 0; r < reps && rs == OH_OK; ++r) rs = run();
+  cudaEventRecord(b, st);
+  cudaError_t e = cudaEventSynchronize(b);
+  float t = 0.f;
+  if (rs == OH_OK && e == cudaSuccess) e = cudaEventElapsedTime(&t, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  OH_TRY(rs);
+  if (e != cudaSuccess) return cuda_fail(e, "autotune timing");
+  unsigned abort_word = 0;
+  OH_CUDA_TRY(cudaMemcpy(&abort_word, static_cast<unsigned*>(P->ctl) + 1, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  if (abort_word) return fail(OH_ERR_TIMEOUT, "batch kernel wait ran out while tuning");
+  *ms = (double)t / reps;
+  return OH_OK;
+}
+
+static oh_status tune_save(oh_ctx* ctx) {
+  if (ctx->tune_file.empty()) return OH_OK;
+  FILE* f = std::fopen(ctx->tune_file.c_str(), "w");
+  if (!f) return fail(OH_ERR_IO, "cannot write tune file " + ctx->tune_file);
+  std::fprintf(f, "# depth-map batch kernel settings: key ctas_per_sm lag col_w row_pairs col_blocks out_rows ms\n");
+  for (const auto& kv : ctx->batch_tune) {
+    const oh_ctx::BatchTune& t = kv.second;
+    std::fprintf(f, "%s %d %d %d %d %d %d %.6f\n", kv.first.c_str(), t.ctas_per_sm, t.lag, t.col_w, t.row_pairs,
+                 t.col_blocks, t.out_rows, t.ms);
+  }
+  std::fclose(f);
+  return OH_OK;
+}
+
+static oh_status batch_autotune(oh_ctx* ctx, const oh_depthmap_frame* frames, int n, int reps, cudaStream_t st) {
+  std::vector<FrameInfo<float>> fi;
+  bool ok = false;
+  OH_TRY(batch_frame_infos(ctx, frames, n, st, &fi, &ok));
+  if (!ok) return fail(OH_ERR_UNSUPPORTED_SIZE, "autotune: a frame is outside what the batch kernel carries");
+  for (int c = 0; c < kBatchNumLens; ++c) {
+    // the square frames of this length
+    std::vector<oh_depthmap_frame> sub;
+    std::vector<FrameInfo<float>> sfi;
+    for (int i = 0; i < n; ++i)
+      if (fi[i].a.Px == kBatchLens[c] && fi[i].a.Py == kBatchLens[c]) { sub.push_back(frames[i]); sfi.push_back(fi[i]); }
+    if (sub.empty()) continue;
+    oh_ctx::BatchTune cur = batch_tune_for(ctx, kBatchLens[c]);
+    auto settings = [&](const oh_ctx::BatchTune& t) {
+      BatchSettings bs;
+      for (int k = 0; k < kBatchNumLens; ++k) bs.per[k] = batch_tune_for(ctx, kBatchLens[k]);
+      bs.per[c] = t;
+      bs.ctas_per_sm = t.ctas_per_sm;
+      bs.lag = t.lag;
+      return bs;
+    };
+    double best = 0.0;
+    OH_TRY(batch_trial(ctx, sub.data(), sfi, settings(cur), reps, st, &best));
+    const int def_w = batch_col_w(c);
+    struct Knob { int oh_ctx::BatchTune::*field; std::vector<int> vals; };
+    const Knob knobs[] = {{&oh_ctx::BatchTune::ctas_per_sm, {1, 2}}, {&oh_ctx::BatchTune::lag, {0, 1}},
+                          {&oh_ctx::BatchTune::col_w, {def_w, 3 - def_w}}, {&oh_ctx::BatchTune::row_pairs, {1, 2, 4}},
+                          {&oh_ctx::BatchTune::col_blocks, {1, 2}}, {&oh_ctx::BatchTune::out_rows, {1, 2, 4, 8}}};
+    for (const Knob& kn : knobs) {
+      for (int v : kn.vals) {
+        oh_ctx::BatchTune t = cur;
+        const int now = cur.*(kn.field) ? cur.*(kn.field) : def_w;
+        if (v == now) continue;
+        if (kn.field == &oh_ctx::BatchTune::col_w && !batch_col_w_ok(c, v)) continue;
+        t.*(kn.field) = v;
+        double ms = 0.0;
+        oh_status rs = batch_trial(ctx, sub.data(), sfi, settings(t), reps, st, &ms);
+        if (rs == OH_ERR_UNSUPPORTED_SIZE) continue;        // e.g. a width whose shared memory does not fit
+        OH_TRY(rs);
+        if (ms < best * 0.99) { best = ms; cur = t; }
+      }
+    }
+    cur.ms = best;
+    ctx->batch_tune[tune_key(kBatchLens[c])] = cur;
+  }
+  OH_CUDA_TRY(cudaStreamSynchronize(st));
+  ctx->batch_plans.clear();             // later batches plan with the new settings
+  return tune_save(ctx);
 }
 
 }  // namespace oh
@@ -1035,6 +1172,74 @@ oh_status oh_depthmap_generate_batch(oh_ctx* ctx, oh_precision prec, const oh_de
   }
   if (g) cudaGraphDestroy(g);
   return rs;
+}
+
+oh_status oh_depthmap_autotune_batch(oh_ctx* ctx, const oh_depthmap_frame* frames, int n, int reps, void* stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  CallScope cs(ctx, st);
+  OH_TRY(cs.status());
+  if (n < 1 || !frames) return fail(OH_ERR_INVALID_ARG, "autotune: empty frame array");
+  if (reps < 1 || reps > 100) return fail(OH_ERR_INVALID_ARG, "autotune: reps must be 1..100");
+  for (int i = 0; i < n; ++i) {
+    OH_TRY(validate(&frames[i].params));
+    if (!frames[i].img || !frames[i].depth || !frames[i].fringe)
+      return fail(OH_ERR_INVALID_ARG, "frame " + std::to_string(i) + ": img, depth and fringe are required");
+    if (frames[i].params.phase_mode == OH_PHASE_ARRAY && !frames[i].phase)
+      return fail(OH_ERR_INVALID_ARG, "frame " + std::to_string(i) + ": OH_PHASE_ARRAY needs a phase array");
+  }
+  if (st) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    OH_CUDA_TRY(cudaStreamIsCapturing(st, &cap));
+    if (cap != cudaStreamCaptureStatusNone) return fail(OH_ERR_INVALID_ARG, "autotune: stream is capturing");
+  }
+  return batch_autotune(ctx, frames, n, reps, st);
+}
+
+oh_status oh_depthmap_batch_tuning(oh_ctx* ctx, int padded_len, int settings[6], double* ms) {
+  if (!ctx || !settings) return fail(OH_ERR_INVALID_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(ctx->device);
+  const oh_ctx::BatchTune t = batch_tune_for(ctx, padded_len);
+  cudaSetDevice(prev);
+  const int cls = batch_class(padded_len);
+  settings[0] = t.ctas_per_sm; settings[1] = t.lag; settings[2] = t.col_w ? t.col_w : (cls >= 0 ? batch_col_w(cls) : 0);
+  settings[3] = t.row_pairs; settings[4] = t.col_blocks; settings[5] = t.out_rows;
+  if (ms) *ms = t.ms;
+  return OH_OK;
+}
+
+oh_status oh_ctx_set_autotune_file(oh_ctx* ctx, const char* path) {
+  if (!ctx) return fail(OH_ERR_INVALID_ARG, "null context");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->tune_file = path ? path : "";
+  if (ctx->tune_file.empty()) return OH_OK;
+  FILE* f = std::fopen(ctx->tune_file.c_str(), "r");
+  if (!f) return OH_OK;                  // written by the first autotune
+  char line[512];
+  while (std::fgets(line, sizeof(line), f)) {
+    if (line[0] == '#') continue;
+    char key[256];
+    oh_ctx::BatchTune t;
+    if (std::sscanf(line, "%255s %d %d %d %d %d %d %lf", key, &t.ctas_per_sm, &t.lag, &t.col_w, &t.row_pairs,
+                    &t.col_blocks, &t.out_rows, &t.ms) != 8 ||
+        t.ctas_per_sm < 1 || t.ctas_per_sm > 2 || t.lag < 0 || t.lag > 1 || t.col_w < 0 || t.col_w > 2 ||
+        t.row_pairs < 1 || t.row_pairs > 64 || t.col_blocks < 1 || t.col_blocks > 64 || t.out_rows < 1 ||
+        t.out_rows > 64) {
+      std::fclose(f);
+      return fail(OH_ERR_IO, "malformed tune file line: " + std::string(line));
+    }
+    ctx->batch_tune[key] = t;
+  }
+  std::fclose(f);
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(ctx->device);
+  cudaDeviceSynchronize();               // plans built with the old settings may still run
+  ctx->batch_plans.clear();
+  cudaSetDevice(prev);
+  return OH_OK;
 }
 
 oh_status oh_depthmap_generate_host(oh_ctx* ctx, oh_precision prec, const oh_depthmap_params* p,

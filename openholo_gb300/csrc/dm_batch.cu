@@ -38,11 +38,11 @@ __device__ __forceinline__ void run_row(const DMArgs<float>& a, int first, int c
     dm_row_body<float, kBatchLens[C], kBatchThreads>(a, b);
   }
 }
-template <int C>
+template <int C, int W>
 __device__ __forceinline__ void run_col(const DMArgs<float>& a, int first, int count) {
   for (int b = first; b < first + count; ++b) {
     if (b > first) __syncthreads();
-    dm_col_body<kBatchLens[C], batch_col_w(C), true, true, false, kBatchThreads, true>(a, b);
+    dm_col_body<kBatchLens[C], W, true, true, false, kBatchThreads, true>(a, b);
   }
 }
 template <int C>
@@ -116,23 +116,16 @@ __global__ void __launch_bounds__(kBatchThreads, 2) dm_batch_kernel(BatchLaunch 
       for (int i = tid; i < (int)(sizeof(DMArgs<float>) / 16); i += kBatchThreads) dst[i] = src[i];
       __syncthreads();
     }
-    const int kind = it.y & 15, cls = it.y >> 4;
-    switch (kind * 8 + cls) {
-      case 0: run_row<0>(a, it.z, it.w); break;
-      case 1: run_row<1>(a, it.z, it.w); break;
-      case 2: run_row<2>(a, it.z, it.w); break;
-      case 3: run_row<3>(a, it.z, it.w); break;
-      case 4: run_row<4>(a, it.z, it.w); break;
-      case 8: run_col<0>(a, it.z, it.w); break;
-      case 9: run_col<1>(a, it.z, it.w); break;
-      case 10: run_col<2>(a, it.z, it.w); break;
-      case 11: run_col<3>(a, it.z, it.w); break;
-      case 12: run_col<4>(a, it.z, it.w); break;
-      case 16: run_out<0>(a, it.z, it.w); break;
-      case 17: run_out<1>(a, it.z, it.w); break;
-      case 18: run_out<2>(a, it.z, it.w); break;
-      case 19: run_out<3>(a, it.z, it.w); break;
-      case 20: run_out<4>(a, it.z, it.w); break;
+    const int kind = it.y & 15;
+    switch (it.y >> 4) {              // class | two-column blocks << 4
+      case 0x00: kind == kItemRow ? run_row<0>(a, it.z, it.w) : kind == kItemCol ? run_col<0, 1>(a, it.z, it.w) : run_out<0>(a, it.z, it.w); break;
+      case 0x01: kind == kItemRow ? run_row<1>(a, it.z, it.w) : kind == kItemCol ? run_col<1, 1>(a, it.z, it.w) : run_out<1>(a, it.z, it.w); break;
+      case 0x02: kind == kItemRow ? run_row<2>(a, it.z, it.w) : kind == kItemCol ? run_col<2, 1>(a, it.z, it.w) : run_out<2>(a, it.z, it.w); break;
+      case 0x03: kind == kItemRow ? run_row<3>(a, it.z, it.w) : kind == kItemCol ? run_col<3, 1>(a, it.z, it.w) : run_out<3>(a, it.z, it.w); break;
+      case 0x04: kind == kItemRow ? run_row<4>(a, it.z, it.w) : kind == kItemCol ? run_col<4, 1>(a, it.z, it.w) : run_out<4>(a, it.z, it.w); break;
+      case 0x10: run_col<0, 2>(a, it.z, it.w); break;
+      case 0x11: run_col<1, 2>(a, it.z, it.w); break;
+      case 0x12: run_col<2, 2>(a, it.z, it.w); break;
       default: break;
     }
     // shared memory written by generic stores here may be filled by bulk

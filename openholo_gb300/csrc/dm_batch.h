@@ -26,9 +26,14 @@ namespace oh {
 constexpr int kBatchLens[] = {1024, 1536, 2048, 3072, 4096};
 constexpr int kBatchNumLens = 5;
 constexpr int kBatchThreads = 256;
-// Columns per column block for each class: one-column blocks over the
-// two-column strips at 3072 and 4096 (as the per-frame pass picks there).
+// Default columns per column block for each class: one-column blocks over
+// the two-column strips at 3072 and 4096 (as the per-frame pass picks
+// there), whole strips below.  The autotuner may pick the other width.
 __host__ __device__ constexpr int batch_col_w(int cls) { return cls >= 3 ? 1 : 2; }
+// Widths the kernel carries: both below 3072; one column at 3072 and 4096,
+// where a two-column block would need 136-178 KB of shared memory (one block
+// per SM) and spill its accumulators at 256 threads.
+__host__ __device__ constexpr bool batch_col_w_ok(int cls, int w) { return w == 1 || (w == 2 && cls < 3); }
 
 enum : int { kItemRow = 0, kItemCol = 1, kItemOut = 2 };
 
@@ -43,7 +48,8 @@ struct alignas(16) BatchFrame {
 static_assert(sizeof(DMArgs<float>) % 16 == 0, "frame arguments are copied as int4 words");
 static_assert(sizeof(BatchFrame) % 16 == 0, "frame records keep 16-byte alignment");
 
-// Item: x = frame, y = kind | class << 4, z = first block, w = blocks.
+// Item: x = frame, y = kind | class << 4 | (column blocks of two columns) << 8,
+// z = first block, w = blocks.
 struct BatchLaunch {
   const BatchFrame* frames;
   const int4* items;

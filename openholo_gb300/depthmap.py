@@ -97,6 +97,12 @@ def generate_batch(ctx: _lib.Context, frames, precision="fp32", graph=False, str
     captures the batch into a CUDA graph on the first call and replays it on
     later calls with the same frames (same parameters and tensors)."""
     prec = OH_FP64 if precision == "fp64" else OH_FP32
+    arr = _frame_array(frames)
+    _lib.call("oh_depthmap_generate_batch", ctx.handle, prec, arr, len(frames),
+              _lib.BATCH_GRAPH if graph else 0, _stream_ptr(stream))
+
+
+def _frame_array(frames):
     arr = (_lib.DepthmapFrame * len(frames))()
     for i, fr in enumerate(frames):
         p, img, depth, fringe = fr[:4]
@@ -107,8 +113,35 @@ def generate_batch(ctx: _lib.Context, frames, precision="fp32", graph=False, str
         arr[i].phase = phase.data_ptr() if phase is not None else None
         arr[i].fringe = fringe.data_ptr()
         arr[i].field = None
-    _lib.call("oh_depthmap_generate_batch", ctx.handle, prec, arr, len(frames),
-              _lib.BATCH_GRAPH if graph else 0, _stream_ptr(stream))
+    return arr
+
+
+def set_batch_mode(ctx: _lib.Context, persistent: bool):
+    """True: batches the persistent kernel carries run as one launch of it
+    (the default); False: every batch runs as per-frame launches."""
+    _lib.call("oh_ctx_set_depthmap_batch_mode", ctx.handle, 1 if persistent else 0)
+
+
+def autotune_batch(ctx: _lib.Context, frames, reps=2, stream=None):
+    """Tune the persistent batch kernel on the square frames of `frames`
+    (oh_depthmap_autotune_batch); later batches on ctx use the result."""
+    arr = _frame_array(frames)
+    _lib.call("oh_depthmap_autotune_batch", ctx.handle, arr, len(frames), reps, _stream_ptr(stream))
+
+
+BATCH_SETTINGS = ("ctas_per_sm", "lag", "col_w", "row_pairs", "col_blocks", "out_rows")
+
+
+def batch_tuning(ctx: _lib.Context, padded_len: int) -> dict:
+    """Settings batches of this padded length use (oh_depthmap_batch_tuning)."""
+    v = (C.c_int * 6)()
+    ms = C.c_double()
+    _lib.call("oh_depthmap_batch_tuning", ctx.handle, padded_len, v, C.byref(ms))
+    return {**dict(zip(BATCH_SETTINGS, list(v))), "ms": ms.value}
+
+
+def set_autotune_file(ctx: _lib.Context, path):
+    _lib.call("oh_ctx_set_autotune_file", ctx.handle, None if path is None else str(path).encode())
 
 
 def generate_host(ctx: _lib.Context, p: DepthmapParams, img: np.ndarray, depth: np.ndarray,

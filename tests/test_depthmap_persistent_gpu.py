@@ -35,7 +35,7 @@ def _frames(seed, spec=FRAMES):
 
 
 def _mode(ctx, persistent):
-    _lib.call("oh_ctx_set_depthmap_batch_mode", ctx.handle, persistent)
+    dm.set_batch_mode(ctx, bool(persistent))
 
 
 def S():
@@ -135,3 +135,41 @@ def test_persistent_batch_wait_runs_out(ctx):
     assert _lib.lib().oh_ctx_device_status(ctx.handle, S()) == 0
     for p, img, depth, fr in frames:
         assert torch.equal(fr, dm.generate(ctx, p, img, depth))
+
+
+def test_autotune_batch(ctx, tmp_path):
+    # two frames of each of two lengths; the tune file keeps the entries
+    spec = [(512, 512, 6, 532e-9), (512, 512, 9, 633e-9), (768, 768, 5, 450e-9), (768, 768, 7, 532e-9),
+            (512, 2048, 4, 532e-9)]
+    frames = _frames(110, spec)
+    path = tmp_path / "tune.txt"
+    dm.set_autotune_file(ctx, path)
+    dm.set_batch_mode(ctx, True)
+    dm.autotune_batch(ctx, frames, reps=1)
+    torch.cuda.synchronize()
+    lines = [l.split() for l in path.read_text().splitlines() if not l.startswith("#")]
+    keys = {l[0].rsplit(":", 1)[1] for l in lines}
+    assert {"1024", "1536"} <= keys
+    for L in (1024, 1536):
+        t = dm.batch_tuning(ctx, L)
+        assert t["ctas_per_sm"] in (1, 2) and t["lag"] in (0, 1) and t["col_w"] in (1, 2)
+        assert t["row_pairs"] in (1, 2, 4) and t["col_blocks"] in (1, 2) and t["out_rows"] in (1, 2, 4, 8)
+        assert t["ms"] > 0
+    # a batch after tuning still equals the per-frame path
+    n0 = launch_count()
+    dm.generate_batch(ctx, frames)
+    torch.cuda.synchronize()
+    assert launch_count() - n0 == 2                # table set-up + batch kernel (new plan)
+    for p, img, depth, fr in frames:
+        assert torch.equal(fr, dm.generate(ctx, p, img, depth))
+    # another context reads the same settings from the file
+    other = _lib.Context(0)
+    dm.set_autotune_file(other, path)
+    try:
+        for L in (1024, 1536):
+            a, b = dm.batch_tuning(other, L), dm.batch_tuning(ctx, L)
+            assert a.pop("ms") == pytest.approx(b.pop("ms"), rel=1e-5)
+            assert a == b
+    finally:
+        other.close()
+    dm.set_autotune_file(ctx, None)
