@@ -427,8 +427,21 @@ static oh_status run_depthmap(oh_ctx* ctx, const oh_depthmap_params* p, const ui
     const bool ext_mode = (ctx->stall_mask & kStallDepthmapColumn) != 0 || nchunks > 1;
     if (narrow && !(ev && std::atoi(ev) == 0) && !ext_mode && !two_fit(2) && two_fit(1)) wcol = 1;
   }
+  // the column pass's two-buffer pipeline (its layer-step SSB form without
+  // layer chunks or the test hook, at the lengths where it keeps two blocks
+  // per SM): the kernel decides the same way at compile time
+  bool col_p2 = false;
+  if (Wfast && a.horner) {
+    const bool ext_mode = (ctx->stall_mask & kStallDepthmapColumn) != 0 || nchunks > 1;
+    with_fast_n(a.Py, [&](auto nc) {
+      constexpr int NY = decltype(nc)::value;
+      if constexpr (NY > 0)
+        col_p2 = a.fkeep == col_ssb_keep<NY>() && !ext_mode && (wcol == 2 ? col_pipe2<NY, 2>() : col_pipe2<NY, 1>());
+    });
+  }
   const size_t smem_col =
-      Wfast ? (size_t)col_layout(col_py, a.pny, wcol, kColStripW, a.horner != 0, occ_stride, su.n_entries, col_tab).total
+      Wfast ? (size_t)col_layout(col_py, a.pny, wcol, kColStripW, a.horner != 0, occ_stride, su.n_entries, col_tab,
+                                 col_p2).total
             : (size_t)W * a.Py * sizeof(C) + W * (sizeof(C) + sizeof(R)) + (size_t)a.Py * sizeof(int);
   int row_tab = 0, row_ls = a.Px;
   with_fast_n_if<sizeof(R) == 4>(a.Px, [&](auto nc) {

@@ -30,7 +30,7 @@
 namespace oh {
 
 struct ColLayout {
-  int buf, stg, ey0, ey1, occ, g, twlo, twhi, tab, exw, lfxw, list, mbar, total;
+  int buf, stg, ey0, ey1, occ, g, twlo, twhi, tab, exw, lfxw, list, mbar, stg1, occ1, total;
 };
 
 // Twiddle-table entries of the middle forward stage of the column FFT
@@ -53,9 +53,11 @@ __host__ __device__ constexpr int col_take(int* o, int bytes) {
 
 // W: spectrum columns a block transforms; sw: columns per strip of the row
 // pass output (the staging buffer holds a whole strip); step: the layer-step
-// variant (its region holds D, float2 per element, instead of g and two Ey rows)
+// variant (its region holds D, float2 per element, instead of g and two Ey
+// rows); pipe2: the two-buffer pipeline (see dm_col_body), whose step region
+// is the second work buffer, plus a second staging buffer and flag row
 __host__ __device__ constexpr ColLayout col_layout(int Py, int pny, int W, int sw, bool step, int occ_stride,
-                                                   int n_entries, int tab_entries) {
+                                                   int n_entries, int tab_entries, bool pipe2 = false) {
   ColLayout L{};
   int o = 0;
   L.buf = col_take(&o, Py * W * 8);
@@ -72,6 +74,8 @@ __host__ __device__ constexpr ColLayout col_layout(int Py, int pny, int W, int s
   L.lfxw = col_take(&o, W * 4);
   L.list = col_take(&o, n_entries * 2 + 2);
   L.mbar = col_take(&o, 24);
+  L.stg1 = pipe2 ? col_take(&o, pny * sw * 8) : 0;
+  L.occ1 = pipe2 ? col_take(&o, occ_stride) : 0;
   L.total = o;
   return L;
 }
@@ -121,6 +125,28 @@ template <int NY, int W, bool STEP, int TT = 0> struct ColCfg {
   static constexpr int MINB = FIT >= 3 && T <= 256 ? 3 : (FIT >= 2 ? 2 : 1);
 };
 
+// The two-buffer pipeline (layer-step form with the SSB crop): taken where
+// it keeps two blocks per SM and the one-buffer kernel has two as well (2x
+// padding, up to kMaxEntries render entries).
+template <int NY, int W> constexpr bool col_pipe2() {
+  constexpr int pny = NY / 2;
+  constexpr int total = col_layout(col_len<NY>(), pny, W, kColStripW, true, (pny + 15) & ~15, kMaxEntries,
+                                   col_tab_entries<NY>(), true).total;
+  return ColCfg<NY, W, true>::MINB == 2 && 2 * (total + 1024 + 512) <= 228 * 1024;
+}
+
+// The step factor D = H(z' - dz) / H(z') = Dx(fx) Dy(fy) exp(-i k dz g) of
+// one spectrum element, g = s^2 / (2 (1 + sqrt(1 - s))^2), s = (lambda fx)^2
+// + (lambda fy)^2 (one expression for every variant, so they agree bit for bit).
+__device__ __forceinline__ float2 col_step_factor(float2 dx, float2 dy, float lfx, float lfy, float kdz_pi) {
+  const float sv = lfx + lfy;
+  const float den = 1.f + sqrtf(1.f - sv);
+  const float g = sv * sv * __fdividef(0.5f, den * den);
+  float sn, cs;
+  sincospif(-kdz_pi * g, &sn, &cs);
+  return cmul(cmul(dx, dy), make_float2(cs, sn));
+}
+
 // One-column blocks (W = 1) over two-column strips, for the lengths where a
 // two-column block's shared memory leaves one block per SM and the second
 // read of each strip still hits L2 (measured faster at 3072 to 4096; at 4096
@@ -152,8 +178,15 @@ template <int NY> constexpr uint32_t col_ssb_keep() {
 // Block body for column block blk (a strip, or one column of a strip when
 // W = 1).  TT: see ColCfg.  PERSIST: the block goes on to other work after
 // this one, so its mbarriers are invalidated at the end.
-template <int NY, int W, bool STEP, bool SSB, bool EXT, int TT, bool PERSIST>
+// PIPE2 (layer-step form with the SSB crop): two work buffers and two
+// staging buffers.  Layer k's last stage and layer k+1's stage 0 share one
+// barrier phase (they use different work buffers), so a layer takes two
+// block barriers instead of three; the strip of layer k+2 is requested as
+// soon as stage 0 of layer k has read its buffer; the step factors of the
+// thread's own outputs are held in registers.
+template <int NY, int W, bool STEP, bool SSB, bool EXT, int TT, bool PERSIST, bool PIPE2 = false>
 __device__ __forceinline__ void dm_col_body(const DMArgs<float>& a, int blk) {
+  static_assert(!PIPE2 || (STEP && SSB && !EXT), "the two-buffer pipeline is the layer-step SSB form");
   typedef float2 C;
   typedef ColCfg<NY, W, STEP, TT> CF;
   constexpr int SW = kColStripW;
@@ -167,7 +200,7 @@ __device__ __forceinline__ void dm_col_body(const DMArgs<float>& a, int blk) {
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int kTab = col_tab_entries<NY>();
   constexpr int R1 = FastSched<NY>::r1;
-  const ColLayout Lo = col_layout(col_len<NY>(), a.pny, W, SW, STEP, a.occ_stride, a.n_entries, kTab);
+  const ColLayout Lo = col_layout(col_len<NY>(), a.pny, W, SW, STEP, a.occ_stride, a.n_entries, kTab, PIPE2);
   // padded layout (see col_padded): element p at p + p / RL
   constexpr bool PADL = col_padded<NY>();
   constexpr int RLP = PADL ? RL + 1 : RL;                     // stored length of RL elements
@@ -244,6 +277,16 @@ __device__ __forceinline__ void dm_col_body(const DMArgs<float>& a, int blk) {
     bulk_g2s(stg, a.Rbuf + ((size_t)u * a.nstrips + s) * pny * SW, strip_bytes, &mbar[0]);
     bulk_g2s(occ, a.occ + (size_t)u * a.occ_stride, (uint32_t)a.occ_stride, &mbar[0]);
   };
+  // PIPE2: strip j goes to staging buffer j & 1 on mbar[j & 1]
+  C* const stg1 = reinterpret_cast<C*>(smem + Lo.stg1);
+  uint8_t* const occ1 = smem + Lo.occ1;
+  auto issue_strip2 = [&](int j) {
+    const int u = a.uslot_of_entry[list[j]];
+    uint64_t* const bar = &mbar[j & 1];
+    mbar_expect_tx(bar, strip_bytes + (uint32_t)a.occ_stride);
+    bulk_g2s((j & 1) ? stg1 : stg, a.Rbuf + ((size_t)u * a.nstrips + s) * pny * SW, strip_bytes, bar);
+    bulk_g2s((j & 1) ? occ1 : occ, a.occ + (size_t)u * a.occ_stride, (uint32_t)a.occ_stride, bar);
+  };
   auto issue_ey = [&](int k) {
     const int e = list[k];
     uint64_t* bar = (k & 1) ? &mbar[2] : &mbar[1];
@@ -253,6 +296,7 @@ __device__ __forceinline__ void dm_col_body(const DMArgs<float>& a, int blk) {
   // the first layer's copies fly while the tables below are built
   if (tid == 0 && nact > 0) {
     issue_strip(0);
+    if (PIPE2 && nact > 1) issue_strip2(1);
     if (!horner) issue_ey(0);
   }
 
@@ -263,7 +307,7 @@ __device__ __forceinline__ void dm_col_body(const DMArgs<float>& a, int blk) {
   // the fy terms of kDB elements before using them.
   C* const dsm = reinterpret_cast<C*>(smem + Lo.g);
   constexpr int kDB = 4;
-  for (int i0 = tid; i0 < NY * W; i0 += kDB * T) {
+  for (int i0 = tid; i0 < (PIPE2 ? 0 : NY * W); i0 += kDB * T) {
     float lfy[kDB];
     C dyv[kDB];
 #pragma unroll
@@ -278,15 +322,12 @@ __device__ __forceinline__ void dm_col_body(const DMArgs<float>& a, int blk) {
       const int idx = i0 + q * T;
       if (idx >= NY * W) break;
       const int p = idx / W, w = idx - p * W;
-      const float sv = lfxw[w] + lfy[q];
-      const float den = 1.f + sqrtf(1.f - sv);
-      const float g = sv * sv * __fdividef(0.5f, den * den);
       if constexpr (horner) {
-        float sn, cs;
-        sincospif(-a.kdz_pi * g, &sn, &cs);
-        dsm[pidx(p) * W + w] = cmul(cmul(dxw[w], dyv[q]), make_float2(cs, sn));
+        dsm[pidx(p) * W + w] = col_step_factor(dxw[w], dyv[q], lfxw[w], lfy[q], a.kdz_pi);
       } else {
-        gsm[pidx(p) * W + w] = g;
+        const float sv = lfxw[w] + lfy[q];
+        const float den = 1.f + sqrtf(1.f - sv);
+        gsm[pidx(p) * W + w] = sv * sv * __fdividef(0.5f, den * den);
       }
     }
   }
@@ -320,125 +361,247 @@ __device__ __forceinline__ void dm_col_body(const DMArgs<float>& a, int blk) {
     }
   }
 
-  for (int k = 0; k < nact; ++k) {
-    // one barrier: layer k's strip and Ey have landed, and the previous
-    // layer's last stage no longer reads the work buffer
-    uint64_t* const bar_e = (k & 1) ? &mbar[2] : &mbar[1];
-    bool ok = mbar_wait_bounded(&mbar[0], (uint32_t)(k & 1));
-    ok = ok && (horner || mbar_wait_bounded(bar_e, (uint32_t)((k >> 1) & 1)));
-    if (__syncthreads_or(!ok)) {
-      if (tid == 0) atomicOr(a.err, 1);
-      // let this block's copies still in flight land before leaving
-      mbar_wait_bounded(&mbar[0], (uint32_t)(k & 1));
-      if (!horner) mbar_wait_bounded(bar_e, (uint32_t)((k >> 1) & 1));
-      return;
-    }
-    if (tid == 0 && k + 1 < nact && !horner) {
-      // Ey buffer (k+1)&1 was last read by layer k-1, finished before the barrier
-      fence_proxy_async_smem();
-      issue_ey(k + 1);
-    }
-    const int e = list[k];
-    if (tid < W && !horner) exw[tid] = a.exc[(size_t)e * a.Px + kxw[tid]];
-    const int gap = e - list[k - 1];
-    if constexpr (horner) {
-      // layers without pixels since the previous one: acc D^(gap - 1)
-      for (int r = 1; r < gap; ++r) {
-#pragma unroll
-        for (int kb = 0; kb < KB; ++kb) {
-          const int bb = tid + kb * T;
-          if (bb < CF::NBL) {
-            const int b = bb / W, w = bb - b * W;
-#pragma unroll
-            for (int f = 0; f < RL; ++f) acc[kb][f] = cmul(acc[kb][f], dsm[(b * RLP + f) * W + w]);
-          }
-        }
-      }
-    }
-    // stage 0 from the staging buffer: inputs j + t*Q0 of the y-shifted line
-    for (int idx = tid; idx < Q0 * W; idx += T) {
-      const int j = idx / W, w = idx - j * W;
-      C x[R0];
-      if (R0 == 16 && a.hzy) {
-        // 2x padding: inputs t = 4..11 are rows of the zero band; with
-        // hy = NY/2 and oy = NY/4 the image row of input t is
-        // j + (t + 4) Q0 (t < 4) or j + (t - 12) Q0 (t >= 12)
-#pragma unroll
-        for (int t = 0; t < R0; ++t) {
-          if (t >= 4 && t < 12) { x[t] = make_float2(0.f, 0.f); continue; }
-          const int yl = j + (t < 4 ? t + 4 : t - 12) * Q0;
-          x[t] = occ[yl] ? stg[yl * SW + csel + w] : make_float2(0.f, 0.f);
-        }
-        dft16_halfzero<-1>(x);
-      } else {
-#pragma unroll
-        for (int t = 0; t < R0; ++t) {
-          int y = j + t * Q0 - a.hy;
-          if (y < 0) y += NY;
-          const int yl = y - a.oy;
-          C v = make_float2(0.f, 0.f);
-          if (yl >= 0 && yl < pny && occ[yl]) v = stg[yl * SW + csel + w];
-          x[t] = v;
-        }
-        DFT<R0, -1, C>::run(x);
-      }
-      if (j) {
-        C wp[R0];
-        twiddle_powers<R0, -1>(tw, j, wp);
-#pragma unroll
-        for (int f = 1; f < R0; ++f) x[f] = cmul(x[f], wp[f]);
-      }
-#pragma unroll
-      for (int f = 0; f < R0; ++f) buf[(pidx(j) + f * Q0P) * W + w] = x[f];
-    }
-    // middle stage(s); the leading barrier also frees the strip buffer
-    __syncthreads();
-    if (tid == 0 && k + 1 < nact) {
-      fence_proxy_async_smem();
-      issue_strip(k + 1);
-    }
-    static_assert(kTab > 0 || !PADL, "the padded layout needs the middle stage's table");
-    if constexpr (kTab > 0) fstage_tab<NY, R1, M1, -1, C, M1P, RLP>(buf, W, 1, W, tab1, true);
-    else fstage_t<NY, R1, NY / R0, -1>(buf, W, 1, W, tw, true);
-    __syncthreads();
-    // last stage (stride 1, no twiddles) fused with the transfer-function
-    // multiply-accumulate: either acc += H x per layer, or the recurrence
-    // acc = acc D^gap + x over the evenly spaced layers (H of the last layer
-    // applied once in the epilogue)
-    const float kz = a.kzp[e];
-    const float* eth = (k & 1) ? ey1 : ey0;       // storage order
-    const float inv2pi = 0.15915494309189533577f, two_pi = 6.28318530717958647692f;
+  if constexpr (PIPE2) {
+    C* const buf1 = reinterpret_cast<C*>(smem + Lo.g);
+    // step factors of this thread's kept outputs
+    C dreg[KB][RL];
 #pragma unroll
     for (int kb = 0; kb < KB; ++kb) {
       const int bb = tid + kb * T;
-      if (bb < CF::NBL) {
-        const int b = bb / W, w = bb - b * W;
-        C x[RL];
 #pragma unroll
-        for (int f = 0; f < RL; ++f) x[f] = buf[(b * RLP + f) * W + w];
-        DFT<RL, -1, C>::run(x);
-        if constexpr (horner) {
+      for (int f = 0; f < RL; ++f) {
+        dreg[kb][f] = make_float2(0.f, 0.f);
+        if (bb < CF::NBL && ((fkeep >> f) & 1u)) {
+          const int b = bb / W, w = bb - b * W, p = b * RL + f;
+          dreg[kb][f] = col_step_factor(dxw[w], a.dyh[p], lfxw[w], a.lfyp[p], a.kdz_pi);
+        }
+      }
+    }
+    // stage 0 of one layer from staging buffer (sg, oc) into work buffer bf
+    auto stage0 = [&](const C* sg, const uint8_t* oc, C* bf) {
+      for (int idx = tid; idx < Q0 * W; idx += T) {
+        const int j = idx / W, w = idx - j * W;
+        C x[R0];
+        if (R0 == 16 && a.hzy) {
+#pragma unroll
+          for (int t = 0; t < R0; ++t) {
+            if (t >= 4 && t < 12) { x[t] = make_float2(0.f, 0.f); continue; }
+            const int yl = j + (t < 4 ? t + 4 : t - 12) * Q0;
+            x[t] = oc[yl] ? sg[yl * SW + csel + w] : make_float2(0.f, 0.f);
+          }
+          dft16_halfzero<-1>(x);
+        } else {
+#pragma unroll
+          for (int t = 0; t < R0; ++t) {
+            int y = j + t * Q0 - a.hy;
+            if (y < 0) y += NY;
+            const int yl = y - a.oy;
+            C v = make_float2(0.f, 0.f);
+            if (yl >= 0 && yl < pny && oc[yl]) v = sg[yl * SW + csel + w];
+            x[t] = v;
+          }
+          DFT<R0, -1, C>::run(x);
+        }
+        if (j) {
+          C wp[R0];
+          twiddle_powers<R0, -1>(tw, j, wp);
+#pragma unroll
+          for (int f = 1; f < R0; ++f) x[f] = cmul(x[f], wp[f]);
+        }
+#pragma unroll
+        for (int f = 0; f < R0; ++f) bf[(pidx(j) + f * Q0P) * W + w] = x[f];
+      }
+    };
+    auto middle = [&](C* bf) {
+      if constexpr (kTab > 0) fstage_tab<NY, R1, M1, -1, C, M1P, RLP>(bf, W, 1, W, tab1, true);
+      else fstage_t<NY, R1, NY / R0, -1>(bf, W, 1, W, tw, true);
+    };
+    // layers without pixels since the previous one (acc D^(gap - 1)), then
+    // the last stage of work buffer bf fused with acc = acc D + x
+    auto last = [&](const C* bf, int gap) {
+#pragma unroll
+      for (int kb = 0; kb < KB; ++kb) {
+        const int bb = tid + kb * T;
+        if (bb < CF::NBL) {
+          const int b = bb / W, w = bb - b * W;
+          for (int r = 1; r < gap; ++r) {
+#pragma unroll
+            for (int f = 0; f < RL; ++f)
+              if ((fkeep >> f) & 1u) acc[kb][f] = cmul(acc[kb][f], dreg[kb][f]);
+          }
+          C x[RL];
+#pragma unroll
+          for (int f = 0; f < RL; ++f) x[f] = bf[(b * RLP + f) * W + w];
+          DFT<RL, -1, C>::run(x);
 #pragma unroll
           for (int f = 0; f < RL; ++f) {
-            if (!((fkeep >> f) & 1u)) continue;         // outside the SSB crop for every b
-            const C d = dsm[(b * RLP + f) * W + w];
+            if (!((fkeep >> f) & 1u)) continue;
+            const C d = dreg[kb][f];
             const C t = acc[kb][f];
             acc[kb][f] = make_float2(fmaf(t.x, d.x, fmaf(-t.y, d.y, x[f].x)), fmaf(t.x, d.y, fmaf(t.y, d.x, x[f].y)));
           }
-          continue;
         }
-        const C ex = exw[w];
-#pragma unroll
-        for (int f = 0; f < RL; ++f) {
-          if (!((fkeep >> f) & 1u)) continue;           // outside the SSB crop for every b
-          const int p = b * RL + f;
-          // H = C Ex exp(i (pi lambda z' fy^2 + k z' g)), both phase parts reduced
-          float ph = fmaf(kz, gsm[(b * RLP + f) * W + w], eth[p]);
-          ph = fmaf(-two_pi, rintf(ph * inv2pi), ph);
-          float sn, cs;
-          __sincosf(ph, &sn, &cs);
-          const C h = cmul(ex, make_float2(cs, sn));
-          acc[kb][f] = cadd(acc[kb][f], cmul(h, x[f]));
+      }
+    };
+    // a wait for strip j ran out: flag it, let the copies in flight (strips
+    // j and j + 1) land, leave
+    auto bail = [&](int j) {
+      if (tid == 0) atomicOr(a.err, 1);
+      for (int q = j; q < nact && q <= j + 1; ++q) mbar_wait_bounded(&mbar[q & 1], (uint32_t)((q >> 1) & 1));
+    };
+    if (nact > 0) {
+      const bool ok = mbar_wait_bounded(&mbar[0], 0u);
+      if (__syncthreads_or(!ok)) { bail(0); return; }
+      stage0(stg, occ, buf);
+      __syncthreads();
+      if (tid == 0 && nact > 2) {
+        fence_proxy_async_smem();
+        issue_strip2(2);
+      }
+      middle(buf);
+      __syncthreads();
+    }
+    for (int k = 0; k < nact; ++k) {
+      C* const bk = (k & 1) ? buf1 : buf;
+      C* const bn = (k & 1) ? buf : buf1;
+      last(bk, list[k] - list[k - 1]);
+      bool ok = true;
+      if (k + 1 < nact) {
+        const int j = k + 1;
+        ok = mbar_wait_bounded(&mbar[j & 1], (uint32_t)((j >> 1) & 1));
+        if (ok) stage0((j & 1) ? stg1 : stg, (j & 1) ? occ1 : occ, bn);
+      }
+      if (__syncthreads_or(!ok)) { bail(k + 1); return; }
+      if (k + 1 < nact) {
+        if (tid == 0 && k + 3 < nact) {
+          fence_proxy_async_smem();
+          issue_strip2(k + 3);       // into the buffer stage 0 of layer k+1 has just read
+        }
+        middle(bn);
+        __syncthreads();
+      }
+    }
+  } else {
+    for (int k = 0; k < nact; ++k) {
+      // one barrier: layer k's strip and Ey have landed, and the previous
+      // layer's last stage no longer reads the work buffer
+      uint64_t* const bar_e = (k & 1) ? &mbar[2] : &mbar[1];
+      bool ok = mbar_wait_bounded(&mbar[0], (uint32_t)(k & 1));
+      ok = ok && (horner || mbar_wait_bounded(bar_e, (uint32_t)((k >> 1) & 1)));
+      if (__syncthreads_or(!ok)) {
+        if (tid == 0) atomicOr(a.err, 1);
+        // let this block's copies still in flight land before leaving
+        mbar_wait_bounded(&mbar[0], (uint32_t)(k & 1));
+        if (!horner) mbar_wait_bounded(bar_e, (uint32_t)((k >> 1) & 1));
+        return;
+      }
+      if (tid == 0 && k + 1 < nact && !horner) {
+        // Ey buffer (k+1)&1 was last read by layer k-1, finished before the barrier
+        fence_proxy_async_smem();
+        issue_ey(k + 1);
+      }
+      const int e = list[k];
+      if (tid < W && !horner) exw[tid] = a.exc[(size_t)e * a.Px + kxw[tid]];
+      const int gap = e - list[k - 1];
+      if constexpr (horner) {
+        // layers without pixels since the previous one: acc D^(gap - 1)
+        for (int r = 1; r < gap; ++r) {
+  #pragma unroll
+          for (int kb = 0; kb < KB; ++kb) {
+            const int bb = tid + kb * T;
+            if (bb < CF::NBL) {
+              const int b = bb / W, w = bb - b * W;
+  #pragma unroll
+              for (int f = 0; f < RL; ++f) acc[kb][f] = cmul(acc[kb][f], dsm[(b * RLP + f) * W + w]);
+            }
+          }
+        }
+      }
+      // stage 0 from the staging buffer: inputs j + t*Q0 of the y-shifted line
+      for (int idx = tid; idx < Q0 * W; idx += T) {
+        const int j = idx / W, w = idx - j * W;
+        C x[R0];
+        if (R0 == 16 && a.hzy) {
+          // 2x padding: inputs t = 4..11 are rows of the zero band; with
+          // hy = NY/2 and oy = NY/4 the image row of input t is
+          // j + (t + 4) Q0 (t < 4) or j + (t - 12) Q0 (t >= 12)
+  #pragma unroll
+          for (int t = 0; t < R0; ++t) {
+            if (t >= 4 && t < 12) { x[t] = make_float2(0.f, 0.f); continue; }
+            const int yl = j + (t < 4 ? t + 4 : t - 12) * Q0;
+            x[t] = occ[yl] ? stg[yl * SW + csel + w] : make_float2(0.f, 0.f);
+          }
+          dft16_halfzero<-1>(x);
+        } else {
+  #pragma unroll
+          for (int t = 0; t < R0; ++t) {
+            int y = j + t * Q0 - a.hy;
+            if (y < 0) y += NY;
+            const int yl = y - a.oy;
+            C v = make_float2(0.f, 0.f);
+            if (yl >= 0 && yl < pny && occ[yl]) v = stg[yl * SW + csel + w];
+            x[t] = v;
+          }
+          DFT<R0, -1, C>::run(x);
+        }
+        if (j) {
+          C wp[R0];
+          twiddle_powers<R0, -1>(tw, j, wp);
+  #pragma unroll
+          for (int f = 1; f < R0; ++f) x[f] = cmul(x[f], wp[f]);
+        }
+  #pragma unroll
+        for (int f = 0; f < R0; ++f) buf[(pidx(j) + f * Q0P) * W + w] = x[f];
+      }
+      // middle stage(s); the leading barrier also frees the strip buffer
+      __syncthreads();
+      if (tid == 0 && k + 1 < nact) {
+        fence_proxy_async_smem();
+        issue_strip(k + 1);
+      }
+      static_assert(kTab > 0 || !PADL, "the padded layout needs the middle stage's table");
+      if constexpr (kTab > 0) fstage_tab<NY, R1, M1, -1, C, M1P, RLP>(buf, W, 1, W, tab1, true);
+      else fstage_t<NY, R1, NY / R0, -1>(buf, W, 1, W, tw, true);
+      __syncthreads();
+      // last stage (stride 1, no twiddles) fused with the transfer-function
+      // multiply-accumulate: either acc += H x per layer, or the recurrence
+      // acc = acc D^gap + x over the evenly spaced layers (H of the last layer
+      // applied once in the epilogue)
+      const float kz = a.kzp[e];
+      const float* eth = (k & 1) ? ey1 : ey0;       // storage order
+      const float inv2pi = 0.15915494309189533577f, two_pi = 6.28318530717958647692f;
+  #pragma unroll
+      for (int kb = 0; kb < KB; ++kb) {
+        const int bb = tid + kb * T;
+        if (bb < CF::NBL) {
+          const int b = bb / W, w = bb - b * W;
+          C x[RL];
+  #pragma unroll
+          for (int f = 0; f < RL; ++f) x[f] = buf[(b * RLP + f) * W + w];
+          DFT<RL, -1, C>::run(x);
+          if constexpr (horner) {
+  #pragma unroll
+            for (int f = 0; f < RL; ++f) {
+              if (!((fkeep >> f) & 1u)) continue;         // outside the SSB crop for every b
+              const C d = dsm[(b * RLP + f) * W + w];
+              const C t = acc[kb][f];
+              acc[kb][f] = make_float2(fmaf(t.x, d.x, fmaf(-t.y, d.y, x[f].x)), fmaf(t.x, d.y, fmaf(t.y, d.x, x[f].y)));
+            }
+            continue;
+          }
+          const C ex = exw[w];
+  #pragma unroll
+          for (int f = 0; f < RL; ++f) {
+            if (!((fkeep >> f) & 1u)) continue;           // outside the SSB crop for every b
+            const int p = b * RL + f;
+            // H = C Ex exp(i (pi lambda z' fy^2 + k z' g)), both phase parts reduced
+            float ph = fmaf(kz, gsm[(b * RLP + f) * W + w], eth[p]);
+            ph = fmaf(-two_pi, rintf(ph * inv2pi), ph);
+            float sn, cs;
+            __sincosf(ph, &sn, &cs);
+            const C h = cmul(ex, make_float2(cs, sn));
+            acc[kb][f] = cadd(acc[kb][f], cmul(h, x[f]));
+          }
         }
       }
     }
@@ -500,7 +663,8 @@ __device__ __forceinline__ void dm_col_body(const DMArgs<float>& a, int blk) {
         int ky = FastSched<NY>::iperm(b * RL + f) + a.hy;      // spectrum row at storage position
         if (ky >= NY) ky -= NY;
         if (a.spectrum) a.spectrum[(size_t)ky * a.Px + kx] = acc[kb][f];
-        const bool keep = kx >= a.cx1 && kx <= a.cx2 && ky >= a.cy1 && ky <= a.cy2;
+        const bool keep = kx >= a.cx1 && kx <= a.cx2 && ky >= a.cy1 && ky <= a.cy2 &&
+                          (!PIPE2 || ((fkeep >> f) & 1u));
         x[f] = keep ? acc[kb][f] : make_float2(0.f, 0.f);
       }
       DFT<RL, 1, C>::run(x);
@@ -531,7 +695,7 @@ __device__ __forceinline__ void dm_col_body(const DMArgs<float>& a, int blk) {
 
 template <int NY, int W, bool STEP, bool SSB = false, bool EXT = false>
 __global__ void __launch_bounds__(ColCfg<NY, W, STEP>::T, ColCfg<NY, W, STEP>::MINB) dm_col_fast(DMArgs<float> a) {
-  dm_col_body<NY, W, STEP, SSB, EXT, 0, false>(a, blockIdx.x);
+  dm_col_body<NY, W, STEP, SSB, EXT, 0, false, STEP && SSB && !EXT && col_pipe2<NY, W>()>(a, blockIdx.x);
 }
 
 }  // namespace oh
