@@ -340,7 +340,7 @@ SQUARE_SIDE, SQUARE_LAYERS = 2048, 16     # --op square: the batch's largest fra
 
 
 def secondary_measurements(ctx, dev, torch, reps=5, ops=SECONDARY_OPS, warmup=1, peaks=None,
-                           samples=UNET_SAMPLES):
+                           samples=UNET_SAMPLES, batch_frames=None, batch_tune=True):
     """The other operators at their own workloads (seeded synthetic inputs):
     pointcloud: KETI exact-r sum 1024x1024 x 5000 points + phase-only encoding;
     pls: the same shape through the paraxial cwoPLS::Fresnel sum (tensor-core
@@ -371,7 +371,7 @@ def secondary_measurements(ctx, dev, torch, reps=5, ops=SECONDARY_OPS, warmup=1,
     if "wrp" in ops:
         _sec_wrp(ctx, dev, torch, st, timed, out, reps + warmup, peaks)
     if "batch" in ops:
-        _sec_batch(ctx, dev, torch, out, reps, warmup)
+        _sec_batch(ctx, dev, torch, out, reps, warmup, batch_frames, batch_tune)
     if "square" in ops:
         _sec_square(ctx, dev, torch, timed, out)
     if "unet" in ops:
@@ -475,9 +475,9 @@ def batch_workload():
     return scenes.batch_workload()
 
 
-def _sec_batch(ctx, dev, torch, out, reps, warmup):
+def _sec_batch(ctx, dev, torch, out, reps, warmup, nframes=None, tune=True):
     from openholo_gb300 import depthmap as dm, launch_count, scenes
-    work = batch_workload()
+    work = batch_workload()[:nframes]
     scene = {}
     frames = []
     for i, (side, L, lam) in enumerate(work):
@@ -509,17 +509,20 @@ def _sec_batch(ctx, dev, torch, out, reps, warmup):
         return a.elapsed_time(b) / reps, (launch_count() - n0) / reps
 
     ms_pf, k_pf = run(0)
-    with torch.cuda.stream(stream):
-        t0 = time.perf_counter()
-        dm.autotune_batch(ctx, frames, reps=2, stream=stream)
-        stream.synchronize()
-        tune_s = time.perf_counter() - t0
+    tune_s = None
+    if tune:
+        with torch.cuda.stream(stream):
+            t0 = time.perf_counter()
+            dm.autotune_batch(ctx, frames, reps=2, stream=stream)
+            stream.synchronize()
+            tune_s = time.perf_counter() - t0
     ms, kernels = run(1)
     out["batch_64_frames_mixed_per_frame_launches"] = {
         "ms_per_batch": ms_pf, "frames_per_s": len(work) * 1000.0 / ms_pf, "kernels_per_batch": k_pf,
         "what": "the same batch as per-frame launches (set-up, row, column and output pass per frame) replayed "
                 "from one CUDA graph"}
     out["batch_64_frames_mixed"] = {
+        "frames": len(work),
         "ms_per_batch": ms, "frames_per_s": len(work) * 1000.0 / ms,
         "model_bytes_per_batch": model, "model_gbs": model / (ms * 1e-3) / 1e9,
         "kernels_per_batch": kernels,
@@ -708,6 +711,10 @@ def main():
                     help="training samples of the learned form (other_operators.unet_surrogate_1024)")
     ap.add_argument("--record", default=None,
                     help="append one JSON-lines accuracy record (max/RMS error, PSNR, fallbacks) to this file")
+    ap.add_argument("--batch-frames", type=int, default=None,
+                    help="--op batch: the first N frames of the 64-frame workload (small profiling case)")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="--op batch: time the batch kernel with its default settings (no autotuning first)")
     ap.add_argument("--op", choices=SECONDARY_OPS, default=None,
                     help="time one secondary workload alone (steps calls after warmup) and print its line")
     args = ap.parse_args()
@@ -721,7 +728,8 @@ def main():
         from openholo_gb300 import Context
         torch.cuda.set_device(local)
         res = secondary_measurements(Context(local), torch.device("cuda", local), torch, reps=args.steps,
-                                     ops=(args.op,), warmup=args.warmup, samples=args.unet_samples)
+                                     ops=(args.op,), warmup=args.warmup, samples=args.unet_samples,
+                                     batch_frames=args.batch_frames, batch_tune=not args.no_tune)
         if rank == 0:
             print(json.dumps({"op": args.op, "steps": args.steps, "warmup": args.warmup, **res}), flush=True)
         return
