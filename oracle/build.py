@@ -21,6 +21,14 @@ build_reference_depthmap():
                    these kernels on a GPU in the reference's call sequence.
                    The depth-map host code (Qt, FFTW) and the WRP sources (the
                    closed CWO DLL) are not built.
+build_reference_pointcloud_gpu():
+                   when the reference tree is present, compiles the device
+                   code of the reference's point-cloud GPU library
+                   (OpenHolo_KETI/.../ophgen_pointcloud_gpu/ophgen_pointcloud_gpu.cpp,
+                   CUDA source in a .cpp file, so nvcc -x cu), where it lies,
+                   into oracle/_ref/pc_ref.cubin for sm_103a.
+                   oracle/pc_reference_gpu.py launches its kernel as the
+                   reference's host function does.
 """
 from __future__ import annotations
 
@@ -95,7 +103,26 @@ def build_reference_depthmap() -> Path | None:
     return out
 
 
+KETI_GPU_SRC = REFERENCE_ROOT / ("OpenHolo_KETI/VS/Openholo_Generation_PointCloud_Library_beta_v1.0/"
+                                 "ophgen_pointcloud_gpu/ophgen_pointcloud_gpu.cpp")
+
+
+def build_reference_pointcloud_gpu() -> Path | None:
+    src = KETI_GPU_SRC
+    if not src.exists():
+        return None
+    REF_OUT.mkdir(exist_ok=True)
+    out = REF_OUT / "pc_ref.cubin"
+    if _fresh(out, [src]):
+        return out
+    nvcc = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
+    _run([nvcc, "-x", "cu", "-cubin", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-w",
+          "-I", str(src.parent), "-I", str(KETI_DIR), "-o", str(out), str(src)])
+    return out
+
+
 if __name__ == "__main__":
     print(build_oracle())
     print(build_reference())
     print(build_reference_depthmap())
+    print(build_reference_pointcloud_gpu())

@@ -1,7 +1,8 @@
 """The reference's own depth-map GPU kernels, run in the reference's call
-sequence — TEST INFRASTRUCTURE ONLY.  Only tests/golden/make_golden_depthmap.py
-uses it, to write golden fixtures; nothing in the product, the tests or the
-benchmark executes it.
+sequence — TEST INFRASTRUCTURE ONLY.  tests/golden/make_golden_depthmap.py uses it to
+write golden fixtures, and tests/test_reference_gpu_gpu.py to compare the
+library with it at full size and to time it as a baseline; nothing in the
+product or the benchmark executes it.
 
 oracle/build.py compiles OpenHolo_DepthMap/Hologram/src/HologramKernel.cu
 (from the reference tree, unchanged) into oracle/_ref/dm_ref.cubin for
@@ -51,7 +52,7 @@ ENTRIES = {
 
 
 class _Driver:
-    def __init__(self, cubin: Path):
+    def __init__(self, cubin: Path, entries: dict | None = None):
         import torch
         if not cubin.exists():
             raise FileNotFoundError(f"{cubin} is missing: build it with oracle/build.py where the reference tree is")
@@ -65,7 +66,7 @@ class _Driver:
         self.mod = C.c_void_p()
         self._ok(self.cu.cuModuleLoad(C.byref(self.mod), str(cubin).encode()), "cuModuleLoad")
         self.fn = {}
-        for k, name in ENTRIES.items():
+        for k, name in (entries or ENTRIES).items():
             f = C.c_void_p()
             self._ok(self.cu.cuModuleGetFunction(C.byref(f), self.mod, name.encode()), "cuModuleGetFunction " + name)
             self.fn[k] = f
@@ -76,6 +77,15 @@ class _Driver:
     def _ok(rc, what):
         if rc != 0:
             raise RuntimeError(f"{what} failed with CUresult {rc}")
+
+    def launch2d(self, name, grid, block, *args):
+        """Launch `name` with a 2-D grid and block (the point-cloud kernel)."""
+        import torch
+        vals = [a if isinstance(a, C._SimpleCData) else C.c_void_p(a) for a in args]
+        ptrs = (C.c_void_p * len(vals))(*[C.cast(C.pointer(v), C.c_void_p) for v in vals])
+        stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        self._ok(self.cu.cuLaunchKernel(self.fn[name], grid[0], grid[1], 1, block[0], block[1], 1, 0, stream, ptrs,
+                                        None), "cuLaunchKernel " + name)
 
     def launch(self, name, n, *args):
         import torch
