@@ -787,8 +787,11 @@ def main():
     h_img = torch.from_numpy(img).pin_memory()
     h_depth = torch.from_numpy(depth).pin_memory()
     h_out = torch.empty((NY, NX), dtype=torch.float32).pin_memory()
+    # a stream of its own, as a serving loop would use: repeated calls with
+    # the same page-locked buffers replay one graph of copies and passes
+    e2e_stream = torch.cuda.Stream(device=dev)
     for _ in range(2):
-        dm.generate_host(ctx, p, h_img.numpy(), h_depth.numpy(), out=h_out.numpy())
+        dm.generate_host(ctx, p, h_img.numpy(), h_depth.numpy(), out=h_out.numpy(), stream=e2e_stream)
     if pg:
         pg.barrier()
     wall = []
@@ -796,7 +799,7 @@ def main():
         flush.fill_(1.0)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        dm.generate_host(ctx, p, h_img.numpy(), h_depth.numpy(), out=h_out.numpy())
+        dm.generate_host(ctx, p, h_img.numpy(), h_depth.numpy(), out=h_out.numpy(), stream=e2e_stream)
         wall.append(time.perf_counter() - t0)
     e2e_ms = 1000.0 * sum(wall) / len(wall)
     e2e_ms = max_over_ranks(e2e_ms, pg, dev)

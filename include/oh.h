@@ -191,7 +191,11 @@ oh_status oh_depthmap_propagate_field(oh_ctx* ctx, oh_precision prec, const oh_d
 /* Same with host buffers; copies in and out on the given stream and waits.
  * A page-locked fringe_host (cudaHostAlloc / cudaHostRegister) is written by
  * the output kernel through its device mapping, with no copy after the frame;
- * a pageable one is filled by a device-to-host copy. */
+ * a pageable one is filled by a device-to-host copy.  When every buffer is
+ * page-locked and the stream is not the legacy default stream, the first
+ * call with given parameters and buffers also captures its copies and passes
+ * into a CUDA graph that later identical calls replay (the library's
+ * per-kernel timing and the test-stall hook turn this off). */
 oh_status oh_depthmap_generate_host(oh_ctx* ctx, oh_precision prec,
                                     const oh_depthmap_params* p,
                                     const uint8_t* img_host,

@@ -58,6 +58,9 @@ void drop_graphs(oh_ctx* ctx) {
   for (auto& kv : ctx->graphs)
     if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
   ctx->graphs.clear();
+  for (auto& kv : ctx->frame_graphs)
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+  ctx->frame_graphs.clear();
   ctx->batch_plans.clear();
 }
 
@@ -65,7 +68,8 @@ oh_status scratch(oh_ctx* ctx, const char* name, size_t bytes, void** out) {
   auto& b = ctx->scratch[name];
   if (b.bytes < bytes) {
     // captured depth-map graphs address the buffer being replaced
-    if (b.p && std::string(name).compare(0, 3, "dm.") == 0) drop_graphs(ctx);
+    // (and the host-buffer frame graphs address "host.io")
+    if (b.p && (std::string(name).compare(0, 3, "dm.") == 0 || std::string(name) == "host.io")) drop_graphs(ctx);
     // the cached tables of a buffer being replaced are gone
     const std::string nm(name);
     if (nm == "dm.tables") ctx->dm_setup_key.clear();

@@ -30,6 +30,8 @@ struct oh_ctx {
   // captured depth-map batches: key -> executable graph and the table key it leaves behind
   struct Graph { cudaGraphExec_t exec = nullptr; std::string dm_key; int launches = 0; };
   std::map<std::string, Graph> graphs;
+  // host-buffer frames: key (parameters, host pointers) -> graph of copies and passes
+  std::map<std::string, Graph> frame_graphs;
   // persistent depth-map batches: key -> plan (descriptors, tables, graph)
   struct BatchPlanBase { virtual ~BatchPlanBase() = default; };
   std::map<std::string, std::unique_ptr<BatchPlanBase>> batch_plans;

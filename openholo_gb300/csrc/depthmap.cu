@@ -1260,42 +1260,103 @@ oh_status oh_depthmap_generate_host(oh_ctx* ctx, oh_precision prec, const oh_dep
                                     const float* phase_host, void* fringe_host, void* stream) {
   OH_TRY(validate(p));
   if (!ctx || !img_host || !depth_host || !fringe_host) return fail(OH_ERR_INVALID_ARG, "null argument");
+  if (p->phase_mode == OH_PHASE_ARRAY && !phase_host) return fail(OH_ERR_INVALID_ARG, "OH_PHASE_ARRAY needs a phase array");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  CallScope cs(ctx, st);
+  OH_TRY(cs.status());
   const size_t n = (size_t)p->pnx * p->pny;
   const size_t fsz = n * (prec == OH_FP64 ? sizeof(double) : sizeof(float));
   void* dev;
+  OH_TRY(scratch(ctx, "host.io", 2 * n + (phase_host ? 4 * n : 0) + fsz + 1024, &dev));
   // A page-locked (or registered) fringe buffer is written by the output
   // kernel itself through its device mapping: the result reaches host memory
   // while the pass runs, with no device-to-host copy after it.  Pageable
   // buffers get the copy.
   // (Reading page-locked inputs through their mappings in the row pass
   // instead of copying them measured slower than the copies.)
-  void* fringe_mapped = nullptr;
-  {
-    std::lock_guard<std::mutex> lk(ctx->mu);
-    int prev = 0; cudaGetDevice(&prev); cudaSetDevice(ctx->device);
-    oh_status s = scratch(ctx, "host.io", 2 * n + (phase_host ? 4 * n : 0) + fsz + 1024, &dev);
+  auto mapped = [](const void* h) -> void* {
     cudaPointerAttributes at{};
-    if (cudaPointerGetAttributes(&at, fringe_host) == cudaSuccess) {
-      if (at.type == cudaMemoryTypeHost && at.devicePointer) fringe_mapped = at.devicePointer;
-    } else {
-      cudaGetLastError();
-    }
-    cudaSetDevice(prev);
-    if (s != OH_OK) return s;
-  }
+    if (cudaPointerGetAttributes(&at, h) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+  };
+  void* fringe_mapped = mapped(fringe_host);
   uint8_t* d_img = (uint8_t*)dev;
   uint8_t* d_depth = d_img + n;
   size_t off = (2 * n + 255) & ~(size_t)255;
   float* d_phase = phase_host ? (float*)((char*)dev + off) : nullptr;
   if (phase_host) off += (4 * n + 255) & ~(size_t)255;
   void* d_fringe = (char*)dev + off;
-  OH_CUDA_TRY(cudaMemcpyAsync(d_img, img_host, n, cudaMemcpyHostToDevice, st));
-  OH_CUDA_TRY(cudaMemcpyAsync(d_depth, depth_host, n, cudaMemcpyHostToDevice, st));
-  if (phase_host) OH_CUDA_TRY(cudaMemcpyAsync(d_phase, phase_host, 4 * n, cudaMemcpyHostToDevice, st));
-  OH_TRY(oh_depthmap_generate(ctx, prec, p, d_img, d_depth, d_phase, fringe_mapped ? fringe_mapped : d_fringe,
-                              nullptr, nullptr, stream));
-  if (!fringe_mapped) OH_CUDA_TRY(cudaMemcpyAsync(fringe_host, d_fringe, fsz, cudaMemcpyDeviceToHost, st));
+  auto enqueue = [&]() -> oh_status {
+    OH_CUDA_TRY(cudaMemcpyAsync(d_img, img_host, n, cudaMemcpyHostToDevice, st));
+    OH_CUDA_TRY(cudaMemcpyAsync(d_depth, depth_host, n, cudaMemcpyHostToDevice, st));
+    if (phase_host) OH_CUDA_TRY(cudaMemcpyAsync(d_phase, phase_host, 4 * n, cudaMemcpyHostToDevice, st));
+    void* out = fringe_mapped ? fringe_mapped : d_fringe;
+    if (prec == OH_FP64) OH_TRY((run_depthmap<double, 18>(ctx, p, d_img, d_depth, d_phase, out, nullptr, nullptr, st)));
+    else OH_TRY((run_depthmap<float, 36>(ctx, p, d_img, d_depth, d_phase, out, nullptr, nullptr, st)));
+    if (!fringe_mapped) OH_CUDA_TRY(cudaMemcpyAsync(fringe_host, d_fringe, fsz, cudaMemcpyDeviceToHost, st));
+    return OH_OK;
+  };
+  // Repeated frames with the same parameters and page-locked host buffers
+  // replay one CUDA graph of the copies and the passes (one launch instead
+  // of the per-call planning and five enqueues).  The graph expects the
+  // parameter tables its capture found in scratch; when another frame has
+  // replaced them, the frame runs directly and is captured again.
+  bool graphable = st != nullptr && fringe_mapped && mapped(img_host) && mapped(depth_host) &&
+                   (!phase_host || mapped(phase_host)) && !ctx->timing && !ctx->stall_mask;
+  if (graphable) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    OH_CUDA_TRY(cudaStreamIsCapturing(st, &cap));
+    graphable = cap == cudaStreamCaptureStatusNone;
+  }
+  if (!graphable) {
+    OH_TRY(enqueue());
+    OH_CUDA_TRY(cudaStreamSynchronize(st));
+    return OH_OK;
+  }
+  std::string key = "host:" + std::to_string((int)prec) + ":";
+  key.append(reinterpret_cast<const char*>(p), sizeof(*p));
+  if (p->render_depth)
+    key.append(reinterpret_cast<const char*>(p->render_depth), (size_t)p->n_render_depth * sizeof(int));
+  const void* ptrs[4] = {img_host, depth_host, phase_host, fringe_host};
+  key.append(reinterpret_cast<const char*>(ptrs), sizeof(ptrs));
+  auto it = ctx->frame_graphs.find(key);
+  if (it != ctx->frame_graphs.end() && it->second.dm_key == ctx->dm_setup_key) {
+    OH_CUDA_TRY(cudaGraphLaunch(it->second.exec, st));
+    note_launch(it->second.launches);
+    OH_CUDA_TRY(cudaStreamSynchronize(st));
+    return OH_OK;
+  }
+  if (it != ctx->frame_graphs.end()) {
+    cudaGraphExecDestroy(it->second.exec);
+    ctx->frame_graphs.erase(it);
+  }
+  OH_TRY(enqueue());                          // this call's frame (builds the tables when needed)
+  if (ctx->frame_graphs.size() >= 16) {
+    for (auto& kv : ctx->frame_graphs) cudaGraphExecDestroy(kv.second.exec);
+    ctx->frame_graphs.clear();
+  }
+  // capture the same work for the next calls (launched kernels are counted
+  // when the graph runs, not while it is captured)
+  const uint64_t l0 = launches_so_far();
+  cudaGraph_t g = nullptr;
+  oh_status rs = OH_OK;
+  cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) rs = cuda_fail(e, "cudaStreamBeginCapture");
+  else {
+    rs = enqueue();
+    e = cudaStreamEndCapture(st, &g);
+    if (rs == OH_OK && e != cudaSuccess) rs = cuda_fail(e, "cudaStreamEndCapture");
+  }
+  const int captured = (int)(launches_so_far() - l0);
+  note_launch(-captured);
+  if (rs == OH_OK) {
+    cudaGraphExec_t ex = nullptr;
+    e = cudaGraphInstantiate(&ex, g, 0);
+    if (e != cudaSuccess) rs = cuda_fail(e, "cudaGraphInstantiate");
+    else ctx->frame_graphs[key] = oh_ctx::Graph{ex, ctx->dm_setup_key, captured};
+  }
+  if (g) cudaGraphDestroy(g);
+  OH_TRY(rs);
   OH_CUDA_TRY(cudaStreamSynchronize(st));
   return OH_OK;
 }
