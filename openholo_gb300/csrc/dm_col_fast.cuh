@@ -234,24 +234,34 @@ __device__ __forceinline__ void dm_col_body(const DMArgs<float>& a, int blk) {
   const int csel = (blk % (SW / W)) * W;              // first of its columns this block takes
   const int kx0 = blk * W;
   const int pny = a.pny;
-  if (tid == 0) {
-    mbar_init(&mbar[0], 1);
-    mbar_init(&mbar[1], 1);
-    mbar_init(&mbar[2], 1);
-    fence_mbar_init();
+  if (tid < 32) {
     // this chunk's active entries, the last active entry before it (the
     // layer-step gap) and the last active entry of the frame (its transfer
-    // function finishes the recurrence)
-    int n = 0, prev = -1, last = -1;
-    for (int e = 0; e < a.n_entries; ++e) {
-      if (!a.slot_any[a.uslot_of_entry[e]]) continue;
-      if (e < a.e0) prev = e;
-      else if (e < a.e1) list[n++] = (int16_t)e;
-      last = e;
+    // function finishes the recurrence): warp 0 reads the layer flags of 32
+    // entries at a time and compacts them with ballots
+    const unsigned lt = (1u << tid) - 1u;
+    int n = 0, prev = -1, last = -1, first = -1;
+    for (int base = 0; base < a.n_entries; base += 32) {
+      const int e = base + tid;
+      const bool act = e < a.n_entries && a.slot_any[a.uslot_of_entry[e]] != 0;
+      const unsigned m = __ballot_sync(0xffffffffu, act);
+      const unsigned mc = __ballot_sync(0xffffffffu, act && e >= a.e0 && e < a.e1);
+      const unsigned mp = __ballot_sync(0xffffffffu, act && e < a.e0);
+      if ((mc >> tid) & 1u) list[n + __popc(mc & lt)] = (int16_t)e;
+      if (mc && first < 0) first = base + __ffs(mc) - 1;
+      n += __popc(mc);
+      if (mp) prev = base + 31 - __clz(mp);
+      if (m) last = base + 31 - __clz(m);
     }
-    s_nact = n;
-    s_last = last;
-    list[-1] = (int16_t)(prev >= 0 ? prev : (n > 0 ? list[0] - 1 : 0));
+    if (tid == 0) {
+      mbar_init(&mbar[0], 1);
+      mbar_init(&mbar[1], 1);
+      mbar_init(&mbar[2], 1);
+      fence_mbar_init();
+      s_nact = n;
+      s_last = last;
+      list[-1] = (int16_t)(prev >= 0 ? prev : (n > 0 ? first - 1 : 0));
+    }
   }
   load_tw_split(twlo, twhi, static_cast<const C*>(a.ply.tw), NY);
   if constexpr (kTab > 0) fill_stage_tab<NY, R1, NY / R0, -1>(tab1, static_cast<const C*>(a.ply.tw));
