@@ -337,6 +337,10 @@ __device__ __forceinline__ void dm_row_body(const DMArgs<R>& a, int blk) {
   // the image and depth bytes of up to kSetupPix pixels per thread are loaded
   // before any is used, so their latency is paid once
   constexpr int kSetupPix = 8;
+  // layer-presence bits of slots 0..63 per row, gathered in registers and
+  // OR-reduced per warp (one shared atomic per warp and word instead of one
+  // per pixel, which all hit the same word); higher slots use the atomics
+  uint32_t pm00 = 0u, pm01 = 0u, pm10 = 0u, pm11 = 0u;     // [row][word], scalars (no local memory)
   for (int base = 0; base < kRowPair * pnx; base += kSetupPix * NT) {
     uint8_t gb[kSetupPix], db[kSetupPix];
 #pragma unroll
@@ -378,11 +382,24 @@ __device__ __forceinline__ void dm_row_body(const DMArgs<R>& a, int blk) {
             sincos_r<R>(ph, &sn, &cs);
             val = mk(amp * cs, amp * sn);
           }
-          atomicOr(&mask[l * 8 + (u >> 5)], 1u << (u & 31));
+          const uint32_t bit = 1u << (u & 31);
+          if (u < 32) { if (l == 0) pm00 |= bit; else pm10 |= bit; }
+          else if (u < 64) { if (l == 0) pm01 |= bit; else pm11 |= bit; }
+          else atomicOr(&mask[l * 8 + (u >> 5)], bit);
         }
       }
       li[l * lip + c] = (int16_t)u;
       v[l * pnx + c] = val;
+    }
+  }
+  {
+    const uint32_t m00 = __reduce_or_sync(0xffffffffu, pm00), m01 = __reduce_or_sync(0xffffffffu, pm01);
+    const uint32_t m10 = __reduce_or_sync(0xffffffffu, pm10), m11 = __reduce_or_sync(0xffffffffu, pm11);
+    if ((threadIdx.x & 31) == 0) {
+      if (m00) atomicOr(&mask[0], m00);
+      if (m01) atomicOr(&mask[1], m01);
+      if (m10) atomicOr(&mask[8], m10);
+      if (m11) atomicOr(&mask[9], m11);
     }
   }
   __syncthreads();
