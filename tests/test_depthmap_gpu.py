@@ -1,7 +1,7 @@
 """Depth-map CGH on the GPU (through the C ABI) against the CPU oracle.
 
-Tolerances: FP64 mode 1e-7 relative field error (the benchmark spec's bound is
-1e-5); FP32 mode 1e-3 relative (the bound for the fast forms).
+Tolerances: FP64 mode 1e-7 relative field error (tighter than the 1e-5 that
+FP64 mode promises); FP32 mode 1e-3 relative (the bound for the fast forms).
 """
 import math
 
