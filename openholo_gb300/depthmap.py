@@ -92,8 +92,8 @@ def propagate_field(ctx: _lib.Context, p: DepthmapParams, field, z: float, preci
 
 def generate_batch(ctx: _lib.Context, frames, precision="fp32", graph=False, stream=None):
     """Run a list of frames in one call (oh_depthmap_generate_batch).  Each
-    entry is (params, img, depth, fringe) or (params, img, depth, fringe,
-    phase) with device tensors; fringe receives the result.  graph=True
+    entry is (params, img, depth, fringe[, phase[, field]]) with device
+    tensors; fringe (and field, complex, when given) receive the result.  graph=True
     captures the batch into a CUDA graph on the first call and replays it on
     later calls with the same frames (same parameters and tensors)."""
     prec = OH_FP64 if precision == "fp64" else OH_FP32
@@ -103,16 +103,18 @@ def generate_batch(ctx: _lib.Context, frames, precision="fp32", graph=False, str
 
 
 def _frame_array(frames):
+    """Entries (params, img, depth, fringe[, phase[, field]]) of device tensors."""
     arr = (_lib.DepthmapFrame * len(frames))()
     for i, fr in enumerate(frames):
         p, img, depth, fringe = fr[:4]
         phase = fr[4] if len(fr) > 4 else None
+        field = fr[5] if len(fr) > 5 else None
         arr[i].params = p
         arr[i].img = img.data_ptr()
         arr[i].depth = depth.data_ptr()
         arr[i].phase = phase.data_ptr() if phase is not None else None
         arr[i].fringe = fringe.data_ptr()
-        arr[i].field = None
+        arr[i].field = field.data_ptr() if field is not None else None
     return arr
 
 

@@ -173,3 +173,52 @@ def test_autotune_batch(ctx, tmp_path):
     finally:
         other.close()
     dm.set_autotune_file(ctx, None)
+
+
+def test_persistent_batch_phase_arrays_and_fields(ctx):
+    # per-pixel phase arrays and complex field outputs through the batch kernel
+    spec = [(512, 512, 7, 532e-9), (768, 512, 5, 450e-9), (1024, 1024, 4, 633e-9)]
+    frames, ref_inputs = [], []
+    for i, (ny, nx, L, lam) in enumerate(spec):
+        img, depth = scenes.depthmap_scene(120 + i, ny, nx)
+        phase = torch.from_numpy(scenes.seeded_phase(500 + i, ny, nx).astype(np.float32)).cuda()
+        p = dm.make_params(pnx=nx, pny=ny, num_of_depth=L, lam=lam, pad=2, phase_mode=dm.OH_PHASE_ARRAY)
+        ti, td = torch.from_numpy(img).cuda(), torch.from_numpy(depth).cuda()
+        fr = torch.empty((ny, nx), dtype=torch.float32, device="cuda")
+        fd = torch.empty((ny, nx), dtype=torch.complex64, device="cuda")
+        frames.append((p, ti, td, fr, phase, fd))
+    _mode(ctx, 1)
+    n0 = launch_count()
+    dm.generate_batch(ctx, frames)
+    torch.cuda.synchronize()
+    assert launch_count() - n0 == 2                        # table set-up + batch kernel
+    for p, ti, td, fr, phase, fd in frames:
+        rf = torch.empty_like(fd)
+        ref = dm.generate(ctx, p, ti, td, phase=phase, field=rf)
+        torch.cuda.synchronize()
+        assert torch.equal(fr, ref)
+        assert torch.equal(fd, rf)
+
+
+def test_persistent_batch_of_one_frame(ctx):
+    frames = _frames(130, [(1024, 1024, 16, 532e-9)])
+    _mode(ctx, 1)
+    dm.generate_batch(ctx, frames)
+    n0 = launch_count()
+    dm.generate_batch(ctx, frames)
+    torch.cuda.synchronize()
+    assert launch_count() - n0 == 1
+    p, img, depth, fr = frames[0]
+    assert torch.equal(fr, dm.generate(ctx, p, img, depth))
+
+
+def test_tune_file_errors(ctx, tmp_path):
+    bad = tmp_path / "bad.txt"
+    bad.write_text("# header\nsm_103:152:1024 2 1 2 1\n")        # too few fields
+    with pytest.raises(_lib.OhError):
+        dm.set_autotune_file(ctx, bad)
+    bad.write_text("sm_103:152:1024 3 1 2 1 1 2 1.0\n")            # 3 blocks per SM is not a setting
+    with pytest.raises(_lib.OhError):
+        dm.set_autotune_file(ctx, bad)
+    dm.set_autotune_file(ctx, tmp_path / "absent.txt")              # created by the first autotune
+    dm.set_autotune_file(ctx, None)
