@@ -11,13 +11,15 @@ grid, symmetrization encoding to a real fringe; FP32 compute.
 value      frames/s with inputs resident in HBM, CUDA events around each
            step on the launching stream; L2 flushed (512 MiB write) between
            timed steps, outside the events.
-e2e        the same frames through oh_depthmap_generate_host: pinned host
-           buffers in, host->device copy, frame, device->host copy of the
-           fringe, wall clock per call.
+e2e        the same frames through oh_depthmap_generate_host from pinned
+           host buffers on a stream of its own: the row pass reads the image
+           and depth bytes from host memory and the output pass writes the
+           fringe there (through the buffers' device mappings), wall clock
+           per call.
 roofline   the dominant kernel's device time (events around its launches on
            its stream) against the measured HBM peak.
-cpu_baseline  the oracle port (numpy/scipy pocketfft, all host cores) on a
-           bounded sample of the same frame, extrapolated to a frame.
+cpu_baseline  the oracle port (numpy/scipy pocketfft, all host cores) on one
+           whole frame.
 --impl reference  times that CPU restatement of the reference's depth-map
            path (Calc_Holo_CPU + encoding_CPU) alone; the reference's own CPU
            code needs Qt and FFTW and cannot be built.

@@ -188,13 +188,13 @@ oh_status oh_depthmap_generate(oh_ctx* ctx, oh_precision prec,
 oh_status oh_depthmap_propagate_field(oh_ctx* ctx, oh_precision prec, const oh_depthmap_params* p,
                                       const void* field_in, double z, void* fringe_out, void* field_out,
                                       void* spectrum_out, void* stream);
-/* Same with host buffers; copies in and out on the given stream and waits.
- * A page-locked fringe_host (cudaHostAlloc / cudaHostRegister) is written by
- * the output kernel through its device mapping, with no copy after the frame;
- * a pageable one is filled by a device-to-host copy.  When every buffer is
- * page-locked and the stream is not the legacy default stream, the first
- * call with given parameters and buffers also captures its copies and passes
- * into a CUDA graph that later identical calls replay (the library's
+/* Same with host buffers, on the given stream; waits for the frame.
+ * Page-locked buffers (cudaHostAlloc / cudaHostRegister) are used through
+ * their device mappings: the passes read the inputs and write the fringe in
+ * host memory, with no copies; pageable ones are copied in and out.  When
+ * every buffer is page-locked and the stream is not the legacy default
+ * stream, the first call with given parameters and buffers also captures its
+ * passes into a CUDA graph that later identical calls replay (the library's
  * per-kernel timing and the test-stall hook turn this off). */
 oh_status oh_depthmap_generate_host(oh_ctx* ctx, oh_precision prec,
                                     const oh_depthmap_params* p,

