@@ -42,7 +42,6 @@ struct oh_ctx {
   struct BatchTune { int ctas_per_sm = 2, lag = 1, col_w = 0, row_pairs = 1, col_blocks = 1, out_rows = 2; double ms = 0; };
   std::map<std::string, BatchTune> batch_tune;
   std::string tune_file;
-  bool tune_loaded = false;
   struct Buf { void* p = nullptr; size_t bytes = 0; };
   std::map<std::string, Buf> scratch;
   struct PlanBufs { oh::FFTPlan plan; void* tw = nullptr; int* perm = nullptr; int* iperm = nullptr; };

@@ -666,7 +666,6 @@ struct BatchPlan : oh_ctx::BatchPlanBase {
   size_t ctl_bytes = 0;
   BatchLaunch L{};
   cudaGraphExec_t exec = nullptr;
-  int n_items = 0;
   ~BatchPlan() override {
     if (exec) cudaGraphExecDestroy(exec);
     if (dev) cudaFree(dev);
@@ -825,7 +824,6 @@ static oh_status batch_plan_build(oh_ctx* ctx, const oh_depthmap_frame* frames, 
   L.wait_cycles = 2000000000LL;
   L.grid = sm_count() * std::min(occ, std::max(1, bs.ctas_per_sm));
   L.smem = smem;
-  P->n_items = (int)items.size();
   *out = std::move(P);
   return OH_OK;
 }
