@@ -52,6 +52,16 @@ __device__ __forceinline__ void run_out(const DMArgs<float>& a, int first, int c
     dm_out_body<float, kBatchLens[C]>(a, b);
   }
 }
+// one item of length class C
+template <int C>
+__device__ __forceinline__ void run_item(const DMArgs<float>& a, int kind, bool two_col, int first, int count) {
+  if (kind == kItemRow) { run_row<C>(a, first, count); return; }
+  if (kind == kItemOut) { run_out<C>(a, first, count); return; }
+  if constexpr (batch_col_w_ok(C, 2)) {
+    if (two_col) { run_col<C, 2>(a, first, count); return; }
+  }
+  run_col<C, 1>(a, first, count);
+}
 
 }  // namespace
 
@@ -117,15 +127,13 @@ __global__ void __launch_bounds__(kBatchThreads, 2) dm_batch_kernel(BatchLaunch 
       __syncthreads();
     }
     const int kind = it.y & 15;
-    switch (it.y >> 4) {              // class | two-column blocks << 4
-      case 0x00: kind == kItemRow ? run_row<0>(a, it.z, it.w) : kind == kItemCol ? run_col<0, 1>(a, it.z, it.w) : run_out<0>(a, it.z, it.w); break;
-      case 0x01: kind == kItemRow ? run_row<1>(a, it.z, it.w) : kind == kItemCol ? run_col<1, 1>(a, it.z, it.w) : run_out<1>(a, it.z, it.w); break;
-      case 0x02: kind == kItemRow ? run_row<2>(a, it.z, it.w) : kind == kItemCol ? run_col<2, 1>(a, it.z, it.w) : run_out<2>(a, it.z, it.w); break;
-      case 0x03: kind == kItemRow ? run_row<3>(a, it.z, it.w) : kind == kItemCol ? run_col<3, 1>(a, it.z, it.w) : run_out<3>(a, it.z, it.w); break;
-      case 0x04: kind == kItemRow ? run_row<4>(a, it.z, it.w) : kind == kItemCol ? run_col<4, 1>(a, it.z, it.w) : run_out<4>(a, it.z, it.w); break;
-      case 0x10: run_col<0, 2>(a, it.z, it.w); break;
-      case 0x11: run_col<1, 2>(a, it.z, it.w); break;
-      case 0x12: run_col<2, 2>(a, it.z, it.w); break;
+    const bool two_col = (it.y >> 8) & 1;
+    switch ((it.y >> 4) & 15) {
+      case 0: run_item<0>(a, kind, two_col, it.z, it.w); break;
+      case 1: run_item<1>(a, kind, two_col, it.z, it.w); break;
+      case 2: run_item<2>(a, kind, two_col, it.z, it.w); break;
+      case 3: run_item<3>(a, kind, two_col, it.z, it.w); break;
+      case 4: run_item<4>(a, kind, two_col, it.z, it.w); break;
       default: break;
     }
     // shared memory written by generic stores here may be filled by bulk
