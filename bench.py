@@ -468,8 +468,16 @@ def _sec_square(ctx, dev, torch, timed, out):
     ti, td = torch.from_numpy(img).to(dev), torch.from_numpy(depth).to(dev)
     fr = torch.empty((side, side), dtype=torch.float32, device=dev)
     ms = timed(lambda: dm.generate(ctx, p, ti, td, fringe=fr))
-    out[f"depthmap_{side}x{side}_L{L}"] = {"ms_per_frame": ms, "frames_per_s": 1000.0 / ms,
-                                           "what": "one frame of the batch workload's largest shape, 2x pad"}
+    npad = (2 * side) ** 2
+    model = L * 32 * npad + 32 * npad + 2 * side * side        # the frame's HBM model, as for the headline frame
+    peak, src = load_peaks()
+    gbs = model / (ms * 1e-3) / 1e9
+    out[f"depthmap_{side}x{side}_L{L}"] = {
+        "ms_per_frame": ms, "frames_per_s": 1000.0 / ms,
+        "roofline": {"bound": "hbm", "unit": "GB/s", "achieved": gbs, "peak": peak, "frac": gbs / peak,
+                     "peak_source": src, "algorithmic_bytes_per_frame": model,
+                     "what": "model bytes (L*32*Np + 32*Np + 2N) per frame time; the kernels skip the zero padding"},
+        "what": "one frame of the batch workload's largest shape, 2x pad"}
 
 
 def batch_workload():
@@ -519,8 +527,12 @@ def _sec_batch(ctx, dev, torch, out, reps, warmup, nframes=None, tune=True):
             stream.synchronize()
             tune_s = time.perf_counter() - t0
     ms, kernels = run(1)
+    peak_bw, peak_src = load_peaks()
     out["batch_64_frames_mixed_per_frame_launches"] = {
         "ms_per_batch": ms_pf, "frames_per_s": len(work) * 1000.0 / ms_pf, "kernels_per_batch": k_pf,
+        "roofline": {"bound": "hbm", "unit": "GB/s", "achieved": model / (ms_pf * 1e-3) / 1e9, "peak": peak_bw,
+                     "frac": model / (ms_pf * 1e-3) / 1e9 / peak_bw, "peak_source": peak_src,
+                     "what": "the batch's model bytes per batch time, as for the persistent kernel"},
         "what": "the same batch as per-frame launches (set-up, row, column and output pass per frame) replayed "
                 "from one CUDA graph"}
     out["batch_64_frames_mixed"] = {
