@@ -222,3 +222,34 @@ def test_tune_file_errors(ctx, tmp_path):
         dm.set_autotune_file(ctx, bad)
     dm.set_autotune_file(ctx, tmp_path / "absent.txt")              # created by the first autotune
     dm.set_autotune_file(ctx, None)
+
+
+def _tune_key(length):
+    maj, mnr = torch.cuda.get_device_capability(0)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    return f"sm_{maj}{mnr}:{sms}:{length}"
+
+
+@pytest.mark.parametrize("ctas,lag,col_w,row_pairs,col_blocks,out_rows", [
+    (1, 0, 1, 4, 2, 8), (2, 0, 2, 2, 1, 1), (1, 1, 1, 1, 2, 4), (2, 1, 1, 4, 2, 1)])
+def test_persistent_batch_settings_keep_results(ctx, tmp_path, ctas, lag, col_w, row_pairs, col_blocks, out_rows):
+    # every setting the tuner can pick gives the per-frame results bit for bit
+    # (settings given through a tune file for the lengths of these frames)
+    spec = [(512, 512, 9, 532e-9), (768, 768, 6, 633e-9), (512, 512, 13, 450e-9), (768, 512, 5, 532e-9)]
+    path = tmp_path / "tune.txt"
+    lines = [f"{_tune_key(n)} {ctas} {lag} {col_w} {row_pairs} {col_blocks} {out_rows} 0.0" for n in (1024, 1536)]
+    path.write_text("\n".join(lines) + "\n")
+    dm.set_autotune_file(ctx, path)
+    try:
+        for L in (1024, 1536):
+            t = dm.batch_tuning(ctx, L)
+            assert (t["ctas_per_sm"], t["lag"], t["col_w"], t["row_pairs"], t["col_blocks"], t["out_rows"]) == \
+                (ctas, lag, col_w, row_pairs, col_blocks, out_rows)
+        frames = _frames(140, spec)
+        _mode(ctx, 1)
+        dm.generate_batch(ctx, frames)
+        torch.cuda.synchronize()
+        for p, img, depth, fr in frames:
+            assert torch.equal(fr, dm.generate(ctx, p, img, depth))
+    finally:
+        dm.set_autotune_file(ctx, None)
