@@ -371,6 +371,50 @@ __device__ __forceinline__ void dm_col_body(const DMArgs<float>& a, int blk) {
     }
   }
 
+  // stage 0 of one layer from staging buffer (sg, oc) into work buffer bf:
+  // inputs j + t*Q0 of the y-shifted line
+  auto stage0 = [&](const C* sg, const uint8_t* oc, C* bf) {
+    for (int idx = tid; idx < Q0 * W; idx += T) {
+      const int j = idx / W, w = idx - j * W;
+      C x[R0];
+      if (R0 == 16 && a.hzy) {
+        // 2x padding: inputs t = 4..11 are rows of the zero band; with
+        // hy = NY/2 and oy = NY/4 the image row of input t is
+        // j + (t + 4) Q0 (t < 4) or j + (t - 12) Q0 (t >= 12)
+#pragma unroll
+        for (int t = 0; t < R0; ++t) {
+          if (t >= 4 && t < 12) { x[t] = make_float2(0.f, 0.f); continue; }
+          const int yl = j + (t < 4 ? t + 4 : t - 12) * Q0;
+          x[t] = oc[yl] ? sg[yl * SW + csel + w] : make_float2(0.f, 0.f);
+        }
+        dft16_halfzero<-1>(x);
+      } else {
+#pragma unroll
+        for (int t = 0; t < R0; ++t) {
+          int y = j + t * Q0 - a.hy;
+          if (y < 0) y += NY;
+          const int yl = y - a.oy;
+          C v = make_float2(0.f, 0.f);
+          if (yl >= 0 && yl < pny && oc[yl]) v = sg[yl * SW + csel + w];
+          x[t] = v;
+        }
+        DFT<R0, -1, C>::run(x);
+      }
+      if (j) {
+        C wp[R0];
+        twiddle_powers<R0, -1>(tw, j, wp);
+#pragma unroll
+        for (int f = 1; f < R0; ++f) x[f] = cmul(x[f], wp[f]);
+      }
+#pragma unroll
+      for (int f = 0; f < R0; ++f) bf[(pidx(j) + f * Q0P) * W + w] = x[f];
+    }
+  };
+  auto middle = [&](C* bf) {
+    if constexpr (kTab > 0) fstage_tab<NY, R1, M1, -1, C, M1P, RLP>(bf, W, 1, W, tab1, true);
+    else fstage_t<NY, R1, NY / R0, -1>(bf, W, 1, W, tw, true);
+  };
+  static_assert(kTab > 0 || !PADL, "the padded layout needs the middle stage's table");
   if constexpr (PIPE2) {
     C* const buf1 = reinterpret_cast<C*>(smem + Lo.g);
     // step factors of this thread's kept outputs
@@ -387,45 +431,6 @@ __device__ __forceinline__ void dm_col_body(const DMArgs<float>& a, int blk) {
         }
       }
     }
-    // stage 0 of one layer from staging buffer (sg, oc) into work buffer bf
-    auto stage0 = [&](const C* sg, const uint8_t* oc, C* bf) {
-      for (int idx = tid; idx < Q0 * W; idx += T) {
-        const int j = idx / W, w = idx - j * W;
-        C x[R0];
-        if (R0 == 16 && a.hzy) {
-#pragma unroll
-          for (int t = 0; t < R0; ++t) {
-            if (t >= 4 && t < 12) { x[t] = make_float2(0.f, 0.f); continue; }
-            const int yl = j + (t < 4 ? t + 4 : t - 12) * Q0;
-            x[t] = oc[yl] ? sg[yl * SW + csel + w] : make_float2(0.f, 0.f);
-          }
-          dft16_halfzero<-1>(x);
-        } else {
-#pragma unroll
-          for (int t = 0; t < R0; ++t) {
-            int y = j + t * Q0 - a.hy;
-            if (y < 0) y += NY;
-            const int yl = y - a.oy;
-            C v = make_float2(0.f, 0.f);
-            if (yl >= 0 && yl < pny && oc[yl]) v = sg[yl * SW + csel + w];
-            x[t] = v;
-          }
-          DFT<R0, -1, C>::run(x);
-        }
-        if (j) {
-          C wp[R0];
-          twiddle_powers<R0, -1>(tw, j, wp);
-#pragma unroll
-          for (int f = 1; f < R0; ++f) x[f] = cmul(x[f], wp[f]);
-        }
-#pragma unroll
-        for (int f = 0; f < R0; ++f) bf[(pidx(j) + f * Q0P) * W + w] = x[f];
-      }
-    };
-    auto middle = [&](C* bf) {
-      if constexpr (kTab > 0) fstage_tab<NY, R1, M1, -1, C, M1P, RLP>(bf, W, 1, W, tab1, true);
-      else fstage_t<NY, R1, NY / R0, -1>(bf, W, 1, W, tw, true);
-    };
     // layers without pixels since the previous one (acc D^(gap - 1)), then
     // the last stage of work buffer bf fused with acc = acc D + x
     auto last = [&](const C* bf, int gap) {
@@ -516,62 +521,25 @@ __device__ __forceinline__ void dm_col_body(const DMArgs<float>& a, int blk) {
       if constexpr (horner) {
         // layers without pixels since the previous one: acc D^(gap - 1)
         for (int r = 1; r < gap; ++r) {
-  #pragma unroll
+#pragma unroll
           for (int kb = 0; kb < KB; ++kb) {
             const int bb = tid + kb * T;
             if (bb < CF::NBL) {
               const int b = bb / W, w = bb - b * W;
-  #pragma unroll
+#pragma unroll
               for (int f = 0; f < RL; ++f) acc[kb][f] = cmul(acc[kb][f], dsm[(b * RLP + f) * W + w]);
             }
           }
         }
       }
-      // stage 0 from the staging buffer: inputs j + t*Q0 of the y-shifted line
-      for (int idx = tid; idx < Q0 * W; idx += T) {
-        const int j = idx / W, w = idx - j * W;
-        C x[R0];
-        if (R0 == 16 && a.hzy) {
-          // 2x padding: inputs t = 4..11 are rows of the zero band; with
-          // hy = NY/2 and oy = NY/4 the image row of input t is
-          // j + (t + 4) Q0 (t < 4) or j + (t - 12) Q0 (t >= 12)
-  #pragma unroll
-          for (int t = 0; t < R0; ++t) {
-            if (t >= 4 && t < 12) { x[t] = make_float2(0.f, 0.f); continue; }
-            const int yl = j + (t < 4 ? t + 4 : t - 12) * Q0;
-            x[t] = occ[yl] ? stg[yl * SW + csel + w] : make_float2(0.f, 0.f);
-          }
-          dft16_halfzero<-1>(x);
-        } else {
-  #pragma unroll
-          for (int t = 0; t < R0; ++t) {
-            int y = j + t * Q0 - a.hy;
-            if (y < 0) y += NY;
-            const int yl = y - a.oy;
-            C v = make_float2(0.f, 0.f);
-            if (yl >= 0 && yl < pny && occ[yl]) v = stg[yl * SW + csel + w];
-            x[t] = v;
-          }
-          DFT<R0, -1, C>::run(x);
-        }
-        if (j) {
-          C wp[R0];
-          twiddle_powers<R0, -1>(tw, j, wp);
-  #pragma unroll
-          for (int f = 1; f < R0; ++f) x[f] = cmul(x[f], wp[f]);
-        }
-  #pragma unroll
-        for (int f = 0; f < R0; ++f) buf[(pidx(j) + f * Q0P) * W + w] = x[f];
-      }
+      stage0(stg, occ, buf);
       // middle stage(s); the leading barrier also frees the strip buffer
       __syncthreads();
       if (tid == 0 && k + 1 < nact) {
         fence_proxy_async_smem();
         issue_strip(k + 1);
       }
-      static_assert(kTab > 0 || !PADL, "the padded layout needs the middle stage's table");
-      if constexpr (kTab > 0) fstage_tab<NY, R1, M1, -1, C, M1P, RLP>(buf, W, 1, W, tab1, true);
-      else fstage_t<NY, R1, NY / R0, -1>(buf, W, 1, W, tw, true);
+      middle(buf);
       __syncthreads();
       // last stage (stride 1, no twiddles) fused with the transfer-function
       // multiply-accumulate: either acc += H x per layer, or the recurrence
@@ -580,17 +548,17 @@ __device__ __forceinline__ void dm_col_body(const DMArgs<float>& a, int blk) {
       const float kz = a.kzp[e];
       const float* eth = (k & 1) ? ey1 : ey0;       // storage order
       const float inv2pi = 0.15915494309189533577f, two_pi = 6.28318530717958647692f;
-  #pragma unroll
+#pragma unroll
       for (int kb = 0; kb < KB; ++kb) {
         const int bb = tid + kb * T;
         if (bb < CF::NBL) {
           const int b = bb / W, w = bb - b * W;
           C x[RL];
-  #pragma unroll
+#pragma unroll
           for (int f = 0; f < RL; ++f) x[f] = buf[(b * RLP + f) * W + w];
           DFT<RL, -1, C>::run(x);
           if constexpr (horner) {
-  #pragma unroll
+#pragma unroll
             for (int f = 0; f < RL; ++f) {
               if (!((fkeep >> f) & 1u)) continue;         // outside the SSB crop for every b
               const C d = dsm[(b * RLP + f) * W + w];
@@ -600,7 +568,7 @@ __device__ __forceinline__ void dm_col_body(const DMArgs<float>& a, int blk) {
             continue;
           }
           const C ex = exw[w];
-  #pragma unroll
+#pragma unroll
           for (int f = 0; f < RL; ++f) {
             if (!((fkeep >> f) & 1u)) continue;           // outside the SSB crop for every b
             const int p = b * RL + f;
