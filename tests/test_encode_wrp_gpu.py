@@ -292,3 +292,22 @@ def test_wrp_matlab_window(ctx, res, precision):
     torch.cuda.synchronize()
     tol = 1e-10 if precision == "fp64" else 1e-5
     assert np.linalg.norm(holo.cpu().numpy() - ref) <= tol * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("method", [_lib.PROP_FRESNEL_TF, _lib.PROP_AS_BANDLIMITED])
+@pytest.mark.parametrize("z", [1e-3, 5e-3])
+def test_propagation_round_trip(ctx, method, z):
+    # known answer: propagating a compact beam by +z and then by -z returns it
+    # (the transfer function is unitary; the band-limited form loses nothing
+    # for a beam that stays inside the window at these distances)
+    ny, nx = 64, 96
+    y, x = np.mgrid[0:ny, 0:nx]
+    g = np.exp(-(((x - nx / 2) / 6.0) ** 2 + ((y - ny / 2) / 5.0) ** 2)) * np.exp(1j * 0.3 * x)
+    for precision, tol in (("fp64", 1e-9), ("fp32", 1e-5)):
+        t = torch.from_numpy(g).to(torch.complex128 if precision == "fp64" else torch.complex64).cuda()
+        for zz in (z, -z):
+            _lib.call("oh_propagate", ctx.handle, 1 if precision == "fp64" else 0, method, nx, ny, 8e-6, 8e-6, zz,
+                      532e-9, C.c_void_p(t.data_ptr()), S())
+        torch.cuda.synchronize()
+        back = t.cpu().numpy().astype(np.complex128)
+        assert np.linalg.norm(back - g) <= tol * np.linalg.norm(g), precision

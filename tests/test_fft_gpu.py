@@ -79,3 +79,14 @@ def test_fft_supported_and_errors(ctx):
         fft2(ctx, x)
     with pytest.raises(OhError):
         fft2(ctx, np.ones((4, 4)), direction=0)
+
+
+@pytest.mark.parametrize("shape", [(120, 90), (1080, 1920), (27, 125)])
+def test_fft2_parseval(ctx, shape):
+    # known answer: the unnormalised forward transform multiplies the energy by N
+    rng = np.random.default_rng(7)
+    x = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    for precision, tol in (("fp64", 1e-12), ("fp32", 1e-6)):
+        X = fft2(ctx, x, -1, precision=precision)
+        ex, eX = np.sum(np.abs(x) ** 2), np.sum(np.abs(X) ** 2) / x.size
+        assert abs(eX - ex) <= tol * ex, precision
