@@ -1,5 +1,6 @@
-// Persistent batch kernel of the depth-map pipeline: shared declarations of
-// the host planner (depthmap.cu) and the kernel (dm_batch.cu).
+// Persistent batch kernel of the depth-map pipeline: declarations shared by
+// the per-frame pipeline (depthmap.cu) and the batch kernel with its host
+// planner and autotuner (dm_batch.cu).
 //
 // A batch of frames becomes one list of work items, each a range of blocks
 // of one pass of one frame (row pairs, column strips or output rows).  One
@@ -18,9 +19,44 @@
 // error-path test hook) sets the launch's abort word and the context's
 // error word; every block then stops at its next item.
 #pragma once
+#include <string>
+#include <type_traits>
 #include "dm_kernels.cuh"
 
 namespace oh {
+
+// Scratch bytes one frame needs: R strips, V rows, occupancy flags, tables.
+struct DMScratch { size_t R, V, occ, tables, acc; };
+
+// Everything run_depthmap decides for one frame before it allocates: the
+// scratch sizes, the kernel arguments (their table pointers hold offsets
+// into the frame's table region, see relocate_tables), the per-frame set-up
+// constants, and the pass configuration.
+template <typename R> struct FrameInfo {
+  DMScratch sz;
+  DMArgs<R> a;
+  DMSetup su;
+  int Wfast = 0, wcol = 0, nchunks = 1;
+  size_t smem_row = 0, smem_col = 0, smem_out = 0;
+};
+
+// Adds the base of a table region to the offsets FrameInfo::a holds.
+template <typename R> void relocate_tables(DMArgs<R>* a, char* base) {
+  auto rel = [&](auto*& p) { p = reinterpret_cast<std::remove_reference_t<decltype(p)>>(base + reinterpret_cast<size_t>(p)); };
+  rel(a->lut); rel(a->uslot_of_entry); rel(a->kzp); rel(a->cst); rel(a->exc); rel(a->ey); rel(a->eth);
+  rel(a->lfx); rel(a->lfy); rel(a->lfyp); rel(a->shy); rel(a->shx); rel(a->slot_any);
+  if (a->dxh) rel(a->dxh);
+  if (a->dyh) rel(a->dyh);
+}
+
+// The planning half of run_depthmap (depthmap.cu) for one FP32 frame: fills
+// info without allocating or launching anything.
+oh_status depthmap_frame_info(oh_ctx* ctx, const oh_depthmap_frame& f, cudaStream_t st, FrameInfo<float>* info);
+oh_status depthmap_validate(const oh_depthmap_params* p);
+// The persistent path of oh_depthmap_generate_batch (dm_batch.cu): *handled
+// = false when some frame is outside what the batch kernel carries.
+oh_status batch_persistent(oh_ctx* ctx, const oh_depthmap_frame* frames, int n, unsigned flags,
+                           const std::string& key, cudaStream_t st, bool* handled);
 
 // Padded lengths (Px and Py) the batch kernel carries, as length classes.
 constexpr int kBatchLens[] = {1024, 1536, 2048, 3072, 4096};
